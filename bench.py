@@ -1,0 +1,324 @@
+#!/usr/bin/env python
+"""Frames/s of the radiance-cascade solve on the 256^3 moving-emitter workload.
+
+A step is one frame: the 32 emissive spheres advance 0.5 voxel, the volume
+under the old and new spheres is recomposed on the device, and all 6
+cascades plus the cascade-0 fluence are solved.
+
+  value  frames/s with the scene resident in HBM, CUDA events on the
+         context stream (per-frame working set ~1.3 GB >> L2)
+  e2e    frames/s through the public C ABI with host buffers: each step
+         copies the frame's sphere array host->device and reads the fluence
+         back into pinned host memory
+  roofline   level kernels: algorithmic bytes per frame / their event time
+  cpu_baseline   the FP32 CPU port of the method, all host threads
+
+--impl reference times the CPU implementation of the same path (the oracle
+port, FP32, all host threads) on the same workload: the reference project
+has no cascade code of its own and its wgpu path cannot run headless here.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "c256"
+WORKLOAD_DESC = ("256^3 voxels, 400 seeded opaque boxes (edges 4-48), 32 emissive spheres (radius 2-8, "
+                 "emission 1-50) moving 0.5 voxel/frame; 6 cascades: 128^3 probes x 16 dirs at cascade 0, "
+                 "x4 dirs and /2 probes per axis per level, intervals 0,1,5,21,85,341,1365")
+
+
+def _env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def algorithmic_bytes(levels, grid, elem_bytes):
+    """Bytes per frame: N_c * S + sum_i W_i + sum_{i>=1} W_i + F (scene 8 B/voxel read once per
+    cascade, merged radiance written once and read once by the level below, fluence written)."""
+    S = 8 * grid ** 3
+    W = [3 * elem_bytes * l.num_dirs * l.probes[0] * l.probes[1] * l.probes[2] for l in levels]
+    F = 12 * levels[0].probes[0] * levels[0].probes[1] * levels[0].probes[2]
+    per_launch = []
+    for i in range(len(levels)):
+        b = S + W[i] + (W[i + 1] if i + 1 < len(levels) else 0) + (F if i == 0 else 0)
+        per_launch.append(b)
+    return sum(per_launch), per_launch
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="rc_clocks_", suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_gbs():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_launch():
+    """DRAM bytes per level-kernel launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "level_kernel_c256_ncu.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1].strip().split()[0])
+    except Exception:
+        pass
+    return None
+
+
+def cpu_port_frames_per_s(frames: int, threads: int, precision=np.float32):
+    """Times the FP32 CPU port of the path on `frames` frames of the workload."""
+    from oracle import oracle as O
+    boxes, spheres = O.config_scene(WORKLOAD)
+    p = O.params(256, 6)
+    t_total = 0.0
+    for f in range(frames):
+        t0 = time.perf_counter()
+        vox = O.voxelise(256, boxes, spheres)
+        O.solve(p, vox, dtype=precision, jump=True, nthreads=threads)
+        t_total += time.perf_counter() - t0
+        O.advance(spheres, 256, 1)
+    return frames / t_total, t_total
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, ROOT)
+    from oracle import build_oracle
+    build_oracle.build()
+    for _ in range(args.warmup):
+        cpu_port_frames_per_s(1, threads)
+    value, secs = cpu_port_frames_per_s(args.steps, threads)
+    line = {
+        "impl": "reference", "metric": "frames/s at 256^3 (radiance cascades, fluence + per-probe radiance)",
+        "value": round(value, 4), "unit": "frames/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000.0 * secs / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_DESC, "precision": "fp32"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": "%d consecutive frames of the 256^3 workload, full frame each "
+                                   "(voxelise + 6 cascades + fluence)" % args.steps},
+        "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference repository holds no radiance-cascade implementation (only a wgpu forward "
+                 "raster pass); this arm times the CPU restatement of the method on all host threads"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--cpu-frames", type=int, default=2, help="frames of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import radiancecascade_gb300 as R
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    boxes, spheres = R.workload_scene(WORKLOAD)
+    params = R.make_params(256, 6, precision=args.precision)
+    eng = R.Engine(params, device=local)
+    eng.set_boxes(boxes)
+    levels = eng.levels
+    # replicas: rank r starts at frame r * steps so the ranks solve different frames
+    sph = spheres.copy()
+    if rank:
+        R.advance_spheres(sph, 256, rank * (args.steps + args.warmup))
+    stream = torch.cuda.ExternalStream(eng.stream(), device=local)
+
+    for _ in range(args.warmup):
+        eng.set_spheres(sph)
+        eng.solve()
+        R.advance_spheres(sph, 256, 1)
+    eng.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for _ in range(args.steps):
+        eng.set_spheres(sph)
+        eng.solve()
+        R.advance_spheres(sph, 256, 1)
+    t_end.record(stream)
+    t_end.synchronize()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    ms = t_start.elapsed_time(t_end)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    value = world * args.steps / (ms / 1000.0)
+    launches_per_step = 1 + params.num_cascades  # recompose + one kernel per cascade
+
+    # ---- e2e: public API, host buffers, H2D of the frame's spheres, D2H of the fluence
+    nflu = 3 * int(np.prod(eng.probes0))
+    host_out = torch.empty(nflu, dtype=torch.float32, pin_memory=True).numpy()
+    for _ in range(2):
+        eng.set_spheres(sph)
+        eng.solve()
+        eng.fluence(out=host_out)
+        R.advance_spheres(sph, 256, 1)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.set_spheres(sph)
+        eng.solve()
+        eng.fluence(out=host_out)
+        R.advance_spheres(sph, 256, 1)
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps / e2e_s
+
+    # ---- roofline of the level kernels (CUDA events around every launch)
+    per_level_ms = eng.profile_levels(iters=10)
+    level_ms = float(per_level_ms[1:].sum())
+    elem = 2 if args.precision == "fp16" else 4
+    B, per_launch = algorithmic_bytes(levels, 256, elem)
+    achieved = B / (level_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peak_gbs()
+    traffic = profile_traffic_per_launch()
+
+    line = {
+        "metric": "frames/s at 256^3 (radiance cascades, fluence + per-probe radiance)",
+        "value": round(value, 3), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16" if args.precision == "fp16" else "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD_DESC, "precision": args.precision, "frames_per_rank": args.steps,
+                   "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (~1.3 GB of scene + radiance per frame)"},
+        "e2e": {"value": round(e2e_value, 3), "unit": "frames/s",
+                "h2d_bytes_per_step": int(sph.nbytes), "d2h_bytes_per_step": int(nflu * 4)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "traffic": traffic,
+                     "kernel": "k_level (one launch per cascade)",
+                     "algorithmic_bytes_per_frame": B,
+                     "level_ms_per_frame": round(level_ms, 4),
+                     "per_level_ms": [round(float(x), 4) for x in per_level_ms[1:]],
+                     "compose_full_ms": round(float(per_level_ms[0]), 4)},
+    }
+    if clock_info:
+        line["clocks"] = clock_info
+
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        from oracle import oracle as O
+        fb, fs = R.workload_scene(WORKLOAD)
+        eng.set_spheres(fs)
+        eng.solve()
+        g = eng.fluence().astype(np.float64)
+        ref, _ = O.solve(O.params(256, 6), O.voxelise(256, fb, fs), jump=True)
+        line["accuracy"] = {"frame": 0, "fluence_rel_l2_vs_fp64":
+                            float(np.linalg.norm(g - ref) / np.linalg.norm(ref)),
+                            "fluence_max_abs_vs_fp64": float(np.abs(g - ref).max())}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, _ = cpu_port_frames_per_s(args.cpu_frames, threads)
+        line["cpu_baseline"] = {"value": round(v, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                                "sample": "%d frames of the same workload (voxelise + 6 cascades + fluence, "
+                                          "FP32, OpenMP)" % args.cpu_frames}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,207 @@
+/*
+ * rc.h -- C ABI of the GB300 radiance-cascade global-illumination engine.
+ *
+ * The reference renderer's only extension point is the RenderStage trait
+ * (reference: src/app.rs:3-7): update() receives per-frame state and uploads it
+ * (src/window/app.rs:112-132, src/renderer.rs:620-631), render() records GPU
+ * work into the frame (src/window/app.rs:246-248, src/renderer.rs:559-613),
+ * resize() rebuilds size-dependent resources (src/window/app.rs:104-110).
+ * A GI pass is a RenderStage implementation; this header is the foreign
+ * function interface such a stage calls:
+ *
+ *   RenderStage::resize  ->  rc_create / rc_destroy            (grid + cascade shape)
+ *   RenderStage::update  ->  rc_scene_upload, rc_scene_set_spheres (scene volume, emitters)
+ *   RenderStage::render  ->  rc_solve                            (all cascades + fluence)
+ *   consumer binding     ->  rc_get_fluence / rc_get_radiance / rc_fluence_device_ptr
+ *
+ * Conventions
+ *   - Every entry point returns an rc_status; nothing aborts or throws across
+ *     the boundary.  rc_last_error() gives a message for the calling thread.
+ *   - The context owns its device memory.  Caller buffers are borrowed for the
+ *     duration of the call only.
+ *   - Calls on one context must be serialised by the caller.  GPU work is
+ *     ordered on the stream passed to rc_solve (or the context's own stream
+ *     when NULL).  rc_solve is asynchronous; rc_get_* synchronise.
+ *   - Only plain C types cross this boundary; no CUDA or framework types.
+ *     Streams are passed as void* (a cudaStream_t).
+ */
+#ifndef RC_H_
+#define RC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RC_ABI_VERSION 1
+
+typedef enum rc_status {
+  RC_OK = 0,
+  RC_ERR_INVALID_ARG = 1,  /* bad pointer, size, dimension or parameter      */
+  RC_ERR_OOM = 2,          /* a device or pinned-host allocation failed       */
+  RC_ERR_CUDA = 3,         /* a CUDA runtime call failed (incl. no device)    */
+  RC_ERR_TIMEOUT = 4,      /* a bounded device-side wait ran out              */
+  RC_ERR_UNSUPPORTED = 5,  /* parameters outside the exact-arithmetic range   */
+  RC_ERR_STATE = 6         /* call out of order (e.g. solve before upload)    */
+} rc_status;
+
+enum { RC_PRECISION_FP32 = 0, RC_PRECISION_FP16 = 1 };
+enum { RC_MEM_HOST = 0, RC_MEM_DEVICE = 1 };
+
+/* Cascade parameters.  Grid edges are in voxels.  Cascade i (0-based) has
+ * probe spacing s_i = probe_spacing0 * 2^i voxels with probe centres at
+ * (m + 1/2) * s_i, (dir_res0 * 2^i)^2 octahedral directions, and covers the
+ * distance interval [b_i, b_{i+1}) with b_0 = 0, b_1 = interval0 and
+ * b_{i+1} = interval_ratio * b_i + interval0.  Every grid edge must be a
+ * multiple of the top cascade's spacing. */
+typedef struct rc_params {
+  int32_t grid[3];
+  int32_t num_cascades;   /* >= 1                                    */
+  int32_t probe_spacing0; /* power of two, >= 2       (default 2)     */
+  int32_t dir_res0;       /* even, >= 2, top level <= 256 (default 4) */
+  int32_t interval0;      /* >= 1                     (default 1)     */
+  int32_t interval_ratio; /* >= 2                     (default 4)     */
+  int32_t precision;      /* RC_PRECISION_FP32 / RC_PRECISION_FP16    */
+  int32_t reserved[7];    /* must be zero                             */
+} rc_params;
+
+/* One voxel of the scene volume, 8 bytes.
+ *   emission:   RGB radiance leaving the voxel, IEEE-754 binary16 bits
+ *   albedo_occ: bit 15 = opaque; bits 10..14 / 5..9 / 0..4 = albedo R/G/B as
+ *               5-bit unorm.
+ * A non-opaque voxel is empty space: its emission and albedo are ignored. */
+typedef struct rc_voxel {
+  uint16_t emission[3];
+  uint16_t albedo_occ;
+} rc_voxel;
+
+#define RC_VOXEL_OPAQUE 0x8000u
+
+/* Axis-aligned box covering voxels lo <= v < hi (clipped to the grid). */
+typedef struct rc_box {
+  int32_t lo[3];
+  int32_t hi[3];
+  rc_voxel value;
+} rc_box;
+
+/* Sphere emitter.  Centre and radius are in voxel units and are quantised to
+ * 1/256 voxel when voxelised; a voxel belongs to the sphere when its centre
+ * lies within the radius.  velocity is in voxels per frame. */
+typedef struct rc_sphere {
+  double centre[3];
+  double radius;
+  double velocity[3];
+  rc_voxel value;
+  uint32_t pad[2];
+} rc_sphere;  /* 72 bytes */
+
+/* Seeded synthetic scene description (boxes, then spheres). */
+typedef struct rc_scene_spec {
+  int32_t grid[3];
+  int32_t num_boxes;
+  int32_t box_edge_min, box_edge_max;  /* integer edges, inclusive range  */
+  int32_t num_spheres;
+  int32_t reserved;
+  double albedo_min, albedo_max;       /* per channel                     */
+  double radius_min, radius_max;       /* voxels                          */
+  double emission_min, emission_max;   /* per channel                     */
+  double speed;                        /* voxels per frame                */
+} rc_scene_spec;
+
+/* Shape of one cascade level as laid out in device memory. */
+typedef struct rc_level_info {
+  int32_t probes[3];      /* probes per axis                            */
+  int32_t spacing;        /* voxels between probe centres               */
+  int32_t dir_res;        /* n: the level has n*n directions            */
+  int32_t num_dirs;
+  int32_t interval_lo;    /* b_i, voxels                                */
+  int32_t interval_hi;    /* b_{i+1}, voxels                            */
+  int64_t radiance_elems; /* 3 * num_dirs * probes (planar RGB)         */
+  int64_t radiance_bytes; /* radiance_elems * element size              */
+} rc_level_info;
+
+typedef struct rc_context rc_context;
+
+/* ---- errors --------------------------------------------------------- */
+const char* rc_status_string(rc_status s);
+/* Message of the last failing call on this thread (never NULL). */
+const char* rc_last_error(void);
+int rc_abi_version(void);
+
+/* ---- host-only helpers (no GPU needed) ------------------------------- */
+rc_status rc_params_default(rc_params* p, int32_t grid_edge, int32_t num_cascades);
+rc_status rc_params_validate(const rc_params* p);
+rc_status rc_level_info_get(const rc_params* p, int32_t level, rc_level_info* out);
+/* Elements of the cascade-0 fluence buffer: 3 * probes0 (RGB interleaved). */
+int64_t rc_fluence_elems(const rc_params* p);
+/* Seeded scene generator: writes spec->num_boxes boxes and
+ * spec->num_spheres spheres. */
+rc_status rc_scene_generate(const rc_scene_spec* spec, uint64_t seed,
+                            rc_box* boxes, rc_sphere* spheres);
+/* Advance spheres by `frames` frames: centre += velocity, reflected so that
+ * the whole sphere stays inside the grid. */
+rc_status rc_spheres_advance(rc_sphere* spheres, int32_t n,
+                             const int32_t grid[3], int32_t frames);
+/* Voxelise boxes then spheres (later objects win) into a host volume of
+ * grid[0]*grid[1]*grid[2] voxels, x fastest. */
+rc_status rc_voxelise_host(const int32_t grid[3], const rc_box* boxes,
+                           int32_t nboxes, const rc_sphere* spheres,
+                           int32_t nspheres, rc_voxel* out);
+/* Octahedral direction table of resolution n: n*n integer vectors (x,y,z)
+ * with |x|+|y|+|z| = n, texel (j,k) at index k*n + j. */
+rc_status rc_directions(int32_t n, int32_t* out_xyz);
+/* Exact solid angle (steradians) of every octahedral texel at resolution n. */
+rc_status rc_solid_angles(int32_t n, double* out);
+
+/* ---- context -------------------------------------------------------- */
+rc_status rc_create(const rc_params* p, int32_t device, rc_context** out);
+rc_status rc_destroy(rc_context* ctx);  /* NULL is accepted */
+rc_status rc_get_params(const rc_context* ctx, rc_params* out);
+
+/* Static scene volume (x fastest).  where = RC_MEM_HOST or RC_MEM_DEVICE.
+ * Replaces the base volume; dynamic spheres are re-applied on top. */
+rc_status rc_scene_upload(rc_context* ctx, const rc_voxel* voxels,
+                          int64_t count, int32_t where);
+/* Voxelise up to 1536 boxes on the device into the base volume (later
+ * boxes win). */
+rc_status rc_scene_set_boxes(rc_context* ctx, const rc_box* boxes,
+                             int32_t n);
+/* Dynamic emitters drawn over the base volume (later spheres win).  Only
+ * the voxels under the previous and the new spheres are rewritten. */
+rc_status rc_scene_set_spheres(rc_context* ctx, const rc_sphere* spheres,
+                               int32_t n);
+
+/* Solve all cascades top-down and the cascade-0 fluence.  stream may be
+ * NULL (context stream).  Asynchronous. */
+rc_status rc_solve(rc_context* ctx, void* stream);
+rc_status rc_synchronize(rc_context* ctx);
+
+/* Cascade-0 fluence, RGB interleaved float32, probe order x fastest. */
+rc_status rc_get_fluence(rc_context* ctx, float* out, int64_t elems,
+                         int32_t where);
+/* Merged radiance of one level, planar [3][num_dirs][pz][py][px], float32
+ * or binary16 according to params.precision. */
+rc_status rc_get_radiance(rc_context* ctx, int32_t level, void* out,
+                          int64_t bytes, int32_t where);
+/* Device pointer of the context-owned fluence buffer (valid until destroy). */
+rc_status rc_fluence_device_ptr(rc_context* ctx, const float** out);
+rc_status rc_radiance_device_ptr(rc_context* ctx, int32_t level,
+                                 const void** out);
+/* The context's own stream (a cudaStream_t), for ordering consumer work
+ * after rc_solve and for timing. */
+rc_status rc_get_stream(rc_context* ctx, void** out);
+
+/* ---- profiling ------------------------------------------------------ */
+/* Runs `iters` solves on the context stream with CUDA events around every
+ * kernel and writes the mean milliseconds per launch: ms_out[0] = scene
+ * composition (full rebuild), ms_out[1 + i] = cascade level i.  Needs
+ * 1 + num_cascades floats.  Synchronises. */
+rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
+                            int32_t count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RC_H_ */

@@ -1,0 +1,122 @@
+"""ctypes bindings of include/rc.h (librc.so, built in-tree by build.py).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "librc.so")
+
+RC_OK, RC_ERR_INVALID_ARG, RC_ERR_OOM, RC_ERR_CUDA, RC_ERR_TIMEOUT, RC_ERR_UNSUPPORTED, RC_ERR_STATE = range(7)
+RC_PRECISION_FP32, RC_PRECISION_FP16 = 0, 1
+RC_MEM_HOST, RC_MEM_DEVICE = 0, 1
+
+VOXEL_DT = np.dtype([("emission", "<u2", (3,)), ("albedo_occ", "<u2")])
+BOX_DT = np.dtype([("lo", "<i4", (3,)), ("hi", "<i4", (3,)), ("value", VOXEL_DT)])
+SPHERE_DT = np.dtype([("centre", "<f8", (3,)), ("radius", "<f8"), ("velocity", "<f8", (3,)),
+                      ("value", VOXEL_DT), ("pad", "<u4", (2,))])
+OPAQUE = 0x8000
+
+
+class Params(C.Structure):
+    _fields_ = [("grid", C.c_int32 * 3), ("num_cascades", C.c_int32), ("probe_spacing0", C.c_int32),
+                ("dir_res0", C.c_int32), ("interval0", C.c_int32), ("interval_ratio", C.c_int32),
+                ("precision", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class SceneSpec(C.Structure):
+    _fields_ = [("grid", C.c_int32 * 3), ("num_boxes", C.c_int32), ("box_edge_min", C.c_int32),
+                ("box_edge_max", C.c_int32), ("num_spheres", C.c_int32), ("reserved", C.c_int32),
+                ("albedo_min", C.c_double), ("albedo_max", C.c_double), ("radius_min", C.c_double),
+                ("radius_max", C.c_double), ("emission_min", C.c_double), ("emission_max", C.c_double),
+                ("speed", C.c_double)]
+
+
+class LevelInfo(C.Structure):
+    _fields_ = [("probes", C.c_int32 * 3), ("spacing", C.c_int32), ("dir_res", C.c_int32),
+                ("num_dirs", C.c_int32), ("interval_lo", C.c_int32), ("interval_hi", C.c_int32),
+                ("radiance_elems", C.c_int64), ("radiance_bytes", C.c_int64)]
+
+
+_P = C.c_void_p
+_S = C.c_int  # rc_status
+
+# name -> (restype, argtypes); the full ABI of include/rc.h
+SIGNATURES = {
+    "rc_status_string": (C.c_char_p, [C.c_int]),
+    "rc_last_error": (C.c_char_p, []),
+    "rc_abi_version": (C.c_int, []),
+    "rc_params_default": (_S, [_P, C.c_int32, C.c_int32]),
+    "rc_params_validate": (_S, [_P]),
+    "rc_level_info_get": (_S, [_P, C.c_int32, _P]),
+    "rc_fluence_elems": (C.c_int64, [_P]),
+    "rc_scene_generate": (_S, [_P, C.c_uint64, _P, _P]),
+    "rc_spheres_advance": (_S, [_P, C.c_int32, _P, C.c_int32]),
+    "rc_voxelise_host": (_S, [_P, _P, C.c_int32, _P, C.c_int32, _P]),
+    "rc_directions": (_S, [C.c_int32, _P]),
+    "rc_solid_angles": (_S, [C.c_int32, _P]),
+    "rc_create": (_S, [_P, C.c_int32, C.POINTER(C.c_void_p)]),
+    "rc_destroy": (_S, [_P]),
+    "rc_get_params": (_S, [_P, _P]),
+    "rc_scene_upload": (_S, [_P, _P, C.c_int64, C.c_int32]),
+    "rc_scene_set_boxes": (_S, [_P, _P, C.c_int32]),
+    "rc_scene_set_spheres": (_S, [_P, _P, C.c_int32]),
+    "rc_solve": (_S, [_P, _P]),
+    "rc_synchronize": (_S, [_P]),
+    "rc_get_fluence": (_S, [_P, _P, C.c_int64, C.c_int32]),
+    "rc_get_radiance": (_S, [_P, C.c_int32, _P, C.c_int64, C.c_int32]),
+    "rc_fluence_device_ptr": (_S, [_P, C.POINTER(C.c_void_p)]),
+    "rc_radiance_device_ptr": (_S, [_P, C.c_int32, C.POINTER(C.c_void_p)]),
+    "rc_get_stream": (_S, [_P, C.POINTER(C.c_void_p)]),
+    "rc_profile_levels": (_S, [_P, C.c_int32, _P, C.c_int32]),
+}
+
+_lib = None
+
+
+class RCError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s: %s" % (status_name(status), message))
+        self.status = status
+        self.message = message
+
+
+def lib() -> C.CDLL:
+    """Load librc.so.  Raises (never falls back) when it was not built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("librc.so is missing at %s: build it first "
+                              "(python -m radiancecascade_gb300.build or __graft_entry__.build())" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_name(s: int) -> str:
+    try:
+        return lib().rc_status_string(s).decode()
+    except Exception:  # pragma: no cover - library not loadable
+        return "RC_STATUS_%d" % s
+
+
+def last_error() -> str:
+    return lib().rc_last_error().decode(errors="replace")
+
+
+def check(status: int) -> None:
+    if status != RC_OK:
+        raise RCError(status, last_error())
+
+
+def ptr(a: np.ndarray) -> C.c_void_p:
+    return a.ctypes.data_as(C.c_void_p)

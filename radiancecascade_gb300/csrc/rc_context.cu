@@ -1,0 +1,572 @@
+// rc_context.cu -- the C ABI of include/rc.h that needs the GPU: context
+// lifetime, scene upload and emitter update, the per-frame solve and result
+// read-back.  One context = one scene on one GPU, ordered on one stream.
+//
+// Reference boundary: a GI stage implementing RenderStage (src/app.rs:3-7)
+// calls rc_create/rc_destroy from resize(), rc_scene_* from update() and
+// rc_solve from render(); see include/rc.h.
+
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "rc_internal.h"
+#include "rc_kernels.cuh"
+
+using namespace rcx;
+
+struct rc_context {
+  rc_params p{};
+  int device = 0;
+  int nlev = 0;
+  LevelGeom geom[kMaxCascades]{};
+  size_t elem = 4;  // bytes per stored radiance value
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // staging slot copies done
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+
+  uint2* base = nullptr;     // static volume (boxes / upload)
+  uint2* vol = nullptr;      // composed volume
+  uint32_t* occ = nullptr;   // opacity bits
+  int W = 0;                 // words per x row
+  DirInfo* dirs = nullptr;   // all levels, concatenated
+  size_t dir_off[kMaxCascades]{};
+  void* rad = nullptr;       // L_i for all levels
+  size_t rad_off[kMaxCascades]{};  // bytes
+  void* avg = nullptr;       // A_i for levels >= 1
+  size_t avg_off[kMaxCascades]{};  // bytes
+  float* fluence = nullptr;
+
+  // dynamic spheres
+  QSphere* d_sph = nullptr;
+  Region* d_reg = nullptr;
+  int sph_cap = 0;
+  void* h_stage = nullptr;  // pinned, two slots of (spheres, regions)
+  size_t slot_bytes = 0;
+  int slot = 0;
+  bool stage_pending[2] = {false, false};
+  std::vector<QSphere> cur;
+  bool have_base = false;
+  LevelArgs args[kMaxCascades]{};
+};
+
+namespace {
+
+rc_status cuda_fail(cudaError_t e, const char* what) {
+  rcx::set_error("%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? RC_ERR_OOM : RC_ERR_CUDA;
+}
+
+#define RC_CUDA(call, what)                         \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool fault_is(const char* name) {
+  const char* f = getenv("RC_FAULT");
+  return f && strcmp(f, name) == 0;
+}
+
+rc_status dev_alloc(void** ptr, size_t bytes, const char* what) {
+  if (fault_is("alloc")) {
+    rcx::set_error("%s: injected allocation failure (RC_FAULT=alloc)", what);
+    return RC_ERR_OOM;
+  }
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    (void)cudaGetLastError();
+    return cuda_fail(e, what);
+  }
+  return RC_OK;
+}
+
+void release(rc_context* c) {
+  if (!c) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  void* bufs[] = {c->base, c->vol, c->occ, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  if (c->ev_in) cudaEventDestroy(c->ev_in);
+  if (c->ev_out) cudaEventDestroy(c->ev_out);
+  for (cudaEvent_t ev : c->ev_stage)
+    if (ev) cudaEventDestroy(ev);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  cudaSetDevice(prev);
+  delete c;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+rc_status check_ctx(const rc_context* c, const char* fn) {
+  if (!c) {
+    rcx::set_error("%s: context is NULL", fn);
+    return RC_ERR_INVALID_ARG;
+  }
+  return RC_OK;
+}
+
+// Grow the sphere/region device buffers and the pinned staging area.
+rc_status ensure_sphere_capacity(rc_context* c, int n) {
+  if (n <= c->sph_cap) return RC_OK;
+  int cap = std::max(64, c->sph_cap);
+  while (cap < n) cap *= 2;
+  for (int k = 0; k < 2; ++k)
+    if (c->stage_pending[k]) {
+      RC_CUDA(cudaEventSynchronize(c->ev_stage[k]), "staging wait");
+      c->stage_pending[k] = false;
+    }
+  if (c->d_sph) cudaFree(c->d_sph);
+  if (c->d_reg) cudaFree(c->d_reg);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  c->d_sph = nullptr;
+  c->d_reg = nullptr;
+  c->h_stage = nullptr;
+  c->sph_cap = 0;
+  rc_status s = dev_alloc((void**)&c->d_sph, sizeof(QSphere) * cap, "sphere buffer");
+  if (s != RC_OK) return s;
+  s = dev_alloc((void**)&c->d_reg, sizeof(Region) * (2 * cap + 1), "region buffer");
+  if (s != RC_OK) return s;
+  c->slot_bytes = sizeof(QSphere) * cap + sizeof(Region) * (2 * cap + 1);
+  RC_CUDA(cudaMallocHost(&c->h_stage, 2 * c->slot_bytes), "pinned staging buffer");
+  c->sph_cap = cap;
+  return RC_OK;
+}
+
+// Recompose the given regions of the volume from the base and the current
+// spheres.  regions == nullptr means the whole grid.
+rc_status recompose(rc_context* c, const Region* regions, int nreg) {
+  const int n = (int)c->cur.size();
+  rc_status s = ensure_sphere_capacity(c, std::max(n, 1));
+  if (s != RC_OK) return s;
+  // Alternate between two pinned slots; a slot is rewritten only after its
+  // previous copies (issued two updates ago) have completed.
+  const int k = c->slot;
+  c->slot ^= 1;
+  if (c->stage_pending[k]) {
+    RC_CUDA(cudaEventSynchronize(c->ev_stage[k]), "staging wait");
+    c->stage_pending[k] = false;
+  }
+  Region whole{0, c->W, 0, c->p.grid[1], 0, c->p.grid[2], {0, 0}};
+  if (!regions) {
+    regions = &whole;
+    nreg = 1;
+  }
+  if (nreg == 0) return RC_OK;
+  char* st = static_cast<char*>(c->h_stage) + k * c->slot_bytes;
+  if (n) memcpy(st, c->cur.data(), sizeof(QSphere) * n);
+  memcpy(st + sizeof(QSphere) * c->sph_cap, regions, sizeof(Region) * nreg);
+  RC_CUDA(cudaMemcpyAsync(c->d_sph, st, sizeof(QSphere) * n, cudaMemcpyHostToDevice, c->stream), "sphere upload");
+  RC_CUDA(cudaMemcpyAsync(c->d_reg, st + sizeof(QSphere) * c->sph_cap, sizeof(Region) * nreg,
+                          cudaMemcpyHostToDevice, c->stream),
+          "region upload");
+  RC_CUDA(cudaEventRecord(c->ev_stage[k], c->stream), "event record");
+  c->stage_pending[k] = true;
+  int64_t words = 0;
+  for (int i = 0; i < nreg; ++i)
+    words = std::max<int64_t>(words, (int64_t)(regions[i].w1 - regions[i].w0) * (regions[i].y1 - regions[i].y0) *
+                                         (regions[i].z1 - regions[i].z0));
+  const int threads = 256;
+  int64_t blocks = (words * 32 + threads - 1) / threads;
+  blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
+  k_compose<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
+      c->base, c->vol, c->occ, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg);
+  RC_CUDA(cudaGetLastError(), "compose launch");
+  return RC_OK;
+}
+
+template <typename T>
+void launch_level(const LevelArgs& a, int level, int nlev, cudaStream_t s) {
+  const int threads = 128;
+  dim3 grid((unsigned)((a.P + threads - 1) / threads), level == 0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
+  const bool top = (level == nlev - 1);
+  if (level == 0) {
+    if (top) k_level_scalar<T, true, true><<<grid, threads, 0, s>>>(a);
+    else k_level_scalar<T, true, false><<<grid, threads, 0, s>>>(a);
+  } else {
+    if (top) k_level_scalar<T, false, true><<<grid, threads, 0, s>>>(a);
+    else k_level_scalar<T, false, false><<<grid, threads, 0, s>>>(a);
+  }
+}
+
+void enqueue_solve(rc_context* c, cudaStream_t s) {
+  for (int i = c->nlev - 1; i >= 0; --i) {
+    if (c->elem == 2) launch_level<__half>(c->args[i], i, c->nlev, s);
+    else launch_level<float>(c->args[i], i, c->nlev, s);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
+  if (!out) {
+    rcx::set_error("rc_create: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  char msg[256];
+  if (!validate_params(p, msg, sizeof msg)) {
+    rcx::set_error("rc_create: invalid rc_params: %s", msg);
+    return RC_ERR_INVALID_ARG;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    (void)cudaGetLastError();
+    rcx::set_error("rc_create: no CUDA device available (%s)", e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+    return RC_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) {
+    rcx::set_error("rc_create: device %d out of range (have %d)", device, ndev);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard guard(device);
+  rc_context* c = new rc_context();
+  c->p = *p;
+  c->device = device;
+  c->nlev = p->num_cascades;
+  c->elem = p->precision == RC_PRECISION_FP16 ? 2 : 4;
+  level_geometry(*p, c->geom);
+  c->W = (p->grid[0] + 31) / 32;
+
+  // Direction tables (host), validated for the exact 32-bit walk.
+  std::vector<DirInfo> tab;
+  for (int i = 0; i < c->nlev; ++i) {
+    c->dir_off[i] = tab.size();
+    tab.resize(tab.size() + c->geom[i].ndirs);
+    if (!build_dir_table(c->geom[i], p->grid, tab.data() + c->dir_off[i], msg, sizeof msg)) {
+      rcx::set_error("rc_create: %s", msg);
+      delete c;
+      return RC_ERR_UNSUPPORTED;
+    }
+  }
+  {
+    std::vector<double> om((size_t)c->geom[0].ndirs);
+    rc_solid_angles(c->geom[0].n, om.data());
+    for (int d = 0; d < c->geom[0].ndirs; ++d) tab[c->dir_off[0] + d].omega = (float)om[d];
+  }
+
+  rc_status s = RC_OK;
+  auto fail = [&](rc_status st) {
+    release(c);
+    return st;
+  };
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "rc_create: stream"));
+  if ((e = cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_stage[0], cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_stage[1], cudaEventDisableTiming)) != cudaSuccess)
+    return fail(cuda_fail(e, "rc_create: events"));
+
+  const int64_t nvox = (int64_t)p->grid[0] * p->grid[1] * p->grid[2];
+  if ((s = dev_alloc((void**)&c->base, nvox * 8, "scene base volume")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&c->vol, nvox * 8, "scene volume")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&c->occ, (size_t)c->W * p->grid[1] * p->grid[2] * 4, "opacity bits")) != RC_OK)
+    return fail(s);
+  if ((s = dev_alloc((void**)&c->dirs, tab.size() * sizeof(DirInfo), "direction tables")) != RC_OK) return fail(s);
+  e = cudaMemcpy(c->dirs, tab.data(), tab.size() * sizeof(DirInfo), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "rc_create: table upload"));
+
+  size_t rad_bytes = 0, avg_bytes = 0;
+  for (int i = 0; i < c->nlev; ++i) {
+    const LevelGeom& g = c->geom[i];
+    c->rad_off[i] = rad_bytes;
+    rad_bytes += ((size_t)3 * g.ndirs * g.probes() * c->elem + 255) & ~(size_t)255;
+    c->avg_off[i] = avg_bytes;
+    if (i >= 1) avg_bytes += ((size_t)3 * c->geom[i - 1].ndirs * g.probes() * c->elem + 255) & ~(size_t)255;
+  }
+  if ((s = dev_alloc(&c->rad, rad_bytes, "cascade radiance")) != RC_OK) return fail(s);
+  if (avg_bytes && (s = dev_alloc(&c->avg, avg_bytes, "child-averaged radiance")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&c->fluence, (size_t)c->geom[0].probes() * 3 * sizeof(float), "fluence")) != RC_OK)
+    return fail(s);
+  if ((s = ensure_sphere_capacity(c, 64)) != RC_OK) return fail(s);
+
+  for (int i = 0; i < c->nlev; ++i) {
+    LevelArgs& a = c->args[i];
+    const LevelGeom& g = c->geom[i];
+    memset(&a, 0, sizeof a);
+    a.occ = c->occ;
+    a.vol = c->vol;
+    for (int ax = 0; ax < 3; ++ax) {
+      a.G[ax] = p->grid[ax];
+      a.M[ax] = g.M[ax];
+      a.UM[ax] = (i + 1 < c->nlev) ? c->geom[i + 1].M[ax] : 1;
+    }
+    a.W = c->W;
+    a.dirs = c->dirs + c->dir_off[i];
+    a.spacing = g.spacing;
+    a.n = g.n;
+    a.ndirs = g.ndirs;
+    a.P = g.probes();
+    a.L = static_cast<char*>(c->rad) + c->rad_off[i];
+    a.A_out = i >= 1 ? static_cast<char*>(c->avg) + c->avg_off[i] : nullptr;
+    a.A_up = (i + 1 < c->nlev) ? static_cast<char*>(c->avg) + c->avg_off[i + 1] : nullptr;
+    a.P_up = (i + 1 < c->nlev) ? c->geom[i + 1].probes() : 0;
+    a.fluence = c->fluence;
+  }
+  *out = c;
+  return RC_OK;
+}
+
+rc_status rc_destroy(rc_context* ctx) {
+  release(ctx);
+  return RC_OK;
+}
+
+rc_status rc_get_params(const rc_context* ctx, rc_params* out) {
+  if (check_ctx(ctx, "rc_get_params") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!out) {
+    rcx::set_error("rc_get_params: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = ctx->p;
+  return RC_OK;
+}
+
+rc_status rc_scene_upload(rc_context* c, const rc_voxel* voxels, int64_t count, int32_t where) {
+  if (check_ctx(c, "rc_scene_upload") != RC_OK) return RC_ERR_INVALID_ARG;
+  const int64_t nvox = (int64_t)c->p.grid[0] * c->p.grid[1] * c->p.grid[2];
+  if (!voxels || count != nvox || (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
+    rcx::set_error("rc_scene_upload: need %lld voxels and where = RC_MEM_HOST/RC_MEM_DEVICE", (long long)nvox);
+    return RC_ERR_INVALID_ARG;
+  }
+  if (fault_is("upload")) {
+    rcx::set_error("rc_scene_upload: injected upload failure (RC_FAULT=upload)");
+    return RC_ERR_CUDA;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaMemcpyAsync(c->base, voxels, nvox * 8,
+                          where == RC_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c->stream),
+          "rc_scene_upload: copy");
+  c->have_base = true;
+  rc_status s = recompose(c, nullptr, 0);
+  if (s != RC_OK) return s;
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_scene_upload: sync");
+  return RC_OK;
+}
+
+rc_status rc_scene_set_boxes(rc_context* c, const rc_box* boxes, int32_t n) {
+  if (check_ctx(c, "rc_scene_set_boxes") != RC_OK) return RC_ERR_INVALID_ARG;
+  // boxes are staged in shared memory: 1536 * 32 B = 48 KB
+  if (n < 0 || (n > 0 && !boxes) || n > 1536) {
+    rcx::set_error("rc_scene_set_boxes: need 0 <= n <= 1536 boxes and a non-NULL array");
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  rc_box* d_boxes = nullptr;
+  if (n) {
+    rc_status s = dev_alloc((void**)&d_boxes, sizeof(rc_box) * n, "box upload");
+    if (s != RC_OK) return s;
+    cudaError_t e = cudaMemcpy(d_boxes, boxes, sizeof(rc_box) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d_boxes);
+      return cuda_fail(e, "rc_scene_set_boxes: copy");
+    }
+  }
+  const int64_t nvox = (int64_t)c->p.grid[0] * c->p.grid[1] * c->p.grid[2];
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>((nvox + threads - 1) / threads, 152 * 32);
+  k_boxes_to_base<<<(unsigned)blocks, threads, sizeof(rc_box) * std::max(n, 1), c->stream>>>(
+      c->base, c->p.grid[0], c->p.grid[1], c->p.grid[2], d_boxes, n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (d_boxes) cudaFree(d_boxes);
+  if (e != cudaSuccess) return cuda_fail(e, "rc_scene_set_boxes: voxelise");
+  c->have_base = true;
+  rc_status s = recompose(c, nullptr, 0);
+  if (s != RC_OK) return s;
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_scene_set_boxes: sync");
+  return RC_OK;
+}
+
+rc_status rc_scene_set_spheres(rc_context* c, const rc_sphere* spheres, int32_t n) {
+  if (check_ctx(c, "rc_scene_set_spheres") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (n < 0 || (n > 0 && !spheres) || n > 65536) {
+    rcx::set_error("rc_scene_set_spheres: need 0 <= n <= 65536 and a non-NULL array");
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!c->have_base) {
+    rcx::set_error("rc_scene_set_spheres: upload a scene (rc_scene_upload / rc_scene_set_boxes) first");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  std::vector<QSphere> next(n);
+  for (int i = 0; i < n; ++i) quantise_sphere(spheres[i], &next[i]);
+  std::vector<Region> regs;
+  bool full = (int)c->cur.size() != n;
+  if (!full) {
+    for (int i = 0; i < n; ++i) {
+      Region r;
+      if (sphere_region(c->cur[i], c->p.grid, &r)) regs.push_back(r);
+      if (sphere_region(next[i], c->p.grid, &r)) regs.push_back(r);
+    }
+  }
+  c->cur.swap(next);
+  rc_status s = ensure_sphere_capacity(c, std::max(n, 1));
+  if (s != RC_OK) return s;
+  return full ? recompose(c, nullptr, 0) : recompose(c, regs.data(), (int)regs.size());
+}
+
+rc_status rc_solve(rc_context* c, void* stream) {
+  if (check_ctx(c, "rc_solve") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!c->have_base) {
+    rcx::set_error("rc_solve: no scene uploaded");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
+  if (s != c->stream) {
+    RC_CUDA(cudaEventRecord(c->ev_in, c->stream), "rc_solve: event");
+    RC_CUDA(cudaStreamWaitEvent(s, c->ev_in, 0), "rc_solve: wait");
+  }
+  enqueue_solve(c, s);
+  RC_CUDA(cudaGetLastError(), "rc_solve: launch");
+  if (s != c->stream) {
+    RC_CUDA(cudaEventRecord(c->ev_out, s), "rc_solve: event");
+    RC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0), "rc_solve: wait");
+  }
+  return RC_OK;
+}
+
+rc_status rc_synchronize(rc_context* c) {
+  if (check_ctx(c, "rc_synchronize") != RC_OK) return RC_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_synchronize");
+  return RC_OK;
+}
+
+static rc_status copy_out(rc_context* c, void* out, const void* src, size_t bytes, int32_t where, const char* fn) {
+  if (where != RC_MEM_HOST && where != RC_MEM_DEVICE) {
+    rcx::set_error("%s: where must be RC_MEM_HOST or RC_MEM_DEVICE", fn);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaMemcpyAsync(out, src, bytes, where == RC_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice,
+                          c->stream),
+          fn);
+  RC_CUDA(cudaStreamSynchronize(c->stream), fn);
+  return RC_OK;
+}
+
+rc_status rc_get_fluence(rc_context* c, float* out, int64_t elems, int32_t where) {
+  if (check_ctx(c, "rc_get_fluence") != RC_OK) return RC_ERR_INVALID_ARG;
+  const int64_t need = 3 * c->geom[0].probes();
+  if (!out || elems != need) {
+    rcx::set_error("rc_get_fluence: need a buffer of exactly %lld floats", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  return copy_out(c, out, c->fluence, need * sizeof(float), where, "rc_get_fluence");
+}
+
+rc_status rc_get_radiance(rc_context* c, int32_t level, void* out, int64_t bytes, int32_t where) {
+  if (check_ctx(c, "rc_get_radiance") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (level < 0 || level >= c->nlev) {
+    rcx::set_error("rc_get_radiance: level %d out of range", level);
+    return RC_ERR_INVALID_ARG;
+  }
+  const LevelGeom& g = c->geom[level];
+  const int64_t need = 3 * (int64_t)g.ndirs * g.probes() * (int64_t)c->elem;
+  if (!out || bytes != need) {
+    rcx::set_error("rc_get_radiance: need a buffer of exactly %lld bytes", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  return copy_out(c, out, static_cast<char*>(c->rad) + c->rad_off[level], need, where, "rc_get_radiance");
+}
+
+rc_status rc_fluence_device_ptr(rc_context* c, const float** out) {
+  if (check_ctx(c, "rc_fluence_device_ptr") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!out) {
+    rcx::set_error("rc_fluence_device_ptr: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = c->fluence;
+  return RC_OK;
+}
+
+rc_status rc_radiance_device_ptr(rc_context* c, int32_t level, const void** out) {
+  if (check_ctx(c, "rc_radiance_device_ptr") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!out || level < 0 || level >= c->nlev) {
+    rcx::set_error("rc_radiance_device_ptr: bad level or NULL out");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = static_cast<char*>(c->rad) + c->rad_off[level];
+  return RC_OK;
+}
+
+rc_status rc_get_stream(rc_context* c, void** out) {
+  if (check_ctx(c, "rc_get_stream") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!out) {
+    rcx::set_error("rc_get_stream: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = c->stream;
+  return RC_OK;
+}
+
+rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t count) {
+  if (check_ctx(c, "rc_profile_levels") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!ms_out || count != 1 + c->nlev || iters < 1) {
+    rcx::set_error("rc_profile_levels: need iters >= 1 and %d output floats", 1 + c->nlev);
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!c->have_base) {
+    rcx::set_error("rc_profile_levels: no scene uploaded");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  cudaEvent_t ev[kMaxCascades + 2];
+  for (int i = 0; i < c->nlev + 2; ++i) RC_CUDA(cudaEventCreate(&ev[i]), "rc_profile_levels: event");
+  double acc[kMaxCascades + 1] = {0};
+  rc_status st = RC_OK;
+  for (int it = 0; it < iters && st == RC_OK; ++it) {
+    cudaEventRecord(ev[0], c->stream);
+    st = recompose(c, nullptr, 0);
+    cudaEventRecord(ev[1], c->stream);
+    for (int i = c->nlev - 1, k = 2; i >= 0; --i, ++k) {
+      if (c->elem == 2) launch_level<__half>(c->args[i], i, c->nlev, c->stream);
+      else launch_level<float>(c->args[i], i, c->nlev, c->stream);
+      cudaEventRecord(ev[k], c->stream);
+    }
+    cudaError_t e = cudaEventSynchronize(ev[c->nlev + 1]);
+    if (e != cudaSuccess) {
+      st = cuda_fail(e, "rc_profile_levels");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    acc[0] += ms;
+    for (int i = c->nlev - 1, k = 2; i >= 0; --i, ++k) {
+      cudaEventElapsedTime(&ms, ev[k - 1], ev[k]);
+      acc[1 + i] += ms;
+    }
+  }
+  for (int i = 0; i < c->nlev + 2; ++i) cudaEventDestroy(ev[i]);
+  if (st != RC_OK) return st;
+  for (int i = 0; i <= c->nlev; ++i) ms_out[i] = (float)(acc[i] / iters);
+  return RC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,240 @@
+// rc_kernels.cuh -- device code of the radiance-cascade engine (sm_103a).
+//
+// Data layout in HBM (one scene):
+//   vol   rc_voxel[Gz][Gy][Gx]               8 B/voxel composed scene
+//   occ   uint32  [Gz][Gy][ceil(Gx/32)]      1 bit/voxel opacity, x fastest
+//   L_i   T       [3][dirs_i][Mz][My][Mx]     merged radiance of level i (T = f32 | f16)
+//   A_i   T       [3][dirs_{i-1}][Mz][My][Mx] L_i averaged over each 2x2 child-texel
+//                                             block; read by level i-1's merge
+//   flu   float   [Mz0][My0][Mx0][3]          cascade-0 fluence
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "rc_internal.h"
+
+namespace rcx {
+
+template <typename T>
+struct Store;
+template <>
+struct Store<float> {
+  static __device__ __forceinline__ float load(const float* p) { return __ldg(p); }
+  static __device__ __forceinline__ void store(float* p, float v) { *p = v; }
+};
+template <>
+struct Store<__half> {
+  static __device__ __forceinline__ float load(const __half* p) { return __half2float(__ldg(p)); }
+  static __device__ __forceinline__ void store(__half* p, float v) { *p = __float2half_rn(v); }
+};
+
+struct LevelArgs {
+  const uint32_t* occ;
+  const uint2* vol;
+  int32_t G[3];
+  int32_t W;           // occupancy words per x row
+  const DirInfo* dirs; // this level's table
+  int32_t M[3];        // probes per axis at this level
+  int32_t spacing;
+  int32_t n;           // direction resolution
+  int32_t ndirs;
+  int64_t P;           // probes at this level
+  void* L;             // out: merged radiance
+  void* A_out;         // out: child-averaged radiance (levels >= 1)
+  const void* A_up;    // in: next level's child-averaged radiance (not top)
+  int32_t UM[3];       // probes per axis at the next level
+  int64_t P_up;
+  float* fluence;      // out: level 0 only
+};
+
+__device__ __forceinline__ bool opaque_at(const uint32_t* __restrict__ occ, int W, int Gy, int x, int y, int z) {
+  return (__ldg(&occ[((int64_t)z * Gy + y) * W + (x >> 5)]) >> (x & 31)) & 1u;
+}
+
+// Exact integer voxel walk of one interval.  Returns the linear index of the
+// first opaque voxel entered inside the interval, or -1 when the ray leaves
+// the interval or the grid first.  (x, y, z) is the start voxel: the voxel at
+// the probe centre for level 0 (tested first), otherwise the last voxel
+// entered before the interval (not tested).
+__device__ __forceinline__ int64_t walk_interval(const uint32_t* __restrict__ occ, const int32_t G[3], int W,
+                                                 int x, int y, int z, const DirInfo& di, bool test_start) {
+  if (test_start && opaque_at(occ, W, G[1], x, y, z)) return ((int64_t)z * G[1] + y) * G[0] + x;
+  int tx = di.first_T[0], ty = di.first_T[1], tz = di.first_T[2];
+  const int sx = di.sgn[0], sy = di.sgn[1], sz = di.sgn[2];
+  const int dx = di.step_T[0], dy = di.step_T[1], dz = di.step_T[2];
+  for (int s = di.steps; s > 0; --s) {
+    if (tx <= ty && tx <= tz) {
+      x += sx;
+      tx += dx;
+    } else if (ty <= tz) {
+      y += sy;
+      ty += dy;
+    } else {
+      z += sz;
+      tz += dz;
+    }
+    if ((unsigned)x >= (unsigned)G[0] || (unsigned)y >= (unsigned)G[1] || (unsigned)z >= (unsigned)G[2]) return -1;
+    if (opaque_at(occ, W, G[1], x, y, z)) return ((int64_t)z * G[1] + y) * G[0] + x;
+  }
+  return -1;
+}
+
+__device__ __forceinline__ void voxel_emission(const uint2* __restrict__ vol, int64_t idx, float r[3]) {
+  const uint2 v = __ldg(&vol[idx]);
+  r[0] = __half2float(__ushort_as_half((unsigned short)(v.x & 0xFFFFu)));
+  r[1] = __half2float(__ushort_as_half((unsigned short)(v.x >> 16)));
+  r[2] = __half2float(__ushort_as_half((unsigned short)(v.y & 0xFFFFu)));
+}
+
+// One thread per probe.  Level 0 (L0) walks every direction and reduces the
+// fluence; other levels walk the four child directions of the parent texel
+// blockIdx.y and write their average for the level below.  Unless TOP, rays
+// that reach the end of their interval take the trilinear blend of the 8
+// nearest next-level probes (child index m sits at parent coordinate
+// m/2 - 1/4, clamped at the border) of the child-averaged radiance.
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(128) k_level_scalar(const LevelArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  const int mx = (int)(p % a.M[0]);
+  const int my = (int)((p / a.M[0]) % a.M[1]);
+  const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
+  const int h = a.spacing >> 1;
+  const int ox = mx * a.spacing + h, oy = my * a.spacing + h, oz = mz * a.spacing + h;
+
+  int64_t tap_off[8];
+  float tap_w[8];
+  if (!TOP) {
+    int q[3][2];
+    float w[3][2];
+    const int m[3] = {mx, my, mz};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const int lo = (m[ax] - 1) >> 1;
+      w[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
+      w[ax][1] = 1.0f - w[ax][0];
+      q[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
+      q[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int tx = t & 1, ty = (t >> 1) & 1, tz = t >> 2;
+      tap_off[t] = ((int64_t)q[2][tz] * a.UM[1] + q[1][ty]) * a.UM[0] + q[0][tx];
+      tap_w[t] = w[2][tz] * w[1][ty] * w[0][tx];
+    }
+  }
+
+  float acc[3] = {0.f, 0.f, 0.f};
+  const int nchild = L0 ? a.ndirs : 4;
+  const int hn = a.n >> 1;
+  const int dp = blockIdx.y;
+  for (int c = 0; c < nchild; ++c) {
+    int d;
+    if (L0) {
+      d = c;
+    } else {
+      const int jp = dp % hn, kp = dp / hn;
+      d = (2 * kp + (c >> 1)) * a.n + 2 * jp + (c & 1);
+    }
+    const DirInfo di = a.dirs[d];
+    const int64_t hit = walk_interval(a.occ, a.G, a.W, ox + di.start_off[0], oy + di.start_off[1],
+                                      oz + di.start_off[2], di, L0);
+    float r[3];
+    if (hit >= 0) {
+      voxel_emission(a.vol, hit, r);
+    } else if (TOP) {
+      r[0] = r[1] = r[2] = 0.f;
+    } else {
+      const T* Au = static_cast<const T*>(a.A_up);
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const T* base = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
+        float s = 0.f;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) s = fmaf(tap_w[t], Store<T>::load(base + tap_off[t]), s);
+        r[ch] = s;
+      }
+    }
+    T* L = static_cast<T*>(a.L);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, r[ch]);
+      acc[ch] = L0 ? fmaf(di.omega, r[ch], acc[ch]) : acc[ch] + r[ch];
+    }
+  }
+  if (L0) {
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
+  } else {
+    T* A = static_cast<T*>(a.A_out);
+    const int64_t npar = (int64_t)hn * hn;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
+  }
+}
+
+// Base volume from boxes: the last box containing a voxel wins.
+__global__ void k_boxes_to_base(uint2* __restrict__ base, int Gx, int Gy, int Gz, const rc_box* __restrict__ boxes,
+                                int nb) {
+  extern __shared__ rc_box sbox[];
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) sbox[i] = boxes[i];
+  __syncthreads();
+  const int64_t total = (int64_t)Gx * Gy * Gz;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(idx % Gx), y = (int)((idx / Gx) % Gy), z = (int)(idx / ((int64_t)Gx * Gy));
+    uint2 v = make_uint2(0u, 0u);
+    for (int b = nb - 1; b >= 0; --b) {
+      const rc_box& B = sbox[b];
+      if (x >= B.lo[0] && x < B.hi[0] && y >= B.lo[1] && y < B.hi[1] && z >= B.lo[2] && z < B.hi[2]) {
+        v.x = (uint32_t)B.value.emission[0] | ((uint32_t)B.value.emission[1] << 16);
+        v.y = (uint32_t)B.value.emission[2] | ((uint32_t)B.value.albedo_occ << 16);
+        break;
+      }
+    }
+    base[idx] = v;
+  }
+}
+
+// Composed volume and opacity bits over a list of regions: each voxel is the
+// base voxel overwritten by every sphere containing its centre (later spheres
+// win).  One warp per 32-voxel x-word; overlapping regions write identical
+// values.
+__global__ void k_compose(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ, int Gx,
+                          int Gy, int Gz, int W, const QSphere* __restrict__ sph, int ns,
+                          const Region* __restrict__ regs) {
+  const Region r = regs[blockIdx.y];
+  const int64_t nw = r.w1 - r.w0, ny = r.y1 - r.y0, nz = r.z1 - r.z0;
+  const int64_t words = nw * ny * nz;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp0; w < words; w += wstride) {
+    const int wx = r.w0 + (int)(w % nw);
+    const int y = r.y0 + (int)((w / nw) % ny);
+    const int z = r.z0 + (int)(w / (nw * ny));
+    const int x = wx * 32 + lane;
+    bool opaque = false;
+    if (x < Gx) {
+      const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
+      uint2 v = base[idx];
+      const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
+      for (int s = 0; s < ns; ++s) {
+        const QSphere& S = sph[s];
+        const int64_t dx = px - S.c[0], dy = py - S.c[1], dz = pz - S.c[2];
+        if (dx > S.r || -dx > S.r || dy > S.r || -dy > S.r || dz > S.r || -dz > S.r) continue;
+        if (dx * dx + dy * dy + dz * dz <= S.r * S.r) {
+          v.x = (uint32_t)S.value.emission[0] | ((uint32_t)S.value.emission[1] << 16);
+          v.y = (uint32_t)S.value.emission[2] | ((uint32_t)S.value.albedo_occ << 16);
+        }
+      }
+      vol[idx] = v;
+      opaque = (v.y >> 31) & 1u;
+    }
+    const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
+    if (lane == 0) occ[((int64_t)z * Gy + y) * W + wx] = bits;
+  }
+}
+
+}  // namespace rcx

@@ -1,0 +1,91 @@
+"""GPU tests of the C ABI's contract: error statuses, state checks, injected
+faults (host-side, no GPU fault), device-memory and external-stream paths."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import radiancecascade_gb300 as R
+from radiancecascade_gb300 import _ffi as F
+from oracle import oracle as O
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def test_state_and_argument_errors():
+    p = R.make_params(32, 4)
+    with R.Engine(p) as e:
+        L = F.lib()
+        assert L.rc_solve(e.handle, None) == F.RC_ERR_STATE
+        assert "scene" in F.last_error()
+        assert L.rc_scene_set_spheres(e.handle, None, 0) == F.RC_ERR_STATE
+        v = np.zeros(10, R.VOXEL_DT)
+        assert L.rc_scene_upload(e.handle, F.ptr(v), 10, F.RC_MEM_HOST) == F.RC_ERR_INVALID_ARG
+        e.set_boxes(np.zeros(0, R.BOX_DT))
+        e.solve()
+        out = np.zeros(5, np.float32)
+        assert L.rc_get_fluence(e.handle, F.ptr(out), 5, F.RC_MEM_HOST) == F.RC_ERR_INVALID_ARG
+        assert L.rc_get_radiance(e.handle, 9, F.ptr(out), 20, F.RC_MEM_HOST) == F.RC_ERR_INVALID_ARG
+        assert L.rc_get_fluence(e.handle, F.ptr(out), 5, 7) == F.RC_ERR_INVALID_ARG
+        # the context is still usable after the errors
+        e.solve()
+        assert not e.fluence().any()
+    h = C.c_void_p()
+    assert F.lib().rc_create(C.byref(p), 99, C.byref(h)) == F.RC_ERR_INVALID_ARG
+
+
+def test_injected_allocation_and_upload_faults(monkeypatch):
+    p = R.make_params(32, 4)
+    monkeypatch.setenv("RC_FAULT", "alloc")
+    with pytest.raises(R.RCError) as ex:
+        R.Engine(p)
+    assert ex.value.status == F.RC_ERR_OOM
+    monkeypatch.setenv("RC_FAULT", "upload")
+    monkeypatch.delenv("RC_FAULT")
+    e = R.Engine(p)
+    monkeypatch.setenv("RC_FAULT", "upload")
+    with pytest.raises(R.RCError) as ex:
+        e.upload(np.zeros(32 ** 3, R.VOXEL_DT))
+    assert ex.value.status == F.RC_ERR_CUDA
+    monkeypatch.delenv("RC_FAULT")
+    e.upload(np.zeros(32 ** 3, R.VOXEL_DT))
+    e.solve()
+    assert not e.fluence().any()
+    e.close()
+
+
+def test_device_upload_external_stream_and_device_outputs():
+    torch = pytest.importorskip("torch")
+    boxes, spheres = R.workload_scene("c64")
+    vox = R.voxelise_host(64, boxes, spheres)
+    dev = torch.from_numpy(vox.view(np.uint16).reshape(-1, 4).copy()).cuda()
+    p = R.make_params(64, 5)
+    with R.Engine(p) as e:
+        e.upload_device(dev.data_ptr(), vox.size)
+        s = torch.cuda.Stream()
+        e.solve(stream=s.cuda_stream)
+        s.synchronize()
+        host = e.fluence()
+        n = host.size
+        out = torch.empty(n, dtype=torch.float32, device="cuda")
+        assert F.lib().rc_get_fluence(e.handle, C.c_void_p(out.data_ptr()), n, F.RC_MEM_DEVICE) == F.RC_OK
+        assert np.array_equal(out.cpu().numpy().reshape(-1, 3), host)
+        assert e.fluence_device_ptr() != 0 and e.radiance_device_ptr(2) != 0
+    oflu, _ = O.solve(O.params(64, 5), vox)
+    assert rel_l2(host, oflu) <= 1e-4
+
+
+def test_gi_stage_render_stage_cycle():
+    """update -> render -> read, then resize to another shape (RenderStage call order)."""
+    boxes, spheres = R.workload_scene("c64")
+    stage = R.GiStage(R.make_params(64, 5), boxes=boxes)
+    got = []
+    for f in R.frames(stage, spheres, 64, 3):
+        got.append(stage.fluence().copy())
+    assert len(got) == 3 and not np.array_equal(got[0], got[2])
+    stage.resize(R.make_params(64, 4))
+    stage.update(R.GiState(spheres=spheres))
+    stage.render()
+    assert stage.fluence().shape == (32 ** 3, 3)
+    stage.close()

@@ -1,0 +1,166 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle.
+
+Tolerances (fluence and every level's merged radiance, against FP64):
+  FP32 path: relative L2 <= 1e-4 (the bar), and since every voxel decision is
+             exact integer arithmetic, max relative error per value <= 1e-5;
+  FP16 path: relative L2 <= 1e-2.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import radiancecascade_gb300 as R
+from oracle import oracle as O
+from tests.helpers import mirror_x, rel_l2, volume
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+FP32_REL_L2 = 1e-4
+FP32_MAX_REL = 1e-5
+FP16_REL_L2 = 1e-2
+
+
+def _solve_gpu(params, vox=None, boxes=None, spheres=None):
+    with R.Engine(params) as e:
+        if vox is not None:
+            e.upload(vox)
+        else:
+            e.set_boxes(boxes)
+            e.set_spheres(spheres)
+        e.solve()
+        e.synchronize()
+        return e.fluence().astype(np.float64), [e.radiance(i).astype(np.float64)
+                                                for i in range(params.num_cascades)]
+
+
+def _check(gflu, gL, oflu, oL, rel=FP32_REL_L2, max_rel=FP32_MAX_REL):
+    assert rel_l2(gflu, oflu) <= rel, rel_l2(gflu, oflu)
+    for g, o in zip(gL, oL):
+        assert g.shape == o.shape
+        assert rel_l2(g, o) <= rel
+        if max_rel is not None:
+            assert np.abs(g - o).max() <= max_rel * max(1.0, np.abs(o).max())
+
+
+@pytest.mark.parametrize("frame", [0, 37])
+def test_c64_fp32_matches_fp64_oracle(frame):
+    boxes, spheres = R.workload_scene("c64", frame=frame)
+    vox = O.voxelise(64, boxes, spheres)
+    oflu, oL = O.solve(O.params(64, 5), vox)
+    gflu, gL = _solve_gpu(R.make_params(64, 5), boxes=boxes, spheres=spheres)
+    _check(gflu, gL, oflu, oL)
+
+
+def test_c64_fp16_storage_within_one_percent():
+    boxes, spheres = R.workload_scene("c64")
+    vox = O.voxelise(64, boxes, spheres)
+    oflu, oL = O.solve(O.params(64, 5), vox)
+    gflu, gL = _solve_gpu(R.make_params(64, 5, precision="fp16"), boxes=boxes, spheres=spheres)
+    err = rel_l2(gflu, oflu)
+    assert err <= FP16_REL_L2
+    _check(gflu, gL, oflu, oL, rel=FP16_REL_L2, max_rel=None)
+
+
+@pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
+def test_golden_fixtures(name):
+    z = np.load(os.path.join(GOLDEN, name))
+    grid = tuple(int(x) for x in z["grid"])
+    N = int(z["num_cascades"])
+    gflu, gL = _solve_gpu(R.make_params(grid, N), vox=z["voxels"].view(R.VOXEL_DT).reshape(-1))
+    _check(gflu, gL, z["fluence"], [z["radiance_%d" % i] for i in range(N)])
+
+
+@pytest.mark.parametrize("grid,N,kw", [
+    ((32, 16, 48), 3, {}),
+    ((32, 32, 32), 2, dict(spacing0=4, dir_res0=2, interval0=2, ratio=3)),
+    ((48, 48, 48), 4, {}),
+])
+def test_other_shapes_match_oracle(grid, N, kw):
+    spec = R.scene_spec(grid, 12, (3, 12), 3, (1.5, 4.0), (1.0, 20.0))
+    boxes, spheres = R.generate_scene(spec, 77)
+    vox = O.voxelise(grid, boxes, spheres)
+    oflu, oL = O.solve(O.params(grid, N, **kw), vox)
+    gflu, gL = _solve_gpu(R.make_params(grid, N, **kw), vox=vox)
+    _check(gflu, gL, oflu, oL)
+
+
+def test_moving_emitters_incremental_update_matches_fresh_solve():
+    boxes, spheres = R.workload_scene("c64")
+    p = R.make_params(64, 5)
+    checks = {0, 1, 9, 40}
+    with R.Engine(p) as e:
+        e.set_boxes(boxes)
+        sph = spheres.copy()
+        for f in range(41):
+            e.set_spheres(sph)
+            if f in checks:
+                e.solve()
+                gflu = e.fluence().astype(np.float64)
+                ob, os_ = O.config_scene("c64", frame=f)
+                oflu, _ = O.solve(O.params(64, 5), O.voxelise(64, ob, os_))
+                assert rel_l2(gflu, oflu) <= FP32_REL_L2
+                assert np.abs(gflu - oflu).max() <= FP32_MAX_REL * oflu.max()
+            R.advance_spheres(sph, 64, 1)
+
+
+def test_empty_scene_is_dark():
+    gflu, gL = _solve_gpu(R.make_params(32, 4), vox=volume(np.zeros((32, 32, 32), bool), 0))
+    assert not gflu.any() and all(not x.any() for x in gL)
+
+
+def test_furnace_all_emitting():
+    gflu, _ = _solve_gpu(R.make_params(32, 4), vox=volume(np.ones((32, 32, 32), bool), O.float_to_half(3.0)))
+    assert np.abs(gflu - 4 * math.pi * 3.0).max() <= 1e-5 * 4 * math.pi * 3.0
+
+
+def test_furnace_cavity_and_slab_single_cascade():
+    occ = np.ones((32, 32, 32), bool)
+    occ[8:24, 8:24, 8:24] = False
+    gflu, _ = _solve_gpu(R.make_params(32, 1, interval0=64), vox=volume(occ, O.float_to_half(5.0)))
+    assert np.abs(gflu - 4 * math.pi * 5.0).max() <= 1e-5 * 4 * math.pi * 5.0
+
+    occ = np.zeros((32, 32, 32), bool)
+    occ[:, :, 0:3] = True
+    em = np.where(occ, O.float_to_half(3.0), 0).astype(np.uint16)
+    occ[:, :, 10:12] = True
+    gflu, _ = _solve_gpu(R.make_params(32, 1, interval0=64), vox=volume(occ, em))
+    f = gflu.reshape(16, 16, 16, 3)
+    assert f[:, :, 6:, :].max() == 0.0 and f[:, :, 2:5, :].min() > 0.0
+
+
+def test_mirror_symmetry_on_gpu():
+    spec = R.scene_spec(32, 10, (3, 10), 3, (1.5, 3.5), (1.0, 20.0))
+    boxes, spheres = R.generate_scene(spec, 5)
+    vox = R.voxelise_host(32, boxes, spheres)
+    p = R.make_params(32, 4)
+    f, _ = _solve_gpu(p, vox=vox)
+    mf, _ = _solve_gpu(p, vox=mirror_x(vox, 32))
+    mf = mf.reshape(16, 16, 16, 3)[:, :, ::-1].reshape(-1, 3)
+    assert np.abs(f - mf).max() <= 1e-5 * f.max()
+
+
+def test_c256_frame0_matches_fp64_oracle():
+    boxes, spheres = R.workload_scene("c256")
+    vox = O.voxelise(256, boxes, spheres)
+    gflu, gL = _solve_gpu(R.make_params(256, 6), boxes=boxes, spheres=spheres)
+    oflu, oL = O.solve(O.params(256, 6), vox, jump=True)
+    _check(gflu, gL, oflu, oL)
+
+
+def test_c256_size_independent_properties():
+    """Full size: energy bounds, furnace and FP16 error."""
+    boxes, spheres = R.workload_scene("c256", frame=120)
+    p = R.make_params(256, 6)
+    gflu, _ = _solve_gpu(p, boxes=boxes, spheres=spheres)
+    emax = float(np.max(spheres["value"]["emission"].view(np.float16).astype(np.float64)))
+    assert gflu.min() >= 0.0 and gflu.max() <= 4 * math.pi * emax * (1 + 1e-6)
+    h, _ = _solve_gpu(R.make_params(256, 6, precision="fp16"), boxes=boxes, spheres=spheres)
+    assert rel_l2(h, gflu) <= FP16_REL_L2
+    full = np.zeros(1, R.BOX_DT)
+    full[0]["lo"], full[0]["hi"] = (0, 0, 0), (256, 256, 256)
+    full[0]["value"]["albedo_occ"] = 0x8000
+    full[0]["value"]["emission"] = [O.float_to_half(2.0)] * 3
+    ff, _ = _solve_gpu(p, boxes=full, spheres=np.zeros(0, R.SPHERE_DT))
+    assert np.abs(ff - 4 * math.pi * 2.0).max() <= 1e-5 * 8 * math.pi
