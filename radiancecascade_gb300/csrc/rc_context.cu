@@ -15,6 +15,7 @@
 
 #include "rc_internal.h"
 #include "rc_kernels.cuh"
+#include "rc_walk_bits.cuh"
 
 using namespace rcx;
 
@@ -34,6 +35,9 @@ struct rc_context {
   uint2* vol = nullptr;      // composed volume
   uint32_t* occ = nullptr;   // opacity bits
   int W = 0;                 // words per x row
+  uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
+  MaskSet mset{};
+  bool bits_level[kMaxCascades]{};
   DirInfo* dirs = nullptr;   // all levels, concatenated
   size_t dir_off[kMaxCascades]{};
   void* rad = nullptr;       // L_i for all levels
@@ -94,7 +98,7 @@ void release(rc_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->base, c->vol, c->occ, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  void* bufs[] = {c->base, c->vol, c->occ, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -189,31 +193,55 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
   const int threads = 256;
   int64_t blocks = (words * 32 + threads - 1) / threads;
   blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
-  k_compose<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
-      c->base, c->vol, c->occ, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg);
+  k_compose_masks<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
+      c->base, c->vol, c->occ, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg, c->mset);
   RC_CUDA(cudaGetLastError(), "compose launch");
   return RC_OK;
 }
 
-template <typename T>
-void launch_level(const LevelArgs& a, int level, int nlev, cudaStream_t s) {
-  const int threads = 128;
-  dim3 grid((unsigned)((a.P + threads - 1) / threads), level == 0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
-  const bool top = (level == nlev - 1);
-  if (level == 0) {
-    if (top) k_level_scalar<T, true, true><<<grid, threads, 0, s>>>(a);
-    else k_level_scalar<T, true, false><<<grid, threads, 0, s>>>(a);
+template <typename T, bool L0, bool TOP>
+void launch_one(const LevelArgs& a, bool bits, cudaStream_t s) {
+  if (bits) {
+    const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 4);
+    const unsigned blocks = (unsigned)a.XW * (unsigned)a.rowblocks * groups;
+    k_level_bits<T, L0, TOP><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
   } else {
-    if (top) k_level_scalar<T, false, true><<<grid, threads, 0, s>>>(a);
-    else k_level_scalar<T, false, false><<<grid, threads, 0, s>>>(a);
+    const int threads = 128;
+    dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
+    k_level_scalar<T, L0, TOP><<<grid, threads, 0, s>>>(a);
+  }
+}
+
+template <typename T>
+void launch_level(const rc_context* c, int level, cudaStream_t s) {
+  const LevelArgs& a = c->args[level];
+  const bool bits = c->bits_level[level];
+  const bool top = (level == c->nlev - 1);
+  if (level == 0) {
+    if (top) launch_one<T, true, true>(a, bits, s);
+    else launch_one<T, true, false>(a, bits, s);
+  } else {
+    if (top) launch_one<T, false, true>(a, bits, s);
+    else launch_one<T, false, false>(a, bits, s);
   }
 }
 
 void enqueue_solve(rc_context* c, cudaStream_t s) {
   for (int i = c->nlev - 1; i >= 0; --i) {
-    if (c->elem == 2) launch_level<__half>(c->args[i], i, c->nlev, s);
-    else launch_level<float>(c->args[i], i, c->nlev, s);
+    if (c->elem == 2) launch_level<__half>(c, i, s);
+    else launch_level<float>(c, i, s);
   }
+}
+
+template <typename T>
+cudaError_t allow_bits_smem() {
+  cudaError_t e = cudaSuccess;
+  const int sm = (int)kBitsSmem;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  return e;
 }
 
 }  // namespace
@@ -286,6 +314,38 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
   if ((s = dev_alloc((void**)&c->vol, nvox * 8, "scene volume")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&c->occ, (size_t)c->W * p->grid[1] * p->grid[2] * 4, "opacity bits")) != RC_OK)
     return fail(s);
+  {
+    // Decimated opacity per level.  A level walks bit-parallel unless the
+    // 32-bit row padding would make its mask more than 8x the full-resolution
+    // bitmask (few probes per row); such a level uses the scalar walk.
+    const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
+    const int64_t full_words = (int64_t)c->W * p->grid[1] * p->grid[2];
+    int64_t total = 0;
+    int64_t off[kMaxCascades];
+    c->mset.n = 0;
+    for (int i = 0; i < c->nlev; ++i) {
+      const LevelGeom& g = c->geom[i];
+      const int64_t xw = (g.M[0] + 31) / 32;
+      const int64_t words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * xw * g.M[1];
+      c->bits_level[i] = !force_scalar && words <= 8 * full_words;
+      off[i] = total;
+      if (c->bits_level[i]) total += (words + 63) & ~(int64_t)63;
+    }
+    if (total && (s = dev_alloc((void**)&c->masks, total * 4, "decimated opacity")) != RC_OK) return fail(s);
+    if (total && (e = cudaMemset(c->masks, 0, total * 4)) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
+    for (int i = 0; i < c->nlev; ++i) {
+      if (!c->bits_level[i]) continue;
+      MaskLevel& m = c->mset.lv[c->mset.n++];
+      const LevelGeom& g = c->geom[i];
+      m.base = c->masks + off[i];
+      m.l2s = 0;
+      while ((1 << m.l2s) < g.spacing) ++m.l2s;
+      for (int a = 0; a < 3; ++a) m.M[a] = g.M[a];
+      m.XW = (g.M[0] + 31) / 32;
+    }
+    if ((e = allow_bits_smem<float>()) != cudaSuccess || (e = allow_bits_smem<__half>()) != cudaSuccess)
+      return fail(cuda_fail(e, "rc_create: shared memory attribute"));
+  }
   if ((s = dev_alloc((void**)&c->dirs, tab.size() * sizeof(DirInfo), "direction tables")) != RC_OK) return fail(s);
   e = cudaMemcpy(c->dirs, tab.data(), tab.size() * sizeof(DirInfo), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return fail(cuda_fail(e, "rc_create: table upload"));
@@ -308,6 +368,13 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     LevelArgs& a = c->args[i];
     const LevelGeom& g = c->geom[i];
     memset(&a, 0, sizeof a);
+    for (int k = 0; k < c->mset.n; ++k)
+      if (c->mset.lv[k].M[0] == g.M[0] && c->mset.lv[k].M[1] == g.M[1] && (1 << c->mset.lv[k].l2s) == g.spacing)
+        a.mask = c->mset.lv[k].base;
+    a.l2s = 0;
+    while ((1 << a.l2s) < g.spacing) ++a.l2s;
+    a.XW = (g.M[0] + 31) / 32;
+    a.rowblocks = (g.M[1] * g.M[2] + kTileRows - 1) / kTileRows;
     a.occ = c->occ;
     a.vol = c->vol;
     for (int ax = 0; ax < 3; ++ax) {
@@ -546,8 +613,8 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
     st = recompose(c, nullptr, 0);
     cudaEventRecord(ev[1], c->stream);
     for (int i = c->nlev - 1, k = 2; i >= 0; --i, ++k) {
-      if (c->elem == 2) launch_level<__half>(c->args[i], i, c->nlev, c->stream);
-      else launch_level<float>(c->args[i], i, c->nlev, c->stream);
+      if (c->elem == 2) launch_level<__half>(c, i, c->stream);
+      else launch_level<float>(c, i, c->stream);
       cudaEventRecord(ev[k], c->stream);
     }
     cudaError_t e = cudaEventSynchronize(ev[c->nlev + 1]);

@@ -30,6 +30,10 @@ struct Store<__half> {
 };
 
 struct LevelArgs {
+  const uint32_t* mask;  // this level's decimated opacity words (bit-parallel walk)
+  int32_t l2s;           // log2(spacing)
+  int32_t XW;            // mask words per coarse x row: ceil(M[0] / 32)
+  int32_t rowblocks;     // ceil(M[1] * M[2] / 32)
   const uint32_t* occ;
   const uint2* vol;
   int32_t G[3];

@@ -44,8 +44,18 @@ def _check(gflu, gL, oflu, oL, rel=FP32_REL_L2, max_rel=FP32_MAX_REL):
             assert np.abs(g - o).max() <= max_rel * max(1.0, np.abs(o).max())
 
 
+@pytest.fixture(params=["bits", "scalar"])
+def walk(request, monkeypatch):
+    """Runs a test with the bit-parallel walk (default) and with the scalar walk."""
+    if request.param == "scalar":
+        monkeypatch.setenv("RC_WALK", "scalar")
+    else:
+        monkeypatch.delenv("RC_WALK", raising=False)
+    return request.param
+
+
 @pytest.mark.parametrize("frame", [0, 37])
-def test_c64_fp32_matches_fp64_oracle(frame):
+def test_c64_fp32_matches_fp64_oracle(frame, walk):
     boxes, spheres = R.workload_scene("c64", frame=frame)
     vox = O.voxelise(64, boxes, spheres)
     oflu, oL = O.solve(O.params(64, 5), vox)
@@ -53,7 +63,7 @@ def test_c64_fp32_matches_fp64_oracle(frame):
     _check(gflu, gL, oflu, oL)
 
 
-def test_c64_fp16_storage_within_one_percent():
+def test_c64_fp16_storage_within_one_percent(walk):
     boxes, spheres = R.workload_scene("c64")
     vox = O.voxelise(64, boxes, spheres)
     oflu, oL = O.solve(O.params(64, 5), vox)
@@ -64,7 +74,7 @@ def test_c64_fp16_storage_within_one_percent():
 
 
 @pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
-def test_golden_fixtures(name):
+def test_golden_fixtures(name, walk):
     z = np.load(os.path.join(GOLDEN, name))
     grid = tuple(int(x) for x in z["grid"])
     N = int(z["num_cascades"])
@@ -77,7 +87,7 @@ def test_golden_fixtures(name):
     ((32, 32, 32), 2, dict(spacing0=4, dir_res0=2, interval0=2, ratio=3)),
     ((48, 48, 48), 4, {}),
 ])
-def test_other_shapes_match_oracle(grid, N, kw):
+def test_other_shapes_match_oracle(grid, N, kw, walk):
     spec = R.scene_spec(grid, 12, (3, 12), 3, (1.5, 4.0), (1.0, 20.0))
     boxes, spheres = R.generate_scene(spec, 77)
     vox = O.voxelise(grid, boxes, spheres)
@@ -141,7 +151,7 @@ def test_mirror_symmetry_on_gpu():
     assert np.abs(f - mf).max() <= 1e-5 * f.max()
 
 
-def test_c256_frame0_matches_fp64_oracle():
+def test_c256_frame0_matches_fp64_oracle(walk):
     boxes, spheres = R.workload_scene("c256")
     vox = O.voxelise(256, boxes, spheres)
     gflu, gL = _solve_gpu(R.make_params(256, 6), boxes=boxes, spheres=spheres)
