@@ -291,7 +291,7 @@ def main():
                      "algorithmic_bytes_per_frame": B,
                      "level_ms_per_frame": round(level_ms, 4),
                      "per_level_ms": [round(float(x), 4) for x in per_level_ms[1:]],
-                     "compose_full_ms": round(float(per_level_ms[0]), 4)},
+                     "compose_ms": round(float(per_level_ms[0]), 4)},
     }
     if clock_info:
         line["clocks"] = clock_info

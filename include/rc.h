@@ -194,10 +194,11 @@ rc_status rc_radiance_device_ptr(rc_context* ctx, int32_t level,
 rc_status rc_get_stream(rc_context* ctx, void** out);
 
 /* ---- profiling ------------------------------------------------------ */
-/* Runs `iters` solves on the context stream with CUDA events around every
+/* Runs `iters` frames on the context stream with CUDA events around every
  * kernel and writes the mean milliseconds per launch: ms_out[0] = scene
- * composition (full rebuild), ms_out[1 + i] = cascade level i.  Needs
- * 1 + num_cascades floats.  Synchronises. */
+ * recomposition under the current spheres (the per-frame emitter update),
+ * ms_out[1 + i] = cascade level i.  Needs 1 + num_cascades floats.
+ * Synchronises. */
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
 

@@ -609,8 +609,14 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
   double acc[kMaxCascades + 1] = {0};
   rc_status st = RC_OK;
   for (int it = 0; it < iters && st == RC_OK; ++it) {
+    // a per-frame update: the current spheres' footprints are recomposed
+    std::vector<Region> regs;
+    for (const QSphere& q : c->cur) {
+      Region r;
+      if (sphere_region(q, c->p.grid, &r)) regs.push_back(r);
+    }
     cudaEventRecord(ev[0], c->stream);
-    st = recompose(c, nullptr, 0);
+    if (!regs.empty()) st = recompose(c, regs.data(), (int)regs.size());
     cudaEventRecord(ev[1], c->stream);
     for (int i = c->nlev - 1, k = 2; i >= 0; --i, ++k) {
       if (c->elem == 2) launch_level<__half>(c, i, c->stream);
