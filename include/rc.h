@@ -202,6 +202,39 @@ rc_status rc_get_stream(rc_context* ctx, void** out);
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
 
+/* ---- allocation-free solve ------------------------------------------ */
+/* No counterpart in the reference.
+ *
+ * Solves one frame of a static scene into buffers the caller owns, without
+ * allocating any memory.  It exists for callers that cannot call cudaMalloc:
+ * a renderer that reserves its whole device-memory budget at start-up and
+ * forbids growth inside the frame loop (a cudaMalloc can also synchronise the
+ * device and stall the frame), or a plugin host that hands each stage fixed
+ * buffers and owns every allocation itself.
+ *
+ *   voxels    device pointer, grid[0]*grid[1]*grid[2] rc_voxel (x fastest)
+ *   fluence   device pointer, rc_fluence_elems(p) floats (RGB interleaved)
+ *   radiance  device pointer, every level's merged radiance back to back in
+ *             level order, each laid out as rc_get_radiance describes
+ *             (sum of rc_level_info.radiance_bytes)
+ *   stream    cudaStream_t or NULL (legacy default stream)
+ *
+ * Its working memory (opacity bits, the per-level decimated opacity, the
+ * child-averaged radiance and the walk tables) lives in one statically sized
+ * device array of RC_NOALLOC_SCRATCH_BYTES (8 MiB, enough for grids up to 64^3
+ * with the default cascade shape) that every GPU loading the library holds
+ * until the process exits.  Parameters that need more return
+ * RC_ERR_UNSUPPORTED with the required size in rc_last_error().
+ *
+ * The first call on a device looks up that array's device address (set-up
+ * done once per device), so make the first call before any stream capture.
+ * All calls share the array: calls whose GPU work overlaps (different
+ * streams, or other host threads) race on it and must be serialised by the
+ * caller.  The call is asynchronous on `stream`. */
+#define RC_NOALLOC_SCRATCH_BYTES (8u << 20)
+rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels,
+                           float* fluence, void* radiance, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

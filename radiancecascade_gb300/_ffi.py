@@ -74,6 +74,7 @@ SIGNATURES = {
     "rc_radiance_device_ptr": (_S, [_P, C.c_int32, C.POINTER(C.c_void_p)]),
     "rc_get_stream": (_S, [_P, C.POINTER(C.c_void_p)]),
     "rc_profile_levels": (_S, [_P, C.c_int32, _P, C.c_int32]),
+    "rc_solve_noalloc": (_S, [_P, _P, _P, _P, _P]),
 }
 
 _lib = None

@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "rc_internal.h"
@@ -643,3 +644,187 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// rc_solve_noalloc: the same kernels as rc_solve, with every piece of working
+// memory carved out of one file-scope device array instead of cudaMalloc.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Working memory shared by every rc_solve_noalloc call in the process.
+__device__ __align__(256) unsigned char g_noalloc_scratch[RC_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_scratch_ptr[kNoallocMaxDevices] = {};
+
+// Host staging of the walk tables.  A pageable cudaMemcpyAsync has copied
+// its source by the time it returns, so one static buffer serves all calls.
+constexpr size_t kNoallocMaxDirs = RC_NOALLOC_SCRATCH_BYTES / sizeof(DirInfo);
+DirInfo g_noalloc_tab[kNoallocMaxDirs];
+double g_noalloc_omega[kNoallocMaxDirs];
+
+// Opacity bits and decimated opacity of a caller-owned volume (the volume is
+// only read).
+__global__ void k_masks_from_volume(const uint2* __restrict__ vol, uint32_t* __restrict__ occ, int Gx, int Gy,
+                                    int Gz, int W, const MaskSet ms) {
+  const int64_t words = (int64_t)W * Gy * Gz;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w = warp0; w < words; w += wstride) {
+    const int wx = (int)(w % W);
+    const int y = (int)((w / W) % Gy);
+    const int z = (int)(w / ((int64_t)W * Gy));
+    const int x = wx * 32 + lane;
+    const bool opaque = x < Gx && ((__ldg(&vol[((int64_t)z * Gy + y) * Gx + x]).y >> 31) & 1u);
+    const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
+    if (lane == 0) occ[((int64_t)z * Gy + y) * W + wx] = bits;
+    update_masks(ms, lane, wx, x, y, z, Gx, bits);
+  }
+}
+
+size_t carve(size_t& off, size_t bytes) {
+  const size_t at = off;
+  off = (off + bytes + 255) & ~(size_t)255;
+  return at;
+}
+
+}  // namespace
+
+extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels, float* fluence, void* radiance,
+                                      void* stream) {
+  char msg[256];
+  if (!validate_params(p, msg, sizeof msg)) {
+    rcx::set_error("rc_solve_noalloc: invalid rc_params: %s", msg);
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!voxels || !fluence || !radiance) {
+    rcx::set_error("rc_solve_noalloc: voxels, fluence and radiance must be device pointers, not NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  int dev = 0;
+  RC_CUDA(cudaGetDevice(&dev), "rc_solve_noalloc: current device");
+  if (dev < 0 || dev >= kNoallocMaxDevices) {
+    rcx::set_error("rc_solve_noalloc: device %d beyond the %d supported", dev, kNoallocMaxDevices);
+    return RC_ERR_UNSUPPORTED;
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+  // A context view that owns nothing: geometry and launch arguments only.
+  rc_context v;
+  v.p = *p;
+  v.device = dev;
+  v.nlev = p->num_cascades;
+  v.elem = p->precision == RC_PRECISION_FP16 ? 2 : 4;
+  level_geometry(*p, v.geom);
+  v.W = (p->grid[0] + 31) / 32;
+
+  // Scratch layout, checked against the static maximum before any GPU work.
+  const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
+  const int64_t full_words = (int64_t)v.W * p->grid[1] * p->grid[2];
+  size_t off = 0;
+  const size_t occ_off = carve(off, (size_t)full_words * 4);
+  size_t mask_off[kMaxCascades] = {}, mask_bytes = 0, mask_begin = off;
+  for (int i = 0; i < v.nlev; ++i) {
+    const LevelGeom& g = v.geom[i];
+    const int64_t xw = (g.M[0] + 31) / 32;
+    const int64_t words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * xw * g.M[1];
+    v.bits_level[i] = !force_scalar && words <= 8 * full_words;
+    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)words * 4);
+  }
+  mask_bytes = off - mask_begin;
+  size_t avg_off[kMaxCascades] = {};
+  for (int i = 1; i < v.nlev; ++i)
+    avg_off[i] = carve(off, (size_t)3 * v.geom[i - 1].ndirs * v.geom[i].probes() * v.elem);
+  size_t ndirs_total = 0;
+  for (int i = 0; i < v.nlev; ++i) ndirs_total += (size_t)v.geom[i].ndirs;
+  const size_t dirs_off = carve(off, ndirs_total * sizeof(DirInfo));
+  if (off > RC_NOALLOC_SCRATCH_BYTES || ndirs_total > kNoallocMaxDirs) {
+    rcx::set_error("rc_solve_noalloc: these parameters need %zu bytes of scratch; the static maximum is %u bytes",
+                   off, (unsigned)RC_NOALLOC_SCRATCH_BYTES);
+    return RC_ERR_UNSUPPORTED;
+  }
+
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  // Once per device, with that device current: the array's device address
+  // and the shared-memory opt-in of the bit-parallel kernel.
+  if (!g_noalloc_scratch_ptr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "rc_solve_noalloc: scratch address");
+    if ((e = allow_bits_smem<float>()) != cudaSuccess || (e = allow_bits_smem<__half>()) != cudaSuccess)
+      return cuda_fail(e, "rc_solve_noalloc: shared memory attribute");
+    g_noalloc_scratch_ptr[dev] = ptr;
+  }
+  char* scratch = static_cast<char*>(g_noalloc_scratch_ptr[dev]);
+
+  // Walk tables, built on the host and copied into the scratch.
+  size_t t = 0;
+  size_t dir_off[kMaxCascades] = {};
+  for (int i = 0; i < v.nlev; ++i) {
+    dir_off[i] = t;
+    if (!build_dir_table(v.geom[i], p->grid, g_noalloc_tab + t, msg, sizeof msg)) {
+      rcx::set_error("rc_solve_noalloc: %s", msg);
+      return RC_ERR_UNSUPPORTED;
+    }
+    t += (size_t)v.geom[i].ndirs;
+  }
+  rc_solid_angles(v.geom[0].n, g_noalloc_omega);
+  for (int d = 0; d < v.geom[0].ndirs; ++d) g_noalloc_tab[d].omega = (float)g_noalloc_omega[d];
+  DirInfo* dirs = reinterpret_cast<DirInfo*>(scratch + dirs_off);
+  RC_CUDA(cudaMemcpyAsync(dirs, g_noalloc_tab, ndirs_total * sizeof(DirInfo), cudaMemcpyHostToDevice, st),
+          "rc_solve_noalloc: table upload");
+  // Decimated opacity keeps unused padding bits at zero; the previous call's
+  // contents are cleared.  Everything else is fully rewritten below.
+  if (mask_bytes) RC_CUDA(cudaMemsetAsync(scratch + mask_begin, 0, mask_bytes, st), "rc_solve_noalloc: clear");
+
+  uint32_t* occ = reinterpret_cast<uint32_t*>(scratch + occ_off);
+  v.mset.n = 0;
+  size_t rad_off = 0;
+  for (int i = 0; i < v.nlev; ++i) {
+    const LevelGeom& g = v.geom[i];
+    LevelArgs& a = v.args[i];
+    memset(&a, 0, sizeof a);
+    int l2s = 0;
+    while ((1 << l2s) < g.spacing) ++l2s;
+    if (v.bits_level[i]) {
+      MaskLevel& m = v.mset.lv[v.mset.n++];
+      m.base = reinterpret_cast<uint32_t*>(scratch + mask_off[i]);
+      m.l2s = l2s;
+      for (int ax = 0; ax < 3; ++ax) m.M[ax] = g.M[ax];
+      m.XW = (g.M[0] + 31) / 32;
+      a.mask = m.base;
+    }
+    a.l2s = l2s;
+    a.XW = (g.M[0] + 31) / 32;
+    a.rowblocks = (g.M[1] * g.M[2] + kTileRows - 1) / kTileRows;
+    a.occ = occ;
+    a.vol = reinterpret_cast<const uint2*>(voxels);
+    for (int ax = 0; ax < 3; ++ax) {
+      a.G[ax] = p->grid[ax];
+      a.M[ax] = g.M[ax];
+      a.UM[ax] = (i + 1 < v.nlev) ? v.geom[i + 1].M[ax] : 1;
+    }
+    a.W = v.W;
+    a.dirs = dirs + dir_off[i];
+    a.spacing = g.spacing;
+    a.n = g.n;
+    a.ndirs = g.ndirs;
+    a.P = g.probes();
+    a.L = static_cast<char*>(radiance) + rad_off;
+    rad_off += (size_t)3 * g.ndirs * g.probes() * v.elem;
+    a.A_out = i >= 1 ? scratch + avg_off[i] : nullptr;
+    a.A_up = (i + 1 < v.nlev) ? scratch + avg_off[i + 1] : nullptr;
+    a.P_up = (i + 1 < v.nlev) ? v.geom[i + 1].probes() : 0;
+    a.fluence = fluence;
+  }
+  const int threads = 256;
+  const int64_t blocks = std::min<int64_t>(std::max<int64_t>((full_words * 32 + threads - 1) / threads, 1), 152 * 16);
+  k_masks_from_volume<<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const uint2*>(voxels), occ,
+                                                             p->grid[0], p->grid[1], p->grid[2], v.W, v.mset);
+  RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: opacity launch");
+  enqueue_solve(&v, st);
+  RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: cascade launch");
+  return RC_OK;
+}
