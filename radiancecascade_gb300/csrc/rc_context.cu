@@ -35,6 +35,7 @@ struct rc_context {
   uint2* base = nullptr;     // static volume (boxes / upload)
   uint2* vol = nullptr;      // composed volume
   uint32_t* occ = nullptr;   // opacity bits
+  uint32_t* emis = nullptr;  // emissive bits (opaque with nonzero emission)
   int W = 0;                 // words per x row
   uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
   MaskSet mset{};
@@ -99,7 +100,7 @@ void release(rc_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->base, c->vol, c->occ, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  void* bufs[] = {c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -195,17 +196,48 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
   int64_t blocks = (words * 32 + threads - 1) / threads;
   blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
   k_compose_masks<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
-      c->base, c->vol, c->occ, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg, c->mset);
+      c->base, c->vol, c->occ, c->emis, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg,
+      c->mset);
   RC_CUDA(cudaGetLastError(), "compose launch");
   return RC_OK;
+}
+
+// Decimated-plane geometry of one level (see rc_walk_bits.cuh).  Levels wider
+// than 256 probes per row walk with the scalar kernel.
+struct MaskGeom {
+  bool bits;
+  int32_t l2px, wpp, tiles;
+  uint32_t rep;
+  int64_t words;
+};
+
+MaskGeom mask_geom(const LevelGeom& g, bool force_scalar) {
+  MaskGeom m{};
+  m.l2px = 0;
+  while ((1 << m.l2px) < g.M[0]) ++m.l2px;
+  const int64_t px = (int64_t)1 << m.l2px;
+  m.wpp = (int32_t)((g.M[1] * px + 31) / 32);
+  m.words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * m.wpp;
+  m.bits = !force_scalar && px <= 256;
+  m.rep = 0;
+  if (px < 32)
+    for (int r = 0; r < 32 / px; ++r) m.rep |= 1u << (r * px);
+  if (m.l2px >= 5) {
+    m.tiles = ((g.M[2] + 1) / 2) * ((m.wpp + 15) / 16);
+  } else {
+    const int tw = std::min(m.wpp, 32), tz = std::max(1, 32 / tw);
+    m.tiles = ((g.M[2] + tz - 1) / tz) * ((m.wpp + tw - 1) / tw);
+  }
+  return m;
 }
 
 template <typename T, bool L0, bool TOP>
 void launch_one(const LevelArgs& a, bool bits, cudaStream_t s) {
   if (bits) {
     const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 4);
-    const unsigned blocks = (unsigned)a.XW * (unsigned)a.rowblocks * groups;
-    k_level_bits<T, L0, TOP><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
+    const unsigned blocks = (unsigned)a.tiles * groups;
+    if (a.l2px >= 5) k_level_bits<T, L0, TOP, true><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
+    else k_level_bits<T, L0, TOP, false><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
   } else {
     const int threads = 128;
     dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
@@ -234,14 +266,22 @@ void enqueue_solve(rc_context* c, cudaStream_t s) {
   }
 }
 
+template <typename T, bool L0, bool TOP, bool WIDE>
+cudaError_t allow_one() {
+  return cudaFuncSetAttribute(k_level_bits<T, L0, TOP, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kBitsSmem);
+}
+
 template <typename T>
 cudaError_t allow_bits_smem() {
-  cudaError_t e = cudaSuccess;
-  const int sm = (int)kBitsSmem;
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_level_bits<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaError_t e = allow_one<T, true, true, true>();
+  if (e == cudaSuccess) e = allow_one<T, true, false, true>();
+  if (e == cudaSuccess) e = allow_one<T, false, true, true>();
+  if (e == cudaSuccess) e = allow_one<T, false, false, true>();
+  if (e == cudaSuccess) e = allow_one<T, true, true, false>();
+  if (e == cudaSuccess) e = allow_one<T, true, false, false>();
+  if (e == cudaSuccess) e = allow_one<T, false, true, false>();
+  if (e == cudaSuccess) e = allow_one<T, false, false, false>();
   return e;
 }
 
@@ -315,34 +355,33 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
   if ((s = dev_alloc((void**)&c->vol, nvox * 8, "scene volume")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&c->occ, (size_t)c->W * p->grid[1] * p->grid[2] * 4, "opacity bits")) != RC_OK)
     return fail(s);
+  if ((s = dev_alloc((void**)&c->emis, (size_t)c->W * p->grid[1] * p->grid[2] * 4, "emissive bits")) != RC_OK)
+    return fail(s);
   {
-    // Decimated opacity per level.  A level walks bit-parallel unless the
-    // 32-bit row padding would make its mask more than 8x the full-resolution
-    // bitmask (few probes per row); such a level uses the scalar walk.
+    // Decimated opacity per level (bit-parallel walk).
     const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
-    const int64_t full_words = (int64_t)c->W * p->grid[1] * p->grid[2];
     int64_t total = 0;
     int64_t off[kMaxCascades];
     c->mset.n = 0;
     for (int i = 0; i < c->nlev; ++i) {
-      const LevelGeom& g = c->geom[i];
-      const int64_t xw = (g.M[0] + 31) / 32;
-      const int64_t words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * xw * g.M[1];
-      c->bits_level[i] = !force_scalar && words <= 8 * full_words;
+      const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
+      c->bits_level[i] = mg.bits;
       off[i] = total;
-      if (c->bits_level[i]) total += (words + 63) & ~(int64_t)63;
+      if (mg.bits) total += (mg.words + 63) & ~(int64_t)63;
     }
     if (total && (s = dev_alloc((void**)&c->masks, total * 4, "decimated opacity")) != RC_OK) return fail(s);
     if (total && (e = cudaMemset(c->masks, 0, total * 4)) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
     for (int i = 0; i < c->nlev; ++i) {
       if (!c->bits_level[i]) continue;
+      const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
       MaskLevel& m = c->mset.lv[c->mset.n++];
       const LevelGeom& g = c->geom[i];
       m.base = c->masks + off[i];
       m.l2s = 0;
       while ((1 << m.l2s) < g.spacing) ++m.l2s;
       for (int a = 0; a < 3; ++a) m.M[a] = g.M[a];
-      m.XW = (g.M[0] + 31) / 32;
+      m.l2px = mg.l2px;
+      m.wpp = mg.wpp;
     }
     if ((e = allow_bits_smem<float>()) != cudaSuccess || (e = allow_bits_smem<__half>()) != cudaSuccess)
       return fail(cuda_fail(e, "rc_create: shared memory attribute"));
@@ -369,13 +408,19 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     LevelArgs& a = c->args[i];
     const LevelGeom& g = c->geom[i];
     memset(&a, 0, sizeof a);
-    for (int k = 0; k < c->mset.n; ++k)
-      if (c->mset.lv[k].M[0] == g.M[0] && c->mset.lv[k].M[1] == g.M[1] && (1 << c->mset.lv[k].l2s) == g.spacing)
-        a.mask = c->mset.lv[k].base;
+    {
+      const MaskGeom mg = mask_geom(g, !c->bits_level[i]);
+      for (int k = 0; k < c->mset.n; ++k)
+        if (c->mset.lv[k].M[0] == g.M[0] && c->mset.lv[k].M[1] == g.M[1] && (1 << c->mset.lv[k].l2s) == g.spacing)
+          a.mask = c->mset.lv[k].base;
+      a.l2px = mg.l2px;
+      a.wpp = mg.wpp;
+      a.rep = mg.rep;
+      a.tiles = mg.tiles;
+    }
     a.l2s = 0;
     while ((1 << a.l2s) < g.spacing) ++a.l2s;
-    a.XW = (g.M[0] + 31) / 32;
-    a.rowblocks = (g.M[1] * g.M[2] + kTileRows - 1) / kTileRows;
+    a.emis = c->emis;
     a.occ = c->occ;
     a.vol = c->vol;
     for (int ax = 0; ax < 3; ++ax) {
@@ -666,8 +711,8 @@ double g_noalloc_omega[kNoallocMaxDirs];
 
 // Opacity bits and decimated opacity of a caller-owned volume (the volume is
 // only read).
-__global__ void k_masks_from_volume(const uint2* __restrict__ vol, uint32_t* __restrict__ occ, int Gx, int Gy,
-                                    int Gz, int W, const MaskSet ms) {
+__global__ void k_masks_from_volume(const uint2* __restrict__ vol, uint32_t* __restrict__ occ,
+                                    uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W, const MaskSet ms) {
   const int64_t words = (int64_t)W * Gy * Gz;
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -677,9 +722,18 @@ __global__ void k_masks_from_volume(const uint2* __restrict__ vol, uint32_t* __r
     const int y = (int)((w / W) % Gy);
     const int z = (int)(w / ((int64_t)W * Gy));
     const int x = wx * 32 + lane;
-    const bool opaque = x < Gx && ((__ldg(&vol[((int64_t)z * Gy + y) * Gx + x]).y >> 31) & 1u);
+    bool opaque = false, emissive = false;
+    if (x < Gx) {
+      const uint2 v = __ldg(&vol[((int64_t)z * Gy + y) * Gx + x]);
+      opaque = (v.y >> 31) & 1u;
+      emissive = opaque && (((v.x & 0x7FFF7FFFu) | (v.y & 0x7FFFu)) != 0u);
+    }
     const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
-    if (lane == 0) occ[((int64_t)z * Gy + y) * W + wx] = bits;
+    const unsigned ebits = __ballot_sync(0xFFFFFFFFu, emissive);
+    if (lane == 0) {
+      occ[((int64_t)z * Gy + y) * W + wx] = bits;
+      emis[((int64_t)z * Gy + y) * W + wx] = ebits;
+    }
     update_masks(ms, lane, wx, x, y, z, Gx, bits);
   }
 }
@@ -725,13 +779,13 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   const int64_t full_words = (int64_t)v.W * p->grid[1] * p->grid[2];
   size_t off = 0;
   const size_t occ_off = carve(off, (size_t)full_words * 4);
+  const size_t emis_off = carve(off, (size_t)full_words * 4);
   size_t mask_off[kMaxCascades] = {}, mask_bytes = 0, mask_begin = off;
+  MaskGeom mgs[kMaxCascades];
   for (int i = 0; i < v.nlev; ++i) {
-    const LevelGeom& g = v.geom[i];
-    const int64_t xw = (g.M[0] + 31) / 32;
-    const int64_t words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * xw * g.M[1];
-    v.bits_level[i] = !force_scalar && words <= 8 * full_words;
-    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)words * 4);
+    mgs[i] = mask_geom(v.geom[i], force_scalar);
+    v.bits_level[i] = mgs[i].bits;
+    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 4);
   }
   mask_bytes = off - mask_begin;
   size_t avg_off[kMaxCascades] = {};
@@ -780,6 +834,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   if (mask_bytes) RC_CUDA(cudaMemsetAsync(scratch + mask_begin, 0, mask_bytes, st), "rc_solve_noalloc: clear");
 
   uint32_t* occ = reinterpret_cast<uint32_t*>(scratch + occ_off);
+  uint32_t* emis = reinterpret_cast<uint32_t*>(scratch + emis_off);
   v.mset.n = 0;
   size_t rad_off = 0;
   for (int i = 0; i < v.nlev; ++i) {
@@ -793,12 +848,16 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
       m.base = reinterpret_cast<uint32_t*>(scratch + mask_off[i]);
       m.l2s = l2s;
       for (int ax = 0; ax < 3; ++ax) m.M[ax] = g.M[ax];
-      m.XW = (g.M[0] + 31) / 32;
+      m.l2px = mgs[i].l2px;
+      m.wpp = mgs[i].wpp;
       a.mask = m.base;
     }
     a.l2s = l2s;
-    a.XW = (g.M[0] + 31) / 32;
-    a.rowblocks = (g.M[1] * g.M[2] + kTileRows - 1) / kTileRows;
+    a.l2px = mgs[i].l2px;
+    a.wpp = mgs[i].wpp;
+    a.rep = mgs[i].rep;
+    a.tiles = mgs[i].tiles;
+    a.emis = emis;
     a.occ = occ;
     a.vol = reinterpret_cast<const uint2*>(voxels);
     for (int ax = 0; ax < 3; ++ax) {
@@ -821,7 +880,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   }
   const int threads = 256;
   const int64_t blocks = std::min<int64_t>(std::max<int64_t>((full_words * 32 + threads - 1) / threads, 1), 152 * 16);
-  k_masks_from_volume<<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const uint2*>(voxels), occ,
+  k_masks_from_volume<<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const uint2*>(voxels), occ, emis,
                                                              p->grid[0], p->grid[1], p->grid[2], v.W, v.mset);
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: opacity launch");
   enqueue_solve(&v, st);

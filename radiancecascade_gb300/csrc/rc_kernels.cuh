@@ -30,10 +30,14 @@ struct Store<__half> {
 };
 
 struct LevelArgs {
-  const uint32_t* mask;  // this level's decimated opacity words (bit-parallel walk)
+  const uint32_t* mask;  // this level's decimated opacity (bit-parallel walk)
+  const uint32_t* emis;  // full-resolution emissive bits, same layout as occ
   int32_t l2s;           // log2(spacing)
-  int32_t XW;            // mask words per coarse x row: ceil(M[0] / 32)
-  int32_t rowblocks;     // ceil(M[1] * M[2] / 32)
+  int32_t l2px;          // log2 of the decimated plane row pitch
+  int32_t wpp;           // words per decimated plane
+  uint32_t rep;          // narrow levels: 1 bit at the start of every row of a word
+  int32_t tiles;         // block tiles per direction group
+  int32_t pad0;
   const uint32_t* occ;
   const uint2* vol;
   int32_t G[3];
@@ -198,46 +202,6 @@ __global__ void k_boxes_to_base(uint2* __restrict__ base, int Gx, int Gy, int Gz
       }
     }
     base[idx] = v;
-  }
-}
-
-// Composed volume and opacity bits over a list of regions: each voxel is the
-// base voxel overwritten by every sphere containing its centre (later spheres
-// win).  One warp per 32-voxel x-word; overlapping regions write identical
-// values.
-__global__ void k_compose(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ, int Gx,
-                          int Gy, int Gz, int W, const QSphere* __restrict__ sph, int ns,
-                          const Region* __restrict__ regs) {
-  const Region r = regs[blockIdx.y];
-  const int64_t nw = r.w1 - r.w0, ny = r.y1 - r.y0, nz = r.z1 - r.z0;
-  const int64_t words = nw * ny * nz;
-  const int lane = threadIdx.x & 31;
-  const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w = warp0; w < words; w += wstride) {
-    const int wx = r.w0 + (int)(w % nw);
-    const int y = r.y0 + (int)((w / nw) % ny);
-    const int z = r.z0 + (int)(w / (nw * ny));
-    const int x = wx * 32 + lane;
-    bool opaque = false;
-    if (x < Gx) {
-      const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
-      uint2 v = base[idx];
-      const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
-      for (int s = 0; s < ns; ++s) {
-        const QSphere& S = sph[s];
-        const int64_t dx = px - S.c[0], dy = py - S.c[1], dz = pz - S.c[2];
-        if (dx > S.r || -dx > S.r || dy > S.r || -dy > S.r || dz > S.r || -dz > S.r) continue;
-        if (dx * dx + dy * dy + dz * dz <= S.r * S.r) {
-          v.x = (uint32_t)S.value.emission[0] | ((uint32_t)S.value.emission[1] << 16);
-          v.y = (uint32_t)S.value.emission[2] | ((uint32_t)S.value.albedo_occ << 16);
-        }
-      }
-      vol[idx] = v;
-      opaque = (v.y >> 31) & 1u;
-    }
-    const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
-    if (lane == 0) occ[((int64_t)z * Gy + y) * W + wx] = bits;
   }
 }
 

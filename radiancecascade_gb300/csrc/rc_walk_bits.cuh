@@ -4,36 +4,39 @@
 // integer arithmetic, so for one direction every probe of a level visits the
 // same sequence of voxel offsets from its own centre.  Probe m (per axis)
 // tests voxel m*s + a, where a = s/2 + offset is shared by all probes; with
-// phase phi = a mod s and coarse shift c = floor(a / s) that voxel is bit
-// (m + c) of the level's phase-phi decimated opacity row.  One lane therefore
-// walks 32 probes of an x row at once: per step it loads two 32-bit words,
-// funnel-shifts them by c and masks the probes already finished.
+// phase phi = a mod s and coarse shift c = floor(a / s) that voxel is coarse
+// cell (m + c) of the level's phase-phi decimated opacity.  One lane walks the
+// 32 probes of one 32-bit word at once: per step it loads two words,
+// funnel-shifts them by the shared coarse shift and masks the probes that
+// have finished or left the grid.
 //
-// Decimated opacity of level i (spacing s = 2^l2s, M probes per axis,
-// XW = ceil(Mx/32) words per coarse row):
-//   mask[phz][phy][phx][zc][xw][yc]   bit b of word xw <-> coarse x = 32 xw + b
-//   = opacity of voxel (xc*s + phx, yc*s + phy, zc*s + phz)
-// y is fastest so that the 32 lanes of a warp (consecutive probe rows) read
-// 32 consecutive words.
+// Decimated opacity of level i (spacing s = 2^l2s, M probes per axis):
+//   each (phase, zc) plane of the coarse grid is a row-major bit array with a
+//   power-of-two row pitch Px >= Mx bits, packed into wpp = ceil(My*Px/32)
+//   words:  mask[phz][phy][phx][zc][word];  bit g = yc*Px + xc of the plane
+//   is the opacity of voxel (xc*s + phx, yc*s + phy, zc*s + phz).
+// Every coarse shift (cx, cy) is a shift of the plane by cy*Px + cx bits, so
+// any Mx uses all 32 bits of a lane.
 #pragma once
 
 #include "rc_kernels.cuh"
 
 namespace rcx {
 
-constexpr int kTileRows = 32;      // probe rows (y, z) per block
+constexpr int kTileSlots = 32;     // words (of 32 probes) per block tile
 constexpr int kTileDirs = 16;      // directions per block pass
-constexpr int kBitsThreads = kTileRows * kTileDirs;
+constexpr int kBitsThreads = kTileSlots * kTileDirs;
 constexpr int kHitStride = 33;     // padded hit-record row (bank spread)
-constexpr uint32_t kMiss = 0xFFFFFFFFu;
-constexpr size_t kBitsSmem = sizeof(uint32_t) * kTileDirs * kTileRows * kHitStride;
+constexpr uint32_t kMiss = 0xFFFFFFFFu;   // no opaque voxel in the interval
+constexpr uint32_t kBlack = 0xFFFFFFFEu;  // opaque voxel without emission
+constexpr size_t kBitsSmem = sizeof(uint32_t) * kTileDirs * kTileSlots * kHitStride;
 
 struct MaskLevel {
   uint32_t* base;
   int32_t l2s;
   int32_t M[3];
-  int32_t XW;
-  int32_t pad;
+  int32_t l2px;  // log2 of the plane row pitch Px
+  int32_t wpp;   // words per (phase, zc) plane
 };
 
 struct MaskSet {
@@ -42,15 +45,30 @@ struct MaskSet {
   MaskLevel lv[kMaxCascades];
 };
 
-__device__ __forceinline__ int64_t mask_word(const MaskLevel& m, int phx, int phy, int phz, int xw, int yc, int zc) {
+__device__ __forceinline__ int64_t plane_base(const MaskLevel& m, int phx, int phy, int phz, int zc) {
   const int64_t phase = ((((int64_t)phz << m.l2s) + phy) << m.l2s) + phx;
-  return (phase * m.M[2] + zc) * ((int64_t)m.XW * m.M[1]) + (int64_t)xw * m.M[1] + yc;
+  return (phase * m.M[2] + zc) * (int64_t)m.wpp;
+}
+
+__device__ __forceinline__ int64_t plane_base_args(const LevelArgs& a, int phx, int phy, int phz, int zc) {
+  const int64_t phase = ((((int64_t)phz << a.l2s) + phy) << a.l2s) + phx;
+  return (phase * a.M[2] + zc) * (int64_t)a.wpp;
+}
+
+__device__ __forceinline__ uint32_t range_bits(int lo, int hi) {
+  // bits [lo, hi) of a word, with lo, hi clamped to [0, 32]
+  lo = max(lo, 0);
+  hi = min(hi, 32);
+  if (hi <= lo) return 0u;
+  const uint32_t upto = hi >= 32 ? 0xFFFFFFFFu : ((1u << hi) - 1u);
+  return upto & ~((1u << lo) - 1u);
 }
 
 // Updates every level's decimated opacity for the 32 voxels x = 32*wx + lane
-// of row (y, z); `bits` is the warp's opacity ballot.  Each (level, phase) bit
-// field belongs to exactly one warp, so clear-then-set is race free (a region
-// processed twice writes the same values).
+// of row (y, z); `bits` is the warp's opacity ballot.  The coarse cells a
+// warp touches in one (level, phase) plane form one bit field that no other
+// warp writes, so clear-then-set is race free (a region processed twice
+// writes the same values).
 __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx, int x, int y, int z, int Gx,
                                              uint32_t bits) {
   for (int i = 0; i < ms.n; ++i) {
@@ -59,31 +77,38 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
     const int phy = y & (s - 1), yc = y >> m.l2s, phz = z & (s - 1), zc = z >> m.l2s;
     if (s < 32) {
       if (lane < s) {
-        const int per = 32 >> m.l2s;  // coarse bits of this phase in the warp's 32 voxels
-        uint32_t field = 0;
-        for (int j = 0; j < per; ++j) field |= ((bits >> (lane + j * s)) & 1u) << j;
+        const int per = 32 >> m.l2s;  // coarse cells of this phase among the warp's 32 voxels
         const int xc0 = (32 * wx) >> m.l2s;
-        uint32_t* w = m.base + mask_word(m, lane, phy, phz, xc0 >> 5, yc, zc);
-        const int sh = xc0 & 31;
-        const uint32_t fmask = (per == 32 ? 0xFFFFFFFFu : ((1u << per) - 1u)) << sh;
-        atomicAnd(w, ~fmask);
-        if (field) atomicOr(w, field << sh);
+        const int width = min(per, m.M[0] - xc0);
+        if (width > 0) {
+          uint32_t field = 0;
+          for (int j = 0; j < width; ++j) field |= ((bits >> (lane + j * s)) & 1u) << j;
+          const int64_t g = ((int64_t)yc << m.l2px) + xc0;
+          uint32_t* w = m.base + plane_base(m, lane, phy, phz, zc) + (g >> 5);
+          const int sh = (int)(g & 31);
+          const uint32_t fmask = (width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u)) << sh;
+          atomicAnd(w, ~fmask);
+          if (field) atomicOr(w, field << sh);
+        }
       }
     } else if (x < Gx) {
       const int xc = x >> m.l2s;
-      uint32_t* w = m.base + mask_word(m, x & (s - 1), phy, phz, xc >> 5, yc, zc);
-      const uint32_t b = 1u << (xc & 31);
+      const int64_t g = ((int64_t)yc << m.l2px) + xc;
+      uint32_t* w = m.base + plane_base(m, x & (s - 1), phy, phz, zc) + (g >> 5);
+      const uint32_t b = 1u << (g & 31);
       if ((bits >> lane) & 1u) atomicOr(w, b);
       else atomicAnd(w, ~b);
     }
   }
 }
 
-// Composed volume, full-resolution opacity and every level's decimated
-// opacity over a list of regions (see k_compose for the composition rule).
+// Composed volume, full-resolution opacity and emissive bits, and every
+// level's decimated opacity over a list of regions (composition rule as in
+// k_compose).
 __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ,
-                                int Gx, int Gy, int Gz, int W, const QSphere* __restrict__ sph, int ns,
-                                const Region* __restrict__ regs, const MaskSet ms) {
+                                uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W,
+                                const QSphere* __restrict__ sph, int ns, const Region* __restrict__ regs,
+                                const MaskSet ms) {
   const Region r = regs[blockIdx.y];
   const int64_t nw = r.w1 - r.w0, ny = r.y1 - r.y0, nz = r.z1 - r.z0;
   const int64_t words = nw * ny * nz;
@@ -95,7 +120,7 @@ __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restric
     const int y = r.y0 + (int)((w / nw) % ny);
     const int z = r.z0 + (int)(w / (nw * ny));
     const int x = wx * 32 + lane;
-    bool opaque = false;
+    bool opaque = false, emissive = false;
     if (x < Gx) {
       const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
       uint2 v = base[idx];
@@ -111,200 +136,355 @@ __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restric
       }
       vol[idx] = v;
       opaque = (v.y >> 31) & 1u;
+      emissive = opaque && (((v.x & 0x7FFF7FFFu) | (v.y & 0x7FFFu)) != 0u);
     }
     const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
-    if (lane == 0) occ[((int64_t)z * Gy + y) * W + wx] = bits;
+    const unsigned ebits = __ballot_sync(0xFFFFFFFFu, emissive);
+    if (lane == 0) {
+      occ[((int64_t)z * Gy + y) * W + wx] = bits;
+      emis[((int64_t)z * Gy + y) * W + wx] = ebits;
+    }
     update_masks(ms, lane, wx, x, y, z, Gx, bits);
   }
 }
 
-// Phase 1 of k_level_bits: walk the interval of direction `di` for the (up
-// to) 32 probes of word `w` in probe row (my, mz); record the first opaque
-// voxel of each probe in `hit[b]`.
-__device__ __forceinline__ void walk_row_bits(const LevelArgs& a, const DirInfo& di, int w, int my, int mz,
-                                              int TX, bool test_start, uint32_t* __restrict__ hit) {
+// Geometry of one block's tile of probe words.
+//   wide levels (Px >= 32): tile = 2 planes x 16 words; slot u -> plane u / 16,
+//     word wt + u % 16.  16 words are 512/Px whole rows of the plane.
+//   narrow levels (Px < 32): tile = TZ planes x TW words (TZ * TW <= 32).
+struct Tile {
+  int z0, w0;     // first plane, first word
+  int TZ, TW;     // planes, words per plane in the tile
+};
+
+__device__ __forceinline__ Tile tile_of(const LevelArgs& a, int tile) {
+  Tile t;
+  if (a.l2px >= 5) {
+    t.TZ = 2;
+    t.TW = 16;
+    const int wt = (a.wpp + 15) / 16;  // tiles per plane pair
+    t.z0 = 2 * (tile / wt);
+    t.w0 = 16 * (tile % wt);
+  } else {
+    t.TW = min(a.wpp, 32);
+    t.TZ = max(1, 32 / t.TW);
+    const int wt = (a.wpp + t.TW - 1) / t.TW;
+    t.z0 = t.TZ * (tile / wt);
+    t.w0 = t.TW * (tile % wt);
+  }
+  return t;
+}
+
+// Phase 1: walk the interval of direction `di` for the 32 probes of plane
+// word `wl` in coarse plane `zl`; record each probe's first opaque voxel.
+__device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di, int zl, int wl, bool test_start,
+                                          uint32_t* __restrict__ hit) {
   const int s = a.spacing, l2s = a.l2s, h = s >> 1;
+  const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
+  const int l2px = a.l2px, Px = 1 << l2px;
+  const int g0 = wl << 5;  // plane bit of this word's bit 0
+  // probes that exist: x < Mx, y < My
+  uint32_t valid;
+  int wy0 = 0, wx0 = 0;  // row and column of bit 0
+  if (l2px >= 5) {
+    wy0 = g0 >> l2px;
+    wx0 = g0 & (Px - 1);
+    valid = wy0 < My ? range_bits(0, Mx - wx0) : 0u;
+  } else {
+    wy0 = g0 >> l2px;
+    const uint32_t row = range_bits(0, Mx);  // within Px bits
+    valid = row * a.rep;                      // replicate over the 32/Px rows of the word
+    valid &= range_bits(0, (My - wy0) * Px);
+  }
+  uint32_t done = ~valid;
+  if (valid == 0u) return;
   int ax = h + di.start_off[0], ay = h + di.start_off[1], az = h + di.start_off[2];
   int tx = di.first_T[0], ty = di.first_T[1], tz = di.first_T[2];
   const int sx = di.sgn[0], sy = di.sgn[1], sz = di.sgn[2];
   const int dx = di.step_T[0], dy = di.step_T[1], dz = di.step_T[2];
-  const uint32_t valid = TX >= 32 ? 0xFFFFFFFFu : ((1u << TX) - 1u);
-  uint32_t done = ~valid;
-  const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   int k = di.steps;
   bool pending_start = test_start;
   for (;;) {
     if (!pending_start) {
       if (k == 0) break;
       --k;
-      if (tx <= ty && tx <= tz) {
-        ax += sx;
-        tx += dx;
-      } else if (ty <= tz) {
-        ay += sy;
-        ty += dy;
-      } else {
-        az += sz;
-        tz += dz;
-      }
+      // branch-free choice of the axis with the nearest crossing (x, then y, then z on ties)
+      const bool bx = (tx <= ty) & (tx <= tz);
+      const bool by = !bx & (ty <= tz);
+      const bool bz = !bx & !by;
+      ax += bx ? sx : 0;
+      tx += bx ? dx : 0;
+      ay += by ? sy : 0;
+      ty += by ? dy : 0;
+      az += bz ? sz : 0;
+      tz += bz ? dz : 0;
     }
     pending_start = false;
-    const int zc = mz + (az >> l2s), yc = my + (ay >> l2s);
-    if ((unsigned)zc >= (unsigned)Mz || (unsigned)yc >= (unsigned)My) break;  // the row left the grid
-    const int X0 = 32 * w + (ax >> l2s);  // coarse x of bit 0
-    // bits b with 0 <= X0 + b < Mx are still inside the grid
-    const int blo = X0 < 0 ? -X0 : 0;
-    const int bhi = Mx - X0;
-    uint32_t inr = 0;
-    if (blo < 32 && bhi > blo) {
-      const uint32_t upto = bhi >= 32 ? 0xFFFFFFFFu : ((1u << bhi) - 1u);
-      inr = upto & ~((1u << blo) - 1u);
+    const int cz = az >> l2s, cy = ay >> l2s, cx = ax >> l2s;
+    const int zc = zl + cz;
+    if ((unsigned)zc >= (unsigned)Mz) break;  // every probe of the word left the grid
+    // probes whose cell (x + cx, y + cy) is still inside the grid
+    uint32_t inr;
+    if (l2px >= 5) {
+      const int yy = wy0 + cy;
+      inr = ((unsigned)yy < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+    } else {
+      // column range kept inside the Px-bit row before it is replicated over the rows
+      inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * a.rep;
+      inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
     }
     done |= ~inr;
     if (done == 0xFFFFFFFFu) break;
-    const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
-    const uint32_t* row = a.mask + (phase * Mz + zc) * ((int64_t)a.XW * My) + yc;
-    const int q = X0 >> 5, sh = X0 & 31;
-    const uint32_t lo = (q >= 0 && q < a.XW) ? __ldg(row + (int64_t)q * My) : 0u;
-    const uint32_t hi = (q + 1 >= 0 && q + 1 < a.XW) ? __ldg(row + (int64_t)(q + 1) * My) : 0u;
+    const uint32_t* plane = a.mask + plane_base_args(a, ax & (s - 1), ay & (s - 1), az & (s - 1), zc);
+    const int gs = g0 + cy * Px + cx;  // plane bit of this word's bit 0 after the shift
+    const int q = gs >> 5, sh = gs & 31;
+    const uint32_t lo = ((unsigned)q < (unsigned)a.wpp) ? __ldg(plane + q) : 0u;
+    const uint32_t hi = ((unsigned)(q + 1) < (unsigned)a.wpp) ? __ldg(plane + q + 1) : 0u;
     uint32_t nw = __funnelshift_r(lo, hi, sh) & ~done;
     if (nw) {
       done |= nw;
-      const int64_t vyz = ((int64_t)(mz * s + az) * a.G[1] + (my * s + ay)) * a.G[0];
       do {
         const int b = __ffs(nw) - 1;
         nw &= nw - 1;
-        hit[b] = (uint32_t)(vyz + (int64_t)(32 * w + b) * s + ax);
+        const int g = g0 + b;
+        const int vx = ((g & (Px - 1)) << l2s) + ax, vy = ((g >> l2px) << l2s) + ay, vz = (zl << l2s) + az;
+        const int64_t idx = ((int64_t)vz * a.G[1] + vy) * a.G[0] + vx;
+        const uint32_t e = __ldg(&a.emis[((int64_t)vz * a.G[1] + vy) * a.W + (vx >> 5)]);
+        hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)idx : kBlack;
       } while (nw);
       if (done == 0xFFFFFFFFu) break;
     }
   }
 }
 
-// Bit-parallel cascade level.  Block = 32 probe rows x 16 directions.
-// Phase 1: lane (row, direction) walks a 32-probe word and records hits in
-// shared memory.  Phase 2: thread (probe) reads the records of all 16
-// directions, takes the hit voxel's emission or (below the top level) the
-// trilinear blend of the next level's child-averaged radiance, writes L_i
-// coalesced along x, and reduces the 2x2-child average (levels >= 1) or the
-// fluence (level 0) in registers.
-template <typename T, bool L0, bool TOP>
+__device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol, uint32_t idx, int ch) {
+  const uint2 v = __ldg(&vol[idx]);
+  const uint32_t w = ch == 2 ? v.y : v.x;
+  return __half2float(__ushort_as_half((unsigned short)(ch == 1 ? (w >> 16) : (w & 0xFFFFu))));
+}
+
+// Direction of block-local slot dl (0..15) in pass `pass`, or -1.
+template <bool L0>
+__device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgroup, int dl) {
+  if (L0) {
+    const int d = pass * kTileDirs + dl;
+    return d < a.ndirs ? d : -1;
+  }
+  const int hn = a.n >> 1;
+  const int dp = dgroup * 4 + (dl >> 2), c = dl & 3;
+  return (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
+}
+
+// Bit-parallel cascade level.  Block = one tile of 32 probe words x 16
+// directions (512 threads).
+// Phase 1: warp = direction, lane = word: walk 32 probes per lane, record the
+//   first opaque voxel of each probe (or kMiss / kBlack) in shared memory.
+// Phase 2, WIDE levels (>= 32 probes per row): warp = (32 x-children x 2 y x
+//   2 z block, 8 directions).  Below the top level, missing rays take the
+//   trilinear blend of the next level's child-averaged radiance: each lane
+//   loads one parent column (3 x 3 values per channel), interpolates z and y
+//   in registers and x through warp shuffles.
+// Phase 2, narrow levels: thread = probe, per-probe 8-tap gather.
+// Level 0 reduces the fluence; other levels write the 2x2-child averages.
+template <typename T, bool L0, bool TOP, bool WIDE>
 __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs a) {
   extern __shared__ uint32_t s_hit[];
-  const int tid = threadIdx.x;
-  const int lrow = tid & 31;
-  const int ldir = tid >> 5;
-  int bid = blockIdx.x;
-  const int w = bid % a.XW;
-  bid /= a.XW;
-  const int rowblk = bid % a.rowblocks;
-  const int dgroup = bid / a.rowblocks;  // levels >= 1: group of 4 parent texels
-  const int Mx = a.M[0], My = a.M[1];
-  const int rows_total = a.M[1] * a.M[2];
-  const int TX = min(Mx - 32 * w, 32);
-  const int hn = a.n >> 1;
-  const int ndir_pass = L0 ? min(a.ndirs, kTileDirs) : kTileDirs;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tile_id = blockIdx.x % a.tiles;
+  const int dgroup = blockIdx.x / a.tiles;
+  const Tile t = tile_of(a, tile_id);
+  const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int npass = L0 ? (a.ndirs + kTileDirs - 1) / kTileDirs : 1;
+  const int hn = a.n >> 1;
+  const int64_t npar = (int64_t)hn * hn;
+  T* L = static_cast<T*>(a.L);
+  const T* Au = static_cast<const T*>(a.A_up);
 
-  float flu[2][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  // wide: lane's child block (x, y0 + ey, z0 + ez), ey, ez in {0, 1}
+  const int unit = warp & 7, half = warp >> 3;
+  const int cl2 = a.l2px - 5;
+  const int c = WIDE ? (unit & ((1 << cl2) - 1)) : 0;
+  const int y0 = WIDE ? ((t.w0 << 5) >> a.l2px) + 2 * (unit >> cl2) : 0;
+  const int x = 32 * c + lane;
+  const int64_t plane = (int64_t)My * Mx;
+  const int64_t p0 = ((int64_t)t.z0 * My + y0) * Mx + x;
+  const int slot0 = (y0 << cl2) + c - t.w0;
+  unsigned okmask = 0;  // bit i = child (ez = i >> 1, ey = i & 1) exists
+  if (WIDE) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (x < Mx && y0 + (i & 1) < My && t.z0 + (i >> 1) < Mz) okmask |= 1u << i;
+  }
+  // wide: parent column of this lane (lanes 0..17 load), rows qy0-1..qy0+1, planes qz0-1..qz0+1
+  const int qx = min(max(16 * c - 1 + lane, 0), a.UM[0] - 1);
+  const bool ploader = lane < 18;
+  const int src_lo = (lane + 1) >> 1;
+  const float wlo = (lane & 1) ? 0.75f : 0.25f, whi = 1.0f - wlo;
+
+  float acc[4][3];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
+
   for (int pass = 0; pass < npass; ++pass) {
-    // ---- phase 1
+    // ---- phase 1: lane = word of the tile, warp = direction
     {
-      uint32_t* hit = s_hit + (ldir * kTileRows + lrow) * kHitStride;
+      uint32_t* hit = s_hit + (warp * kTileSlots + lane) * kHitStride;
 #pragma unroll 8
       for (int b = 0; b < 32; ++b) hit[b] = kMiss;
-      const int r = rowblk * kTileRows + lrow;
-      int d = -1;
-      if (L0) {
-        const int dd = pass * kTileDirs + ldir;
-        if (ldir < ndir_pass && dd < a.ndirs) d = dd;
-      } else {
-        const int dp = dgroup * 4 + (ldir >> 2), c = ldir & 3;
-        d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
-      }
-      if (d >= 0 && r < rows_total) {
+      const int d = block_dir<L0>(a, pass, dgroup, warp);
+      const int zl = t.z0 + lane / t.TW, wl = t.w0 + lane % t.TW;
+      if (d >= 0 && lane < t.TZ * t.TW && zl < Mz && wl < a.wpp) {
         const DirInfo di = a.dirs[d];
-        walk_row_bits(a, di, w, r % My, r / My, TX, L0, hit);
+        walk_word(a, di, zl, wl, L0, hit);
       }
     }
     __syncthreads();
     // ---- phase 2
+    if (WIDE) {
 #pragma unroll 1
-    for (int j = 0; j < 2; ++j) {
-      const int t = tid + kBitsThreads * j;
-      if (t >= TX * kTileRows) break;
-      const int lr = t / TX, b = t - lr * TX;
-      const int r = rowblk * kTileRows + lr;
-      if (r >= rows_total) continue;
-      const int mx = 32 * w + b, my = r % My, mz = r / My;
-      const int64_t p = ((int64_t)mz * My + my) * Mx + mx;
-      int tap_off[8];
-      float tap_w[8];
-      if (!TOP) {
-        int q[3][2];
-        float wt[3][2];
-        const int m[3] = {mx, my, mz};
+      for (int k = 0; k < 8; ++k) {
+        const int dl = half * 8 + k;
+        const int d = block_dir<L0>(a, pass, dgroup, dl);
+        if (d < 0) break;
+        uint32_t rec[4];
+        bool miss = false;
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-          const int lo = (m[ax] - 1) >> 1;
-          wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
-          wt[ax][1] = 1.0f - wt[ax][0];
-          q[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
-          q[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+        for (int i = 0; i < 4; ++i) {
+          const int sl = slot0 + (i >> 1) * 16 + ((i & 1) << cl2);
+          rec[i] = ((okmask >> i) & 1u) ? s_hit[(dl * kTileSlots + sl) * kHitStride + lane] : kBlack;
+          miss |= rec[i] == kMiss;
         }
-#pragma unroll
-        for (int tp = 0; tp < 8; ++tp) {
-          const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
-          tap_off[tp] = (q[2][iz] * a.UM[1] + q[1][iy]) * a.UM[0] + q[0][ix];
-          tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
-        }
-      }
-      T* L = static_cast<T*>(a.L);
-      float acc[3] = {0.f, 0.f, 0.f};
+        const bool merge = !TOP && __any_sync(0xFFFFFFFFu, miss);
+        const float om = L0 ? a.dirs[d].omega : 0.f;
 #pragma unroll 1
-      for (int dl = 0; dl < ndir_pass; ++dl) {
-        int d;
-        if (L0) {
-          d = pass * kTileDirs + dl;
-          if (d >= a.ndirs) break;
-        } else {
-          const int dp = dgroup * 4 + (dl >> 2), c = dl & 3;
-          d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
-        }
-        const uint32_t rec = s_hit[(dl * kTileRows + lr) * kHitStride + b];
-        float rv[3];
-        if (rec != kMiss) {
-          voxel_emission(a.vol, rec, rv);
-        } else if (TOP) {
-          rv[0] = rv[1] = rv[2] = 0.f;
-        } else {
-          const T* Au = static_cast<const T*>(a.A_up);
-#pragma unroll
-          for (int ch = 0; ch < 3; ++ch) {
+        for (int ch = 0; ch < 3; ++ch) {
+          float mv[4] = {0.f, 0.f, 0.f, 0.f};
+          if (merge) {
             const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-            float sum = 0.f;
+            float av[9];
 #pragma unroll
-            for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
-            rv[ch] = sum;
+            for (int kz = 0; kz < 3; ++kz) {
+              const int qz = min(max(t.z0 / 2 - 1 + kz, 0), a.UM[2] - 1);
+#pragma unroll
+              for (int jy = 0; jy < 3; ++jy) {
+                const int qy = min(max(y0 / 2 - 1 + jy, 0), a.UM[1] - 1);
+                av[kz * 3 + jy] = ploader ? Store<T>::load(src + (qz * a.UM[1] + qy) * a.UM[0] + qx) : 0.f;
+              }
+            }
+#pragma unroll
+            for (int ez = 0; ez < 2; ++ez) {
+              float zv[3];
+#pragma unroll
+              for (int jy = 0; jy < 3; ++jy)
+                zv[jy] = ez == 0 ? fmaf(0.25f, av[jy], 0.75f * av[3 + jy]) : fmaf(0.75f, av[3 + jy], 0.25f * av[6 + jy]);
+              const float v0 = fmaf(0.25f, zv[0], 0.75f * zv[1]);
+              const float v1 = fmaf(0.75f, zv[1], 0.25f * zv[2]);
+              const float l0 = __shfl_sync(0xFFFFFFFFu, v0, src_lo), h0 = __shfl_sync(0xFFFFFFFFu, v0, src_lo + 1);
+              const float l1 = __shfl_sync(0xFFFFFFFFu, v1, src_lo), h1 = __shfl_sync(0xFFFFFFFFu, v1, src_lo + 1);
+              mv[ez * 2 + 0] = fmaf(wlo, l0, whi * h0);
+              mv[ez * 2 + 1] = fmaf(wlo, l1, whi * h1);
+            }
+          }
+          T* dst = L + ((int64_t)ch * a.ndirs + d) * a.P + p0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            if (!((okmask >> i) & 1u)) continue;
+            float v;
+            if (rec[i] == kMiss) v = mv[i];
+            else if (rec[i] == kBlack) v = 0.f;
+            else v = emission_channel(a.vol, rec[i], ch);
+            Store<T>::store(dst + (i >> 1) * plane + (i & 1) * Mx, v);
+            acc[i][ch] = L0 ? fmaf(om, v, acc[i][ch]) : acc[i][ch] + v;
           }
         }
+        if (!L0 && (k & 3) == 3) {
+          T* A = static_cast<T*>(a.A_out);
+          const int dp = dgroup * 4 + (dl >> 2);
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
-        if (L0) {
-          const float om = a.dirs[d].omega;
+          for (int ch = 0; ch < 3; ++ch) {
+            T* dst = A + ((int64_t)ch * npar + dp) * a.P + p0;
 #pragma unroll
-          for (int ch = 0; ch < 3; ++ch) flu[j][ch] = fmaf(om, rv[ch], flu[j][ch]);
-        } else {
+            for (int i = 0; i < 4; ++i) {
+              if ((okmask >> i) & 1u) Store<T>::store(dst + (i >> 1) * plane + (i & 1) * Mx, 0.25f * acc[i][ch]);
+              acc[i][ch] = 0.f;
+            }
+          }
+        }
+      }
+    } else {
+      const int ndl = L0 ? min(kTileDirs, a.ndirs - pass * kTileDirs) : kTileDirs;
+#pragma unroll 1
+      for (int j = 0; j < 2; ++j) {
+        const int bit = tid + kBitsThreads * j;
+        const int u = bit >> 5, b = bit & 31;
+        if (u >= t.TZ * t.TW) break;
+        const int zl = t.z0 + u / t.TW, wl = t.w0 + u % t.TW;
+        const int g = (wl << 5) + b;
+        const int py = g >> a.l2px, px = g & ((1 << a.l2px) - 1);
+        if (zl >= Mz || wl >= a.wpp || px >= Mx || py >= My) continue;
+        const int64_t p = ((int64_t)zl * My + py) * Mx + px;
+        int tap_off[8];
+        float tap_w[8];
+        if (!TOP) {
+          int q[3][2];
+          float wt[3][2];
+          const int m[3] = {px, py, zl};
 #pragma unroll
-          for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
-          if ((dl & 3) == 3) {
-            T* A = static_cast<T*>(a.A_out);
-            const int dp = dgroup * 4 + (dl >> 2);
-            const int64_t npar = (int64_t)hn * hn;
+          for (int ax = 0; ax < 3; ++ax) {
+            const int lo = (m[ax] - 1) >> 1;
+            wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
+            wt[ax][1] = 1.0f - wt[ax][0];
+            q[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
+            q[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+          }
 #pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
-              acc[ch] = 0.f;
+          for (int tp = 0; tp < 8; ++tp) {
+            const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
+            tap_off[tp] = (q[2][iz] * a.UM[1] + q[1][iy]) * a.UM[0] + q[0][ix];
+            tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
+          }
+        }
+        float qacc[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int dl = 0; dl < ndl; ++dl) {
+          const int d = block_dir<L0>(a, pass, dgroup, dl);
+          const uint32_t rec = s_hit[(dl * kTileSlots + u) * kHitStride + b];
+          float rv[3];
+          if (rec == kMiss) {
+            if (TOP) {
+              rv[0] = rv[1] = rv[2] = 0.f;
+            } else {
+#pragma unroll
+              for (int ch = 0; ch < 3; ++ch) {
+                const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
+                float sum = 0.f;
+#pragma unroll
+                for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
+                rv[ch] = sum;
+              }
+            }
+          } else if (rec == kBlack) {
+            rv[0] = rv[1] = rv[2] = 0.f;
+          } else {
+            voxel_emission(a.vol, rec, rv);
+          }
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
+          if (L0) {
+            const float om = a.dirs[d].omega;
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) acc[j][ch] = fmaf(om, rv[ch], acc[j][ch]);
+          } else {
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) qacc[ch] += rv[ch];
+            if ((dl & 3) == 3) {
+              T* A = static_cast<T*>(a.A_out);
+              const int dp = dgroup * 4 + (dl >> 2);
+#pragma unroll
+              for (int ch = 0; ch < 3; ++ch) {
+                Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * qacc[ch]);
+                qacc[ch] = 0.f;
+              }
             }
           }
         }
@@ -312,17 +492,41 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
     }
     __syncthreads();
   }
+
   if (L0) {
-#pragma unroll 1
-    for (int j = 0; j < 2; ++j) {
-      const int t = tid + kBitsThreads * j;
-      if (t >= TX * kTileRows) break;
-      const int lr = t / TX, b = t - lr * TX;
-      const int r = rowblk * kTileRows + lr;
-      if (r >= rows_total) continue;
-      const int64_t p = ((int64_t)(r / My) * My + r % My) * Mx + 32 * w + b;
+    if (WIDE) {
+      // fluence = (directions of half 0) + (directions of half 1), in that order
+      float* part = reinterpret_cast<float*>(s_hit);
+      if (half == 1) {
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = flu[j][ch];
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) part[((unit * 4 + i) * 3 + ch) * 32 + lane] = acc[i][ch];
+      }
+      __syncthreads();
+      if (half == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (!((okmask >> i) & 1u)) continue;
+          const int64_t p = p0 + (i >> 1) * plane + (i & 1) * Mx;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[i][ch] + part[((unit * 4 + i) * 3 + ch) * 32 + lane];
+        }
+      }
+    } else {
+#pragma unroll 1
+      for (int j = 0; j < 2; ++j) {
+        const int bit = tid + kBitsThreads * j;
+        const int u = bit >> 5, b = bit & 31;
+        if (u >= t.TZ * t.TW) break;
+        const int zl = t.z0 + u / t.TW, wl = t.w0 + u % t.TW;
+        const int g = (wl << 5) + b;
+        const int py = g >> a.l2px, px = g & ((1 << a.l2px) - 1);
+        if (zl >= Mz || wl >= a.wpp || px >= Mx || py >= My) continue;
+        const int64_t p = ((int64_t)zl * My + py) * Mx + px;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[j][ch];
+      }
     }
   }
 }
