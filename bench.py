@@ -238,7 +238,8 @@ def main():
         ms = float(t.item())
         dist.barrier()
     value = world * args.steps / (ms / 1000.0)
-    launches_per_step = 1 + params.num_cascades  # recompose + one kernel per cascade
+    # recompose + one kernel per cascade + the shared walk of the narrow levels
+    launches_per_step = 1 + params.num_cascades + 1
 
     # ---- e2e: public API, host buffers, H2D of the frame's spheres, D2H of the fluence
     nflu = 3 * int(np.prod(eng.probes0))
@@ -287,7 +288,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": traffic,
-                     "kernel": "k_level (one launch per cascade)",
+                     "kernel": "cascade levels: k_level_bits (wide) + k_walk_queue / k_level_merge (narrow)",
                      "algorithmic_bytes_per_frame": B,
                      "level_ms_per_frame": round(level_ms, 4),
                      "per_level_ms": [round(float(x), 4) for x in per_level_ms[1:]],

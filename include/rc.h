@@ -197,8 +197,9 @@ rc_status rc_get_stream(rc_context* ctx, void** out);
 /* Runs `iters` frames on the context stream with CUDA events around every
  * kernel and writes the mean milliseconds per launch: ms_out[0] = scene
  * recomposition under the current spheres (the per-frame emitter update),
- * ms_out[1 + i] = cascade level i.  Needs 1 + num_cascades floats.
- * Synchronises. */
+ * ms_out[1 + i] = cascade level i (the top level's figure includes the one
+ * launch that walks every level with fewer than 32 probes per row).  Needs
+ * 1 + num_cascades floats.  Synchronises. */
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
 

@@ -17,6 +17,7 @@
 #include "rc_internal.h"
 #include "rc_kernels.cuh"
 #include "rc_walk_bits.cuh"
+#include "rc_walk_queue.cuh"
 
 using namespace rcx;
 
@@ -39,7 +40,14 @@ struct rc_context {
   int W = 0;                 // words per x row
   uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
   MaskSet mset{};
-  bool bits_level[kMaxCascades]{};
+  bool bits_level[kMaxCascades]{};   // level has decimated opacity
+  int mode[kMaxCascades]{};          // how the level is solved (kMode*)
+  uint32_t* recs = nullptr;          // walk records of the queue-walked levels
+  unsigned long long* qcounter = nullptr;
+  QueueArgs qargs{};
+  int queue_blocks = 0;
+  int rec_slots[kMaxCascades]{};
+  const uint32_t* rec_level[kMaxCascades]{};
   DirInfo* dirs = nullptr;   // all levels, concatenated
   size_t dir_off[kMaxCascades]{};
   void* rad = nullptr;       // L_i for all levels
@@ -100,7 +108,7 @@ void release(rc_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  void* bufs[] = {c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -204,8 +212,14 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
 
 // Decimated-plane geometry of one level (see rc_walk_bits.cuh).  Levels wider
 // than 256 probes per row walk with the scalar kernel.
+// How a level is solved: the scalar walk (one thread per probe and direction),
+// the fused bit-parallel kernel (wide levels), or the shared walk queue plus a
+// merge kernel (narrow levels).
+enum { kModeScalar = 0, kModeFused = 1, kModeQueue = 2 };
+
 struct MaskGeom {
   bool bits;
+  int mode;
   int32_t l2px, wpp, tiles;
   uint32_t rep;
   int64_t words;
@@ -218,10 +232,12 @@ MaskGeom mask_geom(const LevelGeom& g, bool force_scalar) {
   const int64_t px = (int64_t)1 << m.l2px;
   m.wpp = (int32_t)((g.M[1] * px + 31) / 32);
   m.words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * m.wpp;
-  m.bits = !force_scalar && px <= 256;
+  // the bit-parallel kernel addresses a level's radiance with 32-bit element offsets
+  m.bits = !force_scalar && px <= 256 && 3 * (int64_t)g.ndirs * g.probes() < ((int64_t)1 << 31);
   m.rep = 0;
   if (px < 32)
     for (int r = 0; r < 32 / px; ++r) m.rep |= 1u << (r * px);
+  m.mode = !m.bits ? kModeScalar : (m.l2px >= 5 ? kModeFused : kModeQueue);
   if (m.l2px >= 5) {
     m.tiles = ((g.M[2] + 1) / 2) * ((m.wpp + 15) / 16);
   } else {
@@ -232,56 +248,130 @@ MaskGeom mask_geom(const LevelGeom& g, bool force_scalar) {
 }
 
 template <typename T, bool L0, bool TOP>
-void launch_one(const LevelArgs& a, bool bits, cudaStream_t s) {
-  if (bits) {
-    const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 4);
-    const unsigned blocks = (unsigned)a.tiles * groups;
-    if (a.l2px >= 5) k_level_bits<T, L0, TOP, true><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
-    else k_level_bits<T, L0, TOP, false><<<blocks, kBitsThreads, kBitsSmem, s>>>(a);
-  } else {
-    const int threads = 128;
-    dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
-    k_level_scalar<T, L0, TOP><<<grid, threads, 0, s>>>(a);
+void launch_one(const rc_context* c, int level, cudaStream_t s) {
+  const LevelArgs& a = c->args[level];
+  const int threads = 128;
+  switch (c->mode[level]) {
+    case kModeFused: {
+      const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2);  // two parent texels per block
+      k_level_bits<T, L0, TOP><<<(unsigned)a.tiles * groups, kBitsThreads, kBitsSmem, s>>>(a);
+      break;
+    }
+    case kModeQueue: {
+      dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2));
+      k_level_merge<T, L0, TOP><<<grid, threads, 0, s>>>(a, c->rec_level[level], c->rec_slots[level]);
+      break;
+    }
+    default: {
+      dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2)));
+      k_level_scalar<T, L0, TOP><<<grid, threads, 0, s>>>(a);
+    }
   }
 }
 
 template <typename T>
 void launch_level(const rc_context* c, int level, cudaStream_t s) {
-  const LevelArgs& a = c->args[level];
-  const bool bits = c->bits_level[level];
   const bool top = (level == c->nlev - 1);
   if (level == 0) {
-    if (top) launch_one<T, true, true>(a, bits, s);
-    else launch_one<T, true, false>(a, bits, s);
+    if (top) launch_one<T, true, true>(c, level, s);
+    else launch_one<T, true, false>(c, level, s);
   } else {
-    if (top) launch_one<T, false, true>(a, bits, s);
-    else launch_one<T, false, false>(a, bits, s);
+    if (top) launch_one<T, false, true>(c, level, s);
+    else launch_one<T, false, false>(c, level, s);
   }
 }
 
+// The walks of every queue level, in one launch (they depend only on the scene).
+void launch_queue_walk(const rc_context* c, cudaStream_t s) {
+  if (!c->queue_blocks) return;
+  cudaMemsetAsync(c->qcounter, 0, sizeof(unsigned long long), s);
+  k_walk_queue<<<(unsigned)c->queue_blocks, kQueueThreads, 0, s>>>(c->qargs);
+}
+
 void enqueue_solve(rc_context* c, cudaStream_t s) {
+  launch_queue_walk(c, s);
   for (int i = c->nlev - 1; i >= 0; --i) {
     if (c->elem == 2) launch_level<__half>(c, i, s);
     else launch_level<float>(c, i, s);
   }
 }
 
-template <typename T, bool L0, bool TOP, bool WIDE>
+// Records size of the queue levels, and the queue arguments once `recs` and
+// `counter` are placed.  Levels with the longest in-grid intervals are queued
+// first so that their walks start early.
+size_t queue_records_bytes(const rc_context* c) {
+  size_t total = 0;
+  for (int i = 0; i < c->nlev; ++i)
+    if (c->mode[i] == kModeQueue) total += (size_t)c->geom[i].ndirs * c->rec_slots[i] * 32 * sizeof(uint32_t);
+  return total;
+}
+
+// Resident blocks of the walk kernel on the current device (SMs x blocks per SM).
+int queue_resident_blocks() {
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue, kQueueThreads, 0) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 152 * 2;
+  }
+  return std::max(1, sms * per_sm);
+}
+
+void setup_queue(rc_context* c, uint32_t* recs, unsigned long long* counter) {
+  QueueArgs& q = c->qargs;
+  memset(&q, 0, sizeof q);
+  c->qcounter = counter;
+  q.emis = c->emis;
+  q.counter = counter;
+  for (int a = 0; a < 3; ++a) q.G[a] = c->p.grid[a];
+  q.W = c->W;
+  const double diag = sqrt((double)c->p.grid[0] * c->p.grid[0] + (double)c->p.grid[1] * c->p.grid[1] +
+                           (double)c->p.grid[2] * c->p.grid[2]);
+  int order[kMaxCascades], n = 0;
+  for (int i = 0; i < c->nlev; ++i)
+    if (c->mode[i] == kModeQueue) order[n++] = i;
+  auto reach = [&](int i) {
+    return std::min<double>((double)c->geom[i].bhi, diag) - std::min<double>((double)c->geom[i].blo, diag);
+  };
+  std::sort(order, order + n, [&](int x, int y) { return reach(x) > reach(y); });
+  size_t off = 0;
+  int64_t items = 0;
+  for (int k = 0; k < n; ++k) {
+    const int i = order[k];
+    const LevelArgs& a = c->args[i];
+    QueueLevel& L = q.lv[k];
+    L.mask = a.mask;
+    L.dirs = a.dirs;
+    L.rec = recs + off;
+    c->rec_level[i] = L.rec;
+    off += (size_t)c->geom[i].ndirs * c->rec_slots[i] * 32;
+    L.item_begin = items;
+    items += (int64_t)c->geom[i].ndirs * c->rec_slots[i];
+    L.slots = c->rec_slots[i];
+    L.l2s = a.l2s;
+    L.l2px = a.l2px;
+    L.wpp = a.wpp;
+    for (int ax = 0; ax < 3; ++ax) L.M[ax] = a.M[ax];
+    L.rep = a.rep;
+    L.test_start = (i == 0);
+  }
+  q.n = n;
+  q.total = items;
+  // one resident wave of blocks; every lane refills itself from the queue
+  c->queue_blocks = n ? (int)std::min<int64_t>((items + kQueueThreads - 1) / kQueueThreads, queue_resident_blocks()) : 0;
+}
+
+template <typename T, bool L0, bool TOP>
 cudaError_t allow_one() {
-  return cudaFuncSetAttribute(k_level_bits<T, L0, TOP, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kBitsSmem);
+  return cudaFuncSetAttribute(k_level_bits<T, L0, TOP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBitsSmem);
 }
 
 template <typename T>
 cudaError_t allow_bits_smem() {
-  cudaError_t e = allow_one<T, true, true, true>();
-  if (e == cudaSuccess) e = allow_one<T, true, false, true>();
-  if (e == cudaSuccess) e = allow_one<T, false, true, true>();
-  if (e == cudaSuccess) e = allow_one<T, false, false, true>();
-  if (e == cudaSuccess) e = allow_one<T, true, true, false>();
-  if (e == cudaSuccess) e = allow_one<T, true, false, false>();
-  if (e == cudaSuccess) e = allow_one<T, false, true, false>();
-  if (e == cudaSuccess) e = allow_one<T, false, false, false>();
+  cudaError_t e = allow_one<T, true, true>();
+  if (e == cudaSuccess) e = allow_one<T, true, false>();
+  if (e == cudaSuccess) e = allow_one<T, false, true>();
+  if (e == cudaSuccess) e = allow_one<T, false, false>();
   return e;
 }
 
@@ -366,6 +456,8 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     for (int i = 0; i < c->nlev; ++i) {
       const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
       c->bits_level[i] = mg.bits;
+      c->mode[i] = mg.mode;
+      c->rec_slots[i] = c->geom[i].M[2] * mg.wpp;
       off[i] = total;
       if (mg.bits) total += (mg.words + 63) & ~(int64_t)63;
     }
@@ -409,7 +501,7 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     const LevelGeom& g = c->geom[i];
     memset(&a, 0, sizeof a);
     {
-      const MaskGeom mg = mask_geom(g, !c->bits_level[i]);
+      const MaskGeom mg = mask_geom(g, false);
       for (int k = 0; k < c->mset.n; ++k)
         if (c->mset.lv[k].M[0] == g.M[0] && c->mset.lv[k].M[1] == g.M[1] && (1 << c->mset.lv[k].l2s) == g.spacing)
           a.mask = c->mset.lv[k].base;
@@ -439,6 +531,15 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     a.A_up = (i + 1 < c->nlev) ? static_cast<char*>(c->avg) + c->avg_off[i + 1] : nullptr;
     a.P_up = (i + 1 < c->nlev) ? c->geom[i + 1].probes() : 0;
     a.fluence = c->fluence;
+  }
+  {
+    const size_t rb = queue_records_bytes(c);
+    if (rb) {
+      if ((s = dev_alloc((void**)&c->recs, rb, "walk records")) != RC_OK) return fail(s);
+      if ((s = dev_alloc((void**)&c->qcounter, sizeof(unsigned long long), "walk queue counter")) != RC_OK)
+        return fail(s);
+    }
+    setup_queue(c, c->recs, c->qcounter);
   }
   *out = c;
   return RC_OK;
@@ -664,6 +765,7 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
     cudaEventRecord(ev[0], c->stream);
     if (!regs.empty()) st = recompose(c, regs.data(), (int)regs.size());
     cudaEventRecord(ev[1], c->stream);
+    launch_queue_walk(c, c->stream);  // counted with the top level, which is launched next
     for (int i = c->nlev - 1, k = 2; i >= 0; --i, ++k) {
       if (c->elem == 2) launch_level<__half>(c, i, c->stream);
       else launch_level<float>(c, i, c->stream);
@@ -785,6 +887,8 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   for (int i = 0; i < v.nlev; ++i) {
     mgs[i] = mask_geom(v.geom[i], force_scalar);
     v.bits_level[i] = mgs[i].bits;
+    v.mode[i] = mgs[i].mode;
+    v.rec_slots[i] = v.geom[i].M[2] * mgs[i].wpp;
     if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 4);
   }
   mask_bytes = off - mask_begin;
@@ -794,6 +898,8 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   size_t ndirs_total = 0;
   for (int i = 0; i < v.nlev; ++i) ndirs_total += (size_t)v.geom[i].ndirs;
   const size_t dirs_off = carve(off, ndirs_total * sizeof(DirInfo));
+  const size_t rec_off = carve(off, queue_records_bytes(&v));
+  const size_t counter_off = carve(off, sizeof(unsigned long long));
   if (off > RC_NOALLOC_SCRATCH_BYTES || ndirs_total > kNoallocMaxDirs) {
     rcx::set_error("rc_solve_noalloc: these parameters need %zu bytes of scratch; the static maximum is %u bytes",
                    off, (unsigned)RC_NOALLOC_SCRATCH_BYTES);
@@ -835,6 +941,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
 
   uint32_t* occ = reinterpret_cast<uint32_t*>(scratch + occ_off);
   uint32_t* emis = reinterpret_cast<uint32_t*>(scratch + emis_off);
+  v.emis = emis;
   v.mset.n = 0;
   size_t rad_off = 0;
   for (int i = 0; i < v.nlev; ++i) {
@@ -883,6 +990,8 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   k_masks_from_volume<<<(unsigned)blocks, threads, 0, st>>>(reinterpret_cast<const uint2*>(voxels), occ, emis,
                                                              p->grid[0], p->grid[1], p->grid[2], v.W, v.mset);
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: opacity launch");
+  setup_queue(&v, reinterpret_cast<uint32_t*>(scratch + rec_off),
+              reinterpret_cast<unsigned long long*>(scratch + counter_off));
   enqueue_solve(&v, st);
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: cascade launch");
   return RC_OK;

@@ -22,11 +22,16 @@ template <>
 struct Store<float> {
   static __device__ __forceinline__ float load(const float* p) { return __ldg(p); }
   static __device__ __forceinline__ void store(float* p, float v) { *p = v; }
+  // write-once outputs: evict-first, so they do not push reused data out of L2
+  static __device__ __forceinline__ void stream(float* p, float v) { __stcs(p, v); }
 };
 template <>
 struct Store<__half> {
   static __device__ __forceinline__ float load(const __half* p) { return __half2float(__ldg(p)); }
   static __device__ __forceinline__ void store(__half* p, float v) { *p = __float2half_rn(v); }
+  static __device__ __forceinline__ void stream(__half* p, float v) {
+    __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
+  }
 };
 
 struct LevelArgs {

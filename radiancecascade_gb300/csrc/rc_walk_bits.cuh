@@ -24,7 +24,7 @@
 namespace rcx {
 
 constexpr int kTileSlots = 32;     // words (of 32 probes) per block tile
-constexpr int kTileDirs = 16;      // directions per block pass
+constexpr int kTileDirs = 8;       // directions per block pass
 constexpr int kBitsThreads = kTileSlots * kTileDirs;
 constexpr int kHitStride = 33;     // padded hit-record row (bank spread)
 constexpr uint32_t kMiss = 0xFFFFFFFFu;   // no opaque voxel in the interval
@@ -177,83 +177,116 @@ __device__ __forceinline__ Tile tile_of(const LevelArgs& a, int tile) {
 
 // Phase 1: walk the interval of direction `di` for the 32 probes of plane
 // word `wl` in coarse plane `zl`; record each probe's first opaque voxel.
+// The voxel sequence does not depend on what is loaded, so the walk runs in
+// batches of kWalkBatch steps: the mask words of a whole batch are requested
+// before the first of them is tested.  Level 0's interval is one voxel long,
+// so it walks in batches of 2; the others in batches of 4.
+template <int kWalkBatch>
 __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di, int zl, int wl, bool test_start,
                                           uint32_t* __restrict__ hit) {
   const int s = a.spacing, l2s = a.l2s, h = s >> 1;
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int l2px = a.l2px, Px = 1 << l2px;
+  const bool wide = l2px >= 5;
   const int g0 = wl << 5;  // plane bit of this word's bit 0
+  const int wy0 = g0 >> l2px, wx0 = g0 & (Px - 1);
   // probes that exist: x < Mx, y < My
   uint32_t valid;
-  int wy0 = 0, wx0 = 0;  // row and column of bit 0
-  if (l2px >= 5) {
-    wy0 = g0 >> l2px;
-    wx0 = g0 & (Px - 1);
+  if (wide) {
     valid = wy0 < My ? range_bits(0, Mx - wx0) : 0u;
   } else {
-    wy0 = g0 >> l2px;
-    const uint32_t row = range_bits(0, Mx);  // within Px bits
-    valid = row * a.rep;                      // replicate over the 32/Px rows of the word
+    valid = range_bits(0, Mx) * a.rep;  // the row pattern replicated over the word's 32/Px rows
     valid &= range_bits(0, (My - wy0) * Px);
   }
-  uint32_t done = ~valid;
   if (valid == 0u) return;
+  uint32_t done = ~valid;
+  const uint32_t* zbase = a.mask + (int64_t)zl * a.wpp;
+  const int64_t phase_stride = (int64_t)Mz * a.wpp;
   int ax = h + di.start_off[0], ay = h + di.start_off[1], az = h + di.start_off[2];
   int tx = di.first_T[0], ty = di.first_T[1], tz = di.first_T[2];
   const int sx = di.sgn[0], sy = di.sgn[1], sz = di.sgn[2];
   const int dx = di.step_T[0], dy = di.step_T[1], dz = di.step_T[2];
   int k = di.steps;
-  bool pending_start = test_start;
+  bool first = test_start;
   for (;;) {
-    if (!pending_start) {
-      if (k == 0) break;
-      --k;
-      // branch-free choice of the axis with the nearest crossing (x, then y, then z on ties)
-      const bool bx = (tx <= ty) & (tx <= tz);
-      const bool by = !bx & (ty <= tz);
-      const bool bz = !bx & !by;
-      ax += bx ? sx : 0;
-      tx += bx ? dx : 0;
-      ay += by ? sy : 0;
-      ty += by ? dy : 0;
-      az += bz ? sz : 0;
-      tz += bz ? dz : 0;
+    int bx_[kWalkBatch], by_[kWalkBatch], bz_[kWalkBatch];
+    uint32_t lo_[kWalkBatch], hi_[kWalkBatch];
+    bool ok_[kWalkBatch];
+#pragma unroll
+    for (int u = 0; u < kWalkBatch; ++u) {
+      bool step_ok;
+      if (first) {
+        first = false;
+        step_ok = true;
+      } else if (k > 0) {
+        --k;
+        // branch-free choice of the axis with the nearest crossing (x, then y, then z on ties)
+        const bool px_ = (tx <= ty) & (tx <= tz);
+        const bool py_ = !px_ & (ty <= tz);
+        const bool pz_ = !px_ & !py_;
+        ax += px_ ? sx : 0;
+        tx += px_ ? dx : 0;
+        ay += py_ ? sy : 0;
+        ty += py_ ? dy : 0;
+        az += pz_ ? sz : 0;
+        tz += pz_ ? dz : 0;
+        step_ok = true;
+      } else {
+        step_ok = false;
+      }
+      bx_[u] = ax;
+      by_[u] = ay;
+      bz_[u] = az;
+      const int zc = zl + (az >> l2s);
+      const bool zin = step_ok && (unsigned)zc < (unsigned)Mz;
+      ok_[u] = step_ok;
+      const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
+      const uint32_t* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * a.wpp;
+      const int gs = g0 + (ay >> l2s) * Px + (ax >> l2s);
+      const int q = gs >> 5;
+      lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp) ? __ldg(plane + q) : 0u;
+      hi_[u] = (zin && (unsigned)(q + 1) < (unsigned)a.wpp) ? __ldg(plane + q + 1) : 0u;
     }
-    pending_start = false;
-    const int cz = az >> l2s, cy = ay >> l2s, cx = ax >> l2s;
-    const int zc = zl + cz;
-    if ((unsigned)zc >= (unsigned)Mz) break;  // every probe of the word left the grid
-    // probes whose cell (x + cx, y + cy) is still inside the grid
-    uint32_t inr;
-    if (l2px >= 5) {
-      const int yy = wy0 + cy;
-      inr = ((unsigned)yy < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
-    } else {
-      // column range kept inside the Px-bit row before it is replicated over the rows
-      inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * a.rep;
-      inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+    bool stop = false;
+#pragma unroll
+    for (int u = 0; u < kWalkBatch; ++u) {
+      if (stop) continue;
+      if (!ok_[u]) {
+        stop = true;
+        continue;
+      }
+      const int cz = bz_[u] >> l2s, cy = by_[u] >> l2s, cx = bx_[u] >> l2s;
+      if ((unsigned)(zl + cz) >= (unsigned)Mz) {  // every probe of the word left the grid
+        stop = true;
+        continue;
+      }
+      // probes whose cell (x + cx, y + cy) is still inside the grid
+      uint32_t inr;
+      if (wide) {
+        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+      } else {
+        inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * a.rep;
+        inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+      }
+      done |= ~inr;
+      const int gs = g0 + cy * Px + cx;
+      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs & 31) & ~done;
+      if (nw) {
+        done |= nw;
+        const int vz = (zl << l2s) + bz_[u];
+        do {
+          const int b = __ffs(nw) - 1;
+          nw &= nw - 1;
+          const int g = g0 + b;
+          const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
+          const int64_t row = (int64_t)vz * a.G[1] + vy;
+          const uint32_t e = __ldg(&a.emis[row * a.W + (vx >> 5)]);
+          hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * a.G[0] + vx) : kBlack;
+        } while (nw);
+      }
+      if (done == 0xFFFFFFFFu) stop = true;
     }
-    done |= ~inr;
-    if (done == 0xFFFFFFFFu) break;
-    const uint32_t* plane = a.mask + plane_base_args(a, ax & (s - 1), ay & (s - 1), az & (s - 1), zc);
-    const int gs = g0 + cy * Px + cx;  // plane bit of this word's bit 0 after the shift
-    const int q = gs >> 5, sh = gs & 31;
-    const uint32_t lo = ((unsigned)q < (unsigned)a.wpp) ? __ldg(plane + q) : 0u;
-    const uint32_t hi = ((unsigned)(q + 1) < (unsigned)a.wpp) ? __ldg(plane + q + 1) : 0u;
-    uint32_t nw = __funnelshift_r(lo, hi, sh) & ~done;
-    if (nw) {
-      done |= nw;
-      do {
-        const int b = __ffs(nw) - 1;
-        nw &= nw - 1;
-        const int g = g0 + b;
-        const int vx = ((g & (Px - 1)) << l2s) + ax, vy = ((g >> l2px) << l2s) + ay, vz = (zl << l2s) + az;
-        const int64_t idx = ((int64_t)vz * a.G[1] + vy) * a.G[0] + vx;
-        const uint32_t e = __ldg(&a.emis[((int64_t)vz * a.G[1] + vy) * a.W + (vx >> 5)]);
-        hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)idx : kBlack;
-      } while (nw);
-      if (done == 0xFFFFFFFFu) break;
-    }
+    if (stop) break;
   }
 }
 
@@ -271,23 +304,23 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
     return d < a.ndirs ? d : -1;
   }
   const int hn = a.n >> 1;
-  const int dp = dgroup * 4 + (dl >> 2), c = dl & 3;
+  const int dp = dgroup * 2 + (dl >> 2), c = dl & 3;  // two parent texels per block
   return (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
 }
 
-// Bit-parallel cascade level.  Block = one tile of 32 probe words x 16
-// directions (512 threads).
+// Bit-parallel cascade level for wide levels (>= 32 probes per row).  Block =
+// one tile of 32 probe words x 8 directions (256 threads).
 // Phase 1: warp = direction, lane = word: walk 32 probes per lane, record the
 //   first opaque voxel of each probe (or kMiss / kBlack) in shared memory.
 // Phase 2, WIDE levels (>= 32 probes per row): warp = (32 x-children x 2 y x
-//   2 z block, 8 directions).  Below the top level, missing rays take the
+//   2 z block, all 8 directions).  Below the top level, missing rays take the
 //   trilinear blend of the next level's child-averaged radiance: each lane
 //   loads one parent column (3 x 3 values per channel), interpolates z and y
 //   in registers and x through warp shuffles.
-// Phase 2, narrow levels: thread = probe, per-probe 8-tap gather.
 // Level 0 reduces the fluence; other levels write the 2x2-child averages.
-template <typename T, bool L0, bool TOP, bool WIDE>
-__global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs a) {
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const LevelArgs a) {
+  constexpr bool WIDE = true;  // narrow levels walk through the work queue (rc_walk_queue.cuh)
   extern __shared__ uint32_t s_hit[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tile_id = blockIdx.x % a.tiles;
@@ -300,23 +333,32 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
 
-  // wide: lane's child block (x, y0 + ey, z0 + ez), ey, ez in {0, 1}
-  const int unit = warp & 7, half = warp >> 3;
+  // wide: lane's child block (x, y0 + ey, z0 + ez), ey, ez in {0, 1}.  Element
+  // offsets fit 32 bits (3 * dirs * probes < 2^31 is checked on the host).
+  const int unit = warp;
   const int cl2 = a.l2px - 5;
   const int c = WIDE ? (unit & ((1 << cl2) - 1)) : 0;
   const int y0 = WIDE ? ((t.w0 << 5) >> a.l2px) + 2 * (unit >> cl2) : 0;
   const int x = 32 * c + lane;
-  const int64_t plane = (int64_t)My * Mx;
-  const int64_t p0 = ((int64_t)t.z0 * My + y0) * Mx + x;
+  const int p0 = (t.z0 * My + y0) * Mx + x;
+  const int cstep[4] = {0, Mx, My * Mx, My * Mx + Mx};  // child i = (ez = i >> 1, ey = i & 1)
   const int slot0 = (y0 << cl2) + c - t.w0;
-  unsigned okmask = 0;  // bit i = child (ez = i >> 1, ey = i & 1) exists
+  unsigned okmask = 0;  // bit i = child i exists
   if (WIDE) {
 #pragma unroll
     for (int i = 0; i < 4; ++i)
       if (x < Mx && y0 + (i & 1) < My && t.z0 + (i >> 1) < Mz) okmask |= 1u << i;
   }
-  // wide: parent column of this lane (lanes 0..17 load), rows qy0-1..qy0+1, planes qz0-1..qz0+1
+  // wide: parent column of this lane (lanes 0..17 load); offsets of the 3 x 3
+  // parents (z-1, z, z+1) x (y-1, y, y+1), clamped at the border
   const int qx = min(max(16 * c - 1 + lane, 0), a.UM[0] - 1);
+  int aoff[9];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj)
+      aoff[k * 3 + jj] = (min(max(t.z0 / 2 - 1 + k, 0), a.UM[2] - 1) * a.UM[1] +
+                          min(max(y0 / 2 - 1 + jj, 0), a.UM[1] - 1)) * a.UM[0] + qx;
   const bool ploader = lane < 18;
   const int src_lo = (lane + 1) >> 1;
   const float wlo = (lane & 1) ? 0.75f : 0.25f, whi = 1.0f - wlo;
@@ -335,7 +377,7 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
       const int zl = t.z0 + lane / t.TW, wl = t.w0 + lane % t.TW;
       if (d >= 0 && lane < t.TZ * t.TW && zl < Mz && wl < a.wpp) {
         const DirInfo di = a.dirs[d];
-        walk_word(a, di, zl, wl, L0, hit);
+        walk_word<L0 ? 2 : 4>(a, di, zl, wl, L0, hit);
       }
     }
     __syncthreads();
@@ -343,34 +385,29 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
     if (WIDE) {
 #pragma unroll 1
       for (int k = 0; k < 8; ++k) {
-        const int dl = half * 8 + k;
+        const int dl = k;
         const int d = block_dir<L0>(a, pass, dgroup, dl);
         if (d < 0) break;
         uint32_t rec[4];
-        bool miss = false;
+        unsigned missm = 0, emism = 0;
+        const uint32_t* hrow = s_hit + (dl * kTileSlots + slot0) * kHitStride + lane;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const int sl = slot0 + (i >> 1) * 16 + ((i & 1) << cl2);
-          rec[i] = ((okmask >> i) & 1u) ? s_hit[(dl * kTileSlots + sl) * kHitStride + lane] : kBlack;
-          miss |= rec[i] == kMiss;
+          rec[i] = ((okmask >> i) & 1u) ? hrow[((i >> 1) * 16 + ((i & 1) << cl2)) * kHitStride] : kBlack;
+          missm |= (rec[i] == kMiss) << i;
+          emism |= (rec[i] < kBlack) << i;
         }
-        const bool merge = !TOP && __any_sync(0xFFFFFFFFu, miss);
+        const bool merge = !TOP && __any_sync(0xFFFFFFFFu, missm != 0);
         const float om = L0 ? a.dirs[d].omega : 0.f;
-#pragma unroll 1
+        float val[4][3];
+#pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
           float mv[4] = {0.f, 0.f, 0.f, 0.f};
           if (merge) {
-            const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
+            const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
             float av[9];
 #pragma unroll
-            for (int kz = 0; kz < 3; ++kz) {
-              const int qz = min(max(t.z0 / 2 - 1 + kz, 0), a.UM[2] - 1);
-#pragma unroll
-              for (int jy = 0; jy < 3; ++jy) {
-                const int qy = min(max(y0 / 2 - 1 + jy, 0), a.UM[1] - 1);
-                av[kz * 3 + jy] = ploader ? Store<T>::load(src + (qz * a.UM[1] + qy) * a.UM[0] + qx) : 0.f;
-              }
-            }
+            for (int q = 0; q < 9; ++q) av[q] = ploader ? Store<T>::load(src + aoff[q]) : 0.f;
 #pragma unroll
             for (int ez = 0; ez < 2; ++ez) {
               float zv[3];
@@ -385,106 +422,33 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
               mv[ez * 2 + 1] = fmaf(wlo, l1, whi * h1);
             }
           }
-          T* dst = L + ((int64_t)ch * a.ndirs + d) * a.P + p0;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) val[i][ch] = ((missm >> i) & 1u) ? mv[i] : 0.f;
+        }
+        if (emism) {  // emissive hits are rare: patch them in
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if ((emism >> i) & 1u) voxel_emission(a.vol, rec[i], val[i]);
+        }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          T* dst = L + (ch * a.ndirs + d) * (int)a.P + p0;
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
-            if (!((okmask >> i) & 1u)) continue;
-            float v;
-            if (rec[i] == kMiss) v = mv[i];
-            else if (rec[i] == kBlack) v = 0.f;
-            else v = emission_channel(a.vol, rec[i], ch);
-            Store<T>::store(dst + (i >> 1) * plane + (i & 1) * Mx, v);
-            acc[i][ch] = L0 ? fmaf(om, v, acc[i][ch]) : acc[i][ch] + v;
+            if ((okmask >> i) & 1u) Store<T>::stream(dst + cstep[i], val[i][ch]);
+            acc[i][ch] = L0 ? fmaf(om, val[i][ch], acc[i][ch]) : acc[i][ch] + val[i][ch];
           }
         }
         if (!L0 && (k & 3) == 3) {
           T* A = static_cast<T*>(a.A_out);
-          const int dp = dgroup * 4 + (dl >> 2);
+          const int dp = dgroup * 2 + (dl >> 2);
 #pragma unroll
           for (int ch = 0; ch < 3; ++ch) {
-            T* dst = A + ((int64_t)ch * npar + dp) * a.P + p0;
+            T* dst = A + (ch * (int)npar + dp) * (int)a.P + p0;
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-              if ((okmask >> i) & 1u) Store<T>::store(dst + (i >> 1) * plane + (i & 1) * Mx, 0.25f * acc[i][ch]);
+              if ((okmask >> i) & 1u) Store<T>::store(dst + cstep[i], 0.25f * acc[i][ch]);
               acc[i][ch] = 0.f;
-            }
-          }
-        }
-      }
-    } else {
-      const int ndl = L0 ? min(kTileDirs, a.ndirs - pass * kTileDirs) : kTileDirs;
-#pragma unroll 1
-      for (int j = 0; j < 2; ++j) {
-        const int bit = tid + kBitsThreads * j;
-        const int u = bit >> 5, b = bit & 31;
-        if (u >= t.TZ * t.TW) break;
-        const int zl = t.z0 + u / t.TW, wl = t.w0 + u % t.TW;
-        const int g = (wl << 5) + b;
-        const int py = g >> a.l2px, px = g & ((1 << a.l2px) - 1);
-        if (zl >= Mz || wl >= a.wpp || px >= Mx || py >= My) continue;
-        const int64_t p = ((int64_t)zl * My + py) * Mx + px;
-        int tap_off[8];
-        float tap_w[8];
-        if (!TOP) {
-          int q[3][2];
-          float wt[3][2];
-          const int m[3] = {px, py, zl};
-#pragma unroll
-          for (int ax = 0; ax < 3; ++ax) {
-            const int lo = (m[ax] - 1) >> 1;
-            wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
-            wt[ax][1] = 1.0f - wt[ax][0];
-            q[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
-            q[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
-          }
-#pragma unroll
-          for (int tp = 0; tp < 8; ++tp) {
-            const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
-            tap_off[tp] = (q[2][iz] * a.UM[1] + q[1][iy]) * a.UM[0] + q[0][ix];
-            tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
-          }
-        }
-        float qacc[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
-        for (int dl = 0; dl < ndl; ++dl) {
-          const int d = block_dir<L0>(a, pass, dgroup, dl);
-          const uint32_t rec = s_hit[(dl * kTileSlots + u) * kHitStride + b];
-          float rv[3];
-          if (rec == kMiss) {
-            if (TOP) {
-              rv[0] = rv[1] = rv[2] = 0.f;
-            } else {
-#pragma unroll
-              for (int ch = 0; ch < 3; ++ch) {
-                const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-                float sum = 0.f;
-#pragma unroll
-                for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
-                rv[ch] = sum;
-              }
-            }
-          } else if (rec == kBlack) {
-            rv[0] = rv[1] = rv[2] = 0.f;
-          } else {
-            voxel_emission(a.vol, rec, rv);
-          }
-#pragma unroll
-          for (int ch = 0; ch < 3; ++ch) Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
-          if (L0) {
-            const float om = a.dirs[d].omega;
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) acc[j][ch] = fmaf(om, rv[ch], acc[j][ch]);
-          } else {
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) qacc[ch] += rv[ch];
-            if ((dl & 3) == 3) {
-              T* A = static_cast<T*>(a.A_out);
-              const int dp = dgroup * 4 + (dl >> 2);
-#pragma unroll
-              for (int ch = 0; ch < 3; ++ch) {
-                Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * qacc[ch]);
-                qacc[ch] = 0.f;
-              }
             }
           }
         }
@@ -495,37 +459,12 @@ __global__ void __launch_bounds__(kBitsThreads, 2) k_level_bits(const LevelArgs 
 
   if (L0) {
     if (WIDE) {
-      // fluence = (directions of half 0) + (directions of half 1), in that order
-      float* part = reinterpret_cast<float*>(s_hit);
-      if (half == 1) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 4; ++i) {
+        if (!((okmask >> i) & 1u)) continue;
+        const int64_t p = p0 + cstep[i];
 #pragma unroll
-          for (int ch = 0; ch < 3; ++ch) part[((unit * 4 + i) * 3 + ch) * 32 + lane] = acc[i][ch];
-      }
-      __syncthreads();
-      if (half == 0) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          if (!((okmask >> i) & 1u)) continue;
-          const int64_t p = p0 + (i >> 1) * plane + (i & 1) * Mx;
-#pragma unroll
-          for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[i][ch] + part[((unit * 4 + i) * 3 + ch) * 32 + lane];
-        }
-      }
-    } else {
-#pragma unroll 1
-      for (int j = 0; j < 2; ++j) {
-        const int bit = tid + kBitsThreads * j;
-        const int u = bit >> 5, b = bit & 31;
-        if (u >= t.TZ * t.TW) break;
-        const int zl = t.z0 + u / t.TW, wl = t.w0 + u % t.TW;
-        const int g = (wl << 5) + b;
-        const int py = g >> a.l2px, px = g & ((1 << a.l2px) - 1);
-        if (zl >= Mz || wl >= a.wpp || px >= Mx || py >= My) continue;
-        const int64_t p = ((int64_t)zl * My + py) * Mx + px;
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[j][ch];
+        for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[i][ch];
       }
     }
   }

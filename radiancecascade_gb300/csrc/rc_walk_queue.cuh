@@ -1,0 +1,317 @@
+// rc_walk_queue.cuh -- load-balanced interval walks for the narrow cascade
+// levels (fewer than 32 probes per row), and their merge kernel (sm_103a).
+//
+// At a narrow level one lane still walks a 32-probe word of the decimated
+// opacity (see rc_walk_bits.cuh), but the level has few probes and long
+// intervals, so the walks of one direction vary widely in length: a warp that
+// owns a direction runs as long as its slowest word.  Here every
+// (level, direction, word) is an item of one work queue over all narrow
+// levels; a lane that finishes takes the next item, so lanes stay busy.  The
+// walks depend only on the scene, never on another level, so all narrow
+// levels walk in one launch; their first-hit records go to a small global
+// buffer (L2-resident) that k_level_merge reads in the usual top-down order.
+//
+// Record layout of a level: rec[d][slot][32], slot = zc * wpp + word, one
+// 32-bit entry per probe: the hit voxel's linear index (emissive hit), kBlack
+// (opaque voxel without emission) or kMiss.
+#pragma once
+
+#include "rc_walk_bits.cuh"
+
+namespace rcx {
+
+struct QueueLevel {
+  const uint32_t* mask;
+  const DirInfo* dirs;
+  uint32_t* rec;
+  int64_t item_begin;  // first queue item of this level
+  int32_t slots;       // M[2] * wpp words per direction
+  int32_t l2s, l2px, wpp;
+  int32_t M[3];
+  uint32_t rep;
+  int32_t test_start;  // level 0: the probe's own voxel belongs to the interval
+  int32_t pad;
+};
+
+struct QueueArgs {
+  const uint32_t* emis;
+  unsigned long long* counter;  // zeroed before every launch
+  int64_t total;                // items over all levels
+  int32_t G[3];
+  int32_t W;
+  int32_t n;
+  int32_t pad;
+  QueueLevel lv[kMaxCascades];
+};
+
+// One lane's walk of one queue item, advanced kWalkBatch steps at a time.
+struct Walker {
+  const uint32_t* mask;
+  uint32_t* rec;
+  int l2s, l2px, wpp, Mx, My, Mz;
+  uint32_t rep;
+  int zl, g0, wy0, wx0;
+  uint32_t valid, done, hits;
+  int ax, ay, az, tx, ty, tz, k;
+  int sx, sy, sz, dx, dy, dz;
+  bool first;
+
+  // Returns false when the item holds no probe.
+  __device__ __forceinline__ bool init(const QueueArgs& q, int64_t item) {
+    int li = 0;
+    while (li + 1 < q.n && item >= q.lv[li + 1].item_begin) ++li;
+    const QueueLevel& L = q.lv[li];
+    const int64_t r = item - L.item_begin;
+    const int d = (int)(r / L.slots), slot = (int)(r - (int64_t)d * L.slots);
+    mask = L.mask;
+    l2s = L.l2s;
+    l2px = L.l2px;
+    wpp = L.wpp;
+    Mx = L.M[0];
+    My = L.M[1];
+    Mz = L.M[2];
+    rep = L.rep;
+    zl = slot / wpp;
+    const int wl = slot - zl * wpp;
+    g0 = wl << 5;
+    const int Px = 1 << l2px;
+    wy0 = g0 >> l2px;
+    wx0 = g0 & (Px - 1);
+    if (l2px >= 5) {
+      valid = wy0 < My ? range_bits(0, Mx - wx0) : 0u;
+    } else {
+      valid = range_bits(0, Mx) * rep;
+      valid &= range_bits(0, (My - wy0) * Px);
+    }
+    if (valid == 0u) return false;
+    rec = L.rec + ((int64_t)d * L.slots + slot) * 32;
+    done = ~valid;
+    hits = 0u;
+    const DirInfo di = L.dirs[d];
+    const int h = 1 << (l2s - 1);
+    ax = h + di.start_off[0];
+    ay = h + di.start_off[1];
+    az = h + di.start_off[2];
+    tx = di.first_T[0];
+    ty = di.first_T[1];
+    tz = di.first_T[2];
+    sx = di.sgn[0];
+    sy = di.sgn[1];
+    sz = di.sgn[2];
+    dx = di.step_T[0];
+    dy = di.step_T[1];
+    dz = di.step_T[2];
+    k = di.steps;
+    first = L.test_start != 0;
+    return true;
+  }
+
+  // Walks up to kBatch steps; returns true when the item is finished.
+  template <int kBatch>
+  __device__ __forceinline__ bool batch(const QueueArgs& q) {
+    const int s = 1 << l2s, Px = 1 << l2px;
+    const int64_t phase_stride = (int64_t)Mz * wpp;
+    const uint32_t* zbase = mask + (int64_t)zl * wpp;
+    int bx_[kBatch], by_[kBatch], bz_[kBatch];
+    uint32_t lo_[kBatch], hi_[kBatch];
+    bool ok_[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      bool step_ok;
+      if (first) {
+        first = false;
+        step_ok = true;
+      } else if (k > 0) {
+        --k;
+        const bool px_ = (tx <= ty) & (tx <= tz);
+        const bool py_ = !px_ & (ty <= tz);
+        const bool pz_ = !px_ & !py_;
+        ax += px_ ? sx : 0;
+        tx += px_ ? dx : 0;
+        ay += py_ ? sy : 0;
+        ty += py_ ? dy : 0;
+        az += pz_ ? sz : 0;
+        tz += pz_ ? dz : 0;
+        step_ok = true;
+      } else {
+        step_ok = false;
+      }
+      bx_[u] = ax;
+      by_[u] = ay;
+      bz_[u] = az;
+      ok_[u] = step_ok;
+      const int zc = zl + (az >> l2s);
+      const bool zin = step_ok && (unsigned)zc < (unsigned)Mz;
+      const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
+      const uint32_t* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * wpp;
+      const int q0 = (g0 + (ay >> l2s) * Px + (ax >> l2s)) >> 5;
+      lo_[u] = (zin && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
+      hi_[u] = (zin && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      if (!ok_[u]) return true;
+      const int cz = bz_[u] >> l2s, cy = by_[u] >> l2s, cx = bx_[u] >> l2s;
+      if ((unsigned)(zl + cz) >= (unsigned)Mz) return true;
+      uint32_t inr;
+      if (l2px >= 5) {
+        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+      } else {
+        inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * rep;
+        inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+      }
+      done |= ~inr;
+      const int gs = g0 + cy * Px + cx;
+      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs & 31) & ~done;
+      if (nw) {
+        done |= nw;
+        hits |= nw;
+        const int vz = (zl << l2s) + bz_[u];
+        do {
+          const int b = __ffs(nw) - 1;
+          nw &= nw - 1;
+          const int g = g0 + b;
+          const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
+          const int64_t row = (int64_t)vz * q.G[1] + vy;
+          const uint32_t e = __ldg(&q.emis[row * q.W + (vx >> 5)]);
+          rec[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+        } while (nw);
+      }
+      if (done == 0xFFFFFFFFu) return true;
+    }
+    return false;
+  }
+
+  __device__ __forceinline__ void finish() {
+    uint32_t m = valid & ~hits;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      rec[b] = kMiss;
+    }
+  }
+};
+
+constexpr int kQueueThreads = 256;
+
+__global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const QueueArgs q) {
+  const int lane = threadIdx.x & 31;
+  Walker w;
+  bool active = false, exhausted = false;
+  for (;;) {
+    const unsigned need = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(q.counter, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xFFFFFFFFu, base, leader);
+      if (!active && !exhausted) {
+        const int64_t item = (int64_t)base + __popc(need & ((1u << lane) - 1u));
+        if (item >= q.total) exhausted = true;
+        else active = w.init(q, item);
+      }
+    }
+    if (!__any_sync(0xFFFFFFFFu, active)) {
+      if (!__any_sync(0xFFFFFFFFu, !exhausted)) break;
+      continue;
+    }
+    if (active && w.batch<4>(q)) {
+      w.finish();
+      active = false;
+    }
+  }
+}
+
+// Merge of a narrow level from its walk records.  One thread per probe; the
+// block row blockIdx.y covers two parent texels (eight child directions), or
+// at level 0 every direction and the fluence.  Rays without a hit take the
+// trilinear blend of the 8 nearest next-level probes of the child-averaged
+// radiance (child index m sits at parent coordinate m/2 - 1/4, clamped).
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const uint32_t* __restrict__ rec,
+                                                     int slots) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  const int Mx = a.M[0], My = a.M[1];
+  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  const int g = (my << a.l2px) + mx;
+  const int64_t rbase = (int64_t)(mz * a.wpp + (g >> 5)) * 32 + (g & 31);
+  int tap_off[8];
+  float tap_w[8];
+  if (!TOP) {
+    int qq[3][2];
+    float wt[3][2];
+    const int m[3] = {mx, my, mz};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const int lo = (m[ax] - 1) >> 1;
+      wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
+      wt[ax][1] = 1.0f - wt[ax][0];
+      qq[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
+      qq[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+    }
+#pragma unroll
+    for (int tp = 0; tp < 8; ++tp) {
+      const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
+      tap_off[tp] = (qq[2][iz] * a.UM[1] + qq[1][iy]) * a.UM[0] + qq[0][ix];
+      tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
+    }
+  }
+  T* L = static_cast<T*>(a.L);
+  const T* Au = static_cast<const T*>(a.A_up);
+  const int hn = a.n >> 1;
+  const int64_t npar = (int64_t)hn * hn;
+  const int ndl = L0 ? a.ndirs : 8;
+  float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int dl = 0; dl < ndl; ++dl) {
+    int d;
+    if (L0) {
+      d = dl;
+    } else {
+      const int dp = blockIdx.y * 2 + (dl >> 2), c = dl & 3;
+      d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
+    }
+    const uint32_t r = __ldg(&rec[(int64_t)d * slots * 32 + rbase]);
+    float rv[3] = {0.f, 0.f, 0.f};
+    if (r == kMiss) {
+      if (!TOP) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
+          float sum = 0.f;
+#pragma unroll
+          for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
+          rv[ch] = sum;
+        }
+      }
+    } else if (r != kBlack) {
+      voxel_emission(a.vol, r, rv);
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) Store<T>::stream(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
+    if (L0) {
+      const float om = a.dirs[d].omega;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) acc[ch] = fmaf(om, rv[ch], acc[ch]);
+    } else {
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
+      if ((dl & 3) == 3) {
+        T* A = static_cast<T*>(a.A_out);
+        const int dp = blockIdx.y * 2 + (dl >> 2);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
+          acc[ch] = 0.f;
+        }
+      }
+    }
+  }
+  if (L0) {
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
+  }
+}
+
+}  // namespace rcx
