@@ -6,6 +6,8 @@
 // calls rc_create/rc_destroy from resize(), rc_scene_* from update() and
 // rc_solve from render(); see include/rc.h.
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdlib.h>
 #include <string.h>
@@ -18,6 +20,7 @@
 #include "rc_kernels.cuh"
 #include "rc_walk_bits.cuh"
 #include "rc_walk_queue.cuh"
+#include "rc_level0.cuh"
 
 using namespace rcx;
 
@@ -48,6 +51,9 @@ struct rc_context {
   int queue_blocks = 0;
   int rec_slots[kMaxCascades]{};
   const uint32_t* rec_level[kMaxCascades]{};
+  CUtensorMap tma0{};                // cascade 1's child-averaged radiance, for k_level0_tma
+  int tma0_py = 0;
+  int* err = nullptr;                // device error flag set by bounded waits
   DirInfo* dirs = nullptr;   // all levels, concatenated
   size_t dir_off[kMaxCascades]{};
   void* rad = nullptr;       // L_i for all levels
@@ -108,7 +114,7 @@ void release(rc_context* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -215,7 +221,7 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
 // How a level is solved: the scalar walk (one thread per probe and direction),
 // the fused bit-parallel kernel (wide levels), or the shared walk queue plus a
 // merge kernel (narrow levels).
-enum { kModeScalar = 0, kModeFused = 1, kModeQueue = 2 };
+enum { kModeScalar = 0, kModeFused = 1, kModeQueue = 2, kModeDirect0 = 3, kModeTma0 = 4 };
 
 struct MaskGeom {
   bool bits;
@@ -237,14 +243,79 @@ MaskGeom mask_geom(const LevelGeom& g, bool force_scalar) {
   m.rep = 0;
   if (px < 32)
     for (int r = 0; r < 32 / px; ++r) m.rep |= 1u << (r * px);
-  m.mode = !m.bits ? kModeScalar : (m.l2px >= 5 ? kModeFused : kModeQueue);
   if (m.l2px >= 5) {
     m.tiles = ((g.M[2] + 1) / 2) * ((m.wpp + 15) / 16);
   } else {
     const int tw = std::min(m.wpp, 32), tz = std::max(1, 32 / tw);
     m.tiles = ((g.M[2] + tz - 1) / tz) * ((m.wpp + tw - 1) / tw);
   }
+  m.mode = !m.bits ? kModeScalar : (m.l2px >= 5 ? kModeFused : kModeQueue);
   return m;
+}
+
+// Cascade 0 needs no walk when its every interval holds only the start voxel
+// (see rc_level0.cuh); then k_level0_direct solves it.
+bool level0_direct(const rc_params& p, const LevelGeom& g0, bool force_scalar) {
+  return !force_scalar && g0.spacing == 2 && g0.M[0] % 4 == 0 && max_level_steps(g0, p.grid) == 0;
+}
+
+
+
+// cuTensorMapEncodeTiled, reached through the runtime (no libcuda link).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    else
+      (void)cudaGetLastError();
+  }
+  return fn;
+}
+
+// Cascade 0 through k_level0_tma: the walk-free cascade 0 with its parent
+// tiles staged by TMA.  Needs a tensor map over cascade 1's child-averaged
+// radiance viewed as [3 * dirs0 * UMz][UMy][UMx] with 16-byte aligned rows.
+bool setup_tma0(rc_context* c) {
+  if (c->nlev < 2 || c->mode[0] != kModeDirect0) return false;
+  const LevelArgs& a = c->args[0];
+  const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
+  const size_t es = c->elem;
+  if (UMx < 2 || UMx > 256 || (UMx * es) % 16 != 0) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const int py = std::min(6, UMy);
+  cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
+  cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
+  cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)py, 3};
+  cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = enc(&c->tma0, es == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                         const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  c->tma0_py = py;
+  c->mode[0] = kModeTma0;
+  return true;
+}
+
+// Reads and clears the device error flag; a bounded wait that ran out
+// becomes RC_ERR_TIMEOUT.
+rc_status check_device_error(rc_context* c, const char* fn) {
+  if (!c->err) return RC_OK;
+  int flag = 0;
+  cudaError_t e = cudaMemcpy(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, fn);
+  if (flag) {
+    cudaMemset(c->err, 0, sizeof(int));
+    rcx::set_error("%s: a bounded device-side wait ran out (results of that solve are incomplete)", fn);
+    return RC_ERR_TIMEOUT;
+  }
+  return RC_OK;
 }
 
 template <typename T, bool L0, bool TOP>
@@ -255,6 +326,23 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
     case kModeFused: {
       const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2);  // two parent texels per block
       k_level_bits<T, L0, TOP><<<(unsigned)a.tiles * groups, kBitsThreads, kBitsSmem, s>>>(a);
+      break;
+    }
+    case kModeTma0: {
+      if (L0 && !TOP) {
+        const int yblocks = (a.M[1] + kL0TmaRows - 1) / kL0TmaRows;
+        const unsigned blocks = (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + 1) / 2));
+        // two 128-byte aligned stages, two mbarriers, and up to 127 bytes to align the base
+        const size_t stage = ((size_t)3 * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127;
+        k_level0_tma<T><<<blocks, kL0Threads, 2 * stage + 16 + 128, s>>>(a, c->tma0, c->tma0_py, c->err);
+      }
+      break;
+    }
+    case kModeDirect0: {
+      if (L0) {
+        const int64_t warps = (int64_t)((a.M[0] + 127) / 128) * a.M[1] * ((a.M[2] + 1) / 2);
+        k_level0_direct<T, TOP><<<(unsigned)((warps * 32 + kL0Threads - 1) / kL0Threads), kL0Threads, 0, s>>>(a);
+      }
       break;
     }
     case kModeQueue: {
@@ -456,7 +544,7 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     for (int i = 0; i < c->nlev; ++i) {
       const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
       c->bits_level[i] = mg.bits;
-      c->mode[i] = mg.mode;
+      c->mode[i] = (i == 0 && level0_direct(*p, c->geom[0], force_scalar)) ? kModeDirect0 : mg.mode;
       c->rec_slots[i] = c->geom[i].M[2] * mg.wpp;
       off[i] = total;
       if (mg.bits) total += (mg.words + 63) & ~(int64_t)63;
@@ -541,6 +629,9 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     }
     setup_queue(c, c->recs, c->qcounter);
   }
+  if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);
+  if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
+  if (!(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) setup_tma0(c);
   *out = c;
   return RC_OK;
 }
@@ -669,7 +760,7 @@ rc_status rc_synchronize(rc_context* c) {
   if (check_ctx(c, "rc_synchronize") != RC_OK) return RC_ERR_INVALID_ARG;
   DeviceGuard g(c->device);
   RC_CUDA(cudaStreamSynchronize(c->stream), "rc_synchronize");
-  return RC_OK;
+  return check_device_error(c, "rc_synchronize");
 }
 
 static rc_status copy_out(rc_context* c, void* out, const void* src, size_t bytes, int32_t where, const char* fn) {
@@ -682,7 +773,7 @@ static rc_status copy_out(rc_context* c, void* out, const void* src, size_t byte
                           c->stream),
           fn);
   RC_CUDA(cudaStreamSynchronize(c->stream), fn);
-  return RC_OK;
+  return check_device_error(c, fn);
 }
 
 rc_status rc_get_fluence(rc_context* c, float* out, int64_t elems, int32_t where) {
@@ -887,7 +978,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   for (int i = 0; i < v.nlev; ++i) {
     mgs[i] = mask_geom(v.geom[i], force_scalar);
     v.bits_level[i] = mgs[i].bits;
-    v.mode[i] = mgs[i].mode;
+    v.mode[i] = (i == 0 && level0_direct(*p, v.geom[0], force_scalar)) ? kModeDirect0 : mgs[i].mode;
     v.rec_slots[i] = v.geom[i].M[2] * mgs[i].wpp;
     if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 4);
   }

@@ -145,6 +145,24 @@ bool build_dir_table(const LevelGeom& g, const int32_t grid[3], DirInfo* out, ch
   return true;
 }
 
+int64_t max_level_steps(const LevelGeom& g, const int32_t grid[3]) {
+  const double diag = sqrt((double)grid[0] * grid[0] + (double)grid[1] * grid[1] + (double)grid[2] * grid[2]);
+  const int64_t reach = (int64_t)ceil(diag) + 1;
+  const int64_t blo = std::min<int64_t>(g.blo, reach), bhi = std::min<int64_t>(g.bhi, reach);
+  int64_t best = 0;
+  for (int k = 0; k < g.n; ++k)
+    for (int j = 0; j < g.n; ++j) {
+      int64_t D[3];
+      oct_dir(g.n, j, k, D);
+      const int64_t A[3] = {D[0] < 0 ? -D[0] : D[0], D[1] < 0 ? -D[1] : D[1], D[2] < 0 ? -D[2] : D[2]};
+      const int64_t S = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+      int64_t steps = 0;
+      for (int a = 0; a < 3; ++a) steps += crossings(bhi, A[a], S) - crossings(blo, A[a], S);
+      best = std::max(best, steps);
+    }
+  return best;
+}
+
 void quantise_sphere(const rc_sphere& s, QSphere* q) {
   memset(q, 0, sizeof *q);
   for (int a = 0; a < 3; ++a) q->c[a] = llround(s.centre[a] * 256.0);

@@ -75,6 +75,8 @@ void level_geometry(const rc_params& p, LevelGeom* out);  // out[num_cascades]
 // Fills the direction table of one level; returns false (with msg) when the
 // integer walk would leave the exact 32-bit range.
 bool build_dir_table(const LevelGeom& g, const int32_t grid[3], DirInfo* out, char* msg, size_t cap);
+// Largest number of voxel crossings any direction of the level takes.
+int64_t max_level_steps(const LevelGeom& g, const int32_t grid[3]);
 void quantise_sphere(const rc_sphere& s, QSphere* q);
 // Bounding region (whole x-words, clipped to the grid) of a quantised sphere.
 bool sphere_region(const QSphere& q, const int32_t grid[3], Region* r);

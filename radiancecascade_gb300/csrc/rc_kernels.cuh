@@ -34,6 +34,9 @@ struct Store<__half> {
   }
 };
 
+__device__ __forceinline__ float to_float(float v) { return v; }
+__device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
+
 struct LevelArgs {
   const uint32_t* mask;  // this level's decimated opacity (bit-parallel walk)
   const uint32_t* emis;  // full-resolution emissive bits, same layout as occ
@@ -98,6 +101,12 @@ __device__ __forceinline__ void voxel_emission(const uint2* __restrict__ vol, in
   r[0] = __half2float(__ushort_as_half((unsigned short)(v.x & 0xFFFFu)));
   r[1] = __half2float(__ushort_as_half((unsigned short)(v.x >> 16)));
   r[2] = __half2float(__ushort_as_half((unsigned short)(v.y & 0xFFFFu)));
+}
+
+__device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol, uint32_t idx, int ch) {
+  const uint2 v = __ldg(&vol[idx]);
+  const uint32_t w = ch == 2 ? v.y : v.x;
+  return __half2float(__ushort_as_half((unsigned short)(ch == 1 ? (w >> 16) : (w & 0xFFFFu))));
 }
 
 // One thread per probe.  Level 0 (L0) walks every direction and reduces the

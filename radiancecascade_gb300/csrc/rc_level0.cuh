@@ -1,0 +1,424 @@
+// rc_level0.cuh -- cascade 0 without a walk (sm_103a).
+//
+// With the default cascade shape every cascade-0 interval [0, b_1) holds only
+// the voxel the ray starts in (the walk tables give 0 crossings for every
+// direction).  That voxel is one of the 8 around the probe's lattice-point
+// centre, picked by the signs of the direction (start_off in {-1, 0}^3).  So
+// cascade 0 reads the opacity and emissive bits of those 8 voxels once per
+// probe and spends the rest on the merge with cascade 1 and the output
+// stores, which bound it.
+//
+// Mapping: one warp = 128 consecutive x-probes of one y row and two z planes;
+// lane l owns probes x0 = 4l .. 4l+3 (float4 stores).  The trilinear merge
+// reads, per parent row, the float2 of parent columns (2l', 2l'+1) and gets
+// columns 2l'-1 and 2l'+2 from the neighbouring lanes.
+#pragma once
+
+#include "rc_kernels.cuh"
+#include "rc_tma.cuh"
+
+namespace rcx {
+
+constexpr int kL0Threads = 256;
+
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  static __device__ __forceinline__ void stream(float* p, float a, float b, float c, float d) {
+    __stcs(reinterpret_cast<float4*>(p), make_float4(a, b, c, d));
+  }
+};
+template <>
+struct Vec4<__half> {
+  static __device__ __forceinline__ void stream(__half* p, float a, float b, float c, float d) {
+    const __half2 lo = __floats2half2_rn(a, b), hi = __floats2half2_rn(c, d);
+    uint2 u;
+    u.x = *reinterpret_cast<const uint32_t*>(&lo);
+    u.y = *reinterpret_cast<const uint32_t*>(&hi);
+    __stcs(reinterpret_cast<uint2*>(p), u);
+  }
+};
+
+template <typename T>
+__device__ __forceinline__ float2 load2(const T* p);
+template <>
+__device__ __forceinline__ float2 load2<float>(const float* p) {
+  return __ldg(reinterpret_cast<const float2*>(p));
+}
+template <>
+__device__ __forceinline__ float2 load2<__half>(const __half* p) {
+  return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+}
+
+// Requires (checked on the host): probe spacing 2 (centres 2m+1, so the 8
+// candidate voxels are 2m, 2m+1 per axis), every cascade-0 direction takes 0
+// steps, and M[0] % 4 == 0.
+template <typename T, bool TOP>
+__global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const LevelArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
+  const int chunks = (Mx + 127) >> 7;
+  int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int cw = (int)(wid % chunks);
+  wid /= chunks;
+  const int y = (int)(wid % My);
+  const int z0 = 2 * (int)(wid / My);
+  if (z0 >= Mz) return;  // whole warp
+  const int lq = 32 * cw + lane;  // quad index along x
+  const int x0 = 4 * lq;
+  const bool active = x0 < Mx;
+  const bool zok1 = z0 + 1 < Mz;
+
+  // Opacity and emissive bits of the 8 voxels around each of the lane's 4
+  // probes in both planes: voxel rows (2y + oy, 2z + oz), x bits 8*lq .. 8*lq+7.
+  uint32_t ow[2] = {0u, 0u}, ew[2] = {0u, 0u};  // [zc]: byte (oz * 2 + oy)
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int zc = r >> 2, oz = (r >> 1) & 1, oy = r & 1;
+    const int vz = 2 * (z0 + zc) + oz, vy = 2 * y + oy;
+    if (active && (zc == 0 || zok1)) {
+      const int64_t w = ((int64_t)vz * a.G[1] + vy) * a.W + ((8 * lq) >> 5);
+      const int sh = (8 * lq) & 31;
+      ow[zc] |= ((__ldg(&a.occ[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+      ew[zc] |= ((__ldg(&a.emis[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+    }
+  }
+
+  // For each of the 8 octants o = ox + 2 oy + 4 oz (the start voxel's offset
+  // from the probe's lower corner), the 8-bit masks of the lane's children
+  // (bit zc * 4 + e) whose start voxel is opaque / emissive.
+  uint32_t oct_opq[2] = {0u, 0u}, oct_ems[2] = {0u, 0u};
+#pragma unroll
+  for (int o = 0; o < 8; ++o) {
+    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
+    uint32_t mo = 0, me = 0;
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      const uint32_t ob = (ow[zc] >> (8 * (oz * 2 + oy))) & 0xFFu, eb = (ew[zc] >> (8 * (oz * 2 + oy))) & 0xFFu;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        mo |= ((ob >> (2 * e + ox)) & 1u) << (zc * 4 + e);
+        me |= ((eb >> (2 * e + ox)) & 1u) << (zc * 4 + e);
+      }
+    }
+    oct_opq[o >> 2] |= mo << (8 * (o & 3));
+    oct_ems[o >> 2] |= me << (8 * (o & 3));
+  }
+
+  // merge geometry: parent rows (qy_lo, qy_hi) with the child row's weights,
+  // parent planes (z0/2 - 1, z0/2, z0/2 + 1), own parent columns 2lq, 2lq+1
+  const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
+  const int ylo = (y - 1) >> 1;
+  const float wy_lo = (y & 1) ? 0.75f : 0.25f, wy_hi = 1.0f - wy_lo;
+  const int qy[2] = {min(max(ylo, 0), UMy - 1), min(max(ylo + 1, 0), UMy - 1)};
+  int qz[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) qz[k] = min(max(z0 / 2 - 1 + k, 0), UMz - 1);
+  const int col0 = min(2 * lq, UMx - 2);  // own float2 (always inside the row when active)
+  const int lcol = max(2 * lq - 1, 0), rcol = min(2 * lq + 2, UMx - 1);
+  // Halo columns 2lq-1 (lane 0) and 2lq+2 (the row's last lane of the warp).
+  // At a row's ends they clamp to the lane's own columns; only a row split
+  // over several warps (Mx > 128) needs loads for them.
+  const bool last_lane = (lane == 31) || (4 * (lq + 1) >= Mx);
+  const bool lhalo_load = (lane == 0) && cw > 0;
+  const bool rhalo_load = last_lane && 4 * (lq + 1) < Mx;
+  int rowoff[2][3];  // element offset of parent row (qy[r], qz[k]) within one direction's plane
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rowoff[r][k] = (qz[k] * UMy + qy[r]) * UMx;
+
+  T* L = static_cast<T*>(a.L);
+  const T* Au = static_cast<const T*>(a.A_up);
+  const int64_t plane = (int64_t)My * Mx;
+  const int64_t p0 = ((int64_t)z0 * My + y) * Mx + x0;  // probe (x0, y, z0)
+  // Channel-outer loop: one channel's 8 fluence sums stay in registers.
+#pragma unroll 1
+  for (int ch = 0; ch < 3; ++ch) {
+    float flu[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll 1
+    for (int d = 0; d < a.ndirs; ++d) {
+      const DirInfo& di = a.dirs[d];
+      const int ox = di.start_off[0] + 1, oy = di.start_off[1] + 1, oz = di.start_off[2] + 1;
+      const int oct = ox + 2 * oy + 4 * oz;
+      const bool hi_oct = oct >= 4;
+      const unsigned opq = ((hi_oct ? oct_opq[1] : oct_opq[0]) >> (8 * (oct & 3))) & 0xFFu;
+      const unsigned ems = ((hi_oct ? oct_ems[1] : oct_ems[0]) >> (8 * (oct & 3))) & 0xFFu;
+      const unsigned valid = active ? (zok1 ? 0xFFu : 0x0Fu) : 0u;
+      const bool merge = !TOP && __any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u);
+      float mv[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+      if (merge) {
+        const T* src = Au + (int64_t)(ch * a.ndirs + d) * a.P_up;
+        // z-interpolated parent columns 2lq-1 .. 2lq+2 for both child planes, per parent row
+        float zr[2][2][4];  // [zc][row][col]
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+          float2 own[3];
+          float lh[3], rh[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const T* row = src + rowoff[r][k];
+            own[k] = active ? load2<T>(row + col0) : make_float2(0.f, 0.f);
+            lh[k] = __shfl_up_sync(0xFFFFFFFFu, own[k].y, 1);
+            rh[k] = __shfl_down_sync(0xFFFFFFFFu, own[k].x, 1);
+            if (lane == 0) lh[k] = own[k].x;
+            if (last_lane) rh[k] = own[k].y;
+            if (chunks > 1) {
+              if (lhalo_load) lh[k] = Store<T>::load(row + lcol);
+              if (rhalo_load) rh[k] = Store<T>::load(row + rcol);
+            }
+          }
+          const float cols[3][4] = {{lh[0], own[0].x, own[0].y, rh[0]},
+                                    {lh[1], own[1].x, own[1].y, rh[1]},
+                                    {lh[2], own[2].x, own[2].y, rh[2]}};
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            zr[0][r][c] = fmaf(0.25f, cols[0][c], 0.75f * cols[1][c]);
+            zr[1][r][c] = fmaf(0.75f, cols[1][c], 0.25f * cols[2][c]);
+          }
+        }
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+          float v[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) v[c] = fmaf(wy_lo, zr[zc][0][c], wy_hi * zr[zc][1][c]);
+          // children e = 0..3 sit at parent coordinates 2lq - 1/4, +1/4, +3/4, +5/4
+          mv[zc][0] = fmaf(0.25f, v[0], 0.75f * v[1]);
+          mv[zc][1] = fmaf(0.75f, v[1], 0.25f * v[2]);
+          mv[zc][2] = fmaf(0.25f, v[1], 0.75f * v[2]);
+          mv[zc][3] = fmaf(0.75f, v[2], 0.25f * v[3]);
+        }
+      }
+      const float om = di.omega;
+      T* lrow = L + (int64_t)(ch * a.ndirs + d) * a.P + p0;
+#pragma unroll
+      for (int zc = 0; zc < 2; ++zc) {
+        float o[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int bit = zc * 4 + e;
+          o[e] = ((opq >> bit) & 1u) ? 0.f : mv[zc][e];
+          if ((ems >> bit) & 1u) {  // emissive start voxel (rare)
+            const int64_t vx = 2 * (x0 + e) + ox;  // start voxel = probe centre 2m+1 plus start_off
+            const int64_t vidx = ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + vx;
+            o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
+          }
+          flu[zc][e] = fmaf(om, o[e], flu[zc][e]);
+        }
+        if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + zc * plane, o[0], o[1], o[2], o[3]);
+      }
+    }
+    // fluence channel ch of the lane's 8 probes (RGB interleaved)
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      if (!(active && (zc == 0 || zok1))) continue;
+      float* f = a.fluence + (p0 + zc * plane) * 3 + ch;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) f[3 * e] = flu[zc][e];
+    }
+  }
+}
+
+// TMA-staged form of k_level0_direct.  Block = 8 child rows (one per warp) x
+// 2 planes of one 128-probe chunk.  For every (channel, direction) the parent
+// tile of cascade 1's child-averaged radiance -- the full parent row width x
+// PY rows x 3 planes -- is brought into shared memory by one
+// cp.async.bulk.tensor while the previous tile is consumed (two stages, one
+// mbarrier each).  Lanes read their 4 parent columns from shared memory.
+// Every barrier wait is bounded: on timeout the block records *err = 1, waits
+// (bounded) for the copy it may still have in flight, and returns.
+constexpr int kL0TmaRows = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kL0Threads, 4)
+    k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int PY, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
+  const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
+  // TMA writes to shared memory must start on a 128-byte boundary: both stages
+  // start at multiples of 128 from a 128-byte aligned base.
+  const int tile_elems = 3 * PY * UMx;
+  const uint32_t tile_bytes = (uint32_t)tile_elems * (uint32_t)sizeof(T);
+  const uint32_t stage_bytes = (tile_bytes + 127u) & ~127u;
+  unsigned char* base = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);
+  T* tiles = reinterpret_cast<T*>(base);
+  const int stage_elems = (int)(stage_bytes / sizeof(T));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * stage_bytes);
+
+  const int chunks = (Mx + 127) >> 7, yblocks = (My + kL0TmaRows - 1) / kL0TmaRows;
+  int bid = blockIdx.x;
+  const int cw = bid % chunks;
+  bid /= chunks;
+  const int yb = (bid % yblocks) * kL0TmaRows;
+  const int z0 = 2 * (bid / yblocks);
+  const int y = yb + warp;
+  const int lq = 32 * cw + lane, x0 = 4 * lq;
+  const bool active = y < My && x0 < Mx && z0 < Mz;
+  const bool zok1 = z0 + 1 < Mz;
+
+  // opacity / emissive masks per octant, as in k_level0_direct
+  uint32_t ow[2] = {0u, 0u}, ew[2] = {0u, 0u};
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const int zc = r >> 2, oz = (r >> 1) & 1, oy = r & 1;
+    if (active && (zc == 0 || zok1)) {
+      const int64_t w = ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.W + ((8 * lq) >> 5);
+      const int sh = (8 * lq) & 31;
+      ow[zc] |= ((__ldg(&a.occ[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+      ew[zc] |= ((__ldg(&a.emis[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+    }
+  }
+  uint32_t oct_opq[2] = {0u, 0u}, oct_ems[2] = {0u, 0u};
+#pragma unroll
+  for (int o = 0; o < 8; ++o) {
+    const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
+    uint32_t mo = 0, me = 0;
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      const uint32_t ob = (ow[zc] >> (8 * (oz * 2 + oy))) & 0xFFu, eb = (ew[zc] >> (8 * (oz * 2 + oy))) & 0xFFu;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        mo |= ((ob >> (2 * e + ox)) & 1u) << (zc * 4 + e);
+        me |= ((eb >> (2 * e + ox)) & 1u) << (zc * 4 + e);
+      }
+    }
+    oct_opq[o >> 2] |= mo << (8 * (o & 3));
+    oct_ems[o >> 2] |= me << (8 * (o & 3));
+  }
+  const unsigned valid = active ? (zok1 ? 0xFFu : 0x0Fu) : 0u;
+
+  // tile origin and this warp's parent rows inside it
+  const int ys = max(0, min(yb / 2 - 1, UMy - PY));
+  const int zs = max(0, min(z0 / 2 - 1, UMz - 3));
+  // inactive warps and lanes still read the tile: keep their rows and columns inside it
+  const int ylo = (min(y, My - 1) - 1) >> 1;
+  const float wy_lo = (y & 1) ? 0.75f : 0.25f, wy_hi = 1.0f - wy_lo;
+  int rowoff[2][3];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int qy = min(max(ylo + r, 0), UMy - 1), qz = min(max(z0 / 2 - 1 + k, 0), UMz - 1);
+      rowoff[r][k] = ((qz - zs) * PY + (qy - ys)) * UMx;
+    }
+  const int c0 = min(2 * lq, UMx - 2), lcol = min(max(2 * lq - 1, 0), UMx - 1), rcol = min(2 * lq + 2, UMx - 1);
+
+  T* L = static_cast<T*>(a.L);
+  const int64_t plane = (int64_t)My * Mx;
+  const int64_t p0 = ((int64_t)z0 * My + y) * Mx + x0;
+  const int total = 3 * a.ndirs;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  // a destination off its 128-byte boundary is reported and never copied to
+  const bool aligned = ((smem_u32(tiles) | stage_bytes) & 127u) == 0u;
+  if (threadIdx.x == 0) {
+    if (aligned) {
+      mbar_arrive_expect_tx(&bar[0], tile_bytes);
+      tma_load_3d(tiles, &tmap, 0, ys, zs, &bar[0]);
+    } else {
+      atomicExch(err, 2);
+    }
+  }
+  float flu[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+  int it = 0;
+  bool failed = false;
+#pragma unroll 1
+  for (; it < total; ++it) {
+    const int ch = it / a.ndirs, d = it - ch * a.ndirs;
+    const int st = it & 1;
+    if (threadIdx.x == 0 && it + 1 < total && aligned) {
+      // the other stage was released by the barrier at the end of the previous iteration
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&bar[st ^ 1], tile_bytes);
+      tma_load_3d(tiles + (st ^ 1) * stage_elems, &tmap, 0, ys, (it + 1) * UMz + zs, &bar[st ^ 1]);
+    }
+    const bool ok = mbar_wait_bounded(&bar[st], (it >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const T* tile = tiles + st * stage_elems;
+    const DirInfo& di = a.dirs[d];
+    const int ox = di.start_off[0] + 1, oy = di.start_off[1] + 1, oz = di.start_off[2] + 1;
+    const int oct = ox + 2 * oy + 4 * oz;
+    const bool hi_oct = oct >= 4;
+    const unsigned opq = ((hi_oct ? oct_opq[1] : oct_opq[0]) >> (8 * (oct & 3))) & 0xFFu;
+    const unsigned ems = ((hi_oct ? oct_ems[1] : oct_ems[0]) >> (8 * (oct & 3))) & 0xFFu;
+    float mv[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    if (__any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u)) {
+      float zr[2][2][4];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        float cv[3][4];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const T* row = tile + rowoff[r][k];
+          cv[k][0] = to_float(row[lcol]);
+          cv[k][1] = to_float(row[c0]);
+          cv[k][2] = to_float(row[c0 + 1]);
+          cv[k][3] = to_float(row[rcol]);
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          zr[0][r][c] = fmaf(0.25f, cv[0][c], 0.75f * cv[1][c]);
+          zr[1][r][c] = fmaf(0.75f, cv[1][c], 0.25f * cv[2][c]);
+        }
+      }
+#pragma unroll
+      for (int zc = 0; zc < 2; ++zc) {
+        float v[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) v[c] = fmaf(wy_lo, zr[zc][0][c], wy_hi * zr[zc][1][c]);
+        mv[zc][0] = fmaf(0.25f, v[0], 0.75f * v[1]);
+        mv[zc][1] = fmaf(0.75f, v[1], 0.25f * v[2]);
+        mv[zc][2] = fmaf(0.25f, v[1], 0.75f * v[2]);
+        mv[zc][3] = fmaf(0.75f, v[2], 0.25f * v[3]);
+      }
+    }
+    const float om = di.omega;
+    T* lrow = L + (int64_t)(ch * a.ndirs + d) * a.P + p0;
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      float o[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int bit = zc * 4 + e;
+        o[e] = ((opq >> bit) & 1u) ? 0.f : mv[zc][e];
+        if ((ems >> bit) & 1u) {  // emissive start voxel (rare)
+          const int64_t vidx =
+              ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + 2 * (x0 + e) + ox;
+          o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
+        }
+        flu[zc][e] = fmaf(om, o[e], flu[zc][e]);
+      }
+      if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + zc * plane, o[0], o[1], o[2], o[3]);
+    }
+    if (d == a.ndirs - 1) {
+#pragma unroll
+      for (int zc = 0; zc < 2; ++zc) {
+        if ((valid >> (zc * 4)) & 1u) {
+          float* f = a.fluence + (p0 + zc * plane) * 3 + ch;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) f[3 * e] = flu[zc][e];
+        }
+        flu[zc][0] = flu[zc][1] = flu[zc][2] = flu[zc][3] = 0.f;
+      }
+    }
+    __syncthreads();  // this stage may be refilled from the next iteration on
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicExch(err, 1);
+    // the copies for iterations it and it + 1 may still be in flight: let them land first
+    (void)mbar_wait_bounded(&bar[it & 1], (it >> 1) & 1);
+    if (it + 1 < total) (void)mbar_wait_bounded(&bar[(it + 1) & 1], ((it + 1) >> 1) & 1);
+  }
+}
+
+}  // namespace rcx

@@ -290,11 +290,6 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
   }
 }
 
-__device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol, uint32_t idx, int ch) {
-  const uint2 v = __ldg(&vol[idx]);
-  const uint32_t w = ch == 2 ? v.y : v.x;
-  return __half2float(__ushort_as_half((unsigned short)(ch == 1 ? (w >> 16) : (w & 0xFFFFu))));
-}
 
 // Direction of block-local slot dl (0..15) in pass `pass`, or -1.
 template <bool L0>

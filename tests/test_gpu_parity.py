@@ -44,13 +44,16 @@ def _check(gflu, gL, oflu, oL, rel=FP32_REL_L2, max_rel=FP32_MAX_REL):
             assert np.abs(g - o).max() <= max_rel * max(1.0, np.abs(o).max())
 
 
-@pytest.fixture(params=["bits", "scalar"])
+@pytest.fixture(params=["default", "no_tma", "scalar"])
 def walk(request, monkeypatch):
-    """Runs a test with the bit-parallel walk (default) and with the scalar walk."""
+    """Runs a test with the default kernels (bit-parallel walks, TMA-staged
+    cascade 0), without the TMA cascade-0 kernel, and with the scalar walk."""
+    monkeypatch.delenv("RC_WALK", raising=False)
+    monkeypatch.delenv("RC_TMA", raising=False)
     if request.param == "scalar":
         monkeypatch.setenv("RC_WALK", "scalar")
-    else:
-        monkeypatch.delenv("RC_WALK", raising=False)
+    elif request.param == "no_tma":
+        monkeypatch.setenv("RC_TMA", "0")
     return request.param
 
 
