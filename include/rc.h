@@ -203,6 +203,37 @@ rc_status rc_get_stream(rc_context* ctx, void** out);
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
 
+/* ---- batched solve --------------------------------------------------- */
+/* Many independent scenes (each with its own rc_params: grid, cascades)
+ * solved together.  rc_batch_solve launches one CUDA graph holding one
+ * persistent kernel that takes (scene, level, tile) items from a queue, top
+ * level first; a level waits (bounded) for the level above of its own scene.
+ * Every scene must use the same precision. */
+typedef struct rc_batch rc_batch;
+rc_status rc_batch_create(const rc_params* params, int32_t nscenes,
+                          int32_t device, rc_batch** out);
+rc_status rc_batch_destroy(rc_batch* b);  /* NULL is accepted */
+/* Voxelises boxes then spheres into scene `scene` (synchronises). */
+rc_status rc_batch_scene_set(rc_batch* b, int32_t scene, const rc_box* boxes,
+                             int32_t nboxes, const rc_sphere* spheres,
+                             int32_t nspheres);
+rc_status rc_batch_solve(rc_batch* b, void* stream);  /* asynchronous */
+/* Synchronises; RC_ERR_TIMEOUT when a bounded wait ran out (the batch stays
+ * usable). */
+rc_status rc_batch_synchronize(rc_batch* b);
+rc_status rc_batch_get_fluence(rc_batch* b, int32_t scene, float* out,
+                               int64_t elems, int32_t where);
+rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level,
+                                void* out, int64_t bytes, int32_t where);
+/* Tile shape of a queue item: probes per item, parent texels per item (each
+ * is 4 child directions; level 0 items hold every direction). */
+rc_status rc_batch_set_tiles(rc_batch* b, int32_t probes_per_item,
+                             int32_t dirs_per_item);
+/* Autotuner: times every candidate tile shape over `iters` solves of the
+ * current scenes, keeps the fastest and reports it. */
+rc_status rc_batch_tune(rc_batch* b, int32_t iters, int32_t* probes_per_item,
+                        int32_t* dirs_per_item, float* best_ms);
+
 /* ---- allocation-free solve ------------------------------------------ */
 /* No counterpart in the reference.
  *

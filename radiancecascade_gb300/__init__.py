@@ -6,7 +6,7 @@ library and raises ImportError when it has not been built -- there is no CPU
 fallback.
 """
 from ._ffi import lib as _load_lib, RCError, VOXEL_DT, BOX_DT, SPHERE_DT  # noqa: F401
-from .engine import (Engine, GiStage, GiState, make_params, level_info, scene_spec, generate_scene,  # noqa: F401
+from .engine import (Engine, Batch, GiStage, GiState, make_params, level_info, scene_spec, generate_scene,  # noqa: F401
                      advance_spheres, voxelise_host, directions, solid_angles, WORKLOADS, workload_scene,
                      frames)
 

@@ -75,6 +75,15 @@ SIGNATURES = {
     "rc_get_stream": (_S, [_P, C.POINTER(C.c_void_p)]),
     "rc_profile_levels": (_S, [_P, C.c_int32, _P, C.c_int32]),
     "rc_solve_noalloc": (_S, [_P, _P, _P, _P, _P]),
+    "rc_batch_create": (_S, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "rc_batch_destroy": (_S, [_P]),
+    "rc_batch_scene_set": (_S, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int32]),
+    "rc_batch_solve": (_S, [_P, _P]),
+    "rc_batch_synchronize": (_S, [_P]),
+    "rc_batch_get_fluence": (_S, [_P, C.c_int32, _P, C.c_int64, C.c_int32]),
+    "rc_batch_get_radiance": (_S, [_P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int32]),
+    "rc_batch_set_tiles": (_S, [_P, C.c_int32, C.c_int32]),
+    "rc_batch_tune": (_S, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
 }
 
 _lib = None

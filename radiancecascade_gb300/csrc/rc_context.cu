@@ -21,6 +21,7 @@
 #include "rc_walk_bits.cuh"
 #include "rc_walk_queue.cuh"
 #include "rc_level0.cuh"
+#include "rc_batch.cuh"
 
 using namespace rcx;
 
@@ -465,9 +466,9 @@ cudaError_t allow_bits_smem() {
 
 }  // namespace
 
-extern "C" {
-
-rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
+// Creates a context.  A minimal context (used for the scenes of a batch)
+// solves every level with the scalar walk and allocates no decimated masks.
+static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc_context** out) {
   if (!out) {
     rcx::set_error("rc_create: out is NULL");
     return RC_ERR_INVALID_ARG;
@@ -537,7 +538,7 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
     return fail(s);
   {
     // Decimated opacity per level (bit-parallel walk).
-    const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
+    const bool force_scalar = minimal || (getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0);
     int64_t total = 0;
     int64_t off[kMaxCascades];
     c->mset.n = 0;
@@ -631,9 +632,15 @@ rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
   }
   if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);
   if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
-  if (!(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) setup_tma0(c);
+  if (!minimal && !(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) setup_tma0(c);
   *out = c;
   return RC_OK;
+}
+
+extern "C" {
+
+rc_status rc_create(const rc_params* p, int32_t device, rc_context** out) {
+  return create_ctx(p, device, false, out);
 }
 
 rc_status rc_destroy(rc_context* ctx) {
@@ -1087,3 +1094,330 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: cascade launch");
   return RC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched solve: many scenes, one persistent launch in a CUDA graph.
+// ---------------------------------------------------------------------------
+struct rc_batch {
+  int device = 0;
+  int n = 0;
+  std::vector<rc_context*> scenes;
+  cudaStream_t stream = nullptr;
+  BatchLevel* d_levels = nullptr;
+  BatchItem* d_items = nullptr;
+  unsigned* d_next = nullptr;
+  unsigned* d_done = nullptr;
+  int* d_err = nullptr;
+  size_t levels_cap = 0, items_cap = 0;
+  int nlevels = 0, nitems = 0;
+  int ppi = 256, qpi = 2;  // tile shape: probes and parent texels per item
+  int blocks = 0;
+  bool fp16 = false;
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace {
+
+void batch_free_graph(rc_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+}
+
+// Level table and top-level-first item queue for tile shape (ppi, qpi).
+rc_status batch_build(rc_batch* b, int ppi, int qpi) {
+  std::vector<BatchLevel> lv;
+  std::vector<int> first(b->n);
+  int maxN = 0;
+  for (int k = 0; k < b->n; ++k) {
+    rc_context* c = b->scenes[k];
+    first[k] = (int)lv.size();
+    maxN = std::max(maxN, c->nlev);
+    for (int i = 0; i < c->nlev; ++i) {
+      BatchLevel L;
+      memset(&L, 0, sizeof L);
+      L.a = c->args[i];
+      L.up = (i + 1 < c->nlev) ? first[k] + i + 1 : -1;
+      L.is_l0 = (i == 0);
+      L.is_top = (i == c->nlev - 1);
+      L.ptiles = (int)((c->geom[i].probes() + ppi - 1) / ppi);
+      const int npar = (i == 0) ? 1 : c->geom[i - 1].ndirs;
+      L.ntiles = L.ptiles * (i == 0 ? 1 : (npar + qpi - 1) / qpi);
+      lv.push_back(L);
+    }
+  }
+  std::vector<BatchItem> items;
+  for (int t = 0; t < maxN; ++t)
+    for (int k = 0; k < b->n; ++k) {
+      const int N = b->scenes[k]->nlev;
+      if (t >= N) continue;
+      const int li = first[k] + N - 1 - t;
+      for (int tile = 0; tile < lv[li].ntiles; ++tile) items.push_back(BatchItem{li, tile});
+    }
+  // Fault injection for tests: one level waits for a tile that never comes.
+  if (fault_is("timeout") && !lv.empty()) lv[first[0] + b->scenes[0]->nlev - 1].ntiles += 1;
+  DeviceGuard g(b->device);
+  if (lv.size() > b->levels_cap) {
+    if (b->d_levels) cudaFree(b->d_levels);
+    if (b->d_done) cudaFree(b->d_done);
+    b->d_levels = nullptr;
+    b->d_done = nullptr;
+    rc_status s = dev_alloc((void**)&b->d_levels, lv.size() * sizeof(BatchLevel), "batch level table");
+    if (s != RC_OK) return s;
+    if ((s = dev_alloc((void**)&b->d_done, lv.size() * sizeof(unsigned), "batch counters")) != RC_OK) return s;
+    b->levels_cap = lv.size();
+  }
+  if (items.size() > b->items_cap) {
+    if (b->d_items) cudaFree(b->d_items);
+    b->d_items = nullptr;
+    rc_status s = dev_alloc((void**)&b->d_items, items.size() * sizeof(BatchItem), "batch items");
+    if (s != RC_OK) return s;
+    b->items_cap = items.size();
+  }
+  RC_CUDA(cudaMemcpy(b->d_levels, lv.data(), lv.size() * sizeof(BatchLevel), cudaMemcpyHostToDevice), "batch upload");
+  RC_CUDA(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(BatchItem), cudaMemcpyHostToDevice),
+          "batch upload");
+  b->nlevels = (int)lv.size();
+  b->nitems = (int)items.size();
+  b->ppi = ppi;
+  b->qpi = qpi;
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  if (b->fp16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<__half>, kBatchThreads, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<float>, kBatchThreads, 0);
+  (void)cudaGetLastError();
+  b->blocks = std::max(1, std::min(b->nitems, std::max(1, sms * std::max(per_sm, 1))));
+  batch_free_graph(b);
+  return RC_OK;
+}
+
+void batch_enqueue(rc_batch* b, cudaStream_t s) {
+  cudaMemsetAsync(b->d_next, 0, sizeof(unsigned), s);
+  cudaMemsetAsync(b->d_done, 0, (size_t)b->nlevels * sizeof(unsigned), s);
+  if (b->fp16)
+    k_batch_persistent<__half><<<b->blocks, kBatchThreads, 0, s>>>(b->d_levels, b->d_items, b->nitems, b->ppi,
+                                                                    b->qpi, b->d_next, b->d_done, b->d_err);
+  else
+    k_batch_persistent<float><<<b->blocks, kBatchThreads, 0, s>>>(b->d_levels, b->d_items, b->nitems, b->ppi,
+                                                                   b->qpi, b->d_next, b->d_done, b->d_err);
+}
+
+// The whole batch solve as one CUDA graph (two counter resets + one launch).
+rc_status batch_graph(rc_batch* b) {
+  if (b->graph) return RC_OK;
+  cudaGraph_t graph = nullptr;
+  RC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture");
+  batch_enqueue(b, b->stream);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+  if (e != cudaSuccess) return cuda_fail(e, "batch capture");
+  e = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    return cuda_fail(e, "batch graph instantiate");
+  }
+  return RC_OK;
+}
+
+rc_status batch_check(const rc_batch* b, const char* fn) {
+  if (!b) {
+    rcx::set_error("%s: batch is NULL", fn);
+    return RC_ERR_INVALID_ARG;
+  }
+  return RC_OK;
+}
+
+rc_status batch_error_flag(rc_batch* b, const char* fn) {
+  int flag = 0;
+  RC_CUDA(cudaMemcpy(&flag, b->d_err, sizeof flag, cudaMemcpyDeviceToHost), fn);
+  if (flag) {
+    cudaMemset(b->d_err, 0, sizeof(int));
+    rcx::set_error("%s: a level waited longer than its bound for the level above (batch results incomplete)", fn);
+    return RC_ERR_TIMEOUT;
+  }
+  return RC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+rc_status rc_batch_create(const rc_params* params, int32_t nscenes, int32_t device, rc_batch** out) {
+  if (!out || !params || nscenes < 1 || nscenes > 4096) {
+    rcx::set_error("rc_batch_create: need 1..4096 scene parameter blocks and a non-NULL out");
+    return RC_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  for (int k = 0; k < nscenes; ++k) {
+    char msg[256];
+    if (!validate_params(&params[k], msg, sizeof msg)) {
+      rcx::set_error("rc_batch_create: scene %d: %s", k, msg);
+      return RC_ERR_INVALID_ARG;
+    }
+    if (params[k].precision != params[0].precision) {
+      rcx::set_error("rc_batch_create: every scene must use the same precision");
+      return RC_ERR_INVALID_ARG;
+    }
+  }
+  rc_batch* b = new rc_batch();
+  b->device = device;
+  b->n = nscenes;
+  b->fp16 = params[0].precision == RC_PRECISION_FP16;
+  auto fail = [&](rc_status st) {
+    rc_batch_destroy(b);
+    return st;
+  };
+  for (int k = 0; k < nscenes; ++k) {
+    rc_context* c = nullptr;
+    rc_status s = create_ctx(&params[k], device, true, &c);
+    if (s != RC_OK) return fail(s);
+    b->scenes.push_back(c);
+  }
+  DeviceGuard g(device);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(cuda_fail(e, "rc_batch_create: stream"));
+  rc_status s;
+  if ((s = dev_alloc((void**)&b->d_next, sizeof(unsigned), "batch queue")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&b->d_err, sizeof(int), "batch error flag")) != RC_OK) return fail(s);
+  if ((e = cudaMemset(b->d_err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_batch_create"));
+  if ((s = batch_build(b, b->ppi, b->qpi)) != RC_OK) return fail(s);
+  *out = b;
+  return RC_OK;
+}
+
+rc_status rc_batch_destroy(rc_batch* b) {
+  if (!b) return RC_OK;
+  {
+    DeviceGuard g(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_free_graph(b);
+    void* bufs[] = {b->d_levels, b->d_items, b->d_next, b->d_done, b->d_err};
+    for (void* x : bufs)
+      if (x) cudaFree(x);
+    if (b->stream) cudaStreamDestroy(b->stream);
+  }
+  for (rc_context* c : b->scenes) release(c);
+  delete b;
+  return RC_OK;
+}
+
+rc_status rc_batch_scene_set(rc_batch* b, int32_t scene, const rc_box* boxes, int32_t nboxes,
+                             const rc_sphere* spheres, int32_t nspheres) {
+  if (batch_check(b, "rc_batch_scene_set") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (scene < 0 || scene >= b->n) {
+    rcx::set_error("rc_batch_scene_set: scene %d out of range", scene);
+    return RC_ERR_INVALID_ARG;
+  }
+  rc_status s = rc_scene_set_boxes(b->scenes[scene], boxes, nboxes);
+  if (s != RC_OK) return s;
+  s = rc_scene_set_spheres(b->scenes[scene], spheres, nspheres);
+  if (s != RC_OK) return s;
+  return rc_synchronize(b->scenes[scene]);
+}
+
+rc_status rc_batch_solve(rc_batch* b, void* stream) {
+  if (batch_check(b, "rc_batch_solve") != RC_OK) return RC_ERR_INVALID_ARG;
+  for (int k = 0; k < b->n; ++k)
+    if (!b->scenes[k]->have_base) {
+      rcx::set_error("rc_batch_solve: scene %d has no scene data", k);
+      return RC_ERR_STATE;
+    }
+  DeviceGuard g(b->device);
+  rc_status s = batch_graph(b);
+  if (s != RC_OK) return s;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  RC_CUDA(cudaGraphLaunch(b->graph, st), "rc_batch_solve: graph launch");
+  if (st != b->stream) {
+    cudaEvent_t ev;
+    RC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "rc_batch_solve: event");
+    cudaEventRecord(ev, st);
+    cudaStreamWaitEvent(b->stream, ev, 0);
+    cudaEventDestroy(ev);
+  }
+  return RC_OK;
+}
+
+rc_status rc_batch_synchronize(rc_batch* b) {
+  if (batch_check(b, "rc_batch_synchronize") != RC_OK) return RC_ERR_INVALID_ARG;
+  DeviceGuard g(b->device);
+  RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_synchronize");
+  return batch_error_flag(b, "rc_batch_synchronize");
+}
+
+rc_status rc_batch_get_fluence(rc_batch* b, int32_t scene, float* out, int64_t elems, int32_t where) {
+  if (batch_check(b, "rc_batch_get_fluence") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (scene < 0 || scene >= b->n) {
+    rcx::set_error("rc_batch_get_fluence: scene %d out of range", scene);
+    return RC_ERR_INVALID_ARG;
+  }
+  rc_status s = rc_batch_synchronize(b);
+  if (s != RC_OK) return s;
+  return rc_get_fluence(b->scenes[scene], out, elems, where);
+}
+
+rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level, void* out, int64_t bytes, int32_t where) {
+  if (batch_check(b, "rc_batch_get_radiance") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (scene < 0 || scene >= b->n) {
+    rcx::set_error("rc_batch_get_radiance: scene %d out of range", scene);
+    return RC_ERR_INVALID_ARG;
+  }
+  rc_status s = rc_batch_synchronize(b);
+  if (s != RC_OK) return s;
+  return rc_get_radiance(b->scenes[scene], level, out, bytes, where);
+}
+
+rc_status rc_batch_set_tiles(rc_batch* b, int32_t probes_per_item, int32_t dirs_per_item) {
+  if (batch_check(b, "rc_batch_set_tiles") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (probes_per_item < 1 || probes_per_item > 65536 || dirs_per_item < 1 || dirs_per_item > 65536) {
+    rcx::set_error("rc_batch_set_tiles: tile sizes must be in [1, 65536]");
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(b->device);
+  RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_set_tiles");
+  return batch_build(b, probes_per_item, dirs_per_item);
+}
+
+rc_status rc_batch_tune(rc_batch* b, int32_t iters, int32_t* probes_per_item, int32_t* dirs_per_item,
+                        float* best_ms) {
+  if (batch_check(b, "rc_batch_tune") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (iters < 1) {
+    rcx::set_error("rc_batch_tune: iters must be >= 1");
+    return RC_ERR_INVALID_ARG;
+  }
+  static const int kPpi[] = {128, 256, 512, 1024};
+  static const int kQpi[] = {1, 2, 4, 8};
+  DeviceGuard g(b->device);
+  cudaEvent_t e0, e1;
+  RC_CUDA(cudaEventCreate(&e0), "rc_batch_tune: event");
+  RC_CUDA(cudaEventCreate(&e1), "rc_batch_tune: event");
+  float best = 3.4e38f;
+  int bp = b->ppi, bq = b->qpi;
+  rc_status st = RC_OK;
+  for (int ppi : kPpi)
+    for (int qpi : kQpi) {
+      if ((st = batch_build(b, ppi, qpi)) != RC_OK) break;
+      if ((st = rc_batch_solve(b, nullptr)) != RC_OK) break;  // warm-up (builds the graph)
+      cudaEventRecord(e0, b->stream);
+      for (int i = 0; i < iters && st == RC_OK; ++i) st = rc_batch_solve(b, nullptr);
+      cudaEventRecord(e1, b->stream);
+      if (st == RC_OK) st = rc_batch_synchronize(b);
+      if (st != RC_OK) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= iters;
+      if (ms < best) {
+        best = ms;
+        bp = ppi;
+        bq = qpi;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != RC_OK) return st;
+  if ((st = batch_build(b, bp, bq)) != RC_OK) return st;
+  if (probes_per_item) *probes_per_item = bp;
+  if (dirs_per_item) *dirs_per_item = bq;
+  if (best_ms) *best_ms = best;
+  return RC_OK;
+}
+
+}  // extern "C"

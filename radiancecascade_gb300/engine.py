@@ -200,6 +200,84 @@ class Engine:
         return p.value
 
 
+class Batch:
+    """Many independent scenes solved by one persistent launch (a CUDA graph).
+
+    Each scene has its own ``rc_params`` (grid, cascade count); all share one
+    precision.  ``solve()`` is asynchronous; the results calls synchronise.
+    """
+
+    def __init__(self, params_list, device: int = 0):
+        self._lib = F.lib()
+        arr = (F.Params * len(params_list))(*params_list)
+        self.params = list(params_list)
+        h = C.c_void_p()
+        F.check(self._lib.rc_batch_create(arr, len(params_list), device, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise RCError(F.RC_ERR_STATE, "batch is closed")
+        return self._h
+
+    def __len__(self) -> int:
+        return len(self.params)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            self._lib.rc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_scene(self, k: int, boxes: np.ndarray, spheres: np.ndarray) -> None:
+        b = np.ascontiguousarray(boxes, dtype=BOX_DT)
+        s = np.ascontiguousarray(spheres, dtype=SPHERE_DT)
+        F.check(self._lib.rc_batch_scene_set(self.handle, k, F.ptr(b), len(b), F.ptr(s), len(s)))
+
+    def solve(self, stream: Optional[int] = None) -> None:
+        F.check(self._lib.rc_batch_solve(self.handle, C.c_void_p(stream) if stream else None))
+
+    def synchronize(self) -> None:
+        F.check(self._lib.rc_batch_synchronize(self.handle))
+
+    def fluence(self, k: int) -> np.ndarray:
+        probes0 = level_info(self.params[k], 0).probes
+        n = 3 * int(np.prod(probes0))
+        out = np.empty(n, np.float32)
+        F.check(self._lib.rc_batch_get_fluence(self.handle, k, F.ptr(out), n, F.RC_MEM_HOST))
+        return out.reshape(-1, 3)
+
+    def radiance(self, k: int, level: int) -> np.ndarray:
+        info = level_info(self.params[k], level)
+        dt = np.float16 if self.params[k].precision == F.RC_PRECISION_FP16 else np.float32
+        out = np.empty(info.radiance_elems, dt)
+        F.check(self._lib.rc_batch_get_radiance(self.handle, k, level, F.ptr(out), info.radiance_bytes,
+                                                F.RC_MEM_HOST))
+        px, py, pz = info.probes
+        return out.reshape(3, info.num_dirs, pz, py, px)
+
+    def set_tiles(self, probes_per_item: int, dirs_per_item: int) -> None:
+        F.check(self._lib.rc_batch_set_tiles(self.handle, probes_per_item, dirs_per_item))
+
+    def tune(self, iters: int = 3):
+        """Times every candidate tile shape, keeps the fastest: (ppi, qpi, ms)."""
+        pp, qq, ms = C.c_int32(), C.c_int32(), C.c_float()
+        F.check(self._lib.rc_batch_tune(self.handle, iters, C.byref(pp), C.byref(qq), C.byref(ms)))
+        return pp.value, qq.value, ms.value
+
+
 @dataclass
 class GiState:
     """Per-frame state a GI stage reads in update(): the emitters."""

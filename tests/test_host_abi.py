@@ -116,6 +116,21 @@ def test_gpu_entry_points_fail_cleanly_without_a_device():
     assert F.lib().rc_solve(None, None) == F.RC_ERR_INVALID_ARG
 
 
+def test_batch_entry_points_check_arguments_before_the_device():
+    p = (F.Params * 1)(R.make_params(32, 3))
+    h = C.c_void_p()
+    assert F.lib().rc_batch_create(p, 0, 0, C.byref(h)) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_batch_create(p, 1, 0, None) == F.RC_ERR_INVALID_ARG
+    bad = (F.Params * 1)(R.make_params(32, 3))
+    bad[0].num_cascades = 0
+    assert F.lib().rc_batch_create(bad, 1, 0, C.byref(h)) == F.RC_ERR_INVALID_ARG
+    assert "scene 0" in F.last_error()
+    assert F.lib().rc_batch_destroy(None) == F.RC_OK
+    assert F.lib().rc_batch_solve(None, None) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_batch_synchronize(None) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_batch_set_tiles(None, 128, 2) == F.RC_ERR_INVALID_ARG
+
+
 def _has_gpu():
     try:
         import torch
