@@ -172,6 +172,165 @@ def run_reference(args, rank, world):
     return 0
 
 
+BATCH_DESC = ("64 cubic scenes (seed 2000+k), edges uniform over {32,48,64,96,128,192}, 64^3 workload's "
+              "box/sphere density, 4-6 cascades by edge; one persistent launch in a CUDA graph, autotuned "
+              "tile shape")
+
+
+def batch_bytes(batch_items, elem_bytes):
+    """Algorithmic bytes of one batch solve: the per-frame formula summed over scenes."""
+    import radiancecascade_gb300 as R
+    total = 0
+    for edge, N, _, _ in batch_items:
+        p = R.make_params(edge, N)
+        total += algorithmic_bytes([R.level_info(p, i) for i in range(N)], edge, elem_bytes)[0]
+    return total
+
+
+def cpu_port_batch_scenes_per_s(items, threads, budget_s=20.0):
+    """Oracle FP32 on the batch's scenes in order until `budget_s` has passed;
+    scenes/s extrapolated by voxel count to the whole batch."""
+    from oracle import oracle as O
+    t_total, vox_done, done = 0.0, 0, 0
+    for edge, N, boxes, spheres in items:
+        t0 = time.perf_counter()
+        O.solve(O.params(edge, N), O.voxelise(edge, boxes, spheres), dtype=np.float32, jump=True,
+                nthreads=threads)
+        t_total += time.perf_counter() - t0
+        vox_done += edge ** 3
+        done += 1
+        if t_total >= budget_s:
+            break
+    vox_all = sum(e ** 3 for e, _, _, _ in items)
+    batch_s = t_total * vox_all / vox_done
+    return len(items) / batch_s, done, t_total
+
+
+def run_batch(args, rank, world):
+    """Scenes/s of the batched workload (replicas: every rank solves its own copy)."""
+    import torch
+    import radiancecascade_gb300 as R
+
+    dist = None
+    local = _env_int("LOCAL_RANK", 0)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    items = R.batch_workload()
+    prec = args.precision
+    b = R.Batch([R.make_params(e, N, precision=prec) for e, N, _, _ in items], device=local)
+    for k, (_, _, boxes, spheres) in enumerate(items):
+        b.set_scene(k, boxes, spheres)
+    tiles, tune_ms = b.tune(iters=2)
+    stream = torch.cuda.Stream(local)
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        b.solve(sp)
+    b.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        b.solve(sp)
+    t1.record(stream)
+    t1.synchronize()
+    b.synchronize()
+    torch.cuda.synchronize()
+    clock_info = clocks.stop()
+    ms = t0.elapsed_time(t1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * len(items) * args.steps / (ms / 1000.0)
+
+    # the same scenes as separate contexts (fastest per-level kernels), one after another
+    engines = []
+    for e, N, boxes, spheres in items:
+        g = R.Engine(R.make_params(e, N, precision=prec), device=local)
+        g.set_boxes(boxes)
+        g.set_spheres(spheres)
+        engines.append(g)
+    for _ in range(2):
+        for g in engines:
+            g.solve(sp)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(args.steps):
+        for g in engines:
+            g.solve(sp)
+    s1.record(stream)
+    s1.synchronize()
+    seq_ms = s0.elapsed_time(s1) / args.steps
+    for g in engines:
+        g.close()
+
+    # e2e: every step re-voxelises each scene from host box/sphere arrays, solves, reads every fluence
+    nbytes_in = sum(int(bx.nbytes + sx.nbytes) for _, _, bx, sx in items)
+    outs = [np.empty((b.fluence(k).size,), np.float32) for k in range(len(items))]
+    nbytes_out = sum(o.nbytes for o in outs)
+    e2e_steps = max(1, min(args.steps, 10))
+    if dist:
+        dist.barrier()
+    w0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k, (_, _, boxes, spheres) in enumerate(items):
+            b.set_scene(k, boxes, spheres)
+        b.solve()
+        for k in range(len(items)):
+            outs[k][:] = b.fluence(k).reshape(-1)
+    e2e_s = time.perf_counter() - w0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * len(items) * e2e_steps / e2e_s
+
+    elem = 2 if prec == "fp16" else 4
+    B = batch_bytes(items, elem)
+    per_batch_s = ms / args.steps / 1000.0
+    achieved = B / per_batch_s / 1e9
+    peak, peak_kind = measured_peak_gbs()
+    line = {
+        "metric": "scenes/s, batched uneven scenes in one persistent launch",
+        "value": round(value, 3), "unit": "scenes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec == "fp16" else "f32",
+        "data": "synthetic",
+        "config": {"workload": BATCH_DESC, "scenes": len(items), "precision": prec,
+                   "tile": dict(tiles, tune_ms=round(tune_ms, 4)),
+                   "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (%.1f GB of scene + radiance)" % (B / 1e9)},
+        "e2e": {"value": round(e2e_value, 3), "unit": "scenes/s", "h2d_bytes_per_step": nbytes_in,
+                "d2h_bytes_per_step": nbytes_out},
+        "gpu_launches": args.steps,
+        "per_scene_contexts_ms_per_batch": round(seq_ms, 4),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
+                     "kernel": "k_batch_persistent", "algorithmic_bytes_per_step": B},
+    }
+    if clock_info:
+        line["clocks"] = clock_info
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, done, secs = cpu_port_batch_scenes_per_s(items, threads)
+        line["cpu_baseline"] = {"value": round(v, 4), "unit": "scenes/s", "cores": threads, "kind": "port",
+                                "sample": "first %d scenes of the batch (%.1f s, FP32, OpenMP), scaled to the "
+                                          "batch by voxel count" % (done, secs)}
+    b.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -182,12 +341,16 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=2, help="frames of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--workload", default="c256", choices=["c256", "batch64"],
+                    help="c256: the 256^3 moving-emitter frame (default); batch64: 64 uneven scenes")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
     rank, world, local = _env_int("RANK", 0), _env_int("WORLD_SIZE", 1), _env_int("LOCAL_RANK", 0)
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "batch64":
+        return run_batch(args, rank, world)
 
     import torch
     import radiancecascade_gb300 as R

@@ -225,14 +225,21 @@ rc_status rc_batch_get_fluence(rc_batch* b, int32_t scene, float* out,
                                int64_t elems, int32_t where);
 rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level,
                                 void* out, int64_t bytes, int32_t where);
-/* Tile shape of a queue item: probes per item, parent texels per item (each
- * is 4 child directions; level 0 items hold every direction). */
-rc_status rc_batch_set_tiles(rc_batch* b, int32_t probes_per_item,
-                             int32_t dirs_per_item);
-/* Autotuner: times every candidate tile shape over `iters` solves of the
- * current scenes, keeps the fastest and reports it. */
-rc_status rc_batch_tune(rc_batch* b, int32_t iters, int32_t* probes_per_item,
-                        int32_t* dirs_per_item, float* best_ms);
+/* Tile shape of the batch's queue items. */
+typedef struct rc_batch_tiles {
+  int32_t probes_per_item;  /* narrow levels: probes per item               */
+  int32_t dirs_per_item;    /* narrow levels: parent texels (or pairs) per item */
+  int32_t blocks_per_item;  /* wide levels, cascade 0: kernel blocks per item */
+  int32_t walks_per_item;   /* walk-queue tasks (32-probe walks) per item    */
+} rc_batch_tiles;
+/* Every field in [1, 65536]; rebuilds the queue (synchronises). */
+rc_status rc_batch_set_tiles(rc_batch* b, const rc_batch_tiles* tiles);
+rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out);
+/* Autotuner: coordinate descent over the tile shape, each candidate timed
+ * over `iters` solves of the current scenes; keeps the fastest and reports it
+ * (outputs may be NULL). */
+rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best,
+                        float* best_ms);
 
 /* ---- allocation-free solve ------------------------------------------ */
 /* No counterpart in the reference.

@@ -8,6 +8,7 @@ fallback.
 from ._ffi import lib as _load_lib, RCError, VOXEL_DT, BOX_DT, SPHERE_DT  # noqa: F401
 from .engine import (Engine, Batch, GiStage, GiState, make_params, level_info, scene_spec, generate_scene,  # noqa: F401
                      advance_spheres, voxelise_host, directions, solid_angles, WORKLOADS, workload_scene,
+                     batch_workload, BATCH_EDGES, BATCH_CASCADES,
                      frames)
 
 _load_lib()

@@ -43,6 +43,11 @@ class LevelInfo(C.Structure):
                 ("radiance_elems", C.c_int64), ("radiance_bytes", C.c_int64)]
 
 
+class BatchTiles(C.Structure):
+    _fields_ = [("probes_per_item", C.c_int32), ("dirs_per_item", C.c_int32), ("blocks_per_item", C.c_int32),
+                ("walks_per_item", C.c_int32)]
+
+
 _P = C.c_void_p
 _S = C.c_int  # rc_status
 
@@ -82,8 +87,9 @@ SIGNATURES = {
     "rc_batch_synchronize": (_S, [_P]),
     "rc_batch_get_fluence": (_S, [_P, C.c_int32, _P, C.c_int64, C.c_int32]),
     "rc_batch_get_radiance": (_S, [_P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int32]),
-    "rc_batch_set_tiles": (_S, [_P, C.c_int32, C.c_int32]),
-    "rc_batch_tune": (_S, [_P, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_float)]),
+    "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
+    "rc_batch_get_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
+    "rc_batch_tune": (_S, [_P, C.c_int32, C.POINTER(BatchTiles), C.POINTER(C.c_float)]),
 }
 
 _lib = None

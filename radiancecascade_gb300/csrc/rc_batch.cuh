@@ -9,23 +9,46 @@
 // always finish -- the launch makes progress whatever the residency.  The
 // wait is bounded: on timeout the block sets *err and every block stops.
 //
-// An item is a tile of `ppi` probes x `qpi` parent texels (their 4 child
-// directions each; level 0: every direction and the fluence), solved with the
-// exact scalar walk.  ppi and qpi are the autotuned tile shape.
+// An item runs the same block routines as the single-scene kernels:
+//   kBatchBits    `upi` blocks of the bit-parallel wide-level kernel;
+//   kBatchDirect0 `upi` blocks (8 warps each) of the walk-free cascade 0;
+//   kBatchWalk    `wpi` walk-queue tasks of one scene's narrow levels (lanes
+//                 refill from a block-local counter).  Walks depend only on
+//                 the scene, so these items come first and never wait;
+//   kBatchMerge   a tile of `ppi` probes x `qpi` parent-texel pairs of a
+//                 narrow level, merged from the walk records (waits for the
+//                 level above and for its scene's walks);
+//   kBatchScalar  a tile of `ppi` probes x `qpi` parent texels with the
+//                 scalar walk (levels without a decimated mask).
+// The tile shape (ppi, qpi, upi, wpi) is autotuned.  Radiance of the level
+// above and the walk records are written during the launch, so every block
+// routine reads them with weak loads after the acquire (never through the
+// read-only path).
 #pragma once
 
 #include "rc_kernels.cuh"
+#include "rc_level0.cuh"
+#include "rc_walk_bits.cuh"
+#include "rc_walk_queue.cuh"
 
 namespace rcx {
 
+enum { kBatchScalar = 0, kBatchBits = 1, kBatchDirect0 = 2, kBatchWalk = 3, kBatchMerge = 4 };
+
 struct BatchLevel {
   LevelArgs a;
-  int32_t up;       // index of the level above in the table, -1 at the top
-  int32_t ntiles;   // items of this level
-  int32_t ptiles;   // probe tiles (items = ptiles * qtiles)
+  const QueueArgs* q;    // walk: the scene's narrow-level walk queue
+  const uint32_t* rec;   // merge: this level's walk records
+  int32_t slots;         // merge: record slots per direction
+  int32_t up;            // index of the level above in the table, -1 at the top
+  int32_t dep2;          // merge: index of the scene's walk entry, else -1
+  int32_t ntiles;        // items of this entry
+  int32_t ptiles;        // scalar / merge: probe tiles (items = ptiles * texel tiles)
+  int32_t units;         // bits / direct0: blocks of the single-scene kernel
+  int32_t mode;          // kBatch*
   int32_t is_l0;
   int32_t is_top;
-  int32_t pad[3];
+  int32_t pad;
 };
 
 struct BatchItem {
@@ -33,7 +56,13 @@ struct BatchItem {
   int32_t tile;
 };
 
-constexpr int kBatchThreads = 128;
+struct BatchTiles {
+  int32_t ppi, qpi, upi, wpi;
+};
+
+constexpr int kBatchWalkSteps = 2;  // walk steps per lane between refills (register budget)
+constexpr int kBatchThreads = kBitsThreads;  // 8 warps, as the block routines expect
+static_assert(kBatchThreads == kL0Threads, "cascade-0 blocks are 8 warps");
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -41,107 +70,88 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// The next level's child-averaged radiance is written during this launch:
-// read it around L1 (coherent at L2).
-template <typename T>
-__device__ __forceinline__ float load_cg(const T* p);
-template <>
-__device__ __forceinline__ float load_cg<float>(const float* p) {
-  return __ldcg(p);
-}
-template <>
-__device__ __forceinline__ float load_cg<__half>(const __half* p) {
-  return __half2float(__ushort_as_half(__ldcg(reinterpret_cast<const unsigned short*>(p))));
+// Flattened (probe, parent texel group) units of a scalar / merge tile.
+struct TileUnits {
+  int64_t p0;
+  int np, g0, ng;
+};
+
+__device__ __forceinline__ TileUnits tile_units(const BatchLevel& lv, int tile, int ppi, int qpi, int ngroups) {
+  TileUnits u;
+  const int pt = tile % lv.ptiles, qt = tile / lv.ptiles;
+  u.p0 = (int64_t)pt * ppi;
+  u.np = (int)min((int64_t)ppi, lv.a.P - u.p0);
+  u.g0 = qt * qpi;
+  u.ng = min(qpi, ngroups - u.g0);
+  return u;
 }
 
-// One probe of one item: the scalar walk and merge of k_level_scalar.
-template <typename T>
-__device__ __forceinline__ void batch_probe(const LevelArgs& a, bool L0, bool TOP, int64_t p, int dp0, int ndp) {
-  const int mx = (int)(p % a.M[0]);
-  const int my = (int)((p / a.M[0]) % a.M[1]);
-  const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
-  const int h = a.spacing >> 1;
-  const int ox = mx * a.spacing + h, oy = my * a.spacing + h, oz = mz * a.spacing + h;
-  int64_t tap_off[8];
-  float tap_w[8];
-  if (!TOP) {
-    int q[3][2];
-    float w[3][2];
-    const int m[3] = {mx, my, mz};
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const int lo = (m[ax] - 1) >> 1;
-      w[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
-      w[ax][1] = 1.0f - w[ax][0];
-      q[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
-      q[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
-    }
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const int tx = t & 1, ty = (t >> 1) & 1, tz = t >> 2;
-      tap_off[t] = ((int64_t)q[2][tz] * a.UM[1] + q[1][ty]) * a.UM[0] + q[0][tx];
-      tap_w[t] = w[2][tz] * w[1][ty] * w[0][tx];
-    }
-  }
-  T* L = static_cast<T*>(a.L);
-  const T* Au = static_cast<const T*>(a.A_up);
+// One function per item kind (not inlined), so that each gets its own
+// register allocation.
+template <typename T, bool L0, bool TOP>
+__device__ __noinline__ void bits_item(const LevelArgs& a, int b0, int b1, uint32_t* s_hit) {
+  for (int bid = b0; bid < b1; ++bid) level_bits_block<T, L0, TOP, true>(a, bid, s_hit);
+}
+
+template <typename T, bool TOP>
+__device__ __noinline__ void direct0_item(const LevelArgs& a, int b0, int b1) {
+  const int warp = threadIdx.x >> 5;
+  for (int blk = b0; blk < b1; ++blk) level0_direct_warp<T, TOP, true>(a, (int64_t)blk * 8 + warp);
+}
+
+template <typename T, bool L0, bool TOP>
+__device__ __noinline__ void merge_item(const LevelArgs& a, const uint32_t* rec, int slots, TileUnits u) {
+  for (int j = threadIdx.x; j < u.np * u.ng; j += blockDim.x)
+    merge_probe<T, L0, TOP, true>(a, rec, slots, u.p0 + j % u.np, u.g0 + j / u.np);
+}
+
+template <typename T, bool L0, bool TOP>
+__device__ __noinline__ void scalar_item(const LevelArgs& a, TileUnits u) {
+  for (int j = threadIdx.x; j < u.np * u.ng; j += blockDim.x)
+    scalar_probe<T, L0, TOP, true>(a, u.p0 + j % u.np, u.g0 + j / u.np, 1);
+}
+
+template <typename T, bool L0, bool TOP>
+__device__ __forceinline__ void batch_item(const BatchLevel& lv, int tile, const BatchTiles& ts, uint32_t* s_hit) {
+  const LevelArgs& a = lv.a;
   const int hn = a.n >> 1;
-  const int64_t npar = (int64_t)hn * hn;
-  float flu[3] = {0.f, 0.f, 0.f};
-  const int nd = L0 ? a.ndirs : 4 * ndp;
-  for (int c = 0; c < nd; ++c) {
-    int d;
-    if (L0) {
-      d = c;
-    } else {
-      const int dp = dp0 + (c >> 2), cc = c & 3;
-      d = (2 * (dp / hn) + (cc >> 1)) * a.n + 2 * (dp % hn) + (cc & 1);
-    }
-    const DirInfo di = a.dirs[d];
-    const int64_t hit = walk_interval(a.occ, a.G, a.W, ox + di.start_off[0], oy + di.start_off[1],
-                                      oz + di.start_off[2], di, L0);
-    float r[3];
-    if (hit >= 0) {
-      voxel_emission(a.vol, hit, r);
-    } else if (TOP) {
-      r[0] = r[1] = r[2] = 0.f;
-    } else {
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        const T* base = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-        float s = 0.f;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) s = fmaf(tap_w[t], load_cg<T>(base + tap_off[t]), s);
-        r[ch] = s;
-      }
-    }
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) {
-      Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, r[ch]);
-      flu[ch] = L0 ? fmaf(di.omega, r[ch], flu[ch]) : flu[ch] + r[ch];
-    }
-    if (!L0 && (c & 3) == 3) {
-      T* A = static_cast<T*>(a.A_out);
-      const int dp = dp0 + (c >> 2);
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * flu[ch]);
-        flu[ch] = 0.f;
-      }
-    }
-  }
-  if (L0) {
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = flu[ch];
+  if (lv.mode == kBatchBits) {
+    bits_item<T, L0, TOP>(a, tile * ts.upi, min((tile + 1) * ts.upi, lv.units), s_hit);
+  } else if (L0 && lv.mode == kBatchDirect0) {
+    direct0_item<T, TOP>(a, tile * ts.upi, min((tile + 1) * ts.upi, lv.units));
+  } else if (lv.mode == kBatchMerge) {
+    merge_item<T, L0, TOP>(a, lv.rec, lv.slots, tile_units(lv, tile, ts.ppi, ts.qpi, L0 ? 1 : hn * hn / 2));
+  } else {
+    scalar_item<T, L0, TOP>(a, tile_units(lv, tile, ts.ppi, ts.qpi, L0 ? 1 : hn * hn));
   }
 }
 
+__device__ __forceinline__ void batch_walk(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+  walk_tasks<kBatchWalkSteps>(q, counter, end);
+}
+
+// Bounded wait (about one second of SM clocks) until entry `e` has finished
+// all its items; false on timeout or when another block gave up.
+__device__ __forceinline__ bool wait_entry(const BatchLevel* levels, const unsigned* done, int e, int* err) {
+  const unsigned need = (unsigned)levels[e].ntiles;
+  const long long start = clock64();
+  while (ld_acquire(&done[e]) < need) {
+    if (*(volatile int*)err || clock64() - start > 2000000000ll) {
+      atomicExch(err, 1);
+      return false;
+    }
+    __nanosleep(256);
+  }
+  return true;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kBatchThreads) k_batch_persistent(const BatchLevel* __restrict__ levels,
-                                                                    const BatchItem* __restrict__ items, int nitems,
-                                                                    int ppi, int qpi, unsigned* next, unsigned* done,
-                                                                    int* err) {
+__global__ void __launch_bounds__(kBatchThreads, 3)
+    k_batch_persistent(const BatchLevel* __restrict__ levels, const BatchItem* __restrict__ items, int nitems,
+                       const BatchTiles ts, unsigned* next, unsigned* done, int* err) {
+  extern __shared__ uint32_t s_hit[];
   __shared__ int s_item, s_stop;
+  __shared__ unsigned long long s_walk;
   for (;;) {
     if (threadIdx.x == 0) {
       s_item = (*(volatile int*)err) ? nitems : (int)atomicAdd(next, 1u);
@@ -152,39 +162,29 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_persistent(const BatchL
     if (it >= nitems) break;
     const BatchItem bi = items[it];
     const BatchLevel& lv = levels[bi.level];
-    if (lv.up >= 0 && threadIdx.x == 0) {
-      // bounded wait for the whole level above (about one second of SM clocks)
-      const unsigned need = (unsigned)levels[lv.up].ntiles;
-      const long long start = clock64();
-      while (ld_acquire(&done[lv.up]) < need) {
-        if (*(volatile int*)err || clock64() - start > 2000000000ll) {
-          atomicExch(err, 1);
-          s_stop = 1;
-          break;
-        }
-        __nanosleep(256);
-      }
+    if (threadIdx.x == 0) {
+      if ((lv.up >= 0 && !wait_entry(levels, done, lv.up, err)) ||
+          (lv.dep2 >= 0 && !wait_entry(levels, done, lv.dep2, err)))
+        s_stop = 1;
+      if (lv.mode == kBatchWalk) s_walk = (unsigned long long)bi.tile * ts.wpi;
     }
     __syncthreads();
     if (s_stop) break;
-    const int pt = bi.tile % lv.ptiles, qt = bi.tile / lv.ptiles;
-    const int hn = lv.a.n >> 1;
-    const int npar = hn * hn;
-    const int dp0 = qt * qpi, ndp = min(qpi, npar - dp0);
-    for (int j = threadIdx.x; j < ppi; j += blockDim.x) {
-      const int64_t p = (int64_t)pt * ppi + j;
-      if (p >= lv.a.P) break;
-      if (lv.is_l0) {
-        if (lv.is_top) batch_probe<T>(lv.a, true, true, p, 0, 0);
-        else batch_probe<T>(lv.a, true, false, p, 0, 0);
-      } else {
-        if (lv.is_top) batch_probe<T>(lv.a, false, true, p, dp0, ndp);
-        else batch_probe<T>(lv.a, false, false, p, dp0, ndp);
-      }
+    if (lv.mode == kBatchWalk) {
+      batch_walk(*lv.q, &s_walk, min((int64_t)(bi.tile + 1) * ts.wpi, lv.q->total));
+    } else if (lv.is_l0) {
+      if (lv.is_top) batch_item<T, true, true>(lv, bi.tile, ts, s_hit);
+      else batch_item<T, true, false>(lv, bi.tile, ts, s_hit);
+    } else {
+      if (lv.is_top) batch_item<T, false, true>(lv, bi.tile, ts, s_hit);
+      else batch_item<T, false, false>(lv, bi.tile, ts, s_hit);
     }
-    __threadfence();  // this block's outputs are visible before the item counts as done
+    // Cascade 0 feeds no other item: its stores drain while the block goes
+    // on.  Otherwise this block's outputs are visible before the item counts.
+    const bool feeds = !lv.is_l0;
+    if (feeds) __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) atomicAdd(&done[bi.level], 1u);
+    if (feeds && threadIdx.x == 0) atomicAdd(&done[bi.level], 1u);
   }
 }
 

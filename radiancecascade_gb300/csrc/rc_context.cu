@@ -466,8 +466,8 @@ cudaError_t allow_bits_smem() {
 
 }  // namespace
 
-// Creates a context.  A minimal context (used for the scenes of a batch)
-// solves every level with the scalar walk and allocates no decimated masks.
+// Creates a context.  A minimal context (a scene of a batch) is solved only
+// through the batch kernel: it sets up no TMA descriptor.
 static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc_context** out) {
   if (!out) {
     rcx::set_error("rc_create: out is NULL");
@@ -538,7 +538,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
     return fail(s);
   {
     // Decimated opacity per level (bit-parallel walk).
-    const bool force_scalar = minimal || (getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0);
+    const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
     int64_t total = 0;
     int64_t off[kMaxCascades];
     c->mset.n = 0;
@@ -1105,12 +1105,13 @@ struct rc_batch {
   cudaStream_t stream = nullptr;
   BatchLevel* d_levels = nullptr;
   BatchItem* d_items = nullptr;
+  QueueArgs* d_qargs = nullptr;  // per scene: its narrow-level walk queue
   unsigned* d_next = nullptr;
   unsigned* d_done = nullptr;
   int* d_err = nullptr;
   size_t levels_cap = 0, items_cap = 0;
   int nlevels = 0, nitems = 0;
-  int ppi = 256, qpi = 2;  // tile shape: probes and parent texels per item
+  BatchTiles tiles{256, 4, 1, 1024};
   int blocks = 0;
   bool fp16 = false;
   cudaGraphExec_t graph = nullptr;
@@ -1123,29 +1124,69 @@ void batch_free_graph(rc_batch* b) {
   b->graph = nullptr;
 }
 
-// Level table and top-level-first item queue for tile shape (ppi, qpi).
-rc_status batch_build(rc_batch* b, int ppi, int qpi) {
+bool tiles_valid(const rc_batch_tiles* t) {
+  auto ok = [](int32_t v) { return v >= 1 && v <= 65536; };
+  return t && ok(t->probes_per_item) && ok(t->dirs_per_item) && ok(t->blocks_per_item) && ok(t->walks_per_item);
+}
+
+// Level table and item queue for tile shape `ts`: every scene's walk tasks
+// first, then the levels top first across scenes.
+rc_status batch_build(rc_batch* b, const BatchTiles& ts) {
   std::vector<BatchLevel> lv;
-  std::vector<int> first(b->n);
+  std::vector<int> first(b->n), walk(b->n, -1);
   int maxN = 0;
   for (int k = 0; k < b->n; ++k) {
     rc_context* c = b->scenes[k];
-    first[k] = (int)lv.size();
     maxN = std::max(maxN, c->nlev);
+    if (c->qargs.total > 0) {
+      BatchLevel W;
+      memset(&W, 0, sizeof W);
+      W.mode = kBatchWalk;
+      W.q = b->d_qargs + k;
+      W.up = W.dep2 = -1;
+      W.ntiles = (int)((c->qargs.total + ts.wpi - 1) / ts.wpi);
+      walk[k] = (int)lv.size();
+      lv.push_back(W);
+    }
+    first[k] = (int)lv.size();
     for (int i = 0; i < c->nlev; ++i) {
       BatchLevel L;
       memset(&L, 0, sizeof L);
-      L.a = c->args[i];
+      const LevelArgs& a = c->args[i];
+      L.a = a;
       L.up = (i + 1 < c->nlev) ? first[k] + i + 1 : -1;
+      L.dep2 = -1;
       L.is_l0 = (i == 0);
       L.is_top = (i == c->nlev - 1);
-      L.ptiles = (int)((c->geom[i].probes() + ppi - 1) / ppi);
-      const int npar = (i == 0) ? 1 : c->geom[i - 1].ndirs;
-      L.ntiles = L.ptiles * (i == 0 ? 1 : (npar + qpi - 1) / qpi);
+      const int64_t npar = (i == 0) ? 1 : c->geom[i - 1].ndirs;
+      if (c->mode[i] == kModeFused) {
+        L.mode = kBatchBits;
+        L.units = a.tiles * (i == 0 ? 1 : (a.n / 2) * (a.n / 2) / 2);
+        L.ntiles = (L.units + ts.upi - 1) / ts.upi;
+      } else if (c->mode[i] == kModeDirect0) {
+        L.mode = kBatchDirect0;
+        const int64_t warps = (int64_t)((a.M[0] + 127) / 128) * a.M[1] * ((a.M[2] + 1) / 2);
+        L.units = (int)((warps + 7) / 8);
+        L.ntiles = (L.units + ts.upi - 1) / ts.upi;
+      } else {
+        const bool merge = c->mode[i] == kModeQueue;
+        L.mode = merge ? kBatchMerge : kBatchScalar;
+        if (merge) {
+          L.rec = c->rec_level[i];
+          L.slots = c->rec_slots[i];
+          L.dep2 = walk[k];
+        }
+        const int64_t groups = (i == 0) ? 1 : (merge ? npar / 2 : npar);
+        L.ptiles = (int)((a.P + ts.ppi - 1) / ts.ppi);
+        L.ntiles = (int)(L.ptiles * ((groups + ts.qpi - 1) / ts.qpi));
+      }
       lv.push_back(L);
     }
   }
   std::vector<BatchItem> items;
+  for (int k = 0; k < b->n; ++k)
+    if (walk[k] >= 0)
+      for (int t = 0; t < lv[walk[k]].ntiles; ++t) items.push_back(BatchItem{walk[k], t});
   for (int t = 0; t < maxN; ++t)
     for (int k = 0; k < b->n; ++k) {
       const int N = b->scenes[k]->nlev;
@@ -1154,7 +1195,7 @@ rc_status batch_build(rc_batch* b, int ppi, int qpi) {
       for (int tile = 0; tile < lv[li].ntiles; ++tile) items.push_back(BatchItem{li, tile});
     }
   // Fault injection for tests: one level waits for a tile that never comes.
-  if (fault_is("timeout") && !lv.empty()) lv[first[0] + b->scenes[0]->nlev - 1].ntiles += 1;
+  if (fault_is("timeout")) lv[first[0] + b->scenes[0]->nlev - 1].ntiles += 1;
   DeviceGuard g(b->device);
   if (lv.size() > b->levels_cap) {
     if (b->d_levels) cudaFree(b->d_levels);
@@ -1178,12 +1219,13 @@ rc_status batch_build(rc_batch* b, int ppi, int qpi) {
           "batch upload");
   b->nlevels = (int)lv.size();
   b->nitems = (int)items.size();
-  b->ppi = ppi;
-  b->qpi = qpi;
+  b->tiles = ts;
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  if (b->fp16) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<__half>, kBatchThreads, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<float>, kBatchThreads, 0);
+  if (b->fp16)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<__half>, kBatchThreads, kBitsSmem);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_persistent<float>, kBatchThreads, kBitsSmem);
   (void)cudaGetLastError();
   b->blocks = std::max(1, std::min(b->nitems, std::max(1, sms * std::max(per_sm, 1))));
   batch_free_graph(b);
@@ -1194,11 +1236,11 @@ void batch_enqueue(rc_batch* b, cudaStream_t s) {
   cudaMemsetAsync(b->d_next, 0, sizeof(unsigned), s);
   cudaMemsetAsync(b->d_done, 0, (size_t)b->nlevels * sizeof(unsigned), s);
   if (b->fp16)
-    k_batch_persistent<__half><<<b->blocks, kBatchThreads, 0, s>>>(b->d_levels, b->d_items, b->nitems, b->ppi,
-                                                                    b->qpi, b->d_next, b->d_done, b->d_err);
+    k_batch_persistent<__half><<<b->blocks, kBatchThreads, kBitsSmem, s>>>(b->d_levels, b->d_items, b->nitems,
+                                                                           b->tiles, b->d_next, b->d_done, b->d_err);
   else
-    k_batch_persistent<float><<<b->blocks, kBatchThreads, 0, s>>>(b->d_levels, b->d_items, b->nitems, b->ppi,
-                                                                   b->qpi, b->d_next, b->d_done, b->d_err);
+    k_batch_persistent<float><<<b->blocks, kBatchThreads, kBitsSmem, s>>>(b->d_levels, b->d_items, b->nitems,
+                                                                          b->tiles, b->d_next, b->d_done, b->d_err);
 }
 
 // The whole batch solve as one CUDA graph (two counter resets + one launch).
@@ -1279,7 +1321,15 @@ rc_status rc_batch_create(const rc_params* params, int32_t nscenes, int32_t devi
   if ((s = dev_alloc((void**)&b->d_next, sizeof(unsigned), "batch queue")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&b->d_err, sizeof(int), "batch error flag")) != RC_OK) return fail(s);
   if ((e = cudaMemset(b->d_err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_batch_create"));
-  if ((s = batch_build(b, b->ppi, b->qpi)) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&b->d_qargs, (size_t)nscenes * sizeof(QueueArgs), "batch walk queues")) != RC_OK)
+    return fail(s);
+  {
+    std::vector<QueueArgs> qa((size_t)nscenes);
+    for (int k = 0; k < nscenes; ++k) qa[k] = b->scenes[k]->qargs;
+    if ((e = cudaMemcpy(b->d_qargs, qa.data(), qa.size() * sizeof(QueueArgs), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(cuda_fail(e, "rc_batch_create: upload"));
+  }
+  if ((s = batch_build(b, b->tiles)) != RC_OK) return fail(s);
   *out = b;
   return RC_OK;
 }
@@ -1290,7 +1340,7 @@ rc_status rc_batch_destroy(rc_batch* b) {
     DeviceGuard g(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     batch_free_graph(b);
-    void* bufs[] = {b->d_levels, b->d_items, b->d_next, b->d_done, b->d_err};
+    void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err};
     for (void* x : bufs)
       if (x) cudaFree(x);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -1306,6 +1356,11 @@ rc_status rc_batch_scene_set(rc_batch* b, int32_t scene, const rc_box* boxes, in
   if (scene < 0 || scene >= b->n) {
     rcx::set_error("rc_batch_scene_set: scene %d out of range", scene);
     return RC_ERR_INVALID_ARG;
+  }
+  {
+    // the scene's volume must not change under a solve in flight
+    DeviceGuard g(b->device);
+    RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_scene_set");
   }
   rc_status s = rc_scene_set_boxes(b->scenes[scene], boxes, nboxes);
   if (s != RC_OK) return s;
@@ -1365,58 +1420,87 @@ rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level, void*
   return rc_get_radiance(b->scenes[scene], level, out, bytes, where);
 }
 
-rc_status rc_batch_set_tiles(rc_batch* b, int32_t probes_per_item, int32_t dirs_per_item) {
+rc_status rc_batch_set_tiles(rc_batch* b, const rc_batch_tiles* tiles) {
   if (batch_check(b, "rc_batch_set_tiles") != RC_OK) return RC_ERR_INVALID_ARG;
-  if (probes_per_item < 1 || probes_per_item > 65536 || dirs_per_item < 1 || dirs_per_item > 65536) {
-    rcx::set_error("rc_batch_set_tiles: tile sizes must be in [1, 65536]");
+  if (!tiles_valid(tiles)) {
+    rcx::set_error("rc_batch_set_tiles: every tile size must be in [1, 65536]");
     return RC_ERR_INVALID_ARG;
   }
   DeviceGuard g(b->device);
   RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_set_tiles");
-  return batch_build(b, probes_per_item, dirs_per_item);
+  const BatchTiles ts{tiles->probes_per_item, tiles->dirs_per_item, tiles->blocks_per_item, tiles->walks_per_item};
+  return batch_build(b, ts);
 }
 
-rc_status rc_batch_tune(rc_batch* b, int32_t iters, int32_t* probes_per_item, int32_t* dirs_per_item,
-                        float* best_ms) {
+rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out) {
+  if (batch_check(b, "rc_batch_get_tiles") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!out) {
+    rcx::set_error("rc_batch_get_tiles: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  out->probes_per_item = b->tiles.ppi;
+  out->dirs_per_item = b->tiles.qpi;
+  out->blocks_per_item = b->tiles.upi;
+  out->walks_per_item = b->tiles.wpi;
+  return RC_OK;
+}
+
+// Coordinate descent over the tile shape: each parameter in turn over its
+// candidates with the others held, two sweeps, every candidate timed over
+// `iters` graph launches after one warm-up launch.
+rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best_out, float* best_ms) {
   if (batch_check(b, "rc_batch_tune") != RC_OK) return RC_ERR_INVALID_ARG;
   if (iters < 1) {
     rcx::set_error("rc_batch_tune: iters must be >= 1");
     return RC_ERR_INVALID_ARG;
   }
-  static const int kPpi[] = {128, 256, 512, 1024};
-  static const int kQpi[] = {1, 2, 4, 8};
+  static const int kCand[4][4] = {{64, 128, 256, 512}, {1, 2, 4, 16}, {1, 2, 4, 8}, {256, 1024, 4096, 16384}};
   DeviceGuard g(b->device);
   cudaEvent_t e0, e1;
   RC_CUDA(cudaEventCreate(&e0), "rc_batch_tune: event");
   RC_CUDA(cudaEventCreate(&e1), "rc_batch_tune: event");
-  float best = 3.4e38f;
-  int bp = b->ppi, bq = b->qpi;
+  BatchTiles best = b->tiles;
+  float best_t = 3.4e38f;
   rc_status st = RC_OK;
-  for (int ppi : kPpi)
-    for (int qpi : kQpi) {
-      if ((st = batch_build(b, ppi, qpi)) != RC_OK) break;
-      if ((st = rc_batch_solve(b, nullptr)) != RC_OK) break;  // warm-up (builds the graph)
-      cudaEventRecord(e0, b->stream);
-      for (int i = 0; i < iters && st == RC_OK; ++i) st = rc_batch_solve(b, nullptr);
-      cudaEventRecord(e1, b->stream);
-      if (st == RC_OK) st = rc_batch_synchronize(b);
-      if (st != RC_OK) break;
-      float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
-      ms /= iters;
-      if (ms < best) {
-        best = ms;
-        bp = ppi;
-        bq = qpi;
+  auto time_shape = [&](const BatchTiles& ts, float* ms) -> rc_status {
+    rc_status r;
+    if ((r = batch_build(b, ts)) != RC_OK) return r;
+    if ((r = rc_batch_solve(b, nullptr)) != RC_OK) return r;  // warm-up (builds the graph)
+    cudaEventRecord(e0, b->stream);
+    for (int i = 0; i < iters; ++i)
+      if ((r = rc_batch_solve(b, nullptr)) != RC_OK) return r;
+    cudaEventRecord(e1, b->stream);
+    if ((r = rc_batch_synchronize(b)) != RC_OK) return r;
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= iters;
+    return RC_OK;
+  };
+  st = time_shape(best, &best_t);
+  for (int sweep = 0; sweep < 2 && st == RC_OK; ++sweep)
+    for (int dim = 0; dim < 4 && st == RC_OK; ++dim)
+      for (int ci = 0; ci < 4 && st == RC_OK; ++ci) {
+        BatchTiles ts = best;
+        int* f[4] = {&ts.ppi, &ts.qpi, &ts.upi, &ts.wpi};
+        if (*f[dim] == kCand[dim][ci]) continue;
+        *f[dim] = kCand[dim][ci];
+        float ms = 0.f;
+        if ((st = time_shape(ts, &ms)) != RC_OK) break;
+        if (ms < best_t) {
+          best_t = ms;
+          best = ts;
+        }
       }
-    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != RC_OK) return st;
-  if ((st = batch_build(b, bp, bq)) != RC_OK) return st;
-  if (probes_per_item) *probes_per_item = bp;
-  if (dirs_per_item) *dirs_per_item = bq;
-  if (best_ms) *best_ms = best;
+  if ((st = batch_build(b, best)) != RC_OK) return st;
+  if (best_out) {
+    best_out->probes_per_item = best.ppi;
+    best_out->dirs_per_item = best.qpi;
+    best_out->blocks_per_item = best.upi;
+    best_out->walks_per_item = best.wpi;
+  }
+  if (best_ms) *best_ms = best_t;
   return RC_OK;
 }
 

@@ -34,6 +34,26 @@ struct Store<__half> {
   }
 };
 
+// Reads of the next level's child-averaged radiance.  It is normally written
+// by an earlier launch and read through the read-only (non-coherent) path.
+// In the batched persistent solve (CG) it is written during the same launch:
+// it is read with ordinary weak loads, after an acquire of the producer's
+// completion counter, never through the read-only path.  (No line of it can
+// sit in L1 before that point: nothing on the SM reads it earlier in the
+// launch, and L1 starts empty of it at every launch.)
+template <typename T, bool CG>
+__device__ __forceinline__ float load_up(const T* p);
+template <>
+__device__ __forceinline__ float load_up<float, false>(const float* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ float load_up<float, true>(const float* p) { return __ldca(p); }
+template <>
+__device__ __forceinline__ float load_up<__half, false>(const __half* p) { return __half2float(__ldg(p)); }
+template <>
+__device__ __forceinline__ float load_up<__half, true>(const __half* p) {
+  return __half2float(__ushort_as_half(__ldca(reinterpret_cast<const unsigned short*>(p))));
+}
+
 __device__ __forceinline__ float to_float(float v) { return v; }
 __device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
 
@@ -109,16 +129,14 @@ __device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol,
   return __half2float(__ushort_as_half((unsigned short)(ch == 1 ? (w >> 16) : (w & 0xFFFFu))));
 }
 
-// One thread per probe.  Level 0 (L0) walks every direction and reduces the
-// fluence; other levels walk the four child directions of the parent texel
-// blockIdx.y and write their average for the level below.  Unless TOP, rays
-// that reach the end of their interval take the trilinear blend of the 8
-// nearest next-level probes (child index m sits at parent coordinate
-// m/2 - 1/4, clamped at the border) of the child-averaged radiance.
-template <typename T, bool L0, bool TOP>
-__global__ void __launch_bounds__(128) k_level_scalar(const LevelArgs a) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.P) return;
+// One probe p, scalar walk.  Level 0 (L0) walks every direction and reduces
+// the fluence; other levels walk the four child directions of each parent
+// texel dp0 .. dp0 + ndp - 1 and write their average for the level below.
+// Unless TOP, rays that reach the end of their interval take the trilinear
+// blend of the 8 nearest next-level probes (child index m sits at parent
+// coordinate m/2 - 1/4, clamped at the border) of the child-averaged radiance.
+template <typename T, bool L0, bool TOP, bool CG>
+__device__ __forceinline__ void scalar_probe(const LevelArgs& a, int64_t p, int dp0, int ndp) {
   const int mx = (int)(p % a.M[0]);
   const int my = (int)((p / a.M[0]) % a.M[1]);
   const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
@@ -147,17 +165,17 @@ __global__ void __launch_bounds__(128) k_level_scalar(const LevelArgs a) {
     }
   }
 
-  float acc[3] = {0.f, 0.f, 0.f};
-  const int nchild = L0 ? a.ndirs : 4;
+  T* L = static_cast<T*>(a.L);
   const int hn = a.n >> 1;
-  const int dp = blockIdx.y;
-  for (int c = 0; c < nchild; ++c) {
+  float acc[3] = {0.f, 0.f, 0.f};
+  const int nd = L0 ? a.ndirs : 4 * ndp;
+  for (int c = 0; c < nd; ++c) {
     int d;
     if (L0) {
       d = c;
     } else {
-      const int jp = dp % hn, kp = dp / hn;
-      d = (2 * kp + (c >> 1)) * a.n + 2 * jp + (c & 1);
+      const int dp = dp0 + (c >> 2), cc = c & 3;
+      d = (2 * (dp / hn) + (cc >> 1)) * a.n + 2 * (dp % hn) + (cc & 1);
     }
     const DirInfo di = a.dirs[d];
     const int64_t hit = walk_interval(a.occ, a.G, a.W, ox + di.start_off[0], oy + di.start_off[1],
@@ -174,26 +192,38 @@ __global__ void __launch_bounds__(128) k_level_scalar(const LevelArgs a) {
         const T* base = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
         float s = 0.f;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) s = fmaf(tap_w[t], Store<T>::load(base + tap_off[t]), s);
+        for (int t = 0; t < 8; ++t) s = fmaf(tap_w[t], load_up<T, CG>(base + tap_off[t]), s);
         r[ch] = s;
       }
     }
-    T* L = static_cast<T*>(a.L);
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
       Store<T>::store(L + ((int64_t)ch * a.ndirs + d) * a.P + p, r[ch]);
       acc[ch] = L0 ? fmaf(di.omega, r[ch], acc[ch]) : acc[ch] + r[ch];
     }
+    if (!L0 && (c & 3) == 3) {
+      T* A = static_cast<T*>(a.A_out);
+      const int64_t npar = (int64_t)hn * hn;
+      const int dp = dp0 + (c >> 2);
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
+        acc[ch] = 0.f;
+      }
+    }
   }
   if (L0) {
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
-  } else {
-    T* A = static_cast<T*>(a.A_out);
-    const int64_t npar = (int64_t)hn * hn;
-#pragma unroll
-    for (int ch = 0; ch < 3; ++ch) Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
   }
+}
+
+// One thread per probe; block row blockIdx.y = parent texel (not level 0).
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(128) k_level_scalar(const __grid_constant__ LevelArgs a) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  scalar_probe<T, L0, TOP, false>(a, p, blockIdx.y, 1);
 }
 
 // Base volume from boxes: the last box containing a voxel wins.

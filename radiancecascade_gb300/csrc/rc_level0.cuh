@@ -40,26 +40,38 @@ struct Vec4<__half> {
   }
 };
 
-template <typename T>
+// Two adjacent values of the next level's child-averaged radiance (CG: data
+// written during the same launch, see load_up).
+template <typename T, bool CG>
 __device__ __forceinline__ float2 load2(const T* p);
 template <>
-__device__ __forceinline__ float2 load2<float>(const float* p) {
+__device__ __forceinline__ float2 load2<float, false>(const float* p) {
   return __ldg(reinterpret_cast<const float2*>(p));
 }
 template <>
-__device__ __forceinline__ float2 load2<__half>(const __half* p) {
+__device__ __forceinline__ float2 load2<float, true>(const float* p) {
+  return __ldca(reinterpret_cast<const float2*>(p));
+}
+template <>
+__device__ __forceinline__ float2 load2<__half, false>(const __half* p) {
   return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+}
+template <>
+__device__ __forceinline__ float2 load2<__half, true>(const __half* p) {
+  const unsigned u = __ldca(reinterpret_cast<const unsigned*>(p));
+  return __half22float2(*reinterpret_cast<const __half2*>(&u));
 }
 
 // Requires (checked on the host): probe spacing 2 (centres 2m+1, so the 8
 // candidate voxels are 2m, 2m+1 per axis), every cascade-0 direction takes 0
 // steps, and M[0] % 4 == 0.
-template <typename T, bool TOP>
-__global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const LevelArgs a) {
+// One warp's share: global warp index `wid` (chunk of 128 probes of a row,
+// two planes).
+template <typename T, bool TOP, bool CG>
+__device__ __forceinline__ void level0_direct_warp(const LevelArgs& a, int64_t wid) {
   const int lane = threadIdx.x & 31;
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int chunks = (Mx + 127) >> 7;
-  int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int cw = (int)(wid % chunks);
   wid /= chunks;
   const int y = (int)(wid % My);
@@ -159,14 +171,14 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const LevelArgs
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
             const T* row = src + rowoff[r][k];
-            own[k] = active ? load2<T>(row + col0) : make_float2(0.f, 0.f);
+            own[k] = active ? load2<T, CG>(row + col0) : make_float2(0.f, 0.f);
             lh[k] = __shfl_up_sync(0xFFFFFFFFu, own[k].y, 1);
             rh[k] = __shfl_down_sync(0xFFFFFFFFu, own[k].x, 1);
             if (lane == 0) lh[k] = own[k].x;
             if (last_lane) rh[k] = own[k].y;
             if (chunks > 1) {
-              if (lhalo_load) lh[k] = Store<T>::load(row + lcol);
-              if (rhalo_load) rh[k] = Store<T>::load(row + rcol);
+              if (lhalo_load) lh[k] = load_up<T, CG>(row + lcol);
+              if (rhalo_load) rh[k] = load_up<T, CG>(row + rcol);
             }
           }
           const float cols[3][4] = {{lh[0], own[0].x, own[0].y, rh[0]},
@@ -218,6 +230,11 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const LevelArgs
       for (int e = 0; e < 4; ++e) f[3 * e] = flu[zc][e];
     }
   }
+}
+
+template <typename T, bool TOP>
+__global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_constant__ LevelArgs a) {
+  level0_direct_warp<T, TOP, false>(a, ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 }
 
 // TMA-staged form of k_level0_direct.  Block = 8 child rows (one per warp) x

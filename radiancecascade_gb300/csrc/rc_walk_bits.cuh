@@ -313,13 +313,15 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
 //   loads one parent column (3 x 3 values per channel), interpolates z and y
 //   in registers and x through warp shuffles.
 // Level 0 reduces the fluence; other levels write the 2x2-child averages.
-template <typename T, bool L0, bool TOP>
-__global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const LevelArgs a) {
+// level_bits_block is one block's share (block index `bid`, shared memory
+// s_hit of kBitsSmem bytes); CG: the next level was written during the same
+// launch (see load_up).
+template <typename T, bool L0, bool TOP, bool CG>
+__device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, uint32_t* s_hit) {
   constexpr bool WIDE = true;  // narrow levels walk through the work queue (rc_walk_queue.cuh)
-  extern __shared__ uint32_t s_hit[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int tile_id = blockIdx.x % a.tiles;
-  const int dgroup = blockIdx.x / a.tiles;
+  const int tile_id = bid % a.tiles;
+  const int dgroup = bid / a.tiles;
   const Tile t = tile_of(a, tile_id);
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int npass = L0 ? (a.ndirs + kTileDirs - 1) / kTileDirs : 1;
@@ -402,7 +404,7 @@ __global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const LevelArgs 
             const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
             float av[9];
 #pragma unroll
-            for (int q = 0; q < 9; ++q) av[q] = ploader ? Store<T>::load(src + aoff[q]) : 0.f;
+            for (int q = 0; q < 9; ++q) av[q] = ploader ? load_up<T, CG>(src + aoff[q]) : 0.f;
 #pragma unroll
             for (int ez = 0; ez < 2; ++ez) {
               float zv[3];
@@ -463,6 +465,12 @@ __global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const LevelArgs 
       }
     }
   }
+}
+
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const __grid_constant__ LevelArgs a) {
+  extern __shared__ uint32_t s_hit[];
+  level_bits_block<T, L0, TOP, false>(a, blockIdx.x, s_hit);
 }
 
 }  // namespace rcx

@@ -194,7 +194,11 @@ struct Walker {
 
 constexpr int kQueueThreads = 256;
 
-__global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const QueueArgs q) {
+// Every warp walks queue items taken from *counter (a global or shared
+// counter) until the items up to `end` are gone; lanes refill one by one.
+// kBatch steps are issued per lane between refills.
+template <int kBatch>
+__device__ __forceinline__ void walk_tasks(const QueueArgs& q, unsigned long long* counter, int64_t end) {
   const int lane = threadIdx.x & 31;
   Walker w;
   bool active = false, exhausted = false;
@@ -203,11 +207,11 @@ __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const QueueArgs q)
     if (need) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(q.counter, (unsigned long long)__popc(need));
+      if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
       base = __shfl_sync(0xFFFFFFFFu, base, leader);
       if (!active && !exhausted) {
         const int64_t item = (int64_t)base + __popc(need & ((1u << lane) - 1u));
-        if (item >= q.total) exhausted = true;
+        if (item >= end) exhausted = true;
         else active = w.init(q, item);
       }
     }
@@ -215,23 +219,26 @@ __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const QueueArgs q)
       if (!__any_sync(0xFFFFFFFFu, !exhausted)) break;
       continue;
     }
-    if (active && w.batch<4>(q)) {
+    if (active && w.batch<kBatch>(q)) {
       w.finish();
       active = false;
     }
   }
 }
 
-// Merge of a narrow level from its walk records.  One thread per probe; the
-// block row blockIdx.y covers two parent texels (eight child directions), or
-// at level 0 every direction and the fluence.  Rays without a hit take the
-// trilinear blend of the 8 nearest next-level probes of the child-averaged
-// radiance (child index m sits at parent coordinate m/2 - 1/4, clamped).
-template <typename T, bool L0, bool TOP>
-__global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const uint32_t* __restrict__ rec,
-                                                     int slots) {
-  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.P) return;
+__global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
+  walk_tasks<4>(q, q.counter, q.total);
+}
+
+// Merge of a narrow level from its walk records, probe p: parent texels
+// 2 dpair and 2 dpair + 1 (eight child directions), or at level 0 every
+// direction and the fluence.  Rays without a hit take the trilinear blend of
+// the 8 nearest next-level probes of the child-averaged radiance (child index
+// m sits at parent coordinate m/2 - 1/4, clamped).  CG: the records and the
+// next level were written during the same launch (see load_up).
+template <typename T, bool L0, bool TOP, bool CG>
+__device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* __restrict__ rec, int slots,
+                                            int64_t p, int dpair) {
   const int Mx = a.M[0], My = a.M[1];
   const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
   const int g = (my << a.l2px) + mx;
@@ -269,10 +276,11 @@ __global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const ui
     if (L0) {
       d = dl;
     } else {
-      const int dp = blockIdx.y * 2 + (dl >> 2), c = dl & 3;
+      const int dp = dpair * 2 + (dl >> 2), c = dl & 3;
       d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
     }
-    const uint32_t r = __ldg(&rec[(int64_t)d * slots * 32 + rbase]);
+    const uint32_t* rp = &rec[(int64_t)d * slots * 32 + rbase];
+    const uint32_t r = CG ? __ldca(rp) : __ldg(rp);
     float rv[3] = {0.f, 0.f, 0.f};
     if (r == kMiss) {
       if (!TOP) {
@@ -281,7 +289,7 @@ __global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const ui
           const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
           float sum = 0.f;
 #pragma unroll
-          for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
+          for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], load_up<T, CG>(src + tap_off[tp]), sum);
           rv[ch] = sum;
         }
       }
@@ -299,7 +307,7 @@ __global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const ui
       for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
       if ((dl & 3) == 3) {
         T* A = static_cast<T*>(a.A_out);
-        const int dp = blockIdx.y * 2 + (dl >> 2);
+        const int dp = dpair * 2 + (dl >> 2);
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
           Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
@@ -312,6 +320,15 @@ __global__ void __launch_bounds__(128) k_level_merge(const LevelArgs a, const ui
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
   }
+}
+
+// One thread per probe; block row blockIdx.y = pair of parent texels.
+template <typename T, bool L0, bool TOP>
+__global__ void __launch_bounds__(128) k_level_merge(const __grid_constant__ LevelArgs a,
+                                                     const uint32_t* __restrict__ rec, int slots) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  merge_probe<T, L0, TOP, false>(a, rec, slots, p, blockIdx.y);
 }
 
 }  // namespace rcx

@@ -95,6 +95,35 @@ WORKLOADS = {
 }
 
 
+# Batched workload: `count` cubic scenes, scene k seeded 2000 + k, edge drawn
+# uniformly from BATCH_EDGES by splitmix64(seed); the 64^3 workload's box and
+# sphere density per voxel (24 boxes and 4 spheres per 64^3, edges 4..20,
+# radius 2..5, emission 1..20, at least one of each); cascade count by edge.
+BATCH_EDGES = (32, 48, 64, 96, 128, 192)
+BATCH_CASCADES = {32: 4, 48: 4, 64: 5, 96: 5, 128: 6, 192: 6}
+
+
+def _splitmix64(x: int) -> int:
+    x = (x + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return x ^ (x >> 31)
+
+
+def batch_workload(count: int = 64, base_seed: int = 2000):
+    """-> [(edge, cascades, boxes, spheres)] for the batched workload."""
+    out = []
+    for k in range(count):
+        seed = base_seed + k
+        edge = BATCH_EDGES[_splitmix64(seed) % len(BATCH_EDGES)]
+        scale = (edge / 64.0) ** 3
+        nb, ns = max(1, round(24 * scale)), max(1, round(4 * scale))
+        spec = scene_spec(edge, nb, (4, 20), ns, (2.0, 5.0), (1.0, 20.0))
+        boxes, spheres = generate_scene(spec, seed)
+        out.append((edge, BATCH_CASCADES[edge], boxes, spheres))
+    return out
+
+
 def workload_scene(name: str, frame: int = 0):
     w = WORKLOADS[name]
     spec = scene_spec(w["grid"], w["boxes"], w["edge"], w["spheres"], w["radius"], w["emission"])
@@ -268,14 +297,21 @@ class Batch:
         px, py, pz = info.probes
         return out.reshape(3, info.num_dirs, pz, py, px)
 
-    def set_tiles(self, probes_per_item: int, dirs_per_item: int) -> None:
-        F.check(self._lib.rc_batch_set_tiles(self.handle, probes_per_item, dirs_per_item))
+    def set_tiles(self, probes_per_item: int, dirs_per_item: int, blocks_per_item: int = 1,
+                  walks_per_item: int = 1024) -> None:
+        t = F.BatchTiles(probes_per_item, dirs_per_item, blocks_per_item, walks_per_item)
+        F.check(self._lib.rc_batch_set_tiles(self.handle, C.byref(t)))
+
+    def tiles(self) -> dict:
+        t = F.BatchTiles()
+        F.check(self._lib.rc_batch_get_tiles(self.handle, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
 
     def tune(self, iters: int = 3):
-        """Times every candidate tile shape, keeps the fastest: (ppi, qpi, ms)."""
-        pp, qq, ms = C.c_int32(), C.c_int32(), C.c_float()
-        F.check(self._lib.rc_batch_tune(self.handle, iters, C.byref(pp), C.byref(qq), C.byref(ms)))
-        return pp.value, qq.value, ms.value
+        """Autotunes the tile shape; -> (tiles dict, ms per solve of the best)."""
+        t, ms = F.BatchTiles(), C.c_float()
+        F.check(self._lib.rc_batch_tune(self.handle, iters, C.byref(t), C.byref(ms)))
+        return {k: getattr(t, k) for k, _ in t._fields_}, ms.value
 
 
 @dataclass

@@ -62,7 +62,7 @@ def _check_all(b, oracle_results, rel=FP32_REL_L2, max_rel=FP32_MAX_REL):
                 assert np.abs(g - o).max() <= max_rel * max(1.0, np.abs(o).max()), (k, i)
 
 
-def test_batch_matches_oracle(oracle_results):
+def test_batch_matches_oracle(oracle_results, walk):
     with _batch() as b:
         b.solve()
         b.synchronize()
@@ -71,10 +71,22 @@ def test_batch_matches_oracle(oracle_results):
         _check_all(b, oracle_results)
 
 
-@pytest.mark.parametrize("ppi,qpi", [(1, 1), (32, 3), (128, 2), (1000, 64)])
-def test_batch_tile_shapes_give_the_same_results(ppi, qpi, oracle_results):
+@pytest.fixture(params=["default", "scalar"])
+def walk(request, monkeypatch):
+    """Batch scenes with the bit-parallel wide levels and walk-free cascade 0
+    (default), or with every level on the scalar walk."""
+    monkeypatch.delenv("RC_WALK", raising=False)
+    if request.param == "scalar":
+        monkeypatch.setenv("RC_WALK", "scalar")
+    return request.param
+
+
+@pytest.mark.parametrize("ppi,qpi,upi,wpi", [(1, 1, 1, 1), (32, 3, 2, 77), (128, 2, 3, 1024),
+                                             (1000, 64, 64, 65536)])
+def test_batch_tile_shapes_give_the_same_results(ppi, qpi, upi, wpi, oracle_results, walk):
     with _batch() as b:
-        b.set_tiles(ppi, qpi)
+        b.set_tiles(ppi, qpi, upi, wpi)
+        assert b.tiles() == dict(probes_per_item=ppi, dirs_per_item=qpi, blocks_per_item=upi, walks_per_item=wpi)
         b.solve()
         _check_all(b, oracle_results)
 
@@ -95,13 +107,13 @@ def test_batch_matches_single_contexts():
 
 def test_batch_autotuner_keeps_a_candidate(oracle_results):
     with _batch() as b:
-        ppi, qpi, ms = b.tune(iters=1)
-        assert ppi in (128, 256, 512, 1024) and qpi in (1, 2, 4, 8) and ms > 0
+        tiles, ms = b.tune(iters=1)
+        assert tiles == b.tiles() and ms > 0
         b.solve()
         _check_all(b, oracle_results)
 
 
-def test_batch_fp16(oracle_results):
+def test_batch_fp16(oracle_results, walk):
     with _batch("fp16") as b:
         b.solve()
         _check_all(b, oracle_results, rel=1e-2, max_rel=None)
@@ -118,7 +130,7 @@ def test_batch_state_and_argument_errors():
         out = np.zeros(3 * 16 ** 3, np.float32)
         assert F.lib().rc_batch_get_fluence(b.handle, 2, F.ptr(out), out.size, F.RC_MEM_HOST) == F.RC_ERR_INVALID_ARG
         with pytest.raises(R.RCError):
-            b.set_tiles(0, 1)
+            b.set_tiles(0, 1, 1, 1)
 
 
 def test_batch_timeout_is_reported_and_batch_stays_usable(monkeypatch, oracle_results):
@@ -132,9 +144,32 @@ def test_batch_timeout_is_reported_and_batch_stays_usable(monkeypatch, oracle_re
             b.synchronize()
         assert ei.value.status == F.RC_ERR_TIMEOUT
         monkeypatch.delenv("RC_FAULT")
-        b.set_tiles(256, 2)  # rebuilds the level table without the fault
+        b.set_tiles(256, 2, 1, 1024)  # rebuilds the level table without the fault
         b.solve()
         b.synchronize()
         _check_all(b, oracle_results)
     finally:
         b.close()
+
+
+def test_batch64_workload_parity_and_properties():
+    """The 64-scene batched workload at full size: one scene of each edge
+    against the FP64 oracle, every scene within the energy bound."""
+    items = R.batch_workload()
+    with R.Batch([R.make_params(e, N) for e, N, _, _ in items]) as b:
+        for k, (_, _, boxes, spheres) in enumerate(items):
+            b.set_scene(k, boxes, spheres)
+        b.tune(iters=1)
+        b.solve()
+        seen = set()
+        for k, (edge, N, boxes, spheres) in enumerate(items):
+            g = b.fluence(k).astype(np.float64)
+            emax = float(np.max(spheres["value"]["emission"].view(np.float16).astype(np.float64)))
+            assert g.min() >= 0.0 and g.max() <= 4 * np.pi * emax * (1 + 1e-6)
+            if edge in seen:
+                continue
+            seen.add(edge)
+            ref, _ = O.solve(O.params(edge, N), O.voxelise(edge, boxes, spheres), jump=True)
+            assert rel_l2(g, ref) <= FP32_REL_L2, (k, edge)
+            assert np.abs(g - ref).max() <= FP32_MAX_REL * max(1.0, ref.max()), (k, edge)
+        assert seen == set(R.BATCH_EDGES)

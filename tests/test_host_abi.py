@@ -128,7 +128,7 @@ def test_batch_entry_points_check_arguments_before_the_device():
     assert F.lib().rc_batch_destroy(None) == F.RC_OK
     assert F.lib().rc_batch_solve(None, None) == F.RC_ERR_INVALID_ARG
     assert F.lib().rc_batch_synchronize(None) == F.RC_ERR_INVALID_ARG
-    assert F.lib().rc_batch_set_tiles(None, 128, 2) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_batch_set_tiles(None, None) == F.RC_ERR_INVALID_ARG
 
 
 def _has_gpu():
