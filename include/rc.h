@@ -241,6 +241,66 @@ rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out);
 rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best,
                         float* best_ms);
 
+/* ---- neural radiance cache ------------------------------------------ */
+/* With the cache enabled, rc_solve serves the far cascades (first_level and
+ * up) from a small network instead of walking their intervals: it predicts
+ * each (probe, direction)'s interval result (R = radiance of the first
+ * opaque voxel, T = 1 when the ray got through) from a multiresolution hash
+ * grid of the probe position and the direction.  Every solve it first walks
+ * 1/2^train_fraction_log2 of the far probes (all their directions) to refit
+ * the network (Adam), and a second such slice, held out, to measure its
+ * error per voxel tile of fallback_tile^3; tiles whose relative L2 error of
+ * (R, T) exceeds fallback_threshold use the plain walk for their probes. */
+typedef struct rc_nrc_params {
+  int32_t first_level;          /* first cascade served (default 2)          */
+  int32_t hash_log2_entries;    /* entries per hash level, log2 (19)        */
+  int32_t base_resolution;      /* coarsest hash grid (16)                  */
+  int32_t max_resolution;       /* finest hash grid (512)                   */
+  float learning_rate;          /* Adam step (1e-2)                         */
+  float beta1, beta2, epsilon;  /* Adam (0.9, 0.99, 1e-10)                  */
+  int32_t train_fraction_log2;  /* training slice 1/2^k of the far probes (4) */
+  int32_t steps_per_solve;      /* Adam steps per solve (1)                 */
+  float fallback_threshold;     /* held-out relative L2 error (0.01)        */
+  int32_t fallback_tile;        /* voxel tile edge, power of two (8)        */
+  float radiance_scale;         /* network predicts R * scale (1/16)        */
+  int32_t pad;
+  uint64_t seed;                /* initial weights                          */
+} rc_nrc_params;
+
+typedef struct rc_nrc_stats {
+  int64_t solves;          /* solves served by the cache                     */
+  int64_t steps;           /* Adam steps taken                               */
+  float last_loss;         /* mean squared error of the last step            */
+  float pad;
+  int64_t fallback_tiles;  /* tiles on the plain walk now                    */
+  int64_t tiles;           /* all tiles                                      */
+} rc_nrc_stats;
+
+rc_status rc_nrc_params_default(rc_nrc_params* out);
+/* Allocates and initialises the cache (all tiles start on the plain walk). */
+rc_status rc_nrc_enable(rc_context* ctx, const rc_nrc_params* params);
+rc_status rc_nrc_disable(rc_context* ctx);
+/* Serialises the parameters (MLP and hash grid, FP32).  With out == NULL or
+ * bytes too small, writes the size needed to *needed and returns
+ * RC_ERR_INVALID_ARG for a short buffer (RC_OK for NULL). */
+rc_status rc_nrc_save(rc_context* ctx, void* out, int64_t bytes, int64_t* needed);
+/* Loads parameters saved by rc_nrc_save with the same rc_nrc_params and
+ * geometry; resets the optimiser state. */
+rc_status rc_nrc_load(rc_context* ctx, const void* in, int64_t bytes);
+rc_status rc_nrc_get_stats(rc_context* ctx, rc_nrc_stats* out);
+/* The cache's (R, G, B, T) for n queries of far cascade `level` (host
+ * arrays): out[4 i .. 4 i + 3] for probe probes[i], direction dirs[i]. */
+rc_status rc_nrc_query(rc_context* ctx, int32_t level, const int32_t* probes,
+                       const int32_t* dirs, int64_t n, float* out);
+/* Gradient of sum((y - f(x))^2) / n over directions d0 .. d0 + n - 1 of one
+ * probe (n <= 128) with targets (R, G, B, T) in `targets` [n][4]: the MLP
+ * parameters' gradient (rc_nrc_param_count() floats, layout as rc_nrc_save's
+ * MLP block) and the probe's 32 position features' gradient.  No update. */
+rc_status rc_nrc_tile_gradient(rc_context* ctx, int32_t level, int32_t probe,
+                               int32_t d0, int32_t n, const float* targets,
+                               float* param_grad, float* pos_grad);
+int32_t rc_nrc_param_count(void);
+
 /* ---- allocation-free solve ------------------------------------------ */
 /* No counterpart in the reference.
  *

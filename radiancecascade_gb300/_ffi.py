@@ -43,6 +43,19 @@ class LevelInfo(C.Structure):
                 ("radiance_elems", C.c_int64), ("radiance_bytes", C.c_int64)]
 
 
+class NrcParams(C.Structure):
+    _fields_ = [("first_level", C.c_int32), ("hash_log2_entries", C.c_int32), ("base_resolution", C.c_int32),
+                ("max_resolution", C.c_int32), ("learning_rate", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("epsilon", C.c_float), ("train_fraction_log2", C.c_int32),
+                ("steps_per_solve", C.c_int32), ("fallback_threshold", C.c_float), ("fallback_tile", C.c_int32),
+                ("radiance_scale", C.c_float), ("pad", C.c_int32), ("seed", C.c_uint64)]
+
+
+class NrcStats(C.Structure):
+    _fields_ = [("solves", C.c_int64), ("steps", C.c_int64), ("last_loss", C.c_float), ("pad", C.c_float),
+                ("fallback_tiles", C.c_int64), ("tiles", C.c_int64)]
+
+
 class BatchTiles(C.Structure):
     _fields_ = [("probes_per_item", C.c_int32), ("dirs_per_item", C.c_int32), ("blocks_per_item", C.c_int32),
                 ("walks_per_item", C.c_int32)]
@@ -90,6 +103,15 @@ SIGNATURES = {
     "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_get_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_tune": (_S, [_P, C.c_int32, C.POINTER(BatchTiles), C.POINTER(C.c_float)]),
+    "rc_nrc_param_count": (C.c_int32, []),
+    "rc_nrc_params_default": (_S, [C.POINTER(NrcParams)]),
+    "rc_nrc_enable": (_S, [_P, C.POINTER(NrcParams)]),
+    "rc_nrc_disable": (_S, [_P]),
+    "rc_nrc_save": (_S, [_P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rc_nrc_load": (_S, [_P, _P, C.c_int64]),
+    "rc_nrc_get_stats": (_S, [_P, C.POINTER(NrcStats)]),
+    "rc_nrc_query": (_S, [_P, C.c_int32, _P, _P, C.c_int64, _P]),
+    "rc_nrc_tile_gradient": (_S, [_P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]),
 }
 
 _lib = None

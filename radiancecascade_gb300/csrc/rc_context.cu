@@ -16,78 +16,18 @@
 #include <mutex>
 #include <vector>
 
-#include "rc_internal.h"
-#include "rc_kernels.cuh"
-#include "rc_walk_bits.cuh"
-#include "rc_walk_queue.cuh"
+#include "rc_ctx.h"
 #include "rc_level0.cuh"
 #include "rc_batch.cuh"
 
 using namespace rcx;
 
-struct rc_context {
-  rc_params p{};
-  int device = 0;
-  int nlev = 0;
-  LevelGeom geom[kMaxCascades]{};
-  size_t elem = 4;  // bytes per stored radiance value
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // staging slot copies done
-  cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
-
-  uint2* base = nullptr;     // static volume (boxes / upload)
-  uint2* vol = nullptr;      // composed volume
-  uint32_t* occ = nullptr;   // opacity bits
-  uint32_t* emis = nullptr;  // emissive bits (opaque with nonzero emission)
-  int W = 0;                 // words per x row
-  uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
-  MaskSet mset{};
-  bool bits_level[kMaxCascades]{};   // level has decimated opacity
-  int mode[kMaxCascades]{};          // how the level is solved (kMode*)
-  uint32_t* recs = nullptr;          // walk records of the queue-walked levels
-  unsigned long long* qcounter = nullptr;
-  QueueArgs qargs{};
-  int queue_blocks = 0;
-  int rec_slots[kMaxCascades]{};
-  const uint32_t* rec_level[kMaxCascades]{};
-  CUtensorMap tma0{};                // cascade 1's child-averaged radiance, for k_level0_tma
-  int tma0_py = 0;
-  int* err = nullptr;                // device error flag set by bounded waits
-  DirInfo* dirs = nullptr;   // all levels, concatenated
-  size_t dir_off[kMaxCascades]{};
-  void* rad = nullptr;       // L_i for all levels
-  size_t rad_off[kMaxCascades]{};  // bytes
-  void* avg = nullptr;       // A_i for levels >= 1
-  size_t avg_off[kMaxCascades]{};  // bytes
-  float* fluence = nullptr;
-
-  // dynamic spheres
-  QSphere* d_sph = nullptr;
-  Region* d_reg = nullptr;
-  int sph_cap = 0;
-  void* h_stage = nullptr;  // pinned, two slots of (spheres, regions)
-  size_t slot_bytes = 0;
-  int slot = 0;
-  bool stage_pending[2] = {false, false};
-  std::vector<QSphere> cur;
-  bool have_base = false;
-  LevelArgs args[kMaxCascades]{};
-};
-
-namespace {
+namespace rcx {
 
 rc_status cuda_fail(cudaError_t e, const char* what) {
   rcx::set_error("%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? RC_ERR_OOM : RC_ERR_CUDA;
 }
-
-#define RC_CUDA(call, what)                         \
-  do {                                              \
-    cudaError_t e_ = (call);                        \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
 
 bool fault_is(const char* name) {
   const char* f = getenv("RC_FAULT");
@@ -108,12 +48,17 @@ rc_status dev_alloc(void** ptr, size_t bytes, const char* what) {
   return RC_OK;
 }
 
+}  // namespace rcx
+
+namespace {
+
 void release(rc_context* c) {
   if (!c) return;
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  nrc_release(c);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
   for (void* b : bufs)
@@ -127,17 +72,6 @@ void release(rc_context* c) {
   cudaSetDevice(prev);
   delete c;
 }
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
 
 rc_status check_ctx(const rc_context* c, const char* fn) {
   if (!c) {
@@ -377,12 +311,26 @@ void launch_queue_walk(const rc_context* c, cudaStream_t s) {
   k_walk_queue<<<(unsigned)c->queue_blocks, kQueueThreads, 0, s>>>(c->qargs);
 }
 
-void enqueue_solve(rc_context* c, cudaStream_t s) {
-  launch_queue_walk(c, s);
-  for (int i = c->nlev - 1; i >= 0; --i) {
+// With the neural radiance cache on, the far levels (from its first level
+// up) come from the cache and the walk queue runs only when a near level
+// needs it.
+rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
+  int near = c->nlev;
+  if (nrc_active(c)) {
+    near = nrc_first_level(c);
+    bool queue_near = false;
+    for (int i = 0; i < near; ++i) queue_near |= c->mode[i] == kModeQueue;
+    if (queue_near) launch_queue_walk(c, s);
+    rc_status st = nrc_enqueue_far(c, s);
+    if (st != RC_OK) return st;
+  } else {
+    launch_queue_walk(c, s);
+  }
+  for (int i = near - 1; i >= 0; --i) {
     if (c->elem == 2) launch_level<__half>(c, i, s);
     else launch_level<float>(c, i, s);
   }
+  return RC_OK;
 }
 
 // Records size of the queue levels, and the queue arguments once `recs` and
@@ -754,7 +702,8 @@ rc_status rc_solve(rc_context* c, void* stream) {
     RC_CUDA(cudaEventRecord(c->ev_in, c->stream), "rc_solve: event");
     RC_CUDA(cudaStreamWaitEvent(s, c->ev_in, 0), "rc_solve: wait");
   }
-  enqueue_solve(c, s);
+  rc_status st = enqueue_solve(c, s);
+  if (st != RC_OK) return st;
   RC_CUDA(cudaGetLastError(), "rc_solve: launch");
   if (s != c->stream) {
     RC_CUDA(cudaEventRecord(c->ev_out, s), "rc_solve: event");
@@ -1090,7 +1039,8 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: opacity launch");
   setup_queue(&v, reinterpret_cast<uint32_t*>(scratch + rec_off),
               reinterpret_cast<unsigned long long*>(scratch + counter_off));
-  enqueue_solve(&v, st);
+  rc_status es = enqueue_solve(&v, st);
+  if (es != RC_OK) return es;
   RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: cascade launch");
   return RC_OK;
 }

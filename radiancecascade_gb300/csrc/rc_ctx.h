@@ -1,0 +1,105 @@
+// rc_ctx.h -- the context object behind the C ABI and the helpers the CUDA
+// translation units share (rc_context.cu: cascades; rc_nrc.cu: the neural
+// radiance cache).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "rc_internal.h"
+#include "rc_kernels.cuh"
+#include "rc_walk_bits.cuh"
+#include "rc_walk_queue.cuh"
+
+namespace rcx {
+struct NrcState;
+}
+
+struct rc_context {
+  rc_params p{};
+  int device = 0;
+  int nlev = 0;
+  rcx::LevelGeom geom[rcx::kMaxCascades]{};
+  size_t elem = 4;  // bytes per stored radiance value
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaEvent_t ev_stage[2] = {nullptr, nullptr};  // staging slot copies done
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+
+  uint2* base = nullptr;     // static volume (boxes / upload)
+  uint2* vol = nullptr;      // composed volume
+  uint32_t* occ = nullptr;   // opacity bits
+  uint32_t* emis = nullptr;  // emissive bits (opaque with nonzero emission)
+  int W = 0;                 // words per x row
+  uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
+  rcx::MaskSet mset{};
+  bool bits_level[rcx::kMaxCascades]{};   // level has decimated opacity
+  int mode[rcx::kMaxCascades]{};          // how the level is solved (kMode*)
+  uint32_t* recs = nullptr;               // walk records of the queue-walked levels
+  unsigned long long* qcounter = nullptr;
+  rcx::QueueArgs qargs{};
+  int queue_blocks = 0;
+  int rec_slots[rcx::kMaxCascades]{};
+  const uint32_t* rec_level[rcx::kMaxCascades]{};
+  CUtensorMap tma0{};                // cascade 1's child-averaged radiance, for k_level0_tma
+  int tma0_py = 0;
+  int* err = nullptr;                // device error flag set by bounded waits
+  rcx::DirInfo* dirs = nullptr;      // all levels, concatenated
+  size_t dir_off[rcx::kMaxCascades]{};
+  void* rad = nullptr;               // L_i for all levels
+  size_t rad_off[rcx::kMaxCascades]{};  // bytes
+  void* avg = nullptr;               // A_i for levels >= 1
+  size_t avg_off[rcx::kMaxCascades]{};  // bytes
+  float* fluence = nullptr;
+
+  // dynamic spheres
+  rcx::QSphere* d_sph = nullptr;
+  rcx::Region* d_reg = nullptr;
+  int sph_cap = 0;
+  void* h_stage = nullptr;  // pinned, two slots of (spheres, regions)
+  size_t slot_bytes = 0;
+  int slot = 0;
+  bool stage_pending[2] = {false, false};
+  std::vector<rcx::QSphere> cur;
+  bool have_base = false;
+  rcx::LevelArgs args[rcx::kMaxCascades]{};
+
+  rcx::NrcState* nrc = nullptr;  // neural radiance cache (rc_nrc_enable), or null
+};
+
+namespace rcx {
+
+rc_status cuda_fail(cudaError_t e, const char* what);
+bool fault_is(const char* name);
+rc_status dev_alloc(void** ptr, size_t bytes, const char* what);
+
+#define RC_CUDA(call, what)                                 \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return ::rcx::cuda_fail(e_, what); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Neural radiance cache hooks (rc_nrc.cu).
+bool nrc_active(const rc_context* c);
+int nrc_first_level(const rc_context* c);  // first cascade the cache serves
+// Enqueues the cache's per-frame work for the far cascades (training-sample
+// walks, refit, inference, fallback walks) and their merges, top level down to
+// the first far level.  Called from the solve before the near levels.
+rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s);
+void nrc_release(rc_context* c);
+
+}  // namespace rcx

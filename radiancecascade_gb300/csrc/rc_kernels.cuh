@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(128) k_level_scalar(const __grid_constant__ Le
 }
 
 // Base volume from boxes: the last box containing a voxel wins.
-__global__ void k_boxes_to_base(uint2* __restrict__ base, int Gx, int Gy, int Gz, const rc_box* __restrict__ boxes,
+static __global__ void k_boxes_to_base(uint2* __restrict__ base, int Gx, int Gy, int Gz, const rc_box* __restrict__ boxes,
                                 int nb) {
   extern __shared__ rc_box sbox[];
   for (int i = threadIdx.x; i < nb; i += blockDim.x) sbox[i] = boxes[i];

@@ -1,0 +1,700 @@
+// rc_nrc.cu -- the neural radiance cache of include/rc.h: state, the
+// per-solve schedule (training-sample walks, held-out error, refit, inference,
+// fallback, merges) and the rc_nrc_* entry points.
+//
+// Reference boundary: the learned form is an engine option behind the same
+// solve; the reference's GI stage (src/app.rs:3-7) sees no difference.
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "rc_ctx.h"
+#include "rc_nrc.cuh"
+
+namespace rcx {
+
+struct NrcState {
+  rc_nrc_params prm{};
+  int first = 2, nlev = 0, nph = 16;
+  int64_t T = 0;       // entries per hash level
+  int64_t hash_n = 0;  // 16 * T * 2
+  NrcHash hash{};
+  float *hash_master = nullptr, *hash_m = nullptr, *hash_v = nullptr, *hash_g = nullptr;
+  __half* hash_half = nullptr;
+  float *mlp = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr, *dbg_g = nullptr;
+  unsigned char* img = nullptr;
+  float* epos = nullptr;
+  __nv_bfloat16* denc = nullptr;
+  __half* rt = nullptr;
+  int64_t total_probes = 0, total_queries = 0, enum_tiles = 0;
+  // sample probes and their tiles, grouped by phase
+  NrcTile* tiles = nullptr;
+  NrcSample* samples = nullptr;
+  std::vector<NrcTile> h_tiles;
+  std::vector<int64_t> tile_begin, sample_begin;
+  int64_t max_tiles2 = 0, max_held = 0, max_samples = 0;
+  float* target = nullptr;
+  float* pred = nullptr;
+  float* epos_grad = nullptr;
+  float* loss = nullptr;
+  float* h_loss = nullptr;  // pinned
+  NrcTile* qtiles = nullptr;  // rc_nrc_query / rc_nrc_tile_gradient scratch
+  float* qout = nullptr;
+  int64_t qcap = 0;
+  // fallback tiles
+  int tile_shift = 3, TX = 0, TY = 0, TZ = 0;
+  float *tnum = nullptr, *tden = nullptr;
+  uint8_t* flag = nullptr;
+  NrcArgs base{};
+  int64_t solves = 0, steps = 0;
+  int64_t loss_rows = 0;
+  int fwd_blocks = 0, train_blocks = 0;
+};
+
+namespace {
+
+uint64_t splitmix(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+float uniform(uint64_t& s, float lo, float hi) {
+  return lo + (hi - lo) * (float)((splitmix(s) >> 11) * (1.0 / 9007199254740992.0));
+}
+
+int nrc_phase(uint64_t seed, int level, int64_t probe, int nph) {
+  uint64_t s = seed ^ ((uint64_t)level << 40) ^ (uint64_t)probe;
+  return (int)(splitmix(s) >> 40) & (nph - 1);
+}
+
+void free_state(NrcState* n) {
+  if (!n) return;
+  void* bufs[] = {n->hash_master, n->hash_m, n->hash_v, n->hash_g, n->hash_half, n->mlp, n->mlp_m, n->mlp_v,
+                  n->mlp_g, n->dbg_g, n->img, n->epos, n->denc, n->rt, n->tiles, n->samples, n->target, n->pred,
+                  n->epos_grad, n->loss, n->qtiles, n->qout, n->tnum, n->tden, n->flag};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (n->h_loss) cudaFreeHost(n->h_loss);
+  delete n;
+}
+
+rc_status check(const rc_context* c, const char* fn, bool need_nrc) {
+  if (!c) {
+    set_error("%s: context is NULL", fn);
+    return RC_ERR_INVALID_ARG;
+  }
+  if (need_nrc && !c->nrc) {
+    set_error("%s: the radiance cache is not enabled", fn);
+    return RC_ERR_STATE;
+  }
+  return RC_OK;
+}
+
+unsigned blocks_for(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads); }
+
+void launch_encode(NrcState* n, cudaStream_t s) {
+  k_nrc_encode<<<blocks_for(n->total_probes * kNrcHashLevels, 256), 256, 0, s>>>(n->base, n->hash, n->total_probes);
+}
+
+void launch_adam(float* p, float* g, float* m, float* v, __half* half_out, int64_t count, const rc_nrc_params& prm,
+                 int64_t t, cudaStream_t s) {
+  AdamArgs a;
+  a.p = p;
+  a.g = g;
+  a.m = m;
+  a.v = v;
+  a.half_out = half_out;
+  a.n = count;
+  a.lr = prm.learning_rate;
+  a.beta1 = prm.beta1;
+  a.beta2 = prm.beta2;
+  a.eps = prm.epsilon;
+  a.c1 = (float)(1.0 - pow((double)prm.beta1, (double)t));
+  a.c2 = (float)(1.0 - pow((double)prm.beta2, (double)t));
+  k_nrc_adam<<<(unsigned)std::min<int64_t>(blocks_for(count, 256), 152 * 8), 256, 0, s>>>(a);
+}
+
+void launch_pack(NrcState* n, cudaStream_t s) {
+  k_nrc_pack<<<blocks_for(kImgBytes / 2, 256), 256, 0, s>>>(n->mlp, n->img);
+}
+
+NrcWalkArgs walk_args(const rc_context* c, const NrcTile* tiles, int64_t ntiles, float* target) {
+  NrcWalkArgs w;
+  memset(&w, 0, sizeof w);
+  for (int i = 0; i < c->nlev; ++i) w.lv[i] = c->args[i];
+  w.tiles = tiles;
+  w.ntiles = ntiles;
+  w.target = target;
+  return w;
+}
+
+rc_status ensure_query(NrcState* n, int64_t count) {
+  if (count <= n->qcap) return RC_OK;
+  if (n->qtiles) cudaFree(n->qtiles);
+  if (n->qout) cudaFree(n->qout);
+  n->qtiles = nullptr;
+  n->qout = nullptr;
+  n->qcap = 0;
+  rc_status s = dev_alloc((void**)&n->qtiles, count * sizeof(NrcTile), "cache query tiles");
+  if (s != RC_OK) return s;
+  if ((s = dev_alloc((void**)&n->qout, count * kNrcThreads * 4 * sizeof(float), "cache query output")) != RC_OK)
+    return s;
+  n->qcap = count;
+  return RC_OK;
+}
+
+void init_params(NrcState* n, std::vector<float>& mlp, std::vector<float>& hash) {
+  uint64_t s = n->prm.seed;
+  mlp.assign(kNrcParams, 0.f);
+  for (int l = 0; l < kNrcHidden; ++l) {
+    const int fan_in = l == 0 ? kNrcPosFeat + kNrcDirFeat : 64;
+    const float r = sqrtf(6.f / (float)fan_in);
+    float* W = mlp.data() + l * kNrcLayerStride;
+    for (int o = 0; o < 64; ++o)
+      for (int i = 0; i < 64; ++i) W[o * 64 + i] = (l == 0 && i >= fan_in) ? 0.f : uniform(s, -r, r);
+  }
+  const float r4 = sqrtf(6.f / 64.f) * 0.1f;
+  for (int o = 0; o < 4; ++o)
+    for (int i = 0; i < 64; ++i) mlp[kNrcW4 + o * 64 + i] = uniform(s, -r4, r4);
+  hash.resize((size_t)n->hash_n);
+  for (auto& v : hash) v = uniform(s, -1e-4f, 1e-4f);
+}
+
+rc_status upload_params(NrcState* n, const std::vector<float>& mlp, const std::vector<float>& hash) {
+  RC_CUDA(cudaMemcpy(n->mlp, mlp.data(), mlp.size() * 4, cudaMemcpyHostToDevice), "cache upload");
+  RC_CUDA(cudaMemcpy(n->hash_master, hash.data(), hash.size() * 4, cudaMemcpyHostToDevice), "cache upload");
+  std::vector<__half> hh(hash.size());
+  for (size_t i = 0; i < hash.size(); ++i) hh[i] = __float2half_rn(hash[i]);
+  RC_CUDA(cudaMemcpy(n->hash_half, hh.data(), hh.size() * 2, cudaMemcpyHostToDevice), "cache upload");
+  RC_CUDA(cudaMemset(n->mlp_m, 0, kNrcParams * 4), "cache init");
+  RC_CUDA(cudaMemset(n->mlp_v, 0, kNrcParams * 4), "cache init");
+  RC_CUDA(cudaMemset(n->mlp_g, 0, kNrcParams * 4), "cache init");
+  RC_CUDA(cudaMemset(n->hash_m, 0, n->hash_n * 4), "cache init");
+  RC_CUDA(cudaMemset(n->hash_v, 0, n->hash_n * 4), "cache init");
+  RC_CUDA(cudaMemset(n->hash_g, 0, n->hash_n * 4), "cache init");
+  launch_pack(n, 0);
+  RC_CUDA(cudaGetLastError(), "cache pack");
+  RC_CUDA(cudaDeviceSynchronize(), "cache init");
+  n->steps = 0;
+  return RC_OK;
+}
+
+}  // namespace
+
+bool nrc_active(const rc_context* c) { return c && c->nrc; }
+int nrc_first_level(const rc_context* c) { return c->nrc ? c->nrc->first : c->nlev; }
+
+void nrc_release(rc_context* c) {
+  if (!c || !c->nrc) return;
+  free_state(c->nrc);
+  c->nrc = nullptr;
+}
+
+rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
+  NrcState* n = c->nrc;
+  const int ph = (int)(n->solves % n->nph), hp = (ph + n->nph / 2) % n->nph;
+  const int64_t tr0 = n->tile_begin[ph], ntr = n->tile_begin[ph + 1] - tr0;
+  const int64_t ho0 = n->tile_begin[hp], nho = n->tile_begin[hp + 1] - ho0;
+  float* ttr = n->target;
+  float* tho = n->target + ntr * kNrcThreads * 4;
+  // plain (R, T) of the training and held-out slices
+  if (ntr) k_nrc_targets<<<blocks_for(ntr * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + tr0, ntr, ttr));
+  if (nho) k_nrc_targets<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + ho0, nho, tho));
+  launch_encode(n, s);
+  // held-out error with the current network -> fallback flags
+  if (nho) {
+    NrcArgs a = n->base;
+    a.tiles = n->tiles + ho0;
+    a.ntiles = nho;
+    a.out = n->pred;
+    k_nrc_forward<false><<<(unsigned)std::min<int64_t>(nho, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(a, nho);
+    k_nrc_tile_error<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(n->tiles + ho0, nho, n->pred, tho, n->base,
+                                                                        n->tile_shift, n->TX, n->TY, n->tnum, n->tden);
+    const float thr = n->prm.fallback_threshold;
+    const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
+    k_nrc_flags<<<blocks_for(cells, 256), 256, 0, s>>>(n->tnum, n->tden, n->flag, cells, thr * thr);
+  }
+  // refit on the training slice
+  const int steps = std::max(1, n->prm.steps_per_solve);
+  const int64_t ns0 = n->sample_begin[ph], nsamp = n->sample_begin[ph + 1] - ns0;
+  if (ntr) {
+    RC_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), s), "cache loss reset");
+    n->loss_rows = 0;
+    for (int st = 0; st < steps; ++st) {
+      const int64_t a0 = ntr * st / steps, a1 = ntr * (st + 1) / steps;
+      if (a1 <= a0) continue;
+      int64_t rows = 0;
+      for (int64_t t = a0; t < a1; ++t) rows += n->h_tiles[tr0 + t].n;
+      n->loss_rows += rows;
+      if (st > 0) launch_encode(n, s);
+      RC_CUDA(cudaMemsetAsync(n->epos_grad, 0, (size_t)nsamp * kNrcPosFeat * sizeof(float), s), "cache grad reset");
+      NrcArgs a = n->base;
+      a.tiles = n->tiles + tr0 + a0;
+      a.ntiles = a1 - a0;
+      a.target = ttr + a0 * kNrcThreads * 4;
+      a.grad = n->mlp_g;
+      a.epos_grad = n->epos_grad;
+      a.loss = n->loss;
+      a.inv_batch = 1.f / (float)std::max<int64_t>(rows, 1);
+      k_nrc_train<<<(unsigned)std::min<int64_t>(a1 - a0, n->train_blocks), kNrcThreads, kTrainSmem, s>>>(a);
+      NrcHash h = n->hash;
+      k_nrc_hash_grad<<<blocks_for(nsamp * kNrcHashLevels, 256), 256, 0, s>>>(a, h, n->samples + ns0, (int)nsamp);
+      ++n->steps;
+      launch_adam(n->mlp, n->mlp_g, n->mlp_m, n->mlp_v, nullptr, kNrcParams, n->prm, n->steps, s);
+      launch_adam(n->hash_master, n->hash_g, n->hash_m, n->hash_v, n->hash_half, n->hash_n, n->prm, n->steps, s);
+      launch_pack(n, s);
+    }
+    RC_CUDA(cudaMemcpyAsync(n->h_loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "cache loss");
+  }
+  // inference over every far query, then the plain walk where flagged
+  launch_encode(n, s);
+  k_nrc_forward<true><<<(unsigned)std::min<int64_t>(n->enum_tiles, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(
+      n->base, n->enum_tiles);
+  {
+    NrcFallbackArgs f;
+    memset(&f, 0, sizeof f);
+    for (int i = 0; i < c->nlev; ++i) f.lv[i] = c->args[i];
+    f.n = n->base;
+    f.flag = n->flag;
+    f.tile_shift = n->tile_shift;
+    f.TX = n->TX;
+    f.TY = n->TY;
+    f.total = n->total_queries;
+    k_nrc_fallback<<<blocks_for(n->total_queries, 256), 256, 0, s>>>(f);
+  }
+  // merges of the far levels, top down
+  for (int i = c->nlev - 1; i >= n->first; --i) {
+    const LevelArgs& a = c->args[i];
+    const __half* rt = n->base.lv[i].rt;
+    dim3 grid(blocks_for(a.P, 128), (unsigned)((a.n / 2) * (a.n / 2) / 2));
+    const bool top = i == c->nlev - 1;
+    if (c->elem == 2) {
+      if (top) k_level_merge_rt<__half, true><<<grid, 128, 0, s>>>(a, rt);
+      else k_level_merge_rt<__half, false><<<grid, 128, 0, s>>>(a, rt);
+    } else {
+      if (top) k_level_merge_rt<float, true><<<grid, 128, 0, s>>>(a, rt);
+      else k_level_merge_rt<float, false><<<grid, 128, 0, s>>>(a, rt);
+    }
+  }
+  RC_CUDA(cudaGetLastError(), "cache launch");
+  ++n->solves;
+  return RC_OK;
+}
+
+}  // namespace rcx
+
+using namespace rcx;
+
+extern "C" {
+
+int32_t rc_nrc_param_count(void) { return kNrcParams; }
+
+rc_status rc_nrc_params_default(rc_nrc_params* out) {
+  if (!out) {
+    set_error("rc_nrc_params_default: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  memset(out, 0, sizeof *out);
+  out->first_level = 2;
+  out->hash_log2_entries = 19;
+  out->base_resolution = 16;
+  out->max_resolution = 512;
+  out->learning_rate = 1e-2f;
+  out->beta1 = 0.9f;
+  out->beta2 = 0.99f;
+  out->epsilon = 1e-10f;
+  out->train_fraction_log2 = 4;
+  out->steps_per_solve = 1;
+  out->fallback_threshold = 0.01f;
+  out->fallback_tile = 8;
+  out->radiance_scale = 1.f / 16.f;
+  out->seed = 0x5EEDull;
+  return RC_OK;
+}
+
+rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
+  if (check(c, "rc_nrc_enable", false) != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!prm) {
+    set_error("rc_nrc_enable: params is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  const rc_nrc_params& q = *prm;
+  const bool pow2_tile = q.fallback_tile >= 1 && (q.fallback_tile & (q.fallback_tile - 1)) == 0;
+  if (q.first_level < 1 || q.first_level >= c->nlev || q.hash_log2_entries < 10 || q.hash_log2_entries > 24 ||
+      q.base_resolution < 2 || q.max_resolution < q.base_resolution || q.max_resolution > 4096 ||
+      !(q.learning_rate > 0.f) || !(q.beta1 >= 0.f && q.beta1 < 1.f) || !(q.beta2 >= 0.f && q.beta2 < 1.f) ||
+      !(q.epsilon > 0.f) || q.train_fraction_log2 < 1 || q.train_fraction_log2 > 8 || q.steps_per_solve < 1 ||
+      q.steps_per_solve > 64 || !(q.fallback_threshold >= 0.f) || !pow2_tile || !(q.radiance_scale > 0.f)) {
+    set_error("rc_nrc_enable: invalid rc_nrc_params (first_level must be in [1, num_cascades))");
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_nrc_enable");
+  nrc_release(c);
+  NrcState* n = new NrcState();
+  n->prm = q;
+  n->first = q.first_level;
+  n->nlev = c->nlev;
+  n->nph = 1 << q.train_fraction_log2;
+  n->T = (int64_t)1 << q.hash_log2_entries;
+  n->hash_n = (int64_t)kNrcHashLevels * n->T * 2;
+  auto fail = [&](rc_status st) {
+    free_state(n);
+    return st;
+  };
+  rc_status s;
+  // hash grid
+  n->hash.log2T = q.hash_log2_entries;
+  const double bgrow = exp((log((double)q.max_resolution) - log((double)q.base_resolution)) / (kNrcHashLevels - 1));
+  for (int l = 0; l < kNrcHashLevels; ++l)
+    n->hash.res[l] = std::max(1, (int)floor((double)q.base_resolution * pow(bgrow, (double)l) + 1e-9));
+  n->hash.inv_extent = 1.f / (float)std::max(c->p.grid[0], std::max(c->p.grid[1], c->p.grid[2]));
+  if ((s = dev_alloc((void**)&n->hash_master, n->hash_n * 4, "hash grid")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->hash_m, n->hash_n * 4, "hash grid moments")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->hash_v, n->hash_n * 4, "hash grid moments")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->hash_g, n->hash_n * 4, "hash grid gradient")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->hash_half, n->hash_n * 2, "hash grid FP16")) != RC_OK) return fail(s);
+  n->hash.table = n->hash_half;
+  n->hash.grad = n->hash_g;
+  // MLP
+  float** mb[] = {&n->mlp, &n->mlp_m, &n->mlp_v, &n->mlp_g, &n->dbg_g};
+  for (float** b : mb)
+    if ((s = dev_alloc((void**)b, kNrcParams * 4, "network parameters")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->img, kImgBytes, "network weight image")) != RC_OK) return fail(s);
+  // far levels: encodings, direction features, (R, T)
+  memset(&n->base, 0, sizeof n->base);
+  n->base.first = n->first;
+  n->base.nlev = c->nlev;
+  int64_t probes = 0, queries = 0, dirs = 0;
+  for (int i = n->first; i < c->nlev; ++i) {
+    probes += c->geom[i].probes();
+    queries += c->geom[i].probes() * c->geom[i].ndirs;
+    dirs += c->geom[i].ndirs;
+  }
+  n->total_probes = probes;
+  n->total_queries = queries;
+  if ((s = dev_alloc((void**)&n->epos, probes * kNrcPosFeat * 4, "position encodings")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->denc, dirs * kNrcDirFeat * 2, "direction features")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->rt, queries * 4 * 2, "cached (R, T)")) != RC_OK) return fail(s);
+  {
+    std::vector<__nv_bfloat16> de((size_t)dirs * kNrcDirFeat);
+    int64_t po = 0, dO = 0, qo = 0, t0 = 0;
+    for (int i = n->first; i < c->nlev; ++i) {
+      const LevelGeom& gm = c->geom[i];
+      NrcLevel& L = n->base.lv[i];
+      L.epos = n->epos + po * kNrcPosFeat;
+      L.denc = n->denc + dO * kNrcDirFeat;
+      L.rt = n->rt + qo * 4;
+      L.P = gm.probes();
+      L.ndirs = gm.ndirs;
+      for (int a = 0; a < 3; ++a) L.M[a] = gm.M[a];
+      L.spacing = gm.spacing;
+      n->base.tile0[i] = t0;
+      t0 += (gm.probes() * gm.ndirs + kNrcThreads - 1) / kNrcThreads;
+      const double pi = 3.14159265358979323846;
+      for (int d = 0; d < gm.ndirs; ++d) {
+        const int tx = d % gm.n, ty = d / gm.n;
+        const double u = (2.0 * tx + 1.0) / gm.n - 1.0, v = (2.0 * ty + 1.0) / gm.n - 1.0;
+        const double f[10] = {u, v, sin(pi * u), cos(pi * u), sin(pi * v), cos(pi * v),
+                              sin(2 * pi * u), cos(2 * pi * u), sin(2 * pi * v), cos(2 * pi * v)};
+        __nv_bfloat16* row = de.data() + (dO + d) * kNrcDirFeat;
+        for (int k = 0; k < 10; ++k) row[k] = __float2bfloat16_rn((float)f[k]);
+        for (int k = 0; k < 6; ++k) row[10 + k] = __float2bfloat16_rn(k == std::min(i - n->first, 5) ? 1.f : 0.f);
+      }
+      po += gm.probes();
+      dO += gm.ndirs;
+      qo += gm.probes() * gm.ndirs;
+    }
+    n->base.tile0[c->nlev] = t0;
+    n->enum_tiles = t0;
+    RC_CUDA(cudaMemcpy(n->denc, de.data(), de.size() * 2, cudaMemcpyHostToDevice), "rc_nrc_enable: upload");
+  }
+  n->base.img = n->img;
+  n->base.params = n->mlp;
+  n->base.scale = q.radiance_scale;
+  n->base.err = c->err;
+  // sample probes by phase and their tiles of up to 128 directions
+  {
+    std::vector<std::vector<NrcSample>> sp(n->nph);
+    for (int i = n->first; i < c->nlev; ++i)
+      for (int64_t p = 0; p < c->geom[i].probes(); ++p)
+        sp[nrc_phase(q.seed ^ 0xA5A5A5A5ull, i, p, n->nph)].push_back(NrcSample{i, (int32_t)p});
+    std::vector<NrcSample> all;
+    n->tile_begin.assign(n->nph + 1, 0);
+    n->sample_begin.assign(n->nph + 1, 0);
+    for (int ph = 0; ph < n->nph; ++ph) {
+      n->tile_begin[ph] = (int64_t)n->h_tiles.size();
+      n->sample_begin[ph] = (int64_t)all.size();
+      for (size_t k = 0; k < sp[ph].size(); ++k) {
+        const NrcSample smp = sp[ph][k];
+        const int nd = c->geom[smp.level].ndirs;
+        for (int d0 = 0; d0 < nd; d0 += kNrcThreads)
+          n->h_tiles.push_back(NrcTile{smp.level, smp.probe, d0, std::min(kNrcThreads, nd - d0), (int32_t)k, 0});
+        all.push_back(smp);
+      }
+      n->max_samples = std::max<int64_t>(n->max_samples, (int64_t)sp[ph].size());
+    }
+    n->tile_begin[n->nph] = (int64_t)n->h_tiles.size();
+    n->sample_begin[n->nph] = (int64_t)all.size();
+    for (int ph = 0; ph < n->nph; ++ph) {
+      const int hp = (ph + n->nph / 2) % n->nph;
+      const int64_t a = n->tile_begin[ph + 1] - n->tile_begin[ph], b = n->tile_begin[hp + 1] - n->tile_begin[hp];
+      n->max_tiles2 = std::max(n->max_tiles2, a + b);
+      n->max_held = std::max(n->max_held, b);
+    }
+    if ((s = dev_alloc((void**)&n->tiles, std::max<size_t>(1, n->h_tiles.size()) * sizeof(NrcTile), "cache tiles")) !=
+        RC_OK)
+      return fail(s);
+    if ((s = dev_alloc((void**)&n->samples, std::max<size_t>(1, all.size()) * sizeof(NrcSample), "cache samples")) !=
+        RC_OK)
+      return fail(s);
+    if (!n->h_tiles.empty())
+      RC_CUDA(cudaMemcpy(n->tiles, n->h_tiles.data(), n->h_tiles.size() * sizeof(NrcTile), cudaMemcpyHostToDevice),
+              "rc_nrc_enable: upload");
+    if (!all.empty())
+      RC_CUDA(cudaMemcpy(n->samples, all.data(), all.size() * sizeof(NrcSample), cudaMemcpyHostToDevice),
+              "rc_nrc_enable: upload");
+  }
+  if ((s = dev_alloc((void**)&n->target, std::max<int64_t>(1, n->max_tiles2) * kNrcThreads * 16, "cache targets")) !=
+      RC_OK)
+    return fail(s);
+  if ((s = dev_alloc((void**)&n->pred, std::max<int64_t>(1, n->max_held) * kNrcThreads * 16, "cache predictions")) !=
+      RC_OK)
+    return fail(s);
+  if ((s = dev_alloc((void**)&n->epos_grad, std::max<int64_t>(1, n->max_samples) * kNrcPosFeat * 4,
+                     "position gradients")) != RC_OK)
+    return fail(s);
+  if ((s = dev_alloc((void**)&n->loss, sizeof(float), "cache loss")) != RC_OK) return fail(s);
+  RC_CUDA(cudaMallocHost((void**)&n->h_loss, sizeof(float)), "rc_nrc_enable: pinned");
+  *n->h_loss = 0.f;
+  // fallback tiles: all start on the plain walk
+  n->tile_shift = 0;
+  while ((1 << n->tile_shift) < q.fallback_tile) ++n->tile_shift;
+  n->TX = (c->p.grid[0] + q.fallback_tile - 1) / q.fallback_tile;
+  n->TY = (c->p.grid[1] + q.fallback_tile - 1) / q.fallback_tile;
+  n->TZ = (c->p.grid[2] + q.fallback_tile - 1) / q.fallback_tile;
+  const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
+  if ((s = dev_alloc((void**)&n->tnum, cells * 4, "tile errors")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->tden, cells * 4, "tile errors")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->flag, cells, "tile flags")) != RC_OK) return fail(s);
+  RC_CUDA(cudaMemset(n->tnum, 0, cells * 4), "rc_nrc_enable: memset");
+  RC_CUDA(cudaMemset(n->tden, 0, cells * 4), "rc_nrc_enable: memset");
+  RC_CUDA(cudaMemset(n->flag, 1, cells), "rc_nrc_enable: memset");
+  // kernels: shared memory and resident blocks
+  RC_CUDA(cudaFuncSetAttribute(k_nrc_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem),
+          "rc_nrc_enable: attribute");
+  RC_CUDA(cudaFuncSetAttribute(k_nrc_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem),
+          "rc_nrc_enable: attribute");
+  RC_CUDA(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem),
+          "rc_nrc_enable: attribute");
+  int sms = 0, per_f = 0, per_t = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, k_nrc_forward<true>, kNrcThreads, kFwdSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_t, k_nrc_train, kNrcThreads, kTrainSmem);
+  (void)cudaGetLastError();
+  // tensor-memory budget: 512 columns per SM (64 per inference block, 512 per training block)
+  n->fwd_blocks = std::max(1, sms * std::min(std::max(per_f, 1), 8));
+  n->train_blocks = std::max(1, sms);
+  {
+    std::vector<float> mlp, hash;
+    init_params(n, mlp, hash);
+    if ((s = upload_params(n, mlp, hash)) != RC_OK) return fail(s);
+  }
+  c->nrc = n;
+  return RC_OK;
+}
+
+rc_status rc_nrc_disable(rc_context* c) {
+  if (check(c, "rc_nrc_disable", false) != RC_OK) return RC_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_nrc_disable");
+  nrc_release(c);
+  return RC_OK;
+}
+
+namespace {
+struct SaveHeader {
+  uint32_t magic;    // 'RCNC'
+  uint32_t version;  // 1
+  uint32_t mlp_count;
+  uint32_t pad;
+  uint64_t hash_count;
+  rc_nrc_params params;
+};
+constexpr uint32_t kSaveMagic = 0x434E4352u;
+}  // namespace
+
+rc_status rc_nrc_save(rc_context* c, void* out, int64_t bytes, int64_t* needed) {
+  if (check(c, "rc_nrc_save", true) != RC_OK) return c ? RC_ERR_STATE : RC_ERR_INVALID_ARG;
+  NrcState* n = c->nrc;
+  const int64_t need = (int64_t)sizeof(SaveHeader) + (int64_t)kNrcParams * 4 + n->hash_n * 4;
+  if (needed) *needed = need;
+  if (!out) return RC_OK;
+  if (bytes < need) {
+    set_error("rc_nrc_save: need %lld bytes", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_nrc_save");
+  SaveHeader h;
+  memset(&h, 0, sizeof h);
+  h.magic = kSaveMagic;
+  h.version = 1;
+  h.mlp_count = kNrcParams;
+  h.hash_count = (uint64_t)n->hash_n;
+  h.params = n->prm;
+  char* o = static_cast<char*>(out);
+  memcpy(o, &h, sizeof h);
+  RC_CUDA(cudaMemcpy(o + sizeof h, n->mlp, kNrcParams * 4, cudaMemcpyDeviceToHost), "rc_nrc_save");
+  RC_CUDA(cudaMemcpy(o + sizeof h + kNrcParams * 4, n->hash_master, n->hash_n * 4, cudaMemcpyDeviceToHost),
+          "rc_nrc_save");
+  return RC_OK;
+}
+
+rc_status rc_nrc_load(rc_context* c, const void* in, int64_t bytes) {
+  if (check(c, "rc_nrc_load", true) != RC_OK) return c ? RC_ERR_STATE : RC_ERR_INVALID_ARG;
+  NrcState* n = c->nrc;
+  const int64_t need = (int64_t)sizeof(SaveHeader) + (int64_t)kNrcParams * 4 + n->hash_n * 4;
+  if (!in || bytes != need) {
+    set_error("rc_nrc_load: expected %lld bytes", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  SaveHeader h;
+  memcpy(&h, in, sizeof h);
+  if (h.magic != kSaveMagic || h.version != 1 || h.mlp_count != (uint32_t)kNrcParams ||
+      h.hash_count != (uint64_t)n->hash_n || h.params.hash_log2_entries != n->prm.hash_log2_entries ||
+      h.params.base_resolution != n->prm.base_resolution || h.params.max_resolution != n->prm.max_resolution ||
+      h.params.first_level != n->prm.first_level) {
+    set_error("rc_nrc_load: the saved cache does not match this cache's parameters");
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_nrc_load");
+  const char* p = static_cast<const char*>(in) + sizeof h;
+  std::vector<float> mlp(kNrcParams), hash((size_t)n->hash_n);
+  memcpy(mlp.data(), p, kNrcParams * 4);
+  memcpy(hash.data(), p + kNrcParams * 4, n->hash_n * 4);
+  return upload_params(n, mlp, hash);
+}
+
+rc_status rc_nrc_get_stats(rc_context* c, rc_nrc_stats* out) {
+  if (check(c, "rc_nrc_get_stats", true) != RC_OK) return c ? RC_ERR_STATE : RC_ERR_INVALID_ARG;
+  if (!out) {
+    set_error("rc_nrc_get_stats: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  NrcState* n = c->nrc;
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_nrc_get_stats");
+  const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
+  std::vector<uint8_t> f((size_t)cells);
+  RC_CUDA(cudaMemcpy(f.data(), n->flag, cells, cudaMemcpyDeviceToHost), "rc_nrc_get_stats");
+  memset(out, 0, sizeof *out);
+  out->solves = n->solves;
+  out->steps = n->steps;
+  out->last_loss = n->loss_rows ? *n->h_loss / (float)n->loss_rows : 0.f;
+  out->fallback_tiles = std::count(f.begin(), f.end(), (uint8_t)1);
+  out->tiles = cells;
+  return RC_OK;
+}
+
+rc_status rc_nrc_query(rc_context* c, int32_t level, const int32_t* probes, const int32_t* dirs, int64_t count,
+                       float* out) {
+  if (check(c, "rc_nrc_query", true) != RC_OK) return c ? RC_ERR_STATE : RC_ERR_INVALID_ARG;
+  NrcState* n = c->nrc;
+  if (level < n->first || level >= c->nlev || count < 0 || (count && (!probes || !dirs || !out))) {
+    set_error("rc_nrc_query: level must be a far cascade and the arrays non-NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!count) return RC_OK;
+  std::vector<NrcTile> t((size_t)count);
+  for (int64_t i = 0; i < count; ++i) {
+    if (probes[i] < 0 || probes[i] >= c->geom[level].probes() || dirs[i] < 0 || dirs[i] >= c->geom[level].ndirs) {
+      set_error("rc_nrc_query: query %lld out of range", (long long)i);
+      return RC_ERR_INVALID_ARG;
+    }
+    t[i] = NrcTile{level, probes[i], dirs[i], 1, -1, 0};
+  }
+  DeviceGuard g(c->device);
+  rc_status s = ensure_query(n, count);
+  if (s != RC_OK) return s;
+  cudaStream_t st = c->stream;
+  RC_CUDA(cudaMemcpyAsync(n->qtiles, t.data(), count * sizeof(NrcTile), cudaMemcpyHostToDevice, st), "rc_nrc_query");
+  launch_encode(n, st);
+  NrcArgs a = n->base;
+  a.tiles = n->qtiles;
+  a.ntiles = count;
+  a.out = n->qout;
+  k_nrc_forward<false><<<(unsigned)std::min<int64_t>(count, n->fwd_blocks), kNrcThreads, kFwdSmem, st>>>(a, count);
+  RC_CUDA(cudaGetLastError(), "rc_nrc_query: launch");
+  std::vector<float> raw((size_t)count * kNrcThreads * 4);
+  RC_CUDA(cudaMemcpyAsync(raw.data(), n->qout, raw.size() * 4, cudaMemcpyDeviceToHost, st), "rc_nrc_query");
+  RC_CUDA(cudaStreamSynchronize(st), "rc_nrc_query");
+  int flag = 0;
+  RC_CUDA(cudaMemcpy(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost), "rc_nrc_query");
+  if (flag) {
+    cudaMemset(c->err, 0, sizeof(int));
+    set_error("rc_nrc_query: a bounded device-side wait ran out");
+    return RC_ERR_TIMEOUT;
+  }
+  for (int64_t i = 0; i < count; ++i) {
+    const float* r = raw.data() + i * kNrcThreads * 4;  // row 0 of tile i
+    for (int k = 0; k < 3; ++k) out[4 * i + k] = std::max(r[k] / n->prm.radiance_scale, 0.f);
+    out[4 * i + 3] = std::min(std::max(r[3], 0.f), 1.f);
+  }
+  return RC_OK;
+}
+
+rc_status rc_nrc_tile_gradient(rc_context* c, int32_t level, int32_t probe, int32_t d0, int32_t count,
+                               const float* targets, float* param_grad, float* pos_grad) {
+  if (check(c, "rc_nrc_tile_gradient", true) != RC_OK) return c ? RC_ERR_STATE : RC_ERR_INVALID_ARG;
+  NrcState* n = c->nrc;
+  if (level < n->first || level >= c->nlev || probe < 0 || probe >= c->geom[level].probes() || d0 < 0 ||
+      count < 1 || count > kNrcThreads || d0 + count > c->geom[level].ndirs || !targets || !param_grad ||
+      !pos_grad) {
+    set_error("rc_nrc_tile_gradient: arguments out of range");
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  rc_status s = ensure_query(n, 1);
+  if (s != RC_OK) return s;
+  cudaStream_t st = c->stream;
+  const NrcTile t{level, probe, d0, count, 0, 0};
+  std::vector<float> tg((size_t)kNrcThreads * 4, 0.f);
+  memcpy(tg.data(), targets, (size_t)count * 16);
+  RC_CUDA(cudaMemcpyAsync(n->qtiles, &t, sizeof t, cudaMemcpyHostToDevice, st), "rc_nrc_tile_gradient");
+  RC_CUDA(cudaMemcpyAsync(n->qout, tg.data(), tg.size() * 4, cudaMemcpyHostToDevice, st), "rc_nrc_tile_gradient");
+  RC_CUDA(cudaMemsetAsync(n->dbg_g, 0, kNrcParams * 4, st), "rc_nrc_tile_gradient");
+  RC_CUDA(cudaMemsetAsync(n->epos_grad, 0, kNrcPosFeat * 4, st), "rc_nrc_tile_gradient");
+  launch_encode(n, st);
+  NrcArgs a = n->base;
+  a.tiles = n->qtiles;
+  a.ntiles = 1;
+  a.target = n->qout;
+  a.grad = n->dbg_g;
+  a.epos_grad = n->epos_grad;
+  a.loss = nullptr;
+  a.inv_batch = 1.f / (float)count;
+  k_nrc_train<<<1, kNrcThreads, kTrainSmem, st>>>(a);
+  RC_CUDA(cudaGetLastError(), "rc_nrc_tile_gradient: launch");
+  RC_CUDA(cudaMemcpyAsync(param_grad, n->dbg_g, kNrcParams * 4, cudaMemcpyDeviceToHost, st), "rc_nrc_tile_gradient");
+  RC_CUDA(cudaMemcpyAsync(pos_grad, n->epos_grad, kNrcPosFeat * 4, cudaMemcpyDeviceToHost, st),
+          "rc_nrc_tile_gradient");
+  RC_CUDA(cudaStreamSynchronize(st), "rc_nrc_tile_gradient");
+  int flag = 0;
+  RC_CUDA(cudaMemcpy(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost), "rc_nrc_tile_gradient");
+  if (flag) {
+    cudaMemset(c->err, 0, sizeof(int));
+    set_error("rc_nrc_tile_gradient: a bounded device-side wait ran out");
+    return RC_ERR_TIMEOUT;
+  }
+  return RC_OK;
+}
+
+}  // extern "C"

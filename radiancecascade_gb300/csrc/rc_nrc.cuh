@@ -1,0 +1,852 @@
+// rc_nrc.cuh -- neural radiance cache for the far cascades (sm_103a).
+//
+// For a far cascade i >= F the cache stands in for the interval walk: it maps
+// (probe position, direction, cascade) to the walk's result (R, T) -- the
+// radiance leaving the first opaque voxel of the interval (RGB) and whether
+// the ray got through (T = 1) -- and the usual top-down merge then forms
+// L_i = R + T * merge(A_{i+1}).
+//
+// Model (Mueller et al. 2022, "Instant neural graphics primitives", for the
+// encoding): a multiresolution hash grid of the probe centre -- 16 levels x 2
+// FP16 features, 2^19 entries per level, resolutions 16 .. 512 in geometric
+// steps, trilinear interpolation, spatial hash (x * 1) ^ (y * 2654435761) ^
+// (z * 805459861) mod 2^19 where a level's dense grid does not fit -- plus 16
+// direction features (the octahedral texel centre u, v and sin / cos of pi,
+// 2 pi times each, and a one-hot of the cascade), zero-padded to 64 inputs.
+// MLP: 4 hidden layers of width 64 with ReLU, then a 16-wide linear output
+// layer of which 4 are used (R, G, B scaled by radiance_scale, and T).
+// BF16 weights and activations, FP32 accumulation in tensor memory; every
+// layer is one tcgen05 M = 128 GEMM (one query per row).  Training: MSE on
+// (R * scale, T), gradients through the same GEMMs (transposed operands in
+// shared memory), Adam on FP32 master copies of the MLP and of the hash table.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "rc_kernels.cuh"
+#include "rc_umma.cuh"
+
+namespace rcx {
+
+constexpr int kNrcThreads = 128;     // one query row per thread; M = 128 per tile
+constexpr int kNrcHashLevels = 16;
+constexpr int kNrcPosFeat = 2 * kNrcHashLevels;  // 32
+constexpr int kNrcDirFeat = 16;
+constexpr int kNrcHidden = 4;
+
+// FP32 master parameters: W_l [64 out][64 in] then b_l [64] for l = 0..3,
+// then W_4 [16][64], b_4 [16].
+constexpr int kNrcLayerStride = 64 * 64 + 64;
+constexpr int kNrcW4 = 4 * kNrcLayerStride;
+constexpr int kNrcB4 = kNrcW4 + 16 * 64;
+constexpr int kNrcParams = kNrcB4 + 16;  // 17680
+
+// BF16 weight image (byte offsets), already in the K-major core layout:
+//   l = 0..3:  F_l = W_l as [64 n = out][64 k = in]     at 16384 l
+//              B_l = W_l^T as [64 n = in][64 k = out]   at 16384 l + 8192
+//   W4F = W_4 as [16][64] at 65536,  W4B = W_4^T as [64][16] at 67584
+constexpr int kImgW4F = 65536;
+constexpr int kImgW4B = 67584;
+constexpr int kImgBytes = 69632;
+
+// One tile of 128 queries.  probe >= 0: the queries are directions d0 ..
+// d0 + n - 1 of that probe; slot indexes the probe's position-gradient row.
+struct NrcTile {
+  int32_t level;
+  int32_t probe;
+  int32_t d0;
+  int32_t n;
+  int32_t slot;
+  int32_t pad;
+};
+
+struct NrcLevel {
+  const float* epos;          // [P][32] position encoding of every probe
+  const __nv_bfloat16* denc;  // [ndirs][16] direction + cascade features
+  __half* rt;                 // [4][ndirs][P]: R, G, B, T
+  int64_t P;
+  int32_t ndirs;
+  int32_t M[3];
+  int32_t spacing;
+  int32_t pad;
+};
+
+struct NrcArgs {
+  const unsigned char* img;  // BF16 weight image
+  const float* params;       // FP32 master (biases)
+  NrcLevel lv[kMaxCascades];
+  int32_t first;             // first far cascade
+  int32_t nlev;
+  int64_t tile0[kMaxCascades + 1];  // enumeration: first tile of each far level
+  const NrcTile* tiles;      // explicit tile list (or null: enumerate the far levels)
+  int64_t ntiles;
+  float* out;                // explicit tiles: raw outputs [tile][128][4]
+  const float* target;       // training: [tile][128][4] (R, G, B, T)
+  float* grad;               // training: FP32 gradient of the master parameters
+  float* epos_grad;          // training: [slot][32]
+  float* loss;               // training: sum of squared errors
+  float scale;               // radiance scale of the outputs
+  float inv_batch;           // training: 1 / (queries in the step)
+  int* err;
+};
+
+__device__ __forceinline__ unsigned char* align128(unsigned char* p) {
+  return reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(p) + 127) & ~(uintptr_t)127);
+}
+
+// Resolves row r of tile t: (level, probe, direction); false for an empty row.
+__device__ __forceinline__ bool nrc_query(const NrcArgs& a, int64_t t, int r, int& li, int64_t& p, int& d,
+                                          int& slot) {
+  if (a.tiles) {
+    const NrcTile tl = a.tiles[t];
+    li = tl.level;
+    p = tl.probe;
+    d = tl.d0 + r;
+    slot = tl.slot;
+    return r < tl.n;
+  }
+  li = a.first;
+  while (li + 1 < a.nlev && t >= a.tile0[li + 1]) ++li;
+  const NrcLevel& L = a.lv[li];
+  const int64_t q = (t - a.tile0[li]) * kNrcThreads + r;
+  slot = -1;
+  if (q >= L.P * L.ndirs) return false;
+  d = (int)(q / L.P);
+  p = q - (int64_t)d * L.P;
+  return true;
+}
+
+// Input row: 32 position features, 16 direction features, 16 zeros.
+__device__ __forceinline__ void nrc_input(const NrcArgs& a, bool valid, int li, int64_t p, int d, float* x) {
+#pragma unroll
+  for (int j = 0; j < 64; ++j) x[j] = 0.f;
+  if (!valid) return;
+  const NrcLevel& L = a.lv[li];
+  const float4* ep = reinterpret_cast<const float4*>(L.epos + p * kNrcPosFeat);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float4 v = __ldg(ep + j);
+    x[4 * j] = v.x;
+    x[4 * j + 1] = v.y;
+    x[4 * j + 2] = v.z;
+    x[4 * j + 3] = v.w;
+  }
+  const uint4* dp = reinterpret_cast<const uint4*>(L.denc + (int64_t)d * kNrcDirFeat);
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const uint4 u = __ldg(dp + j);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float2 f = __bfloat1622float2(h[k]);
+      x[32 + 8 * j + 2 * k] = f.x;
+      x[32 + 8 * j + 2 * k + 1] = f.y;
+    }
+  }
+}
+
+__device__ __forceinline__ void copy_smem(unsigned char* dst, const unsigned char* src, int bytes) {
+  for (int i = threadIdx.x * 16; i < bytes; i += blockDim.x * 16)
+    *reinterpret_cast<uint4*>(dst + i) = __ldg(reinterpret_cast<const uint4*>(src + i));
+}
+
+// Waits for the MMA group committed on `bar`; every thread of the block gets
+// the same answer.  On timeout *err = 3.
+__device__ __forceinline__ bool nrc_wait(uint64_t* bar, uint32_t& phase, int* err) {
+  const bool ok = mbar_wait_bounded(bar, phase);
+  phase ^= 1u;
+  const bool any_fail = __syncthreads_or(!ok);
+  if (any_fail && threadIdx.x == 0) atomicExch(err, 3);
+  return !any_fail;
+}
+
+// ---------------------------------------------------------------------------
+// Inference.  Block = 128 threads, persistent over tiles; shared memory: the
+// activation operand (16 KB), the forward weights (34 KB), biases.
+// RT: write (R, T) planes of the enumerated far levels; else raw outputs.
+// ---------------------------------------------------------------------------
+constexpr int kFwdSmem = 16384 + 4 * 8192 + 2048 + 272 * 4 + 64 + 128;
+
+template <bool RT>
+__global__ void __launch_bounds__(kNrcThreads) k_nrc_forward(const __grid_constant__ NrcArgs a, int64_t ntiles) {
+  extern __shared__ unsigned char sm_raw[];
+  unsigned char* sm = align128(sm_raw);
+  unsigned char* XA = sm;
+  unsigned char* WF = sm + 16384;
+  unsigned char* W4F = WF + 4 * 8192;
+  float* sb = reinterpret_cast<float*>(W4F + 2048);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sb + 272);
+  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int l = 0; l < 4; ++l) copy_smem(WF + 8192 * l, a.img + 16384 * l, 8192);
+  copy_smem(W4F, a.img + kImgW4F, 2048);
+  for (int j = tid; j < 272; j += blockDim.x)
+    sb[j] = j < 256 ? a.params[(j >> 6) * kNrcLayerStride + 4096 + (j & 63)] : a.params[kNrcB4 + j - 256];
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(s_taddr, 64);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_taddr;
+  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true;
+
+  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    int li, d, slot;
+    int64_t p;
+    const bool valid = nrc_query(a, t, tid, li, p, d, slot);
+    {
+      float x[64];
+      nrc_input(a, valid, li, p, d, x);
+      store_row64_bf16(XA, tid, x);
+    }
+    fence_proxy_async();
+    __syncthreads();
+    float o[16];
+    for (int l = 0; l < 5 && ok; ++l) {
+      if (tid == 0) {
+        tc_fence_after();
+        umma_gemm(tmem, smem_u32(XA), smem_u32(l < 4 ? WF + 8192 * l : W4F), 128, l < 4 ? 64 : 16, 64, false);
+        umma_commit(bar);
+      }
+      if (!(ok = nrc_wait(bar, phase, a.err))) break;
+      tc_fence_after();
+      if (l < 4) {
+        float v[64];
+        tmem_ld64(tl, v);
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] = fmaxf(v[j] + sb[64 * l + j], 0.f);
+        store_row64_bf16(XA, tid, v);
+        tc_fence_before();
+        fence_proxy_async();
+        __syncthreads();
+      } else {
+        tmem_ld16(tl, o);
+        tc_fence_before();
+      }
+    }
+    if (!ok || !valid) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) o[c] += sb[256 + c];
+    if (RT) {
+      const NrcLevel& L = a.lv[li];
+      const int64_t plane = (int64_t)L.ndirs * L.P;
+      const int64_t off = (int64_t)d * L.P + p;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) L.rt[c * plane + off] = __float2half_rn(fmaxf(o[c] / a.scale, 0.f));
+      L.rt[3 * plane + off] = __float2half_rn(fminf(fmaxf(o[3], 0.f), 1.f));
+    } else {
+      float4 r4 = make_float4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<float4*>(a.out + (t * kNrcThreads + tid) * 4) = r4;
+    }
+  }
+  if (!ok) mbar_wait_bounded(bar, phase ^ 1u);  // the group that timed out, if it still runs
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------------------
+// Training.  Block = 128 threads, persistent over training tiles (all rows of
+// a tile share one probe).  Per tile: forward (keeping x_1..x_4 transposed and
+// the ReLU masks), output error, then layer by layer
+//   dW_l += dz_l^T x_l   (M = 128 with dz_l^T in rows 0..63, accumulated in
+//                         tensor memory over the block's tiles)
+//   dx_l  = dz_l W_l     (M = 128, N = 64, K = 64)
+// and the probe's position-feature gradient (column sums of dx_1[:, 0:32]).
+// Output layer and bias gradients: FP32 reductions in shared memory.
+// Tensor memory: columns 0..63 the per-layer product, 64 + 64 l the dW_l.
+// ---------------------------------------------------------------------------
+constexpr int kTrWF = 0;           // 4 x 8192
+constexpr int kTrWB = 32768;       // 4 x 8192
+constexpr int kTrW4F = 65536;      // 2048
+constexpr int kTrW4B = 67584;      // 2048
+constexpr int kTrXA = 69632;       // [128][64]        16384
+constexpr int kTrXT = 86016;       // 4 x [64][128]    65536
+constexpr int kTrDZ = 151552;      // [128][64]        16384
+constexpr int kTrDZT = 167936;     // [128][128]       32768 (rows 64..127 stay zero)
+constexpr int kTrDO = 200704;      // [128][16]        4096
+constexpr int kTrMisc = 204800;
+// misc (floats): biases 272, dW4/db4 accumulators 4 x 64 + 4, db accumulators
+// 4 x 64, output errors 128 x 4, position-gradient sums 32; then the barrier
+constexpr int kTrMiscFloats = 272 + 260 + 256 + 512 + 32;
+constexpr int kTrainSmem = kTrMisc + kTrMiscFloats * 4 + 16 + 128;
+
+__global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant__ NrcArgs a) {
+  extern __shared__ unsigned char sm_raw[];
+  unsigned char* sm = align128(sm_raw);
+  float* sb = reinterpret_cast<float*>(sm + kTrMisc);
+  float* acc4 = sb + 272;        // dW4 rows 0..3 (4 x 64), db4 (4)
+  float* accb = acc4 + 260;      // db_l, l = 0..3 (4 x 64)
+  float* sdo = accb + 256;       // output errors [128][4]
+  float* spos = sdo + 512;       // position-gradient sums [32]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(spos + 32);
+  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  for (int l = 0; l < 4; ++l) {
+    copy_smem(sm + kTrWF + 8192 * l, a.img + 16384 * l, 8192);
+    copy_smem(sm + kTrWB + 8192 * l, a.img + 16384 * l + 8192, 8192);
+  }
+  copy_smem(sm + kTrW4F, a.img + kImgW4F, 2048);
+  copy_smem(sm + kTrW4B, a.img + kImgW4B, 2048);
+  for (int j = tid; j < 272; j += blockDim.x)
+    sb[j] = j < 256 ? a.params[(j >> 6) * kNrcLayerStride + 4096 + (j & 63)] : a.params[kNrcB4 + j - 256];
+  for (int j = tid; j < 260 + 256 + 32; j += blockDim.x) acc4[j] = 0.f;
+  for (int i = tid * 16; i < 32768; i += blockDim.x * 16)
+    *reinterpret_cast<uint4*>(sm + kTrDZT + i) = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_fence_init();
+  }
+  if (warp == 0) tmem_alloc(s_taddr, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *s_taddr;
+  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+  float loss = 0.f;
+  unsigned char* XA = sm + kTrXA;
+  unsigned char* DZ = sm + kTrDZ;
+  unsigned char* DZT = sm + kTrDZT;
+
+  for (int64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+    int li, d, slot;
+    int64_t p;
+    const bool valid = nrc_query(a, t, tid, li, p, d, slot);
+    uint64_t mask[4];  // ReLU masks of x_2 .. x_5 (bit j = feature j > 0)
+    {
+      float x[64];
+      nrc_input(a, valid, li, p, d, x);
+      store_row64_bf16(XA, tid, x);
+#pragma unroll
+      for (int j = 0; j < 64; ++j)
+        reinterpret_cast<__nv_bfloat16*>(sm + kTrXT + core_off(j, tid, 128))[0] = __float2bfloat16_rn(x[j]);
+    }
+    fence_proxy_async();
+    __syncthreads();
+    // ---- forward
+    float o[16];
+    for (int l = 0; l < 5 && ok; ++l) {
+      if (tid == 0) {
+        tc_fence_after();
+        umma_gemm(tmem, smem_u32(XA), smem_u32(sm + (l < 4 ? kTrWF + 8192 * l : kTrW4F)), 128, l < 4 ? 64 : 16, 64,
+                  false);
+        umma_commit(bar);
+      }
+      if (!(ok = nrc_wait(bar, phase, a.err))) break;
+      tc_fence_after();
+      if (l < 4) {
+        float v[64];
+        tmem_ld64(tl, v);
+        uint64_t m = 0;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) {
+          v[j] = fmaxf(v[j] + sb[64 * l + j], 0.f);
+          m |= (uint64_t)(v[j] > 0.f) << j;
+        }
+        mask[l] = m;
+        store_row64_bf16(XA, tid, v);
+        if (l < 3) {
+          unsigned char* xt = sm + kTrXT + 16384 * (l + 1);
+#pragma unroll
+          for (int j = 0; j < 64; ++j)
+            reinterpret_cast<__nv_bfloat16*>(xt + core_off(j, tid, 128))[0] = __float2bfloat16_rn(v[j]);
+        }
+        tc_fence_before();
+        fence_proxy_async();
+        __syncthreads();
+      } else {
+        tmem_ld16(tl, o);
+        tc_fence_before();
+      }
+    }
+    if (!ok) break;
+    // ---- output error
+    {
+      float e[4] = {0.f, 0.f, 0.f, 0.f};
+      if (valid) {
+        const float4 y = *reinterpret_cast<const float4*>(a.target + (t * kNrcThreads + tid) * 4);
+        const float yv[4] = {y.x * a.scale, y.y * a.scale, y.z * a.scale, y.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const float diff = o[c] + sb[256 + c] - yv[c];
+          loss = fmaf(diff, diff, loss);
+          e[c] = 2.f * diff * a.inv_batch;
+        }
+      }
+      float eo[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) eo[c] = c < 4 ? e[c] : 0.f;
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        __nv_bfloat162 h[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(eo[8 * c + 2 * j], eo[8 * c + 2 * j + 1]);
+        *reinterpret_cast<uint4*>(sm + kTrDO + core_off(tid, 8 * c, 16)) = *reinterpret_cast<const uint4*>(h);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) sdo[tid * 4 + c] = e[c];
+    }
+    fence_proxy_async();
+    __syncthreads();
+    // dx_5 = e W_4 (K = 16), issued before the FP32 reductions below
+    if (tid == 0) {
+      tc_fence_after();
+      umma_gemm(tmem, smem_u32(sm + kTrDO), smem_u32(sm + kTrW4B), 128, 64, 16, false);
+      umma_commit(bar);
+    }
+    {
+      // dW_4 [c][k] += sum_m e[m][c] x_5[m][k]; thread: k = tid & 63, c = 2 (tid >> 6) + {0, 1}
+      const int k = tid & 63, c0 = 2 * (tid >> 6);
+      float s0 = 0.f, s1 = 0.f;
+      for (int m = 0; m < kNrcThreads; ++m) {
+        const float xv = __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(XA + core_off(m, k, 64))[0]);
+        s0 = fmaf(sdo[m * 4 + c0], xv, s0);
+        s1 = fmaf(sdo[m * 4 + c0 + 1], xv, s1);
+      }
+      acc4[c0 * 64 + k] += s0;
+      acc4[(c0 + 1) * 64 + k] += s1;
+      if (tid < 4) {
+        float s = 0.f;
+        for (int m = 0; m < kNrcThreads; ++m) s += sdo[m * 4 + tid];
+        acc4[256 + tid] += s;
+      }
+    }
+    if (!(ok = nrc_wait(bar, phase, a.err))) break;
+    tc_fence_after();
+    // ---- hidden layers, top down: dz_l from dx_{l+1}, then dW_l and dx_l
+    for (int l = 3; l >= 0 && ok; --l) {
+      {
+        float v[64];
+        tmem_ld64(tl, v);
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] = ((mask[l] >> j) & 1u) ? v[j] : 0.f;
+        store_row64_bf16(DZ, tid, v);
+#pragma unroll
+        for (int j = 0; j < 64; ++j)
+          reinterpret_cast<__nv_bfloat16*>(DZT + core_off(j, tid, 128))[0] = __float2bfloat16_rn(v[j]);
+      }
+      tc_fence_before();
+      fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc_fence_after();
+        umma_gemm(tmem + 64u + 64u * l, smem_u32(DZT), smem_u32(sm + kTrXT + 16384 * l), 128, 64, 128, !first);
+        umma_gemm(tmem, smem_u32(DZ), smem_u32(sm + kTrWB + 8192 * l), 128, 64, 64, false);
+        umma_commit(bar);
+      }
+      if (tid < 64) {  // db_l: column sums of dz_l
+        float s = 0.f;
+        for (int m = 0; m < kNrcThreads; ++m)
+          s += __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(DZT + core_off(tid, m, 128))[0]);
+        accb[64 * l + tid] += s;
+      }
+      if (!(ok = nrc_wait(bar, phase, a.err))) break;
+      tc_fence_after();
+    }
+    if (!ok) break;
+    // ---- position-feature gradient of the tile's probe: sum over rows of dx_1[:, 0:32]
+    {
+      float v[64];
+      tmem_ld64(tl, v);
+      tc_fence_before();
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        float s = v[j];
+#pragma unroll
+        for (int sh = 16; sh > 0; sh >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, sh);
+        if (lane == 0) atomicAdd(&spos[j], s);
+      }
+      __syncthreads();
+      if (tid < 32) {
+        const NrcTile tl0 = a.tiles[t];
+        if (tl0.slot >= 0) atomicAdd(&a.epos_grad[(int64_t)tl0.slot * kNrcPosFeat + tid], spos[tid]);
+        spos[tid] = 0.f;
+      }
+    }
+    first = false;
+    __syncthreads();
+  }
+  if (!ok) mbar_wait_bounded(bar, phase ^ 1u);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (ok && !first) {
+    // dW_l rows (out features) sit in tensor-memory lanes 0..63: warps 0 and 1
+    if (warp < 2) {
+      for (int l = 0; l < 4; ++l) {
+        float v[64];
+        tmem_ld64(tl + 64u + 64u * l, v);
+        float* g = a.grad + l * kNrcLayerStride + tid * 64;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) atomicAdd(&g[j], v[j]);
+      }
+    }
+    for (int j = tid; j < 256; j += blockDim.x) {
+      atomicAdd(&a.grad[(j >> 6) * kNrcLayerStride + 4096 + (j & 63)], accb[j]);
+      atomicAdd(&a.grad[kNrcW4 + j], acc4[j]);
+    }
+    if (tid < 4) atomicAdd(&a.grad[kNrcB4 + tid], acc4[256 + tid]);
+  }
+  // loss: one atomic per warp
+#pragma unroll
+  for (int sh = 16; sh > 0; sh >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, sh);
+  if (lane == 0 && a.loss) atomicAdd(a.loss, loss);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// ---------------------------------------------------------------------------
+// Hash-grid encoding and its gradient.
+// ---------------------------------------------------------------------------
+struct NrcHash {
+  const __half* table;  // [16][T][2]
+  float* grad;          // [16][T][2]
+  int32_t log2T;
+  int32_t res[kNrcHashLevels];
+  float inv_extent;     // 1 / max grid edge
+};
+
+__device__ __forceinline__ uint32_t nrc_hash_index(const NrcHash& h, int l, int x, int y, int z) {
+  const uint32_t T = 1u << h.log2T;
+  const uint32_t r1 = (uint32_t)h.res[l] + 1u;
+  if ((uint64_t)r1 * r1 * r1 <= T) return (uint32_t)x + r1 * ((uint32_t)y + r1 * (uint32_t)z);
+  return ((uint32_t)x ^ ((uint32_t)y * 2654435761u) ^ ((uint32_t)z * 805459861u)) & (T - 1u);
+}
+
+// Probe centre (voxel units) of probe p of level L, scaled to [0, 1].
+__device__ __forceinline__ void nrc_probe_pos(const NrcLevel& L, int64_t p, float inv_extent, float* u) {
+  const int mx = (int)(p % L.M[0]);
+  const int my = (int)((p / L.M[0]) % L.M[1]);
+  const int mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const float h = 0.5f * (float)L.spacing;
+  u[0] = ((float)mx * L.spacing + h) * inv_extent;
+  u[1] = ((float)my * L.spacing + h) * inv_extent;
+  u[2] = ((float)mz * L.spacing + h) * inv_extent;
+}
+
+// One thread per (probe, hash level) of every far level.
+__global__ void k_nrc_encode(const __grid_constant__ NrcArgs a, const __grid_constant__ NrcHash h,
+                             int64_t total_probes) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total_probes * kNrcHashLevels) return;
+  const int l = (int)(i % kNrcHashLevels);
+  int64_t p = i / kNrcHashLevels;
+  int li = a.first;
+  while (li < a.nlev && p >= a.lv[li].P) p -= a.lv[li++].P;
+  if (li >= a.nlev) return;
+  const NrcLevel& L = a.lv[li];
+  float u[3];
+  nrc_probe_pos(L, p, h.inv_extent, u);
+  const float r = (float)h.res[l];
+  int c[3];
+  float f[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float s = u[k] * r;
+    c[k] = min((int)floorf(s), h.res[l] - 1);
+    f[k] = s - (float)c[k];
+  }
+  float e0 = 0.f, e1 = 0.f;
+  const uint32_t T = 1u << h.log2T;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+    const float w = (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) * (dz ? f[2] : 1.f - f[2]);
+    const uint32_t idx = nrc_hash_index(h, l, c[0] + dx, c[1] + dy, c[2] + dz);
+    const __half2 v = *reinterpret_cast<const __half2*>(h.table + ((size_t)l * T + idx) * 2);
+    const float2 fv = __half22float2(v);
+    e0 = fmaf(w, fv.x, e0);
+    e1 = fmaf(w, fv.y, e1);
+  }
+  float* out = const_cast<float*>(L.epos) + p * kNrcPosFeat + 2 * l;
+  out[0] = e0;
+  out[1] = e1;
+}
+
+struct NrcSample {
+  int32_t level;
+  int32_t probe;
+};
+
+// Scatter of the position-feature gradients of the step's training probes.
+__global__ void k_nrc_hash_grad(const __grid_constant__ NrcArgs a, const __grid_constant__ NrcHash h,
+                                const NrcSample* __restrict__ samples, int nsamples) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)nsamples * kNrcHashLevels) return;
+  const int l = (int)(i % kNrcHashLevels);
+  const int s = (int)(i / kNrcHashLevels);
+  const NrcSample smp = samples[s];
+  const float g0 = a.epos_grad[(int64_t)s * kNrcPosFeat + 2 * l];
+  const float g1 = a.epos_grad[(int64_t)s * kNrcPosFeat + 2 * l + 1];
+  if (g0 == 0.f && g1 == 0.f) return;
+  float u[3];
+  nrc_probe_pos(a.lv[smp.level], smp.probe, h.inv_extent, u);
+  const float r = (float)h.res[l];
+  int c[3];
+  float f[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float sc = u[k] * r;
+    c[k] = min((int)floorf(sc), h.res[l] - 1);
+    f[k] = sc - (float)c[k];
+  }
+  const uint32_t T = 1u << h.log2T;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+    const float w = (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) * (dz ? f[2] : 1.f - f[2]);
+    const uint32_t idx = nrc_hash_index(h, l, c[0] + dx, c[1] + dy, c[2] + dz);
+    float* g = h.grad + ((size_t)l * T + idx) * 2;
+    atomicAdd(g, w * g0);
+    atomicAdd(g + 1, w * g1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adam (Kingma and Ba 2015) on FP32 masters; clears the gradient.  Writes the
+// FP16 copy of the hash table when half_out is set.
+// ---------------------------------------------------------------------------
+struct AdamArgs {
+  float* p;
+  float* g;
+  float* m;
+  float* v;
+  __half* half_out;
+  int64_t n;
+  float lr, beta1, beta2, eps;
+  float c1, c2;  // bias corrections 1 - beta^t
+};
+
+__global__ void k_nrc_adam(const __grid_constant__ AdamArgs a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float g = a.g[i];
+    const float m = fmaf(a.beta1, a.m[i], (1.f - a.beta1) * g);
+    const float v = fmaf(a.beta2, a.v[i], (1.f - a.beta2) * g * g);
+    a.m[i] = m;
+    a.v[i] = v;
+    a.g[i] = 0.f;
+    const float step = a.lr * (m / a.c1) / (sqrtf(v / a.c2) + a.eps);
+    const float p = a.p[i] - step;
+    a.p[i] = p;
+    if (a.half_out) a.half_out[i] = __float2half_rn(p);
+  }
+}
+
+// BF16 weight image from the FP32 masters (one thread per image element).
+__global__ void k_nrc_pack(const float* __restrict__ params, unsigned char* __restrict__ img) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kImgBytes / 2) return;
+  const int byte = 2 * i;
+  float w;
+  if (byte < kImgW4F) {
+    const int l = byte / 16384, part = (byte % 16384) / 8192, off = byte % 8192;
+    // invert core_off for a 64 x 64 operand: off = (n/8)*1024 + (k/8)*128 + (n%8)*16 + (k%8)*2
+    const int n = (off / 1024) * 8 + (off % 128) / 16, k = ((off % 1024) / 128) * 8 + (off % 16) / 2;
+    const float* W = params + l * kNrcLayerStride;
+    w = part == 0 ? W[n * 64 + k] : W[k * 64 + n];
+  } else if (byte < kImgW4B) {
+    const int off = byte - kImgW4F;  // [16 n][64 k]
+    const int n = (off / 1024) * 8 + (off % 128) / 16, k = ((off % 1024) / 128) * 8 + (off % 16) / 2;
+    w = params[kNrcW4 + n * 64 + k];
+  } else {
+    const int off = byte - kImgW4B;  // [64 n][16 k]: SBO = 256
+    const int n = (off / 256) * 8 + (off % 128) / 16, k = ((off % 256) / 128) * 8 + (off % 16) / 2;
+    w = params[kNrcW4 + k * 64 + n];
+  }
+  reinterpret_cast<__nv_bfloat16*>(img)[i] = __float2bfloat16_rn(w);
+}
+
+// ---------------------------------------------------------------------------
+// Plain (R, T) of queries: training targets and the fallback.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void nrc_walk(const LevelArgs& a, int64_t p, int d, float* rt) {
+  const int mx = (int)(p % a.M[0]);
+  const int my = (int)((p / a.M[0]) % a.M[1]);
+  const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
+  const int h = a.spacing >> 1;
+  const DirInfo di = a.dirs[d];
+  const int64_t hit = walk_interval(a.occ, a.G, a.W, mx * a.spacing + h + di.start_off[0],
+                                    my * a.spacing + h + di.start_off[1], mz * a.spacing + h + di.start_off[2], di,
+                                    false);
+  rt[0] = rt[1] = rt[2] = 0.f;
+  rt[3] = hit < 0 ? 1.f : 0.f;
+  if (hit >= 0) voxel_emission(a.vol, hit, rt);
+}
+
+struct NrcWalkArgs {
+  LevelArgs lv[kMaxCascades];
+  const NrcTile* tiles;
+  int64_t ntiles;
+  float* target;  // [tile][128][4]
+};
+
+__global__ void k_nrc_targets(const __grid_constant__ NrcWalkArgs w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= w.ntiles * kNrcThreads) return;
+  const NrcTile t = w.tiles[i / kNrcThreads];
+  const int r = (int)(i % kNrcThreads);
+  float rt[4] = {0.f, 0.f, 0.f, 0.f};
+  if (r < t.n) nrc_walk(w.lv[t.level], t.probe, t.d0 + r, rt);
+  *reinterpret_cast<float4*>(w.target + i * 4) = make_float4(rt[0], rt[1], rt[2], rt[3]);
+}
+
+// Held-out error of the cache per fallback tile (voxel tile of the probe
+// centre): sum of squared errors and of squared targets.
+__global__ void k_nrc_tile_error(const NrcTile* __restrict__ tiles, int64_t ntiles, const float* __restrict__ pred,
+                                 const float* __restrict__ target, const __grid_constant__ NrcArgs a, int tile_shift,
+                                 int TX, int TY, float* __restrict__ num, float* __restrict__ den) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntiles * kNrcThreads) return;
+  const NrcTile t = tiles[i / kNrcThreads];
+  const int r = (int)(i % kNrcThreads);
+  if (r >= t.n) return;
+  const float4 pr = *reinterpret_cast<const float4*>(pred + i * 4);
+  const float4 y = *reinterpret_cast<const float4*>(target + i * 4);
+  const float R[4] = {fmaxf(pr.x / a.scale, 0.f), fmaxf(pr.y / a.scale, 0.f), fmaxf(pr.z / a.scale, 0.f),
+                      fminf(fmaxf(pr.w, 0.f), 1.f)};
+  const float Y[4] = {y.x, y.y, y.z, y.w};
+  float e = 0.f, s = 0.f;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    e = fmaf(R[c] - Y[c], R[c] - Y[c], e);
+    s = fmaf(Y[c], Y[c], s);
+  }
+  const NrcLevel& L = a.lv[t.level];
+  const int64_t p = t.probe;
+  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const int h = L.spacing >> 1;
+  const int tx = (mx * L.spacing + h) >> tile_shift, ty = (my * L.spacing + h) >> tile_shift,
+            tz = (mz * L.spacing + h) >> tile_shift;
+  const int64_t cell = ((int64_t)tz * TY + ty) * TX + tx;
+  atomicAdd(&num[cell], e);
+  atomicAdd(&den[cell], s);
+}
+
+// Fallback flags from the accumulated errors; cells without held-out samples
+// this frame keep their flag.  Clears the accumulators.
+__global__ void k_nrc_flags(float* __restrict__ num, float* __restrict__ den, uint8_t* __restrict__ flag, int64_t n,
+                            float thr2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float e = num[i], s = den[i];
+  if (e > 0.f || s > 0.f) flag[i] = (e > thr2 * fmaxf(s, 1e-6f)) ? 1 : 0;
+  num[i] = 0.f;
+  den[i] = 0.f;
+}
+
+// Fallback: plain (R, T) for every query of probes in flagged tiles.
+struct NrcFallbackArgs {
+  LevelArgs lv[kMaxCascades];
+  NrcArgs n;
+  const uint8_t* flag;
+  int tile_shift, TX, TY;
+  int64_t total;  // queries over all far levels
+};
+
+__global__ void k_nrc_fallback(const __grid_constant__ NrcFallbackArgs f) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= f.total) return;
+  int li = f.n.first;
+  int64_t q = i;
+  while (li < f.n.nlev && q >= f.n.lv[li].P * f.n.lv[li].ndirs) q -= f.n.lv[li].P * f.n.lv[li++].ndirs;
+  if (li >= f.n.nlev) return;
+  const NrcLevel& L = f.n.lv[li];
+  const int d = (int)(q / L.P);
+  const int64_t p = q - (int64_t)d * L.P;
+  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const int h = L.spacing >> 1;
+  const int64_t cell = ((int64_t)((mz * L.spacing + h) >> f.tile_shift) * f.TY + ((my * L.spacing + h) >> f.tile_shift)) *
+                           f.TX + ((mx * L.spacing + h) >> f.tile_shift);
+  if (!f.flag[cell]) return;
+  float rt[4];
+  nrc_walk(f.lv[li], p, d, rt);
+  const int64_t plane = (int64_t)L.ndirs * L.P;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) L.rt[c * plane + q] = __float2half_rn(rt[c]);
+}
+
+// ---------------------------------------------------------------------------
+// Merge of a far level from (R, T): L = R + T * trilinear(A_{i+1}); one thread
+// per probe, block row = a pair of parent texels (eight child directions).
+// ---------------------------------------------------------------------------
+template <typename T, bool TOP>
+__global__ void __launch_bounds__(128) k_level_merge_rt(const __grid_constant__ LevelArgs a,
+                                                        const __half* __restrict__ rt) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.P) return;
+  const int Mx = a.M[0], My = a.M[1];
+  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  int tap_off[8];
+  float tap_w[8];
+  if (!TOP) {
+    int qq[3][2];
+    float wt[3][2];
+    const int m[3] = {mx, my, mz};
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const int lo = (m[ax] - 1) >> 1;
+      wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
+      wt[ax][1] = 1.0f - wt[ax][0];
+      qq[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
+      qq[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+    }
+#pragma unroll
+    for (int tp = 0; tp < 8; ++tp) {
+      const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
+      tap_off[tp] = (qq[2][iz] * a.UM[1] + qq[1][iy]) * a.UM[0] + qq[0][ix];
+      tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
+    }
+  }
+  T* L = static_cast<T*>(a.L);
+  const T* Au = static_cast<const T*>(a.A_up);
+  const int hn = a.n >> 1;
+  const int64_t npar = (int64_t)hn * hn;
+  const int64_t plane = (int64_t)a.ndirs * a.P;
+  float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int dl = 0; dl < 8; ++dl) {
+    const int dp = blockIdx.y * 2 + (dl >> 2), c = dl & 3;
+    const int d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
+    const int64_t off = (int64_t)d * a.P + p;
+    float rv[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) rv[ch] = __half2float(rt[ch * plane + off]);
+    const float tr = __half2float(rt[3 * plane + off]);
+    if (!TOP && tr > 0.f) {
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
+        float sum = 0.f;
+#pragma unroll
+        for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
+        rv[ch] = fmaf(tr, sum, rv[ch]);
+      }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      Store<T>::stream(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
+      acc[ch] += rv[ch];
+    }
+    if ((dl & 3) == 3) {
+      T* A = static_cast<T*>(a.A_out);
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
+        acc[ch] = 0.f;
+      }
+    }
+  }
+}
+
+}  // namespace rcx

@@ -105,7 +105,7 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
 // Composed volume, full-resolution opacity and emissive bits, and every
 // level's decimated opacity over a list of regions (composition rule as in
 // k_compose).
-__global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ,
+static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ,
                                 uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W,
                                 const QSphere* __restrict__ sph, int ns, const Region* __restrict__ regs,
                                 const MaskSet ms) {

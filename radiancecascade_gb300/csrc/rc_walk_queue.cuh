@@ -226,7 +226,7 @@ __device__ __forceinline__ void walk_tasks(const QueueArgs& q, unsigned long lon
   }
 }
 
-__global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
+static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
   walk_tasks<4>(q, q.counter, q.total);
 }
 

@@ -228,6 +228,52 @@ class Engine:
         F.check(self._lib.rc_radiance_device_ptr(self.handle, level, C.byref(p)))
         return p.value
 
+    # ---- neural radiance cache ----------------------------------------
+    @staticmethod
+    def nrc_params(**kw) -> F.NrcParams:
+        p = F.NrcParams()
+        F.check(F.lib().rc_nrc_params_default(C.byref(p)))
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def nrc_enable(self, params: Optional[F.NrcParams] = None, **kw) -> None:
+        p = params if params is not None else self.nrc_params(**kw)
+        F.check(self._lib.rc_nrc_enable(self.handle, C.byref(p)))
+
+    def nrc_disable(self) -> None:
+        F.check(self._lib.rc_nrc_disable(self.handle))
+
+    def nrc_stats(self) -> dict:
+        st = F.NrcStats()
+        F.check(self._lib.rc_nrc_get_stats(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_ if k != "pad"}
+
+    def nrc_save(self) -> bytes:
+        need = C.c_int64()
+        F.check(self._lib.rc_nrc_save(self.handle, None, 0, C.byref(need)))
+        buf = (C.c_char * need.value)()
+        F.check(self._lib.rc_nrc_save(self.handle, buf, need.value, C.byref(need)))
+        return bytes(buf)
+
+    def nrc_load(self, blob: bytes) -> None:
+        buf = (C.c_char * len(blob)).from_buffer_copy(blob)
+        F.check(self._lib.rc_nrc_load(self.handle, buf, len(blob)))
+
+    def nrc_query(self, level: int, probes, dirs) -> np.ndarray:
+        pr = np.ascontiguousarray(probes, np.int32)
+        di = np.ascontiguousarray(dirs, np.int32)
+        out = np.zeros((len(pr), 4), np.float32)
+        F.check(self._lib.rc_nrc_query(self.handle, level, F.ptr(pr), F.ptr(di), len(pr), F.ptr(out)))
+        return out
+
+    def nrc_tile_gradient(self, level: int, probe: int, d0: int, targets: np.ndarray):
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 4)
+        pg = np.zeros(F.lib().rc_nrc_param_count(), np.float32)
+        eg = np.zeros(32, np.float32)
+        F.check(self._lib.rc_nrc_tile_gradient(self.handle, level, probe, d0, len(t), F.ptr(t), F.ptr(pg), F.ptr(eg)))
+        return pg, eg
+
 
 class Batch:
     """Many independent scenes solved by one persistent launch (a CUDA graph).

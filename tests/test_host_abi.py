@@ -137,3 +137,14 @@ def _has_gpu():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def test_nrc_defaults_and_argument_checks():
+    p = F.NrcParams()
+    assert F.lib().rc_nrc_params_default(C.byref(p)) == F.RC_OK
+    assert (p.first_level, p.hash_log2_entries, p.base_resolution, p.max_resolution) == (2, 19, 16, 512)
+    assert abs(p.learning_rate - 1e-2) < 1e-9 and p.train_fraction_log2 == 4 and p.fallback_tile == 8
+    assert F.lib().rc_nrc_param_count() == 4 * (64 * 64 + 64) + 16 * 64 + 16
+    assert F.lib().rc_nrc_enable(None, C.byref(p)) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_nrc_disable(None) == F.RC_ERR_INVALID_ARG
+    assert F.lib().rc_nrc_params_default(None) == F.RC_ERR_INVALID_ARG
