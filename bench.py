@@ -12,6 +12,12 @@ cascades plus the cascade-0 fluence are solved.
          back into pinned host memory
   roofline   level kernels: algorithmic bytes per frame / their event time
   cpu_baseline   the FP32 CPU port of the method, all host threads
+  learned    the learned+FP16 form on the same workload (FP16 radiance, far
+             cascades from the neural radiance cache): frames/s, speed-up over
+             the plain FP32 value, fluence error against the FP64 oracle
+
+--workload batch64 measures the batched form instead (64 uneven scenes, one
+persistent launch), in scenes/s.
 
 --impl reference times the CPU implementation of the same path (the oracle
 port, FP32, all host threads) on the same workload: the reference project
@@ -143,6 +149,63 @@ def cpu_port_frames_per_s(frames: int, threads: int, precision=np.float32):
         t_total += time.perf_counter() - t0
         O.advance(spheres, 256, 1)
     return frames / t_total, t_total
+
+
+def timed_frames(eng, R, sph, frames, local):
+    """Event-timed frames (set emitters + solve) on the engine's stream; -> (ms, spheres of the last frame)."""
+    import torch
+    stream = torch.cuda.ExternalStream(eng.stream(), device=local)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    last = sph.copy()
+    for _ in range(frames):
+        last = sph.copy()
+        eng.set_spheres(sph)
+        eng.solve()
+        R.advance_spheres(sph, 256, 1)
+    t1.record(stream)
+    t1.synchronize()
+    return t0.elapsed_time(t1), last
+
+
+def learned_form(args, R, local, boxes, spheres, plain_fps):
+    """The learned+FP16 form of the same moving-emitter workload: FP16 radiance,
+    cascades 2-5 from the neural radiance cache, refit every frame on a 1/16
+    slice of walked probes, per-8^3-tile fallback at 1% held-out error.  The
+    cache first learns for `learned_warmup` frames; the timed frames follow."""
+    from oracle import oracle as O
+    out = {}
+    eng = R.Engine(R.make_params(256, 6, precision="fp16"), device=local)
+    eng.set_boxes(boxes)
+    sph = spheres.copy()
+    for _ in range(3):
+        eng.set_spheres(sph)
+        eng.solve()
+    eng.synchronize()
+    ms, _ = timed_frames(eng, R, sph.copy(), args.steps, local)
+    out["plain_fp16_frames_per_s"] = round(args.steps / (ms / 1000.0), 3)
+    eng.nrc_enable()
+    for _ in range(args.learned_warmup):
+        eng.set_spheres(sph)
+        eng.solve()
+        R.advance_spheres(sph, 256, 1)
+    eng.synchronize()
+    ms, last = timed_frames(eng, R, sph, args.steps, local)
+    fps = args.steps / (ms / 1000.0)
+    g = eng.fluence().astype(np.float64)
+    st = eng.nrc_stats()
+    eng.close()
+    ref, _ = O.solve(O.params(256, 6), O.voxelise(256, boxes, last), jump=True)
+    out.update({
+        "frames_per_s": round(fps, 3), "ms_per_frame": round(ms / args.steps, 4),
+        "speedup_vs_plain_fp32": round(fps / plain_fps, 4),
+        "fluence_rel_l2_vs_fp64": float(np.linalg.norm(g - ref) / np.linalg.norm(ref)),
+        "fallback_tiles": int(st["fallback_tiles"]), "tiles": int(st["tiles"]),
+        "cascades_from_network": [i for i in range(6) if (st["served_levels"] >> i) & 1],
+        "frames_learned_before_timing": args.learned_warmup, "frames_timed": args.steps,
+        "storage": "radiance f16, network bf16 with f32 accumulation",
+    })
+    return out
 
 
 def run_reference(args, rank, world):
@@ -341,6 +404,9 @@ def main():
     ap.add_argument("--cpu-frames", type=int, default=2, help="frames of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--learned-warmup", type=int, default=48,
+                    help="frames the radiance cache learns before the learned form is timed")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned+FP16 form")
     ap.add_argument("--workload", default="c256", choices=["c256", "batch64"],
                     help="c256: the 256^3 moving-emitter frame (default); batch64: 64 uneven scenes")
     args = ap.parse_args()
@@ -470,6 +536,8 @@ def main():
         line["accuracy"] = {"frame": 0, "fluence_rel_l2_vs_fp64":
                             float(np.linalg.norm(g - ref) / np.linalg.norm(ref)),
                             "fluence_max_abs_vs_fp64": float(np.abs(g - ref).max())}
+    if rank == 0 and world == 1 and not args.no_learned:
+        line["learned"] = learned_form(args, R, local, boxes, spheres, value)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, _ = cpu_port_frames_per_s(args.cpu_frames, threads)

@@ -250,7 +250,8 @@ rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best,
  * 1/2^train_fraction_log2 of the far probes (all their directions) to refit
  * the network (Adam), and a second such slice, held out, to measure its
  * error per voxel tile of fallback_tile^3; tiles whose relative L2 error of
- * (R, T) exceeds fallback_threshold use the plain walk for their probes. */
+ * (R, T) exceeds fallback_threshold use the plain walk for their probes;
+ * a far cascade mostly in such tiles runs its plain kernels instead. */
 typedef struct rc_nrc_params {
   int32_t first_level;          /* first cascade served (default 2)          */
   int32_t hash_log2_entries;    /* entries per hash level, log2 (19)        */
@@ -262,8 +263,10 @@ typedef struct rc_nrc_params {
   int32_t steps_per_solve;      /* Adam steps per solve (1)                 */
   float fallback_threshold;     /* held-out relative L2 error (0.01)        */
   int32_t fallback_tile;        /* voxel tile edge, power of two (8)        */
-  float radiance_scale;         /* network predicts R * scale (1/16)        */
-  int32_t pad;
+  float radiance_scale;         /* network predicts R * scale (1/4)         */
+  float plain_level_fraction;   /* a far cascade with at least this share of
+                                   its probes in fallback tiles runs the plain
+                                   walk for the whole cascade (0.5)         */
   uint64_t seed;                /* initial weights                          */
 } rc_nrc_params;
 
@@ -271,7 +274,8 @@ typedef struct rc_nrc_stats {
   int64_t solves;          /* solves served by the cache                     */
   int64_t steps;           /* Adam steps taken                               */
   float last_loss;         /* mean squared error of the last step            */
-  float pad;
+  int32_t served_levels;   /* bit i: cascade i came from the network in the
+                              last solve (else its plain kernels ran)       */
   int64_t fallback_tiles;  /* tiles on the plain walk now                    */
   int64_t tiles;           /* all tiles                                      */
 } rc_nrc_stats;

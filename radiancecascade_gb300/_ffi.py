@@ -48,11 +48,11 @@ class NrcParams(C.Structure):
                 ("max_resolution", C.c_int32), ("learning_rate", C.c_float), ("beta1", C.c_float),
                 ("beta2", C.c_float), ("epsilon", C.c_float), ("train_fraction_log2", C.c_int32),
                 ("steps_per_solve", C.c_int32), ("fallback_threshold", C.c_float), ("fallback_tile", C.c_int32),
-                ("radiance_scale", C.c_float), ("pad", C.c_int32), ("seed", C.c_uint64)]
+                ("radiance_scale", C.c_float), ("plain_level_fraction", C.c_float), ("seed", C.c_uint64)]
 
 
 class NrcStats(C.Structure):
-    _fields_ = [("solves", C.c_int64), ("steps", C.c_int64), ("last_loss", C.c_float), ("pad", C.c_float),
+    _fields_ = [("solves", C.c_int64), ("steps", C.c_int64), ("last_loss", C.c_float), ("served_levels", C.c_int32),
                 ("fallback_tiles", C.c_int64), ("tiles", C.c_int64)]
 
 

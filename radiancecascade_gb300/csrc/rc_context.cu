@@ -311,6 +311,19 @@ void launch_queue_walk(const rc_context* c, cudaStream_t s) {
   k_walk_queue<<<(unsigned)c->queue_blocks, kQueueThreads, 0, s>>>(c->qargs);
 }
 
+}  // namespace
+
+namespace rcx {
+void plain_level(const rc_context* c, int level, cudaStream_t s) {
+  if (c->elem == 2) launch_level<__half>(c, level, s);
+  else launch_level<float>(c, level, s);
+}
+void plain_queue_walk(const rc_context* c, cudaStream_t s) { launch_queue_walk(c, s); }
+bool level_uses_queue(const rc_context* c, int level) { return c->mode[level] == kModeQueue; }
+}  // namespace rcx
+
+namespace {
+
 // With the neural radiance cache on, the far levels (from its first level
 // up) come from the cache and the walk queue runs only when a near level
 // needs it.

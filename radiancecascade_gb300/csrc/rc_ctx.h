@@ -93,6 +93,12 @@ struct DeviceGuard {
   }
 };
 
+// Plain solve of one level (its usual kernel), the walk queue of the narrow
+// levels, and whether a level reads walk records (rc_context.cu).
+void plain_level(const rc_context* c, int level, cudaStream_t s);
+void plain_queue_walk(const rc_context* c, cudaStream_t s);
+bool level_uses_queue(const rc_context* c, int level);
+
 // Neural radiance cache hooks (rc_nrc.cu).
 bool nrc_active(const rc_context* c);
 int nrc_first_level(const rc_context* c);  // first cascade the cache serves

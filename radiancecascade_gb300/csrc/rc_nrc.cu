@@ -23,26 +23,28 @@ struct NrcState {
   int first = 2, nlev = 0, nph = 16;
   int64_t T = 0;       // entries per hash level
   int64_t hash_n = 0;  // 16 * T * 2
-  NrcHash hash{};
   float *hash_master = nullptr, *hash_m = nullptr, *hash_v = nullptr, *hash_g = nullptr;
   __half* hash_half = nullptr;
   float *mlp = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr, *dbg_g = nullptr;
   unsigned char* img = nullptr;
-  float* epos = nullptr;
   __nv_bfloat16* denc = nullptr;
   __half* rt = nullptr;
-  int64_t total_probes = 0, total_queries = 0, enum_tiles = 0;
-  // sample probes and their tiles, grouped by phase
+  int64_t total_queries = 0, enum_tiles = 0;
+  // tiles of the sample probes (all their directions), grouped by phase
   NrcTile* tiles = nullptr;
-  NrcSample* samples = nullptr;
   std::vector<NrcTile> h_tiles;
-  std::vector<int64_t> tile_begin, sample_begin;
-  int64_t max_tiles2 = 0, max_held = 0, max_samples = 0;
+  std::vector<int64_t> tile_begin;
+  int64_t max_tiles2 = 0, max_held = 0;
   float* target = nullptr;
   float* pred = nullptr;
   float* epos_grad = nullptr;
   float* loss = nullptr;
   float* h_loss = nullptr;  // pinned
+  unsigned* count = nullptr;    // probes in fallback tiles per far level
+  unsigned* h_count = nullptr;  // pinned copy
+  cudaEvent_t ev_count = nullptr;
+  int64_t total_probes = 0;
+  int served[kMaxCascades]{};  // levels served by the network in the last solve
   NrcTile* qtiles = nullptr;  // rc_nrc_query / rc_nrc_tile_gradient scratch
   float* qout = nullptr;
   int64_t qcap = 0;
@@ -76,11 +78,14 @@ int nrc_phase(uint64_t seed, int level, int64_t probe, int nph) {
 void free_state(NrcState* n) {
   if (!n) return;
   void* bufs[] = {n->hash_master, n->hash_m, n->hash_v, n->hash_g, n->hash_half, n->mlp, n->mlp_m, n->mlp_v,
-                  n->mlp_g, n->dbg_g, n->img, n->epos, n->denc, n->rt, n->tiles, n->samples, n->target, n->pred,
+                  n->mlp_g, n->dbg_g, n->img, n->denc, n->rt, n->tiles, n->target, n->pred,
                   n->epos_grad, n->loss, n->qtiles, n->qout, n->tnum, n->tden, n->flag};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (n->h_loss) cudaFreeHost(n->h_loss);
+  if (n->count) cudaFree(n->count);
+  if (n->h_count) cudaFreeHost(n->h_count);
+  if (n->ev_count) cudaEventDestroy(n->ev_count);
   delete n;
 }
 
@@ -97,10 +102,6 @@ rc_status check(const rc_context* c, const char* fn, bool need_nrc) {
 }
 
 unsigned blocks_for(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads); }
-
-void launch_encode(NrcState* n, cudaStream_t s) {
-  k_nrc_encode<<<blocks_for(n->total_probes * kNrcHashLevels, 256), 256, 0, s>>>(n->base, n->hash, n->total_probes);
-}
 
 void launch_adam(float* p, float* g, float* m, float* v, __half* half_out, int64_t count, const rc_nrc_params& prm,
                  int64_t t, cudaStream_t s) {
@@ -196,6 +197,14 @@ void nrc_release(rc_context* c) {
   c->nrc = nullptr;
 }
 
+// One solve's far cascades:
+//   1. plain (R, T) of this solve's training slice and held-out slice;
+//   2. held-out error of the current network -> fallback flags -> probes in
+//      fallback tiles per level (copied to the host);
+//   3. refit (Adam) on the training slice;
+//   4. per level: served by the network when less than plain_level_fraction
+//      of its probes is in fallback tiles (inference for the level, plain walk
+//      for its fallback probes, merge from (R, T)), else its plain kernels.
 rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   NrcState* n = c->nrc;
   const int ph = (int)(n->solves % n->nph), hp = (ph + n->nph / 2) % n->nph;
@@ -203,11 +212,8 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   const int64_t ho0 = n->tile_begin[hp], nho = n->tile_begin[hp + 1] - ho0;
   float* ttr = n->target;
   float* tho = n->target + ntr * kNrcThreads * 4;
-  // plain (R, T) of the training and held-out slices
   if (ntr) k_nrc_targets<<<blocks_for(ntr * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + tr0, ntr, ttr));
   if (nho) k_nrc_targets<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + ho0, nho, tho));
-  launch_encode(n, s);
-  // held-out error with the current network -> fallback flags
   if (nho) {
     NrcArgs a = n->base;
     a.tiles = n->tiles + ho0;
@@ -220,9 +226,14 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
     k_nrc_flags<<<blocks_for(cells, 256), 256, 0, s>>>(n->tnum, n->tden, n->flag, cells, thr * thr);
   }
-  // refit on the training slice
+  RC_CUDA(cudaMemsetAsync(n->count, 0, kMaxCascades * sizeof(unsigned), s), "cache count reset");
+  k_nrc_count<<<blocks_for(n->total_probes, 256), 256, 0, s>>>(n->base, n->flag, n->tile_shift, n->TX, n->TY,
+                                                                n->total_probes, n->count);
+  RC_CUDA(cudaMemcpyAsync(n->h_count, n->count, kMaxCascades * sizeof(unsigned), cudaMemcpyDeviceToHost, s),
+          "cache count");
+  RC_CUDA(cudaEventRecord(n->ev_count, s), "cache count");
+  // refit on the training slice (enqueued before the host waits for the counts)
   const int steps = std::max(1, n->prm.steps_per_solve);
-  const int64_t ns0 = n->sample_begin[ph], nsamp = n->sample_begin[ph + 1] - ns0;
   if (ntr) {
     RC_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), s), "cache loss reset");
     n->loss_rows = 0;
@@ -232,19 +243,15 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
       int64_t rows = 0;
       for (int64_t t = a0; t < a1; ++t) rows += n->h_tiles[tr0 + t].n;
       n->loss_rows += rows;
-      if (st > 0) launch_encode(n, s);
-      RC_CUDA(cudaMemsetAsync(n->epos_grad, 0, (size_t)nsamp * kNrcPosFeat * sizeof(float), s), "cache grad reset");
       NrcArgs a = n->base;
       a.tiles = n->tiles + tr0 + a0;
       a.ntiles = a1 - a0;
       a.target = ttr + a0 * kNrcThreads * 4;
       a.grad = n->mlp_g;
-      a.epos_grad = n->epos_grad;
+      a.epos_grad = nullptr;
       a.loss = n->loss;
       a.inv_batch = 1.f / (float)std::max<int64_t>(rows, 1);
       k_nrc_train<<<(unsigned)std::min<int64_t>(a1 - a0, n->train_blocks), kNrcThreads, kTrainSmem, s>>>(a);
-      NrcHash h = n->hash;
-      k_nrc_hash_grad<<<blocks_for(nsamp * kNrcHashLevels, 256), 256, 0, s>>>(a, h, n->samples + ns0, (int)nsamp);
       ++n->steps;
       launch_adam(n->mlp, n->mlp_g, n->mlp_m, n->mlp_v, nullptr, kNrcParams, n->prm, n->steps, s);
       launch_adam(n->hash_master, n->hash_g, n->hash_m, n->hash_v, n->hash_half, n->hash_n, n->prm, n->steps, s);
@@ -252,11 +259,27 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     }
     RC_CUDA(cudaMemcpyAsync(n->h_loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "cache loss");
   }
-  // inference over every far query, then the plain walk where flagged
-  launch_encode(n, s);
-  k_nrc_forward<true><<<(unsigned)std::min<int64_t>(n->enum_tiles, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(
-      n->base, n->enum_tiles);
-  {
+  // which levels the network serves this solve
+  RC_CUDA(cudaEventSynchronize(n->ev_count), "cache count wait");
+  NrcArgs inf = n->base;
+  int64_t t0 = 0, served_queries = 0;
+  bool any_served = false, queue_plain = false;
+  for (int i = n->first; i < c->nlev; ++i) {
+    const int64_t P = c->geom[i].probes();
+    n->served[i] = (double)n->h_count[i] < (double)n->prm.plain_level_fraction * (double)P;
+    inf.tile0[i] = t0;
+    if (n->served[i]) {
+      t0 += (P * c->geom[i].ndirs + kNrcThreads - 1) / kNrcThreads;
+      served_queries += P * c->geom[i].ndirs;
+      any_served = true;
+    } else {
+      queue_plain |= level_uses_queue(c, i);
+    }
+  }
+  inf.tile0[c->nlev] = t0;
+  if (queue_plain) plain_queue_walk(c, s);
+  if (any_served) {
+    k_nrc_forward<true><<<(unsigned)std::min<int64_t>(t0, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(inf, t0);
     NrcFallbackArgs f;
     memset(&f, 0, sizeof f);
     for (int i = 0; i < c->nlev; ++i) f.lv[i] = c->args[i];
@@ -265,11 +288,17 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     f.tile_shift = n->tile_shift;
     f.TX = n->TX;
     f.TY = n->TY;
+    for (int i = 0; i < kMaxCascades; ++i) f.served[i] = n->served[i];
     f.total = n->total_queries;
     k_nrc_fallback<<<blocks_for(n->total_queries, 256), 256, 0, s>>>(f);
   }
-  // merges of the far levels, top down
+  (void)served_queries;
+  // far levels, top down
   for (int i = c->nlev - 1; i >= n->first; --i) {
+    if (!n->served[i]) {
+      plain_level(c, i, s);
+      continue;
+    }
     const LevelArgs& a = c->args[i];
     const __half* rt = n->base.lv[i].rt;
     dim3 grid(blocks_for(a.P, 128), (unsigned)((a.n / 2) * (a.n / 2) / 2));
@@ -313,7 +342,8 @@ rc_status rc_nrc_params_default(rc_nrc_params* out) {
   out->steps_per_solve = 1;
   out->fallback_threshold = 0.01f;
   out->fallback_tile = 8;
-  out->radiance_scale = 1.f / 16.f;
+  out->radiance_scale = 0.25f;
+  out->plain_level_fraction = 0.5f;
   out->seed = 0x5EEDull;
   return RC_OK;
 }
@@ -330,7 +360,8 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
       q.base_resolution < 2 || q.max_resolution < q.base_resolution || q.max_resolution > 4096 ||
       !(q.learning_rate > 0.f) || !(q.beta1 >= 0.f && q.beta1 < 1.f) || !(q.beta2 >= 0.f && q.beta2 < 1.f) ||
       !(q.epsilon > 0.f) || q.train_fraction_log2 < 1 || q.train_fraction_log2 > 8 || q.steps_per_solve < 1 ||
-      q.steps_per_solve > 64 || !(q.fallback_threshold >= 0.f) || !pow2_tile || !(q.radiance_scale > 0.f)) {
+      q.steps_per_solve > 64 || !(q.fallback_threshold >= 0.f) || !pow2_tile || !(q.radiance_scale > 0.f) ||
+      !(q.plain_level_fraction >= 0.f && q.plain_level_fraction <= 1.f)) {
     set_error("rc_nrc_enable: invalid rc_nrc_params (first_level must be in [1, num_cascades))");
     return RC_ERR_INVALID_ARG;
   }
@@ -350,49 +381,49 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   };
   rc_status s;
   // hash grid
-  n->hash.log2T = q.hash_log2_entries;
+  NrcHash& hh = n->base.hash;
+  hh.log2T = q.hash_log2_entries;
   const double bgrow = exp((log((double)q.max_resolution) - log((double)q.base_resolution)) / (kNrcHashLevels - 1));
-  for (int l = 0; l < kNrcHashLevels; ++l)
-    n->hash.res[l] = std::max(1, (int)floor((double)q.base_resolution * pow(bgrow, (double)l) + 1e-9));
-  n->hash.inv_extent = 1.f / (float)std::max(c->p.grid[0], std::max(c->p.grid[1], c->p.grid[2]));
+  for (int l = 0; l < kNrcHashLevels; ++l) {
+    hh.res[l] = std::max(1, (int)floor((double)q.base_resolution * pow(bgrow, (double)l) + 1e-9));
+    hh.dres[l] = std::max(1, (int)floor(2.0 * pow(64.0, (double)l / (kNrcHashLevels - 1)) + 1e-9));
+  }
+  hh.inv_extent = 1.f / (float)std::max(c->p.grid[0], std::max(c->p.grid[1], c->p.grid[2]));
   if ((s = dev_alloc((void**)&n->hash_master, n->hash_n * 4, "hash grid")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->hash_m, n->hash_n * 4, "hash grid moments")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->hash_v, n->hash_n * 4, "hash grid moments")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->hash_g, n->hash_n * 4, "hash grid gradient")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->hash_half, n->hash_n * 2, "hash grid FP16")) != RC_OK) return fail(s);
-  n->hash.table = n->hash_half;
-  n->hash.grad = n->hash_g;
+  hh.table = n->hash_half;
+  hh.grad = n->hash_g;
   // MLP
   float** mb[] = {&n->mlp, &n->mlp_m, &n->mlp_v, &n->mlp_g, &n->dbg_g};
   for (float** b : mb)
     if ((s = dev_alloc((void**)b, kNrcParams * 4, "network parameters")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->img, kImgBytes, "network weight image")) != RC_OK) return fail(s);
-  // far levels: encodings, direction features, (R, T)
-  memset(&n->base, 0, sizeof n->base);
+  // far levels: direction features, (R, T)
   n->base.first = n->first;
   n->base.nlev = c->nlev;
-  int64_t probes = 0, queries = 0, dirs = 0;
+  int64_t queries = 0, dirs = 0;
   for (int i = n->first; i < c->nlev; ++i) {
-    probes += c->geom[i].probes();
     queries += c->geom[i].probes() * c->geom[i].ndirs;
     dirs += c->geom[i].ndirs;
+    n->total_probes += c->geom[i].probes();
   }
-  n->total_probes = probes;
   n->total_queries = queries;
-  if ((s = dev_alloc((void**)&n->epos, probes * kNrcPosFeat * 4, "position encodings")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->denc, dirs * kNrcDirFeat * 2, "direction features")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->rt, queries * 4 * 2, "cached (R, T)")) != RC_OK) return fail(s);
   {
     std::vector<__nv_bfloat16> de((size_t)dirs * kNrcDirFeat);
-    int64_t po = 0, dO = 0, qo = 0, t0 = 0;
+    int64_t dO = 0, qo = 0, t0 = 0;
     for (int i = n->first; i < c->nlev; ++i) {
       const LevelGeom& gm = c->geom[i];
       NrcLevel& L = n->base.lv[i];
-      L.epos = n->epos + po * kNrcPosFeat;
       L.denc = n->denc + dO * kNrcDirFeat;
       L.rt = n->rt + qo * 4;
       L.P = gm.probes();
       L.ndirs = gm.ndirs;
+      L.n = gm.n;
       for (int a = 0; a < 3; ++a) L.M[a] = gm.M[a];
       L.spacing = gm.spacing;
       n->base.tile0[i] = t0;
@@ -407,7 +438,6 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
         for (int k = 0; k < 10; ++k) row[k] = __float2bfloat16_rn((float)f[k]);
         for (int k = 0; k < 6; ++k) row[10 + k] = __float2bfloat16_rn(k == std::min(i - n->first, 5) ? 1.f : 0.f);
       }
-      po += gm.probes();
       dO += gm.ndirs;
       qo += gm.probes() * gm.ndirs;
     }
@@ -421,27 +451,20 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   n->base.err = c->err;
   // sample probes by phase and their tiles of up to 128 directions
   {
-    std::vector<std::vector<NrcSample>> sp(n->nph);
+    std::vector<std::vector<std::pair<int, int32_t>>> sp(n->nph);
     for (int i = n->first; i < c->nlev; ++i)
       for (int64_t p = 0; p < c->geom[i].probes(); ++p)
-        sp[nrc_phase(q.seed ^ 0xA5A5A5A5ull, i, p, n->nph)].push_back(NrcSample{i, (int32_t)p});
-    std::vector<NrcSample> all;
+        sp[nrc_phase(q.seed ^ 0xA5A5A5A5ull, i, p, n->nph)].push_back({i, (int32_t)p});
     n->tile_begin.assign(n->nph + 1, 0);
-    n->sample_begin.assign(n->nph + 1, 0);
     for (int ph = 0; ph < n->nph; ++ph) {
       n->tile_begin[ph] = (int64_t)n->h_tiles.size();
-      n->sample_begin[ph] = (int64_t)all.size();
-      for (size_t k = 0; k < sp[ph].size(); ++k) {
-        const NrcSample smp = sp[ph][k];
-        const int nd = c->geom[smp.level].ndirs;
+      for (const auto& smp : sp[ph]) {
+        const int nd = c->geom[smp.first].ndirs;
         for (int d0 = 0; d0 < nd; d0 += kNrcThreads)
-          n->h_tiles.push_back(NrcTile{smp.level, smp.probe, d0, std::min(kNrcThreads, nd - d0), (int32_t)k, 0});
-        all.push_back(smp);
+          n->h_tiles.push_back(NrcTile{smp.first, smp.second, d0, std::min(kNrcThreads, nd - d0), 0, 0});
       }
-      n->max_samples = std::max<int64_t>(n->max_samples, (int64_t)sp[ph].size());
     }
     n->tile_begin[n->nph] = (int64_t)n->h_tiles.size();
-    n->sample_begin[n->nph] = (int64_t)all.size();
     for (int ph = 0; ph < n->nph; ++ph) {
       const int hp = (ph + n->nph / 2) % n->nph;
       const int64_t a = n->tile_begin[ph + 1] - n->tile_begin[ph], b = n->tile_begin[hp + 1] - n->tile_begin[hp];
@@ -451,14 +474,8 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
     if ((s = dev_alloc((void**)&n->tiles, std::max<size_t>(1, n->h_tiles.size()) * sizeof(NrcTile), "cache tiles")) !=
         RC_OK)
       return fail(s);
-    if ((s = dev_alloc((void**)&n->samples, std::max<size_t>(1, all.size()) * sizeof(NrcSample), "cache samples")) !=
-        RC_OK)
-      return fail(s);
     if (!n->h_tiles.empty())
       RC_CUDA(cudaMemcpy(n->tiles, n->h_tiles.data(), n->h_tiles.size() * sizeof(NrcTile), cudaMemcpyHostToDevice),
-              "rc_nrc_enable: upload");
-    if (!all.empty())
-      RC_CUDA(cudaMemcpy(n->samples, all.data(), all.size() * sizeof(NrcSample), cudaMemcpyHostToDevice),
               "rc_nrc_enable: upload");
   }
   if ((s = dev_alloc((void**)&n->target, std::max<int64_t>(1, n->max_tiles2) * kNrcThreads * 16, "cache targets")) !=
@@ -467,12 +484,13 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   if ((s = dev_alloc((void**)&n->pred, std::max<int64_t>(1, n->max_held) * kNrcThreads * 16, "cache predictions")) !=
       RC_OK)
     return fail(s);
-  if ((s = dev_alloc((void**)&n->epos_grad, std::max<int64_t>(1, n->max_samples) * kNrcPosFeat * 4,
-                     "position gradients")) != RC_OK)
-    return fail(s);
+  if ((s = dev_alloc((void**)&n->epos_grad, kNrcPosFeat * 4, "feature gradient probe")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->loss, sizeof(float), "cache loss")) != RC_OK) return fail(s);
   RC_CUDA(cudaMallocHost((void**)&n->h_loss, sizeof(float)), "rc_nrc_enable: pinned");
   *n->h_loss = 0.f;
+  if ((s = dev_alloc((void**)&n->count, kMaxCascades * sizeof(unsigned), "cache counts")) != RC_OK) return fail(s);
+  RC_CUDA(cudaMallocHost((void**)&n->h_count, kMaxCascades * sizeof(unsigned)), "rc_nrc_enable: pinned");
+  RC_CUDA(cudaEventCreateWithFlags(&n->ev_count, cudaEventDisableTiming), "rc_nrc_enable: event");
   // fallback tiles: all start on the plain walk
   n->tile_shift = 0;
   while ((1 << n->tile_shift) < q.fallback_tile) ++n->tile_shift;
@@ -493,13 +511,20 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
           "rc_nrc_enable: attribute");
   RC_CUDA(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem),
           "rc_nrc_enable: attribute");
-  int sms = 0, per_f = 0, per_t = 0;
+  // Resident blocks: shared memory and registers per SM, and the tensor-memory
+  // budget of 512 columns per SM (64 per inference block, 512 per training
+  // block) -- so that no allocation ever waits.
+  int sms = 0, smem_sm = 0, regs_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_f, k_nrc_forward<true>, kNrcThreads, kFwdSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_t, k_nrc_train, kNrcThreads, kTrainSmem);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c->device);
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, c->device);
+  cudaFuncAttributes fa{};
+  int fwd_regs = 128;
+  if (cudaFuncGetAttributes(&fa, k_nrc_forward<true>) == cudaSuccess) fwd_regs = std::max(fa.numRegs, 1);
   (void)cudaGetLastError();
-  // tensor-memory budget: 512 columns per SM (64 per inference block, 512 per training block)
-  n->fwd_blocks = std::max(1, sms * std::min(std::max(per_f, 1), 8));
+  const int by_smem = smem_sm / (kFwdSmem + 1024);
+  const int by_regs = regs_sm / (((fwd_regs + 7) & ~7) * kNrcThreads);
+  n->fwd_blocks = std::max(1, sms * std::max(1, std::min(std::min(by_smem, by_regs), 8)));
   n->train_blocks = std::max(1, sms);
   {
     std::vector<float> mlp, hash;
@@ -600,6 +625,8 @@ rc_status rc_nrc_get_stats(rc_context* c, rc_nrc_stats* out) {
   out->steps = n->steps;
   out->last_loss = n->loss_rows ? *n->h_loss / (float)n->loss_rows : 0.f;
   out->fallback_tiles = std::count(f.begin(), f.end(), (uint8_t)1);
+  for (int i = n->first; i < c->nlev; ++i)
+    if (n->served[i]) out->served_levels |= 1 << i;
   out->tiles = cells;
   return RC_OK;
 }
@@ -626,7 +653,6 @@ rc_status rc_nrc_query(rc_context* c, int32_t level, const int32_t* probes, cons
   if (s != RC_OK) return s;
   cudaStream_t st = c->stream;
   RC_CUDA(cudaMemcpyAsync(n->qtiles, t.data(), count * sizeof(NrcTile), cudaMemcpyHostToDevice, st), "rc_nrc_query");
-  launch_encode(n, st);
   NrcArgs a = n->base;
   a.tiles = n->qtiles;
   a.ntiles = count;
@@ -643,11 +669,7 @@ rc_status rc_nrc_query(rc_context* c, int32_t level, const int32_t* probes, cons
     set_error("rc_nrc_query: a bounded device-side wait ran out");
     return RC_ERR_TIMEOUT;
   }
-  for (int64_t i = 0; i < count; ++i) {
-    const float* r = raw.data() + i * kNrcThreads * 4;  // row 0 of tile i
-    for (int k = 0; k < 3; ++k) out[4 * i + k] = std::max(r[k] / n->prm.radiance_scale, 0.f);
-    out[4 * i + 3] = std::min(std::max(r[3], 0.f), 1.f);
-  }
+  for (int64_t i = 0; i < count; ++i) nrc_serve(raw.data() + i * kNrcThreads * 4, n->prm.radiance_scale, out + 4 * i);
   return RC_OK;
 }
 
@@ -672,8 +694,8 @@ rc_status rc_nrc_tile_gradient(rc_context* c, int32_t level, int32_t probe, int3
   RC_CUDA(cudaMemcpyAsync(n->qout, tg.data(), tg.size() * 4, cudaMemcpyHostToDevice, st), "rc_nrc_tile_gradient");
   RC_CUDA(cudaMemsetAsync(n->dbg_g, 0, kNrcParams * 4, st), "rc_nrc_tile_gradient");
   RC_CUDA(cudaMemsetAsync(n->epos_grad, 0, kNrcPosFeat * 4, st), "rc_nrc_tile_gradient");
-  launch_encode(n, st);
   NrcArgs a = n->base;
+  a.hash.grad = nullptr;  // a probe: nothing is scattered into the table gradient
   a.tiles = n->qtiles;
   a.ntiles = 1;
   a.target = n->qout;

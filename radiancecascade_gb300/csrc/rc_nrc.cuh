@@ -6,15 +6,23 @@
 // the ray got through (T = 1) -- and the usual top-down merge then forms
 // L_i = R + T * merge(A_{i+1}).
 //
-// Model (Mueller et al. 2022, "Instant neural graphics primitives", for the
-// encoding): a multiresolution hash grid of the probe centre -- 16 levels x 2
-// FP16 features, 2^19 entries per level, resolutions 16 .. 512 in geometric
-// steps, trilinear interpolation, spatial hash (x * 1) ^ (y * 2654435761) ^
-// (z * 805459861) mod 2^19 where a level's dense grid does not fit -- plus 16
-// direction features (the octahedral texel centre u, v and sin / cos of pi,
-// 2 pi times each, and a one-hot of the cascade), zero-padded to 64 inputs.
+// Model.  Input encoding: a multiresolution hash encoding in the manner of
+// Mueller et al. 2022 ("Instant neural graphics primitives") over the query's
+// probe centre, its direction texel and its cascade: 16 levels x 2 FP16
+// features, 2^19 entries per level; level l quantises the probe centre
+// (scaled to [0, 1]) at resolution r_l (16 .. 512, geometric) and the
+// octahedral texel centre at resolution q_l (2 .. 128, geometric), and reads
+// the features of that one cell (queries sit exactly on the probe and texel
+// lattices, so no interpolation is needed) at hash(x, y, z, u, v, cascade) =
+// x ^ 2654435761 y ^ 805459861 z ^ 0x85EBCA77 u ^ 0xC2B2AE3D v ^ 0x27D4EB2F c
+// mod 2^19.  Plus 16 direction features (the texel centre u, v, sin / cos of
+// pi and 2 pi times each, and a one-hot of the cascade); zero-padded to 64.
 // MLP: 4 hidden layers of width 64 with ReLU, then a 16-wide linear output
 // layer of which 4 are used (R, G, B scaled by radiance_scale, and T).
+// Served values follow the walk's structure -- T is 0 or 1 and a ray that got
+// through carries no radiance: T = [o_3 >= 1/2], R = T ? 0 : max(o / scale, 0).
+// (Clamping the raw outputs instead would turn the network's zero-mean error
+// on the many empty rays into a positive bias of the fluence.)
 // BF16 weights and activations, FP32 accumulation in tensor memory; every
 // layer is one tcgen05 M = 128 GEMM (one query per row).  Training: MSE on
 // (R * scale, T), gradients through the same GEMMs (transposed operands in
@@ -50,8 +58,7 @@ constexpr int kImgW4F = 65536;
 constexpr int kImgW4B = 67584;
 constexpr int kImgBytes = 69632;
 
-// One tile of 128 queries.  probe >= 0: the queries are directions d0 ..
-// d0 + n - 1 of that probe; slot indexes the probe's position-gradient row.
+// One tile of up to 128 queries: directions d0 .. d0 + n - 1 of one probe.
 struct NrcTile {
   int32_t level;
   int32_t probe;
@@ -62,19 +69,28 @@ struct NrcTile {
 };
 
 struct NrcLevel {
-  const float* epos;          // [P][32] position encoding of every probe
   const __nv_bfloat16* denc;  // [ndirs][16] direction + cascade features
   __half* rt;                 // [4][ndirs][P]: R, G, B, T
   int64_t P;
   int32_t ndirs;
+  int32_t n;                  // direction resolution (n x n texels)
   int32_t M[3];
   int32_t spacing;
-  int32_t pad;
+};
+
+struct NrcHash {
+  const __half* table;  // [16][T][2]
+  float* grad;          // [16][T][2] (null: no scatter)
+  int32_t log2T;
+  int32_t res[kNrcHashLevels];   // position resolution per level
+  int32_t dres[kNrcHashLevels];  // direction resolution per level
+  float inv_extent;              // 1 / max grid edge
 };
 
 struct NrcArgs {
   const unsigned char* img;  // BF16 weight image
   const float* params;       // FP32 master (biases)
+  NrcHash hash;
   NrcLevel lv[kMaxCascades];
   int32_t first;             // first far cascade
   int32_t nlev;
@@ -84,7 +100,7 @@ struct NrcArgs {
   float* out;                // explicit tiles: raw outputs [tile][128][4]
   const float* target;       // training: [tile][128][4] (R, G, B, T)
   float* grad;               // training: FP32 gradient of the master parameters
-  float* epos_grad;          // training: [slot][32]
+  float* epos_grad;          // tile gradient: sum over rows of the 32 hash features' gradient
   float* loss;               // training: sum of squared errors
   float scale;               // radiance scale of the outputs
   float inv_batch;           // training: 1 / (queries in the step)
@@ -117,26 +133,66 @@ __device__ __forceinline__ bool nrc_query(const NrcArgs& a, int64_t t, int r, in
   return true;
 }
 
-// Input row: 32 position features, 16 direction features, 16 zeros.
+// Probe centre (voxel units) of probe p of level L, scaled to [0, 1].
+__device__ __forceinline__ void nrc_probe_pos(const NrcLevel& L, int64_t p, float inv_extent, float* u) {
+  const int mx = (int)(p % L.M[0]);
+  const int my = (int)((p / L.M[0]) % L.M[1]);
+  const int mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const float h = 0.5f * (float)L.spacing;
+  u[0] = ((float)mx * L.spacing + h) * inv_extent;
+  u[1] = ((float)my * L.spacing + h) * inv_extent;
+  u[2] = ((float)mz * L.spacing + h) * inv_extent;
+}
+
+// Table row of hash level l for a query (see the file comment).
+__device__ __forceinline__ uint32_t nrc_hash_row(const NrcHash& h, int l, const float* u, float du, float dv,
+                                                 int casc) {
+  const int r = h.res[l], q = h.dres[l];
+  const uint32_t x = (uint32_t)min((int)(u[0] * (float)r), r - 1);
+  const uint32_t y = (uint32_t)min((int)(u[1] * (float)r), r - 1);
+  const uint32_t z = (uint32_t)min((int)(u[2] * (float)r), r - 1);
+  const uint32_t a = (uint32_t)min((int)(du * (float)q), q - 1);
+  const uint32_t b = (uint32_t)min((int)(dv * (float)q), q - 1);
+  const uint32_t hv = x ^ (y * 2654435761u) ^ (z * 805459861u) ^ (a * 0x85EBCA77u) ^ (b * 0xC2B2AE3Du) ^
+                      ((uint32_t)casc * 0x27D4EB2Fu);
+  return (uint32_t)l * (1u << h.log2T) + (hv & ((1u << h.log2T) - 1u));
+}
+
+struct NrcQuery {
+  float u[3];   // probe centre in [0, 1]
+  float du, dv; // texel centre in [0, 1]
+  int casc;
+};
+
+__device__ __forceinline__ NrcQuery nrc_make_query(const NrcArgs& a, int li, int64_t p, int d) {
+  NrcQuery q;
+  const NrcLevel& L = a.lv[li];
+  nrc_probe_pos(L, p, a.hash.inv_extent, q.u);
+  q.du = ((float)(d % L.n) + 0.5f) / (float)L.n;
+  q.dv = ((float)(d / L.n) + 0.5f) / (float)L.n;
+  q.casc = li;
+  return q;
+}
+
+// Input row: 32 hash features, 16 direction features, 16 zeros.
 __device__ __forceinline__ void nrc_input(const NrcArgs& a, bool valid, int li, int64_t p, int d, float* x) {
 #pragma unroll
   for (int j = 0; j < 64; ++j) x[j] = 0.f;
   if (!valid) return;
   const NrcLevel& L = a.lv[li];
-  const float4* ep = reinterpret_cast<const float4*>(L.epos + p * kNrcPosFeat);
+  const NrcQuery q = nrc_make_query(a, li, p, d);
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const float4 v = __ldg(ep + j);
-    x[4 * j] = v.x;
-    x[4 * j + 1] = v.y;
-    x[4 * j + 2] = v.z;
-    x[4 * j + 3] = v.w;
+  for (int l = 0; l < kNrcHashLevels; ++l) {
+    const uint32_t row = nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc);
+    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(a.hash.table) + row));
+    x[2 * l] = f.x;
+    x[2 * l + 1] = f.y;
   }
   const uint4* dp = reinterpret_cast<const uint4*>(L.denc + (int64_t)d * kNrcDirFeat);
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
-    const uint4 u = __ldg(dp + j);
-    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+    const uint4 w = __ldg(dp + j);
+    const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&w);
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const float2 f = __bfloat1622float2(h[k]);
@@ -159,6 +215,14 @@ __device__ __forceinline__ bool nrc_wait(uint64_t* bar, uint32_t& phase, int* er
   const bool any_fail = __syncthreads_or(!ok);
   if (any_fail && threadIdx.x == 0) atomicExch(err, 3);
   return !any_fail;
+}
+
+// Served (R, G, B, T) from the raw outputs (see the file comment).
+__device__ __host__ __forceinline__ void nrc_serve(const float* o, float scale, float* sv) {
+  const bool through = o[3] >= 0.5f;
+  sv[3] = through ? 1.f : 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) sv[c] = through ? 0.f : fmaxf(o[c] / scale, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -238,9 +302,10 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_forward(const __grid_consta
       const NrcLevel& L = a.lv[li];
       const int64_t plane = (int64_t)L.ndirs * L.P;
       const int64_t off = (int64_t)d * L.P + p;
+      float sv[4];
+      nrc_serve(o, a.scale, sv);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) L.rt[c * plane + off] = __float2half_rn(fmaxf(o[c] / a.scale, 0.f));
-      L.rt[3 * plane + off] = __float2half_rn(fminf(fmaxf(o[3], 0.f), 1.f));
+      for (int c = 0; c < 4; ++c) L.rt[c * plane + off] = __float2half_rn(sv[c]);
     } else {
       float4 r4 = make_float4(o[0], o[1], o[2], o[3]);
       *reinterpret_cast<float4*>(a.out + (t * kNrcThreads + tid) * 4) = r4;
@@ -454,23 +519,33 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant
       tc_fence_after();
     }
     if (!ok) break;
-    // ---- position-feature gradient of the tile's probe: sum over rows of dx_1[:, 0:32]
+    // ---- hash-feature gradient: scattered per row into the table gradient
     {
       float v[64];
       tmem_ld64(tl, v);
       tc_fence_before();
+      if (valid && a.hash.grad) {
+        const NrcQuery q = nrc_make_query(a, li, p, d);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        float s = v[j];
-#pragma unroll
-        for (int sh = 16; sh > 0; sh >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, sh);
-        if (lane == 0) atomicAdd(&spos[j], s);
+        for (int l = 0; l < kNrcHashLevels; ++l) {
+          const uint32_t row = nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc);
+          if (v[2 * l] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row, v[2 * l]);
+          if (v[2 * l + 1] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row + 1, v[2 * l + 1]);
+        }
       }
-      __syncthreads();
-      if (tid < 32) {
-        const NrcTile tl0 = a.tiles[t];
-        if (tl0.slot >= 0) atomicAdd(&a.epos_grad[(int64_t)tl0.slot * kNrcPosFeat + tid], spos[tid]);
-        spos[tid] = 0.f;
+      if (a.epos_grad) {  // tile-gradient probe: row sums of the 32 features' gradient
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          float sum = v[j];
+#pragma unroll
+          for (int sh = 16; sh > 0; sh >>= 1) sum += __shfl_xor_sync(0xFFFFFFFFu, sum, sh);
+          if (lane == 0) atomicAdd(&spos[j], sum);
+        }
+        __syncthreads();
+        if (tid < 32) {
+          atomicAdd(&a.epos_grad[tid], spos[tid]);
+          spos[tid] = 0.f;
+        }
       }
     }
     first = false;
@@ -504,113 +579,6 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, 512);
-}
-
-// ---------------------------------------------------------------------------
-// Hash-grid encoding and its gradient.
-// ---------------------------------------------------------------------------
-struct NrcHash {
-  const __half* table;  // [16][T][2]
-  float* grad;          // [16][T][2]
-  int32_t log2T;
-  int32_t res[kNrcHashLevels];
-  float inv_extent;     // 1 / max grid edge
-};
-
-__device__ __forceinline__ uint32_t nrc_hash_index(const NrcHash& h, int l, int x, int y, int z) {
-  const uint32_t T = 1u << h.log2T;
-  const uint32_t r1 = (uint32_t)h.res[l] + 1u;
-  if ((uint64_t)r1 * r1 * r1 <= T) return (uint32_t)x + r1 * ((uint32_t)y + r1 * (uint32_t)z);
-  return ((uint32_t)x ^ ((uint32_t)y * 2654435761u) ^ ((uint32_t)z * 805459861u)) & (T - 1u);
-}
-
-// Probe centre (voxel units) of probe p of level L, scaled to [0, 1].
-__device__ __forceinline__ void nrc_probe_pos(const NrcLevel& L, int64_t p, float inv_extent, float* u) {
-  const int mx = (int)(p % L.M[0]);
-  const int my = (int)((p / L.M[0]) % L.M[1]);
-  const int mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
-  const float h = 0.5f * (float)L.spacing;
-  u[0] = ((float)mx * L.spacing + h) * inv_extent;
-  u[1] = ((float)my * L.spacing + h) * inv_extent;
-  u[2] = ((float)mz * L.spacing + h) * inv_extent;
-}
-
-// One thread per (probe, hash level) of every far level.
-__global__ void k_nrc_encode(const __grid_constant__ NrcArgs a, const __grid_constant__ NrcHash h,
-                             int64_t total_probes) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= total_probes * kNrcHashLevels) return;
-  const int l = (int)(i % kNrcHashLevels);
-  int64_t p = i / kNrcHashLevels;
-  int li = a.first;
-  while (li < a.nlev && p >= a.lv[li].P) p -= a.lv[li++].P;
-  if (li >= a.nlev) return;
-  const NrcLevel& L = a.lv[li];
-  float u[3];
-  nrc_probe_pos(L, p, h.inv_extent, u);
-  const float r = (float)h.res[l];
-  int c[3];
-  float f[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float s = u[k] * r;
-    c[k] = min((int)floorf(s), h.res[l] - 1);
-    f[k] = s - (float)c[k];
-  }
-  float e0 = 0.f, e1 = 0.f;
-  const uint32_t T = 1u << h.log2T;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-    const float w = (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) * (dz ? f[2] : 1.f - f[2]);
-    const uint32_t idx = nrc_hash_index(h, l, c[0] + dx, c[1] + dy, c[2] + dz);
-    const __half2 v = *reinterpret_cast<const __half2*>(h.table + ((size_t)l * T + idx) * 2);
-    const float2 fv = __half22float2(v);
-    e0 = fmaf(w, fv.x, e0);
-    e1 = fmaf(w, fv.y, e1);
-  }
-  float* out = const_cast<float*>(L.epos) + p * kNrcPosFeat + 2 * l;
-  out[0] = e0;
-  out[1] = e1;
-}
-
-struct NrcSample {
-  int32_t level;
-  int32_t probe;
-};
-
-// Scatter of the position-feature gradients of the step's training probes.
-__global__ void k_nrc_hash_grad(const __grid_constant__ NrcArgs a, const __grid_constant__ NrcHash h,
-                                const NrcSample* __restrict__ samples, int nsamples) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (int64_t)nsamples * kNrcHashLevels) return;
-  const int l = (int)(i % kNrcHashLevels);
-  const int s = (int)(i / kNrcHashLevels);
-  const NrcSample smp = samples[s];
-  const float g0 = a.epos_grad[(int64_t)s * kNrcPosFeat + 2 * l];
-  const float g1 = a.epos_grad[(int64_t)s * kNrcPosFeat + 2 * l + 1];
-  if (g0 == 0.f && g1 == 0.f) return;
-  float u[3];
-  nrc_probe_pos(a.lv[smp.level], smp.probe, h.inv_extent, u);
-  const float r = (float)h.res[l];
-  int c[3];
-  float f[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float sc = u[k] * r;
-    c[k] = min((int)floorf(sc), h.res[l] - 1);
-    f[k] = sc - (float)c[k];
-  }
-  const uint32_t T = 1u << h.log2T;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-    const float w = (dx ? f[0] : 1.f - f[0]) * (dy ? f[1] : 1.f - f[1]) * (dz ? f[2] : 1.f - f[2]);
-    const uint32_t idx = nrc_hash_index(h, l, c[0] + dx, c[1] + dy, c[2] + dz);
-    float* g = h.grad + ((size_t)l * T + idx) * 2;
-    atomicAdd(g, w * g0);
-    atomicAdd(g + 1, w * g1);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -713,8 +681,9 @@ __global__ void k_nrc_tile_error(const NrcTile* __restrict__ tiles, int64_t ntil
   if (r >= t.n) return;
   const float4 pr = *reinterpret_cast<const float4*>(pred + i * 4);
   const float4 y = *reinterpret_cast<const float4*>(target + i * 4);
-  const float R[4] = {fmaxf(pr.x / a.scale, 0.f), fmaxf(pr.y / a.scale, 0.f), fmaxf(pr.z / a.scale, 0.f),
-                      fminf(fmaxf(pr.w, 0.f), 1.f)};
+  const float po[4] = {pr.x, pr.y, pr.z, pr.w};
+  float R[4];
+  nrc_serve(po, a.scale, R);
   const float Y[4] = {y.x, y.y, y.z, y.w};
   float e = 0.f, s = 0.f;
 #pragma unroll
@@ -745,12 +714,33 @@ __global__ void k_nrc_flags(float* __restrict__ num, float* __restrict__ den, ui
   den[i] = 0.f;
 }
 
-// Fallback: plain (R, T) for every query of probes in flagged tiles.
+__device__ __forceinline__ int64_t nrc_cell(const NrcLevel& L, int64_t p, int shift, int TX, int TY) {
+  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const int h = L.spacing >> 1;
+  return ((int64_t)((mz * L.spacing + h) >> shift) * TY + ((my * L.spacing + h) >> shift)) * TX +
+         ((mx * L.spacing + h) >> shift);
+}
+
+// Probes of each far level that sit in fallback tiles.
+__global__ void k_nrc_count(const __grid_constant__ NrcArgs a, const uint8_t* __restrict__ flag, int shift, int TX,
+                            int TY, int64_t total_probes, unsigned* __restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total_probes) return;
+  int li = a.first;
+  int64_t p = i;
+  while (li < a.nlev && p >= a.lv[li].P) p -= a.lv[li++].P;
+  if (li >= a.nlev) return;
+  if (flag[nrc_cell(a.lv[li], p, shift, TX, TY)]) atomicAdd(&count[li], 1u);
+}
+
+// Fallback: plain (R, T) for every query of probes in flagged tiles of the
+// levels the network serves (served[level]).
 struct NrcFallbackArgs {
   LevelArgs lv[kMaxCascades];
   NrcArgs n;
   const uint8_t* flag;
   int tile_shift, TX, TY;
+  int32_t served[kMaxCascades];
   int64_t total;  // queries over all far levels
 };
 
@@ -760,15 +750,11 @@ __global__ void k_nrc_fallback(const __grid_constant__ NrcFallbackArgs f) {
   int li = f.n.first;
   int64_t q = i;
   while (li < f.n.nlev && q >= f.n.lv[li].P * f.n.lv[li].ndirs) q -= f.n.lv[li].P * f.n.lv[li++].ndirs;
-  if (li >= f.n.nlev) return;
+  if (li >= f.n.nlev || !f.served[li]) return;
   const NrcLevel& L = f.n.lv[li];
   const int d = (int)(q / L.P);
   const int64_t p = q - (int64_t)d * L.P;
-  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
-  const int h = L.spacing >> 1;
-  const int64_t cell = ((int64_t)((mz * L.spacing + h) >> f.tile_shift) * f.TY + ((my * L.spacing + h) >> f.tile_shift)) *
-                           f.TX + ((mx * L.spacing + h) >> f.tile_shift);
-  if (!f.flag[cell]) return;
+  if (!f.flag[nrc_cell(L, p, f.tile_shift, f.TX, f.TY)]) return;
   float rt[4];
   nrc_walk(f.lv[li], p, d, rt);
   const int64_t plane = (int64_t)L.ndirs * L.P;

@@ -1,8 +1,8 @@
 """NumPy restatement of the neural radiance cache's network, for the GPU tests.
 
-Mirrors radiancecascade_gb300/csrc/rc_nrc.cuh: the hash-grid encoding of the
-probe centre (FP16 table, FP32 trilinear weights), the 16 direction/cascade
-features, and the MLP with BF16 weights and activations and wide (here FP64)
+Mirrors radiancecascade_gb300/csrc/rc_nrc.cuh: the multiresolution hash
+encoding of (probe centre, direction texel, cascade) (FP16 table, one cell per
+level), the 16 direction/cascade features, and the MLP with BF16 weights and activations and wide (here FP64)
 accumulation, forward and backward.  Test infrastructure only.
 """
 import numpy as np
@@ -44,31 +44,27 @@ def resolutions(base, top):
     return [max(1, int(np.floor(base * g ** l + 1e-9))) for l in range(HASH_LEVELS)]
 
 
-def encode(table16, res, log2T, probe_xyz, spacing, extent):
-    """Position features (32) of probes at lattice indices probe_xyz [n, 3]."""
+def dir_resolutions():
+    return [max(1, int(np.floor(2.0 * 64.0 ** (l / (HASH_LEVELS - 1)) + 1e-9))) for l in range(HASH_LEVELS)]
+
+
+def encode(table16, res, dres, log2T, probe_xyz, spacing, extent, dirs, n, cascade):
+    """Hash features (32) of queries: probes at lattice indices probe_xyz [q, 3],
+    direction texels dirs [q] of an n x n octahedral map, cascade index."""
     T = 1 << log2T
     inv = np.float32(1.0) / np.float32(extent)
     u = ((probe_xyz.astype(np.float32) * np.float32(spacing) + np.float32(0.5 * spacing)) * inv).astype(np.float32)
+    du = ((dirs % n).astype(np.float32) + np.float32(0.5)) / np.float32(n)
+    dv = ((dirs // n).astype(np.float32) + np.float32(0.5)) / np.float32(n)
     out = np.zeros((len(u), 32), np.float32)
-    for l, r in enumerate(res):
-        s = (u * np.float32(r)).astype(np.float32)
-        c = np.minimum(np.floor(s).astype(np.int64), r - 1)
-        f = (s - c.astype(np.float32)).astype(np.float32)
-        acc = np.zeros((len(u), 2), np.float32)
-        for k in range(8):
-            d = np.array([k & 1, (k >> 1) & 1, k >> 2])
-            w = np.ones(len(u), np.float32)
-            for a in range(3):
-                w = (w * (f[:, a] if d[a] else np.float32(1) - f[:, a])).astype(np.float32)
-            x, y, z = (c + d).T.astype(np.uint64)
-            r1 = r + 1
-            if r1 ** 3 <= T:
-                idx = x + r1 * (y + r1 * z)
-            else:
-                idx = (x ^ ((y * 2654435761) & 0xFFFFFFFF) ^ ((z * 805459861) & 0xFFFFFFFF)) & (T - 1)
-            v = table16[l, idx.astype(np.int64)].astype(np.float32)
-            acc = (acc + w[:, None] * v).astype(np.float32)
-        out[:, 2 * l:2 * l + 2] = acc
+    m32 = 0xFFFFFFFF
+    for l, (r, q) in enumerate(zip(res, dres)):
+        c = [np.minimum((u[:, a] * np.float32(r)).astype(np.int64), r - 1).astype(np.uint64) for a in range(3)]
+        a_ = np.minimum((du * np.float32(q)).astype(np.int64), q - 1).astype(np.uint64)
+        b_ = np.minimum((dv * np.float32(q)).astype(np.int64), q - 1).astype(np.uint64)
+        h = (c[0] ^ ((c[1] * 2654435761) & m32) ^ ((c[2] * 805459861) & m32) ^ ((a_ * 0x85EBCA77) & m32)
+             ^ ((b_ * 0xC2B2AE3D) & m32) ^ ((cascade * 0x27D4EB2F) & m32))
+        out[:, 2 * l:2 * l + 2] = table16[l, (h & (T - 1)).astype(np.int64)].astype(np.float32)
     return out
 
 
@@ -96,7 +92,9 @@ def forward(W, b, x):
 
 
 def served(o, scale):
-    return np.concatenate([np.maximum(o[:, :3] / scale, 0.0), np.clip(o[:, 3:4], 0.0, 1.0)], 1)
+    """T = [o_3 >= 1/2]; R = 0 where T = 1, else max(o / scale, 0)."""
+    t = (o[:, 3:4] >= 0.5).astype(np.float64)
+    return np.concatenate([np.where(t > 0, 0.0, np.maximum(o[:, :3] / scale, 0.0)), t], 1)
 
 
 def backward(W, b, x, y, scale):
