@@ -125,7 +125,7 @@ def measured_peak_gbs():
 
 def profile_traffic_per_launch():
     """DRAM bytes per level-kernel launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "level_kernel_c256_ncu.md")
+    path = os.path.join(ROOT, "profiles", "frame_c256_launch_list.md")
     try:
         with open(path) as f:
             for line in f:
