@@ -470,22 +470,25 @@ def main():
     # recompose + one kernel per cascade + the shared walk of the narrow levels
     launches_per_step = 1 + params.num_cascades + 1
 
-    # ---- e2e: public API, host buffers, H2D of the frame's spheres, D2H of the fluence
+    # ---- e2e: public API, host buffers, H2D of the frame's spheres, D2H of every frame's
+    # fluence into pinned host memory (the read-back of frame f overlaps the solve of f+1)
     nflu = 3 * int(np.prod(eng.probes0))
-    host_out = torch.empty(nflu, dtype=torch.float32, pin_memory=True).numpy()
-    for _ in range(2):
+    host_out = [torch.empty(nflu, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+    for f in range(2):
         eng.set_spheres(sph)
         eng.solve()
-        eng.fluence(out=host_out)
+        eng.fluence_async(host_out[f & 1])
         R.advance_spheres(sph, 256, 1)
+    eng.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for f in range(args.steps):
         eng.set_spheres(sph)
         eng.solve()
-        eng.fluence(out=host_out)
+        eng.fluence_async(host_out[f & 1])
         R.advance_spheres(sph, 256, 1)
+    eng.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
         t = torch.tensor([e2e_s], device="cuda")

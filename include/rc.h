@@ -185,8 +185,16 @@ rc_status rc_get_fluence(rc_context* ctx, float* out, int64_t elems,
  * or binary16 according to params.precision. */
 rc_status rc_get_radiance(rc_context* ctx, int32_t level, void* out,
                           int64_t bytes, int32_t where);
-/* Device pointer of the context-owned fluence buffer (valid until destroy). */
+/* Device pointer of the fluence written by the last solve (context-owned,
+ * valid until destroy; once rc_get_fluence_async is in use, solves alternate
+ * between two buffers, so ask again after each solve). */
 rc_status rc_fluence_device_ptr(rc_context* ctx, const float** out);
+/* Starts copying the last solve's fluence into host memory `out` (pinned
+ * memory overlaps; pageable memory works but copies synchronously) on the
+ * context's copy stream and returns; the copy overlaps the next solve, which
+ * writes the other of two device fluence buffers.  `out` is complete after
+ * rc_synchronize. */
+rc_status rc_get_fluence_async(rc_context* ctx, float* out, int64_t elems);
 rc_status rc_radiance_device_ptr(rc_context* ctx, int32_t level,
                                  const void** out);
 /* The context's own stream (a cudaStream_t), for ordering consumer work

@@ -93,6 +93,7 @@ SIGNATURES = {
     "rc_get_stream": (_S, [_P, C.POINTER(C.c_void_p)]),
     "rc_profile_levels": (_S, [_P, C.c_int32, _P, C.c_int32]),
     "rc_solve_noalloc": (_S, [_P, _P, _P, _P, _P]),
+    "rc_get_fluence_async": (_S, [_P, _P, C.c_int64]),
     "rc_batch_create": (_S, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "rc_batch_destroy": (_S, [_P]),
     "rc_batch_scene_set": (_S, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int32]),

@@ -58,9 +58,16 @@ void release(rc_context* c) {
   cudaGetDevice(&prev);
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   nrc_release(c);
+  if (c->flu[1]) cudaFree(c->flu[1]);
+  for (int k = 0; k < 2; ++k) {
+    if (c->ev_solved[k]) cudaEventDestroy(c->ev_solved[k]);
+    if (c->ev_copied[k]) cudaEventDestroy(c->ev_copied[k]);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->fluence, c->d_sph, c->d_reg};
+  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -542,8 +549,9 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
   }
   if ((s = dev_alloc(&c->rad, rad_bytes, "cascade radiance")) != RC_OK) return fail(s);
   if (avg_bytes && (s = dev_alloc(&c->avg, avg_bytes, "child-averaged radiance")) != RC_OK) return fail(s);
-  if ((s = dev_alloc((void**)&c->fluence, (size_t)c->geom[0].probes() * 3 * sizeof(float), "fluence")) != RC_OK)
+  if ((s = dev_alloc((void**)&c->flu[0], (size_t)c->geom[0].probes() * 3 * sizeof(float), "fluence")) != RC_OK)
     return fail(s);
+  c->fluence = c->flu[0];
   if ((s = ensure_sphere_capacity(c, 64)) != RC_OK) return fail(s);
 
   for (int i = 0; i < c->nlev; ++i) {
@@ -715,6 +723,14 @@ rc_status rc_solve(rc_context* c, void* stream) {
     RC_CUDA(cudaEventRecord(c->ev_in, c->stream), "rc_solve: event");
     RC_CUDA(cudaStreamWaitEvent(s, c->ev_in, 0), "rc_solve: wait");
   }
+  if (c->flu[1]) {
+    // alternate fluence buffers; wait for a read-back still copying the one reused
+    const int b = c->flu_cur ^ 1;
+    if (c->copy_pending[b]) RC_CUDA(cudaStreamWaitEvent(s, c->ev_copied[b], 0), "rc_solve: wait");
+    c->flu_cur = b;
+    c->fluence = c->flu[b];
+    c->args[0].fluence = c->flu[b];
+  }
   rc_status st = enqueue_solve(c, s);
   if (st != RC_OK) return st;
   RC_CUDA(cudaGetLastError(), "rc_solve: launch");
@@ -729,6 +745,10 @@ rc_status rc_synchronize(rc_context* c) {
   if (check_ctx(c, "rc_synchronize") != RC_OK) return RC_ERR_INVALID_ARG;
   DeviceGuard g(c->device);
   RC_CUDA(cudaStreamSynchronize(c->stream), "rc_synchronize");
+  if (c->copy_stream) {
+    RC_CUDA(cudaStreamSynchronize(c->copy_stream), "rc_synchronize");
+    c->copy_pending[0] = c->copy_pending[1] = false;
+  }
   return check_device_error(c, "rc_synchronize");
 }
 
@@ -768,6 +788,33 @@ rc_status rc_get_radiance(rc_context* c, int32_t level, void* out, int64_t bytes
     return RC_ERR_INVALID_ARG;
   }
   return copy_out(c, out, static_cast<char*>(c->rad) + c->rad_off[level], need, where, "rc_get_radiance");
+}
+
+rc_status rc_get_fluence_async(rc_context* c, float* out, int64_t elems) {
+  if (check_ctx(c, "rc_get_fluence_async") != RC_OK) return RC_ERR_INVALID_ARG;
+  const int64_t need = 3 * c->geom[0].probes();
+  if (!out || elems != need) {
+    rcx::set_error("rc_get_fluence_async: need a host buffer of exactly %lld floats", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(c->device);
+  if (!c->flu[1]) {
+    rc_status s = dev_alloc((void**)&c->flu[1], (size_t)need * sizeof(float), "second fluence buffer");
+    if (s != RC_OK) return s;
+    RC_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking), "rc_get_fluence_async: stream");
+    for (int k = 0; k < 2; ++k) {
+      RC_CUDA(cudaEventCreateWithFlags(&c->ev_solved[k], cudaEventDisableTiming), "rc_get_fluence_async: event");
+      RC_CUDA(cudaEventCreateWithFlags(&c->ev_copied[k], cudaEventDisableTiming), "rc_get_fluence_async: event");
+    }
+  }
+  const int b = c->flu_cur;
+  RC_CUDA(cudaEventRecord(c->ev_solved[b], c->stream), "rc_get_fluence_async: event");
+  RC_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_solved[b], 0), "rc_get_fluence_async: wait");
+  RC_CUDA(cudaMemcpyAsync(out, c->flu[b], (size_t)need * sizeof(float), cudaMemcpyDeviceToHost, c->copy_stream),
+          "rc_get_fluence_async: copy");
+  RC_CUDA(cudaEventRecord(c->ev_copied[b], c->copy_stream), "rc_get_fluence_async: event");
+  c->copy_pending[b] = true;
+  return RC_OK;
 }
 
 rc_status rc_fluence_device_ptr(rc_context* c, const float** out) {

@@ -53,7 +53,15 @@ struct rc_context {
   size_t rad_off[rcx::kMaxCascades]{};  // bytes
   void* avg = nullptr;               // A_i for levels >= 1
   size_t avg_off[rcx::kMaxCascades]{};  // bytes
-  float* fluence = nullptr;
+  float* fluence = nullptr;          // written by the last solve
+  // asynchronous read-back (rc_get_fluence_async): two device fluence
+  // buffers used alternately, copies on their own stream
+  float* flu[2] = {nullptr, nullptr};
+  int flu_cur = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_solved[2] = {nullptr, nullptr};
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr};
+  bool copy_pending[2] = {false, false};
 
   // dynamic spheres
   rcx::QSphere* d_sph = nullptr;

@@ -199,6 +199,14 @@ class Engine:
         F.check(self._lib.rc_get_fluence(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
         return out.reshape(-1, 3)
 
+    def fluence_async(self, out: np.ndarray) -> None:
+        """Starts the read-back of the last solve's fluence into `out` (float32,
+        3 x probes; pinned memory overlaps the next solve); complete after
+        synchronize()."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous or out.size != 3 * int(np.prod(self.probes0)):
+            raise ValueError("out must be a contiguous float32 array of 3 x cascade-0 probes")
+        F.check(self._lib.rc_get_fluence_async(self.handle, F.ptr(out), out.size))
+
     def radiance(self, level: int) -> np.ndarray:
         info = self.levels[level]
         dt = np.float16 if self.params.precision == F.RC_PRECISION_FP16 else np.float32
