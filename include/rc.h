@@ -168,6 +168,19 @@ rc_status rc_scene_upload(rc_context* ctx, const rc_voxel* voxels,
  * boxes win). */
 rc_status rc_scene_set_boxes(rc_context* ctx, const rc_box* boxes,
                              int32_t n);
+/* Voxelises a triangle mesh into the static scene, replacing boxes or an
+ * earlier mesh (spheres are composed on top as usual).  positions: nverts x 3
+ * floats in grid units (voxel (x, y, z) covers [x, x+1) x ...), each within
+ * [-1024, 2048]; indices: ntris x 3; tri_material: ntris indices into
+ * materials (NULL: material 0 everywhere).  Positions are rounded to 1/256
+ * voxel and a voxel is set when a triangle touches its closed box (exact
+ * integer separating-axis test), so walls are watertight; where triangles
+ * overlap, the later triangle wins. */
+rc_status rc_scene_set_mesh(rc_context* ctx, const float* positions,
+                            int64_t nverts, const uint32_t* indices,
+                            int64_t ntris, const uint16_t* tri_material,
+                            const rc_voxel* materials, int32_t nmaterials);
+
 /* Dynamic emitters drawn over the base volume (later spheres win).  Only
  * the voxels under the previous and the new spheres are rewritten. */
 rc_status rc_scene_set_spheres(rc_context* ctx, const rc_sphere* spheres,
@@ -189,6 +202,9 @@ rc_status rc_get_radiance(rc_context* ctx, int32_t level, void* out,
  * valid until destroy; once rc_get_fluence_async is in use, solves alternate
  * between two buffers, so ask again after each solve). */
 rc_status rc_fluence_device_ptr(rc_context* ctx, const float** out);
+/* The composed scene volume (static scene + spheres), count = grid voxels. */
+rc_status rc_get_volume(rc_context* ctx, rc_voxel* out, int64_t count,
+                        int32_t where);
 /* Starts copying the last solve's fluence into host memory `out` (pinned
  * memory overlaps; pageable memory works but copies synchronously) on the
  * context's copy stream and returns; the copy overlaps the next solve, which

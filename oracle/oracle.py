@@ -56,6 +56,7 @@ def lib():
         L.rco_spheres_advance.argtypes = [P, C.c_int, P, C.c_int]
         L.rco_spheres_advance.restype = None
         L.rco_voxelise.argtypes = [P, P, C.c_int, P, C.c_int, P]
+        L.rco_voxelise_mesh.argtypes = [P, P, C.c_int64, P, C.c_int64, P, P, C.c_int, P]
         _lib = L
     return _lib
 
@@ -126,6 +127,20 @@ def generate(spec: SceneSpec, seed: int):
 def advance(spheres: np.ndarray, grid, frames: int):
     g = (C.c_int32 * 3)(*((grid,) * 3 if isinstance(grid, int) else grid))
     lib().rco_spheres_advance(_ptr(spheres), len(spheres), g, frames)
+
+
+def voxelise_mesh(grid, positions, indices, tri_material, materials):
+    """Triangle mesh (positions in grid units) -> rc_voxel volume, later triangles win."""
+    g3 = (grid,) * 3 if isinstance(grid, int) else tuple(grid)
+    out = np.zeros(g3[0] * g3[1] * g3[2], VOXEL_DT)
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    idx = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+    mats = np.ascontiguousarray(materials, VOXEL_DT)
+    tm = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint16)
+    g = (C.c_int32 * 3)(*g3)
+    lib().rco_voxelise_mesh(g, _ptr(pos), len(pos), _ptr(idx), len(idx), None if tm is None else _ptr(tm),
+                            _ptr(mats), len(mats), _ptr(out))
+    return out
 
 
 def voxelise(grid, boxes, spheres):

@@ -575,4 +575,84 @@ int rco_voxelise(const int32_t grid[3], const rc_box* boxes, int nb, const rc_sp
   return 0;
 }
 
+// Triangle mesh voxelisation.  Positions in grid units are rounded to 1/256
+// voxel; voxel (x, y, z) is the closed box [256x, 256x+256] x ... in those
+// units.  A voxel belongs to a triangle when no separating axis exists among
+// the box normals, the triangle normal and the nine cross products of the
+// triangle edges with the box normals (Akenine-Moeller 2001), with touching
+// counted as overlap.  Triangles in order, a later triangle overwrites.
+// Every quantity is an exact 64-bit integer.
+static bool separated(const int64_t q[3][3], const int64_t axis[3], int64_t half) {
+  int64_t pmin = 0, pmax = 0, radius = 0;
+  for (int k = 0; k < 3; ++k) {
+    const int64_t proj = axis[0] * q[k][0] + axis[1] * q[k][1] + axis[2] * q[k][2];
+    pmin = k ? std::min(pmin, proj) : proj;
+    pmax = k ? std::max(pmax, proj) : proj;
+  }
+  for (int c = 0; c < 3; ++c) radius += half * (axis[c] < 0 ? -axis[c] : axis[c]);
+  return pmin > radius || pmax < -radius;
+}
+
+int rco_voxelise_mesh(const int32_t grid[3], const float* positions, int64_t nverts, const uint32_t* indices,
+                      int64_t ntris, const uint16_t* tri_material, const rc_voxel* materials, int nmaterials,
+                      rc_voxel* out) {
+  const size_t G0 = grid[0], G1 = grid[1], G2 = grid[2];
+  std::memset(out, 0, G0 * G1 * G2 * sizeof(rc_voxel));
+  std::vector<int64_t> qv((size_t)nverts * 3);
+  for (int64_t i = 0; i < nverts * 3; ++i) qv[i] = std::llround((double)positions[i] * 256.0);
+  for (int64_t t = 0; t < ntris; ++t) {
+    int64_t tri[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) tri[k][c] = qv[(size_t)indices[3 * t + k] * 3 + c];
+    int lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) {
+      const int64_t mn = std::min(tri[0][c], std::min(tri[1][c], tri[2][c]));
+      const int64_t mx = std::max(tri[0][c], std::max(tri[1][c], tri[2][c]));
+      // voxels whose closed extent [256 x, 256 x + 256] meets [mn, mx]
+      const int64_t first = (int64_t)std::ceil((double)(mn - 256) / 256.0);
+      const int64_t last = (int64_t)std::floor((double)mx / 256.0);
+      lo[c] = (int)std::max<int64_t>(first, 0);
+      hi[c] = (int)std::min<int64_t>(last, grid[c] - 1);
+    }
+    int m = tri_material ? tri_material[t] : 0;
+    if (m >= nmaterials) m = nmaterials - 1;
+    const int64_t e[3][3] = {{tri[1][0] - tri[0][0], tri[1][1] - tri[0][1], tri[1][2] - tri[0][2]},
+                             {tri[2][0] - tri[1][0], tri[2][1] - tri[1][1], tri[2][2] - tri[1][2]},
+                             {tri[0][0] - tri[2][0], tri[0][1] - tri[2][1], tri[0][2] - tri[2][2]}};
+    std::vector<std::array<int64_t, 3>> axes;
+    for (int c = 0; c < 3; ++c) {
+      std::array<int64_t, 3> u = {0, 0, 0};
+      u[c] = 1;
+      axes.push_back(u);
+    }
+    axes.push_back({e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                    e[0][0] * e[1][1] - e[0][1] * e[1][0]});
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 3; ++c) {
+        // e_i x unit(c)
+        std::array<int64_t, 3> a = {0, 0, 0};
+        const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+        a[c1] = e[i][c2];
+        a[c2] = -e[i][c1];
+        axes.push_back(a);
+      }
+    for (int z = lo[2]; z <= hi[2]; ++z)
+      for (int y = lo[1]; y <= hi[1]; ++y)
+        for (int x = lo[0]; x <= hi[0]; ++x) {
+          const int64_t centre[3] = {256 * (int64_t)x + 128, 256 * (int64_t)y + 128, 256 * (int64_t)z + 128};
+          int64_t q[3][3];
+          for (int k = 0; k < 3; ++k)
+            for (int c = 0; c < 3; ++c) q[k][c] = tri[k][c] - centre[c];
+          bool hit = true;
+          for (const auto& ax : axes)
+            if (separated(q, ax.data(), 128)) {
+              hit = false;
+              break;
+            }
+          if (hit) out[((size_t)z * G1 + y) * G0 + x] = materials[m];
+        }
+  }
+  return 0;
+}
+
 }  // extern "C"

@@ -8,7 +8,8 @@ fallback.
 from ._ffi import lib as _load_lib, RCError, VOXEL_DT, BOX_DT, SPHERE_DT  # noqa: F401
 from .engine import (Engine, Batch, GiStage, GiState, make_params, level_info, scene_spec, generate_scene,  # noqa: F401
                      advance_spheres, voxelise_host, directions, solid_angles, WORKLOADS, workload_scene,
-                     batch_workload, BATCH_EDGES, BATCH_CASCADES,
+                     batch_workload, BATCH_EDGES, BATCH_CASCADES, load_obj, mesh_to_grid, mesh_materials,
+                     room_mesh,
                      frames)
 
 _load_lib()

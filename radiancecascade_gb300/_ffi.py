@@ -94,6 +94,8 @@ SIGNATURES = {
     "rc_profile_levels": (_S, [_P, C.c_int32, _P, C.c_int32]),
     "rc_solve_noalloc": (_S, [_P, _P, _P, _P, _P]),
     "rc_get_fluence_async": (_S, [_P, _P, C.c_int64]),
+    "rc_scene_set_mesh": (_S, [_P, _P, C.c_int64, _P, C.c_int64, _P, _P, C.c_int32]),
+    "rc_get_volume": (_S, [_P, _P, C.c_int64, C.c_int32]),
     "rc_batch_create": (_S, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "rc_batch_destroy": (_S, [_P]),
     "rc_batch_scene_set": (_S, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int32]),

@@ -19,6 +19,7 @@
 #include "rc_ctx.h"
 #include "rc_level0.cuh"
 #include "rc_batch.cuh"
+#include "rc_mesh.cuh"
 
 using namespace rcx;
 
@@ -683,6 +684,86 @@ rc_status rc_scene_set_boxes(rc_context* c, const rc_box* boxes, int32_t n) {
   return RC_OK;
 }
 
+rc_status rc_scene_set_mesh(rc_context* c, const float* positions, int64_t nverts, const uint32_t* indices,
+                            int64_t ntris, const uint16_t* tri_material, const rc_voxel* materials,
+                            int32_t nmaterials) {
+  if (check_ctx(c, "rc_scene_set_mesh") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (nverts < 0 || ntris < 0 || nverts > (1 << 26) || ntris > (1 << 26) || (nverts && !positions) ||
+      (ntris && !indices) || nmaterials < 1 || !materials) {
+    rcx::set_error("rc_scene_set_mesh: need vertex and index arrays, at most 2^26 of each, and >= 1 material");
+    return RC_ERR_INVALID_ARG;
+  }
+  std::vector<int32_t> q((size_t)nverts * 3);
+  for (int64_t i = 0; i < nverts * 3; ++i) {
+    const double v = (double)positions[i] * 256.0;
+    if (!(v >= -262144.0 && v <= 524288.0)) {
+      rcx::set_error("rc_scene_set_mesh: vertex %lld lies outside [-1024, 2048] voxels", (long long)(i / 3));
+      return RC_ERR_INVALID_ARG;
+    }
+    q[i] = (int32_t)llround(v);
+  }
+  for (int64_t i = 0; i < ntris * 3; ++i)
+    if (indices[i] >= (uint64_t)nverts) {
+      rcx::set_error("rc_scene_set_mesh: triangle %lld indexes vertex %u of %lld", (long long)(i / 3), indices[i],
+                     (long long)nverts);
+      return RC_ERR_INVALID_ARG;
+    }
+  if (tri_material)
+    for (int64_t t = 0; t < ntris; ++t)
+      if (tri_material[t] >= nmaterials) {
+        rcx::set_error("rc_scene_set_mesh: triangle %lld uses material %u of %d", (long long)t, tri_material[t],
+                       nmaterials);
+        return RC_ERR_INVALID_ARG;
+      }
+  DeviceGuard g(c->device);
+  const int64_t nvox = (int64_t)c->p.grid[0] * c->p.grid[1] * c->p.grid[2];
+  int32_t* d_v = nullptr;
+  uint32_t *d_i = nullptr, *d_owner = nullptr;
+  uint16_t* d_m = nullptr;
+  rc_voxel* d_mat = nullptr;
+  auto done = [&](rc_status st) {
+    void* bufs[] = {d_v, d_i, d_owner, d_m, d_mat};
+    for (void* b : bufs)
+      if (b) cudaFree(b);
+    return st;
+  };
+  rc_status s;
+  if ((s = dev_alloc((void**)&d_v, std::max<size_t>(1, q.size()) * 4, "mesh vertices")) != RC_OK) return done(s);
+  if ((s = dev_alloc((void**)&d_i, std::max<int64_t>(1, ntris * 3) * 4, "mesh indices")) != RC_OK) return done(s);
+  if ((s = dev_alloc((void**)&d_owner, nvox * 4, "voxel owners")) != RC_OK) return done(s);
+  if ((s = dev_alloc((void**)&d_mat, (size_t)nmaterials * sizeof(rc_voxel), "mesh materials")) != RC_OK)
+    return done(s);
+  if (tri_material && (s = dev_alloc((void**)&d_m, std::max<int64_t>(1, ntris) * 2, "triangle materials")) != RC_OK)
+    return done(s);
+  cudaError_t e = cudaSuccess;
+  if (nverts) e = cudaMemcpy(d_v, q.data(), q.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ntris) e = cudaMemcpy(d_i, indices, (size_t)ntris * 12, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && d_m) e = cudaMemcpy(d_m, tri_material, (size_t)ntris * 2, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_mat, materials, (size_t)nmaterials * sizeof(rc_voxel), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_owner, 0, nvox * 4, c->stream);
+  if (e != cudaSuccess) return done(cuda_fail(e, "rc_scene_set_mesh: upload"));
+  MeshArgs a;
+  a.verts = d_v;
+  a.indices = d_i;
+  a.ntris = ntris;
+  a.owner = d_owner;
+  for (int k = 0; k < 3; ++k) a.G[k] = c->p.grid[k];
+  a.pad = 0;
+  if (ntris) {
+    const int64_t blocks = std::min<int64_t>((ntris * 32 + 255) / 256, 152 * 16);
+    k_mesh_owner<<<(unsigned)blocks, 256, 0, c->stream>>>(a);
+  }
+  k_mesh_materials<<<(unsigned)std::min<int64_t>((nvox + 255) / 256, 152 * 32), 256, 0, c->stream>>>(
+      d_owner, d_m, d_mat, nmaterials, c->base, nvox);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return done(cuda_fail(e, "rc_scene_set_mesh: voxelise"));
+  c->have_base = true;
+  if ((s = recompose(c, nullptr, 0)) != RC_OK) return done(s);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_scene_set_mesh: sync");
+  return done(RC_OK);
+}
+
 rc_status rc_scene_set_spheres(rc_context* c, const rc_sphere* spheres, int32_t n) {
   if (check_ctx(c, "rc_scene_set_spheres") != RC_OK) return RC_ERR_INVALID_ARG;
   if (n < 0 || (n > 0 && !spheres) || n > 65536) {
@@ -788,6 +869,20 @@ rc_status rc_get_radiance(rc_context* c, int32_t level, void* out, int64_t bytes
     return RC_ERR_INVALID_ARG;
   }
   return copy_out(c, out, static_cast<char*>(c->rad) + c->rad_off[level], need, where, "rc_get_radiance");
+}
+
+rc_status rc_get_volume(rc_context* c, rc_voxel* out, int64_t count, int32_t where) {
+  if (check_ctx(c, "rc_get_volume") != RC_OK) return RC_ERR_INVALID_ARG;
+  const int64_t need = (int64_t)c->p.grid[0] * c->p.grid[1] * c->p.grid[2];
+  if (!out || count != need) {
+    rcx::set_error("rc_get_volume: need a buffer of exactly %lld voxels", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!c->have_base) {
+    rcx::set_error("rc_get_volume: no scene uploaded");
+    return RC_ERR_STATE;
+  }
+  return copy_out(c, out, c->vol, (size_t)need * sizeof(rc_voxel), where, "rc_get_volume");
 }
 
 rc_status rc_get_fluence_async(rc_context* c, float* out, int64_t elems) {

@@ -10,6 +10,7 @@ the library's status and message instead of panicking.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from typing import Optional, Sequence
 
@@ -93,6 +94,161 @@ WORKLOADS = {
     "c256": dict(grid=256, cascades=6, boxes=400, edge=(4, 48), spheres=32, radius=(2.0, 8.0),
                  emission=(1.0, 50.0), seed=1002),
 }
+
+
+# ---- triangle meshes ----------------------------------------------------------
+def load_obj(path: str) -> dict:
+    """Wavefront OBJ (+ its MTL library) as the reference renderer loads it
+    (src/primitives.rs:104-175 through tobj with triangulate + single_index):
+    polygons fan-triangulated, triangle winding reversed (src/primitives.rs:
+    369-376), per-triangle material, and the light position -- the centroid of
+    the positions of the first object whose material is named "Light"
+    (src/renderer.rs:176, src/primitives.rs:133-155), or None.
+    -> dict(positions [n,3] f32, indices [m,3] u32, tri_material [m] u16,
+            materials [{name, Ka, Kd, Ks, Ke, Ns}], light)"""
+    base = os.path.dirname(path)
+    verts, tris, tri_mat, objects = [], [], [], []
+    mat_index, materials = {}, []
+    cur_mat = -1
+
+    def material_id(name):
+        if name not in mat_index:
+            mat_index[name] = len(materials)
+            materials.append({"name": name, "Ka": None, "Kd": None, "Ks": None, "Ke": None, "Ns": None})
+        return mat_index[name]
+
+    def load_mtl(fn):
+        cur = None
+        try:
+            with open(os.path.join(base, fn), errors="replace") as f:
+                for line in f:
+                    t = line.split()
+                    if not t:
+                        continue
+                    if t[0] == "newmtl":
+                        cur = materials[material_id(" ".join(t[1:]))]
+                    elif cur is not None and t[0] in ("Ka", "Kd", "Ks", "Ke") and len(t) >= 4:
+                        cur[t[0]] = [float(x) for x in t[1:4]]
+                    elif cur is not None and t[0] == "Ns":
+                        cur["Ns"] = float(t[1])
+        except OSError:
+            pass
+
+    obj_start = 0
+    with open(path, errors="replace") as f:
+        for line in f:
+            t = line.split()
+            if not t:
+                continue
+            if t[0] == "v":
+                verts.append([float(x) for x in t[1:4]])
+            elif t[0] == "mtllib":
+                load_mtl(" ".join(t[1:]))
+            elif t[0] == "usemtl":
+                cur_mat = material_id(" ".join(t[1:]))
+            elif t[0] in ("o", "g"):
+                objects.append((obj_start, len(tris)))
+                obj_start = len(tris)
+            elif t[0] == "f":
+                ids = []
+                for v in t[1:]:
+                    k = int(v.split("/")[0])
+                    ids.append(k - 1 if k > 0 else len(verts) + k)
+                for i in range(1, len(ids) - 1):
+                    tris.append([ids[i + 1], ids[i], ids[0]])  # fan, winding reversed
+                    tri_mat.append(max(cur_mat, 0))
+    objects.append((obj_start, len(tris)))
+    positions = np.asarray(verts, np.float32).reshape(-1, 3)
+    indices = np.asarray(tris, np.uint32).reshape(-1, 3)
+    tri_material = np.asarray(tri_mat, np.uint16)
+    light = None
+    for a, b in objects:
+        if b > a and materials and materials[tri_material[a]]["name"] == "Light":
+            used = np.unique(indices[a:b])
+            light = positions[used].mean(0)
+            break
+    if not materials:
+        materials.append({"name": "default", "Ka": None, "Kd": None, "Ks": None, "Ke": None, "Ns": None})
+    return dict(positions=positions, indices=indices, tri_material=tri_material, materials=materials, light=light)
+
+
+def mesh_to_grid(positions: np.ndarray, grid, margin: float = 1.0) -> np.ndarray:
+    """Uniform scale + offset placing the mesh's bounding box inside the grid."""
+    g = np.asarray((grid,) * 3 if isinstance(grid, int) else grid, np.float64)
+    p = np.asarray(positions, np.float64)
+    lo, hi = p.min(0), p.max(0)
+    scale = float(np.min((g - 2 * margin) / np.maximum(hi - lo, 1e-12)))
+    return ((p - (lo + hi) / 2) * scale + g / 2).astype(np.float32)
+
+
+def mesh_materials(materials, emission_scale: float = 1.0, light_emission=(10.0, 10.0, 10.0)) -> np.ndarray:
+    """rc_voxel per material: albedo from Kd, emission from Ke (times
+    emission_scale), and `light_emission` for a material named "Light"."""
+    out = np.zeros(len(materials), VOXEL_DT)
+    for i, m in enumerate(materials):
+        kd = m["Kd"] if m["Kd"] is not None else [0.8, 0.8, 0.8]
+        ke = m["Ke"] if m["Ke"] is not None else [0.0, 0.0, 0.0]
+        if m["name"] == "Light":
+            ke = list(light_emission)
+            emission_scale_i = 1.0
+        else:
+            emission_scale_i = emission_scale
+        a = [min(31, max(0, int(round(float(c) * 31)))) for c in kd]
+        out[i]["albedo_occ"] = 0x8000 | (a[0] << 10) | (a[1] << 5) | a[2]
+        out[i]["emission"] = [int(np.float16(float(c) * emission_scale_i).view(np.uint16)) for c in ke]
+    return out
+
+
+def room_mesh(grid: int, boxes: int = 6, seed: int = 7):
+    """Procedural test mesh in grid units: a closed room (6 walls, inward),
+    axis-aligned blocks and a tessellated sphere (material 2, emissive),
+    -> positions, indices, tri_material, materials (3 rc_voxels)."""
+    rng = np.random.default_rng(seed)
+    P, I, M = [], [], []
+
+    def quad(a, b, c, d, m):
+        k = sum(len(x) for x in P)
+        P.append(np.array([a, b, c, d], np.float32))
+        I.extend([[k, k + 1, k + 2], [k, k + 2, k + 3]])
+        M.extend([m, m])
+
+    def block(lo, hi, m):
+        x0, y0, z0 = lo
+        x1, y1, z1 = hi
+        quad((x0, y0, z0), (x1, y0, z0), (x1, y1, z0), (x0, y1, z0), m)
+        quad((x0, y0, z1), (x0, y1, z1), (x1, y1, z1), (x1, y0, z1), m)
+        quad((x0, y0, z0), (x0, y1, z0), (x0, y1, z1), (x0, y0, z1), m)
+        quad((x1, y0, z0), (x1, y0, z1), (x1, y1, z1), (x1, y1, z0), m)
+        quad((x0, y0, z0), (x0, y0, z1), (x1, y0, z1), (x1, y0, z0), m)
+        quad((x0, y1, z0), (x1, y1, z0), (x1, y1, z1), (x0, y1, z1), m)
+
+    e = grid - 0.5
+    block((0.5, 0.5, 0.5), (e, e, e), 0)
+    for _ in range(boxes):
+        lo = rng.uniform(2, grid - 10, 3)
+        block(tuple(lo), tuple(lo + rng.uniform(2, grid / 4, 3)), 1)
+    # UV sphere
+    c = rng.uniform(grid * 0.3, grid * 0.7, 3)
+    r = grid * 0.08
+    nu, nv = 16, 8
+    k0 = sum(len(x) for x in P)
+    sp = []
+    for j in range(nv + 1):
+        th = np.pi * j / nv
+        for i in range(nu):
+            ph = 2 * np.pi * i / nu
+            sp.append(c + r * np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)]))
+    P.append(np.asarray(sp, np.float32))
+    for j in range(nv):
+        for i in range(nu):
+            a, b = k0 + j * nu + i, k0 + j * nu + (i + 1) % nu
+            I.extend([[a, b + nu, b], [a, a + nu, b + nu]])
+            M.extend([2, 2])
+    mats = np.zeros(3, VOXEL_DT)
+    mats["albedo_occ"] = [0x8000 | (20 << 10) | (20 << 5) | 20, 0x8000 | (25 << 10) | (12 << 5) | 8,
+                          0x8000 | (31 << 10) | (31 << 5) | 31]
+    mats[2]["emission"] = [int(np.float16(v).view(np.uint16)) for v in (12.0, 9.0, 4.0)]
+    return (np.concatenate(P).astype(np.float32), np.asarray(I, np.uint32), np.asarray(M, np.uint16), mats)
 
 
 # Batched workload: `count` cubic scenes, scene k seeded 2000 + k, edge drawn
@@ -180,6 +336,16 @@ class Engine:
         b = np.ascontiguousarray(boxes, dtype=BOX_DT)
         F.check(self._lib.rc_scene_set_boxes(self.handle, F.ptr(b), len(b)))
 
+    def set_mesh(self, positions: np.ndarray, indices: np.ndarray, materials: np.ndarray,
+                 tri_material: Optional[np.ndarray] = None) -> None:
+        """Voxelise a triangle mesh (positions in grid units) as the static scene."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1, 3)
+        mats = np.ascontiguousarray(materials, VOXEL_DT).reshape(-1)
+        tm = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint16)
+        F.check(self._lib.rc_scene_set_mesh(self.handle, F.ptr(pos), len(pos), F.ptr(idx), len(idx),
+                                            None if tm is None else F.ptr(tm), F.ptr(mats), len(mats)))
+
     def set_spheres(self, spheres: np.ndarray) -> None:
         s = np.ascontiguousarray(spheres, dtype=SPHERE_DT)
         F.check(self._lib.rc_scene_set_spheres(self.handle, F.ptr(s), len(s)))
@@ -198,6 +364,13 @@ class Engine:
             out = np.empty(n, np.float32)
         F.check(self._lib.rc_get_fluence(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
         return out.reshape(-1, 3)
+
+    def volume(self) -> np.ndarray:
+        """The composed scene volume (rc_voxel per voxel, x fastest)."""
+        g = self.params.grid
+        out = np.zeros(g[0] * g[1] * g[2], VOXEL_DT)
+        F.check(self._lib.rc_get_volume(self.handle, F.ptr(out), out.size, F.RC_MEM_HOST))
+        return out
 
     def fluence_async(self, out: np.ndarray) -> None:
         """Starts the read-back of the last solve's fluence into `out` (float32,
