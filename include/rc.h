@@ -265,6 +265,53 @@ rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out);
 rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best,
                         float* best_ms);
 
+/* ---- headless raster + Blinn-Phong shading --------------------------- */
+/* The reference renderer's forward pass (src/shader.wgsl:30-43, 76-100;
+ * pipeline state src/renderer.rs:330-358) for one triangle list into an RGBA
+ * float image, plus an optional global-illumination term from the context's
+ * last fluence: gi_scale / (4 pi) x fluence at the fragment (trilinear
+ * between cascade-0 probes) joins the light colour.  gi_scale = 0 is the
+ * reference shading exactly. */
+typedef struct rc_shade_material {
+  float ambient[4];   /* rgb, w = 1 when the material defines it (0: absent) */
+  float diffuse[4];
+  float specular[4];
+  float shininess;
+  uint32_t enable_bit;      /* bit 0 colour texture, bit 1 normal map        */
+  int32_t color_texture;    /* index into the texture list (when bit 0)     */
+  int32_t normal_texture;   /* index into the texture list (when bit 1)     */
+} rc_shade_material;
+
+typedef struct rc_texture {
+  const uint8_t* rgba;  /* host RGBA8 rows, width x height                 */
+  int32_t width, height;
+  int32_t srgb;         /* 1: colour texture (sRGB-encoded), 0: normal map */
+  int32_t pad;
+} rc_texture;
+
+typedef struct rc_shade_view {
+  float view_proj[16];     /* column-major: clip = view_proj * (p, 1)      */
+  float eye[3];            /* camera position (view_position)              */
+  float light[3];          /* point light position                         */
+  int32_t width, height;   /* image size in pixels                         */
+  float world_to_grid[12]; /* grid = A p + b, row-major 3 x 4 (GI lookup)   */
+  float gi_scale;          /* 0: no GI term                                */
+  int32_t pad;
+} rc_shade_view;
+
+/* vertices: nverts x 17 floats (position, colour, normal, tangent,
+ * bitangent, uv -- src/renderer.rs:370-410); indices: ntris x 3;
+ * tri_material: ntris indices (NULL: material 0).  Pixels no triangle
+ * covers are (0, 0, 0, 1).  out: width x height x 4 floats, row 0 at the
+ * top, host or device (where). */
+rc_status rc_shade(rc_context* ctx, const rc_shade_view* view,
+                   const float* vertices, int64_t nverts,
+                   const uint32_t* indices, int64_t ntris,
+                   const uint16_t* tri_material,
+                   const rc_shade_material* materials, int32_t nmaterials,
+                   const rc_texture* textures, int32_t ntextures,
+                   float* out, int32_t where);
+
 /* ---- neural radiance cache ------------------------------------------ */
 /* With the cache enabled, rc_solve serves the far cascades (first_level and
  * up) from a small network instead of walking their intervals: it predicts

@@ -57,6 +57,7 @@ def lib():
         L.rco_spheres_advance.restype = None
         L.rco_voxelise.argtypes = [P, P, C.c_int, P, C.c_int, P]
         L.rco_voxelise_mesh.argtypes = [P, P, C.c_int64, P, C.c_int64, P, P, C.c_int, P]
+        L.rco_shade.argtypes = [P, P, C.c_int64, P, C.c_int64, P, P, P, C.c_int, P, P, C.c_int, P]
         _lib = L
     return _lib
 
@@ -140,6 +141,21 @@ def voxelise_mesh(grid, positions, indices, tri_material, materials):
     g = (C.c_int32 * 3)(*g3)
     lib().rco_voxelise_mesh(g, _ptr(pos), len(pos), _ptr(idx), len(idx), None if tm is None else _ptr(tm),
                             _ptr(mats), len(mats), _ptr(out))
+    return out
+
+
+def shade(view, vertices, indices, tri_material, materials, textures, fluence=None, probes=(1, 1, 1), spacing=2):
+    """CPU restatement of the shading pass -> (H, W, 4) float32 image.  view,
+    materials, textures: the ctypes structures of the C ABI."""
+    out = np.zeros((view.height, view.width, 4), np.float32)
+    v = np.ascontiguousarray(vertices, np.float32)
+    i = np.ascontiguousarray(indices, np.uint32)
+    tm = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint16)
+    fl = None if fluence is None else np.ascontiguousarray(fluence, np.float32)
+    pr = (C.c_int32 * 3)(*probes)
+    lib().rco_shade(C.byref(view), _ptr(v), len(v), _ptr(i), len(i), None if tm is None else _ptr(tm),
+                    materials, textures, len(textures) if textures else 0,
+                    None if fl is None else _ptr(fl), pr, spacing, _ptr(out))
     return out
 
 

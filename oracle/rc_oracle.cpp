@@ -655,4 +655,217 @@ int rco_voxelise_mesh(const int32_t grid[3], const float* positions, int64_t nve
   return 0;
 }
 
+// Headless forward pass of the reference renderer (src/shader.wgsl:30-43,
+// 76-100; src/renderer.rs:330-358): homogeneous rasterisation, depth Less,
+// nearest then earlier triangle, Blinn-Phong fragment shading, optional
+// fluence term (gi_scale / 4 pi x trilinear fluence between cascade-0
+// probes).  FP32 throughout, written independently of the product.
+namespace {
+struct Tex {
+  const uint8_t* p;
+  int w, h, srgb;
+};
+float s2l(float c) { return c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f); }
+void texel(const Tex& t, int x, int y, float* o) {
+  const uint8_t* q = t.p + ((size_t)y * t.w + x) * 4;
+  for (int k = 0; k < 4; ++k) o[k] = q[k] / 255.f;
+  if (t.srgb)
+    for (int k = 0; k < 3; ++k) o[k] = s2l(o[k]);
+}
+float mirror(float u) {
+  float f = u - 2.f * std::floor(u * 0.5f);
+  return f > 1.f ? 2.f - f : f;
+}
+void sample(const Tex& t, float u, float v, bool linear, float* o) {
+  const float mu = mirror(u) * t.w, mv = mirror(v) * t.h;
+  auto cx = [&](int x) { return std::min(std::max(x, 0), t.w - 1); };
+  auto cy = [&](int y) { return std::min(std::max(y, 0), t.h - 1); };
+  if (!linear) {
+    texel(t, cx((int)std::floor(mu)), cy((int)std::floor(mv)), o);
+    return;
+  }
+  const float fx = mu - 0.5f, fy = mv - 0.5f;
+  const int xi = (int)std::floor(fx), yi = (int)std::floor(fy);
+  const float ax = fx - xi, ay = fy - yi;
+  float a[4], b[4], c[4], d[4];
+  texel(t, cx(xi), cy(yi), a);
+  texel(t, cx(xi + 1), cy(yi), b);
+  texel(t, cx(xi), cy(yi + 1), c);
+  texel(t, cx(xi + 1), cy(yi + 1), d);
+  for (int k = 0; k < 4; ++k) o[k] = (a[k] * (1 - ax) + b[k] * ax) * (1 - ay) + (c[k] * (1 - ax) + d[k] * ax) * ay;
+}
+void norm(float* v) {
+  const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int k = 0; k < 3; ++k) v[k] /= l;
+}
+struct TriSetup {
+  float clip[3][4];
+  float inv[3][3];
+  bool ok;
+};
+TriSetup setup_tri(const float* vp, const float* verts, const uint32_t* idx, int64_t t) {
+  TriSetup s{};
+  for (int k = 0; k < 3; ++k) {
+    const float* p = verts + (size_t)idx[3 * t + k] * 17;
+    for (int r = 0; r < 4; ++r) s.clip[k][r] = vp[r] * p[0] + vp[4 + r] * p[1] + vp[8 + r] * p[2] + vp[12 + r];
+  }
+  // M = rows (x, y, w) of the three vertices as columns; inverse via the adjugate
+  const float m[3][3] = {{s.clip[0][0], s.clip[1][0], s.clip[2][0]},
+                         {s.clip[0][1], s.clip[1][1], s.clip[2][1]},
+                         {s.clip[0][3], s.clip[1][3], s.clip[2][3]}};
+  float adj[3][3];
+  adj[0][0] = m[1][1] * m[2][2] - m[1][2] * m[2][1];
+  adj[0][1] = m[0][2] * m[2][1] - m[0][1] * m[2][2];
+  adj[0][2] = m[0][1] * m[1][2] - m[0][2] * m[1][1];
+  adj[1][0] = m[1][2] * m[2][0] - m[1][0] * m[2][2];
+  adj[1][1] = m[0][0] * m[2][2] - m[0][2] * m[2][0];
+  adj[1][2] = m[0][2] * m[1][0] - m[0][0] * m[1][2];
+  adj[2][0] = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+  adj[2][1] = m[0][1] * m[2][0] - m[0][0] * m[2][1];
+  adj[2][2] = m[0][0] * m[1][1] - m[0][1] * m[1][0];
+  const float det = m[0][0] * adj[0][0] + m[0][1] * adj[1][0] + m[0][2] * adj[2][0];
+  s.ok = std::fabs(det) > 1e-30f;
+  if (s.ok)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) s.inv[i][j] = adj[i][j] * (1.f / det);
+  return s;
+}
+void bary(const TriSetup& s, float px, float py, float* g) {
+  for (int k = 0; k < 3; ++k) g[k] = s.inv[k][0] * px + s.inv[k][1] * py + s.inv[k][2];
+}
+void attrs(const TriSetup& s, const float* verts, const uint32_t* idx, int64_t t, float px, float py, float* at) {
+  float g[3];
+  bary(s, px, py, g);
+  const float w = 1.f / (g[0] + g[1] + g[2]);
+  for (int j = 0; j < 17; ++j) at[j] = 0.f;
+  for (int k = 0; k < 3; ++k) {
+    const float* v = verts + (size_t)idx[3 * t + k] * 17;
+    const float b = g[k] * w;
+    for (int j = 0; j < 17; ++j) at[j] += b * v[j];
+  }
+}
+}  // namespace
+
+int rco_shade(const rc_shade_view* view, const float* verts, int64_t nverts, const uint32_t* idx, int64_t ntris,
+              const uint16_t* tmat, const rc_shade_material* mats, const rc_texture* textures, int ntex,
+              const float* fluence, const int32_t probes[3], int spacing, float* out) {
+  (void)nverts;
+  const int W = view->width, H = view->height;
+  std::vector<Tex> tex;
+  for (int k = 0; k < ntex; ++k) tex.push_back(Tex{textures[k].rgba, textures[k].width, textures[k].height, textures[k].srgb});
+  std::vector<uint64_t> zb((size_t)W * H, ~0ull);
+  std::vector<TriSetup> su((size_t)ntris);
+  for (int64_t t = 0; t < ntris; ++t) su[t] = setup_tri(view->view_proj, verts, idx, t);
+  for (int64_t t = 0; t < ntris; ++t) {
+    if (!su[t].ok) continue;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        const float px = (2.f * ((float)x + 0.5f)) / (float)W - 1.f;
+        const float py = 1.f - (2.f * ((float)y + 0.5f)) / (float)H;
+        float g[3];
+        bary(su[t], px, py, g);
+        if (!(g[0] >= 0.f && g[1] >= 0.f && g[2] >= 0.f) || g[0] + g[1] + g[2] <= 0.f) continue;
+        const float z = g[0] * su[t].clip[0][2] + g[1] * su[t].clip[1][2] + g[2] * su[t].clip[2][2];
+        if (!(z >= 0.f && z < 1.f)) continue;
+        uint32_t zb32;
+        std::memcpy(&zb32, &z, 4);
+        const uint64_t key = ((uint64_t)zb32 << 32) | (uint64_t)t;
+        uint64_t& cur = zb[(size_t)y * W + x];
+        if (key < cur) cur = key;
+      }
+  }
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float* o = out + ((size_t)y * W + x) * 4;
+      o[0] = o[1] = o[2] = 0.f;
+      o[3] = 1.f;
+      const uint64_t key = zb[(size_t)y * W + x];
+      if (key == ~0ull) continue;
+      const int64_t t = (int64_t)(key & 0xFFFFFFFFull);
+      const float px = (2.f * ((float)x + 0.5f)) / (float)W - 1.f;
+      const float py = 1.f - (2.f * ((float)y + 0.5f)) / (float)H;
+      float at[17], ax[17], ay[17];
+      attrs(su[t], verts, idx, t, px, py, at);
+      const rc_shade_material& m = mats[tmat ? tmat[t] : 0];
+      const uint32_t eb = m.enable_bit;
+      float du[2] = {0, 0}, dv[2] = {0, 0};
+      if (eb & 3u) {
+        attrs(su[t], verts, idx, t, px + 2.f / W, py, ax);
+        attrs(su[t], verts, idx, t, px, py - 2.f / H, ay);
+        du[0] = ax[15] - at[15];
+        dv[0] = ax[16] - at[16];
+        du[1] = ay[15] - at[15];
+        dv[1] = ay[16] - at[16];
+      }
+      auto mag = [&](const Tex& tt) {
+        const float x2 = du[0] * tt.w * du[0] * tt.w + dv[0] * tt.h * dv[0] * tt.h;
+        const float y2 = du[1] * tt.w * du[1] * tt.w + dv[1] * tt.h * dv[1] * tt.h;
+        return std::max(x2, y2) <= 1.f;
+      };
+      const float u = at[15], v = 1.f - at[16];
+      float col[3] = {at[3], at[4], at[5]};
+      if (eb & 1u) {
+        float s4[4];
+        sample(tex[m.color_texture], u, v, mag(tex[m.color_texture]), s4);
+        for (int k = 0; k < 3; ++k) col[k] = s4[k];
+      }
+      float lc[3];
+      for (int k = 0; k < 3; ++k) lc[k] = m.ambient[k] * 0.05f * m.ambient[3];
+      float n[3] = {at[6], at[7], at[8]};
+      if (eb & 2u) {
+        float s4[4];
+        sample(tex[m.normal_texture], u, v, mag(tex[m.normal_texture]), s4);
+        float tg[3] = {at[9], at[10], at[11]}, bt[3] = {at[12], at[13], at[14]};
+        norm(tg);
+        norm(bt);
+        const float cf[3] = {s4[0] * 2.f - 1.f, s4[1] * 2.f - 1.f, s4[2] * 2.f - 1.f};
+        for (int k = 0; k < 3; ++k) n[k] = cf[0] * tg[k] + cf[1] * bt[k] + cf[2] * at[6 + k];
+      }
+      norm(n);
+      float vd[3] = {view->eye[0] - at[0], view->eye[1] - at[1], view->eye[2] - at[2]};
+      norm(vd);
+      const float ndv = vd[0] * n[0] + vd[1] * n[1] + vd[2] * n[2];
+      if (ndv < 0.f)
+        for (int k = 0; k < 3; ++k) n[k] = -n[k];
+      float ld[3] = {view->light[0] - at[0], view->light[1] - at[1], view->light[2] - at[2]};
+      norm(ld);
+      const float ndl = std::max(ld[0] * n[0] + ld[1] * n[1] + ld[2] * n[2], 0.f);
+      for (int k = 0; k < 3; ++k) lc[k] += m.diffuse[k] * 0.7f * ndl * m.diffuse[3];
+      float hd[3] = {vd[0] + ld[0], vd[1] + ld[1], vd[2] + ld[2]};
+      norm(hd);
+      const float st = std::pow(std::max(n[0] * hd[0] + n[1] * hd[1] + n[2] * hd[2], 0.f), m.shininess);
+      const float on = ndv > 1e-6f ? 1.f : 0.f;
+      for (int k = 0; k < 3; ++k) lc[k] += m.specular[k] * st * 1.f * m.specular[3] * on;
+      if (view->gi_scale > 0.f && fluence) {
+        float gp[3];
+        for (int r = 0; r < 3; ++r)
+          gp[r] = view->world_to_grid[4 * r] * at[0] + view->world_to_grid[4 * r + 1] * at[1] +
+                  view->world_to_grid[4 * r + 2] * at[2] + view->world_to_grid[4 * r + 3];
+        int i0[3], i1[3];
+        float w1[3];
+        for (int k = 0; k < 3; ++k) {
+          const float mm = gp[k] / (float)spacing - 0.5f, fl = std::floor(mm);
+          w1[k] = mm - fl;
+          i0[k] = std::min(std::max((int)fl, 0), probes[k] - 1);
+          i1[k] = std::min(std::max((int)fl + 1, 0), probes[k] - 1);
+        }
+        float f[3] = {0, 0, 0};
+        for (int k = 0; k < 8; ++k) {
+          const int xx = (k & 1) ? i1[0] : i0[0], yy = (k & 2) ? i1[1] : i0[1], zz = (k & 4) ? i1[2] : i0[2];
+          const float w = ((k & 1) ? w1[0] : 1.f - w1[0]) * ((k & 2) ? w1[1] : 1.f - w1[1]) *
+                          ((k & 4) ? w1[2] : 1.f - w1[2]);
+          const float* sp = fluence + (((size_t)zz * probes[1] + yy) * probes[0] + xx) * 3;
+          for (int c = 0; c < 3; ++c) f[c] += w * sp[c];
+        }
+        const float sc = view->gi_scale * 0.0795774715f;
+        for (int k = 0; k < 3; ++k) lc[k] += sc * f[k];
+      }
+      float pr[3];
+      for (int k = 0; k < 3; ++k) pr[k] = (m.ambient[k] - 1e-5f) + (m.diffuse[k] - 1e-5f) + (m.specular[k] - 1e-5f);
+      const float none = (pr[0] + pr[1] + pr[2]) <= 0.f ? 1.f : 0.f;
+      for (int k = 0; k < 3; ++k) o[k] = (lc[k] + none) * col[k];
+    }
+  return 0;
+}
+
 }  // extern "C"

@@ -9,7 +9,7 @@ from ._ffi import lib as _load_lib, RCError, VOXEL_DT, BOX_DT, SPHERE_DT  # noqa
 from .engine import (Engine, Batch, GiStage, GiState, make_params, level_info, scene_spec, generate_scene,  # noqa: F401
                      advance_spheres, voxelise_host, directions, solid_angles, WORKLOADS, workload_scene,
                      batch_workload, BATCH_EDGES, BATCH_CASCADES, load_obj, mesh_to_grid, mesh_materials,
-                     room_mesh,
+                     room_mesh, camera_view_proj, shade_vertices, shade_material, mesh_tbn,
                      frames)
 
 _load_lib()

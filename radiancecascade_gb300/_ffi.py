@@ -56,6 +56,23 @@ class NrcStats(C.Structure):
                 ("fallback_tiles", C.c_int64), ("tiles", C.c_int64)]
 
 
+class ShadeMaterial(C.Structure):
+    _fields_ = [("ambient", C.c_float * 4), ("diffuse", C.c_float * 4), ("specular", C.c_float * 4),
+                ("shininess", C.c_float), ("enable_bit", C.c_uint32), ("color_texture", C.c_int32),
+                ("normal_texture", C.c_int32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("srgb", C.c_int32),
+                ("pad", C.c_int32)]
+
+
+class ShadeView(C.Structure):
+    _fields_ = [("view_proj", C.c_float * 16), ("eye", C.c_float * 3), ("light", C.c_float * 3),
+                ("width", C.c_int32), ("height", C.c_int32), ("world_to_grid", C.c_float * 12),
+                ("gi_scale", C.c_float), ("pad", C.c_int32)]
+
+
 class BatchTiles(C.Structure):
     _fields_ = [("probes_per_item", C.c_int32), ("dirs_per_item", C.c_int32), ("blocks_per_item", C.c_int32),
                 ("walks_per_item", C.c_int32)]
@@ -96,6 +113,8 @@ SIGNATURES = {
     "rc_get_fluence_async": (_S, [_P, _P, C.c_int64]),
     "rc_scene_set_mesh": (_S, [_P, _P, C.c_int64, _P, C.c_int64, _P, _P, C.c_int32]),
     "rc_get_volume": (_S, [_P, _P, C.c_int64, C.c_int32]),
+    "rc_shade": (_S, [_P, C.POINTER(ShadeView), _P, C.c_int64, _P, C.c_int64, _P, C.POINTER(ShadeMaterial),
+                      C.c_int32, C.POINTER(Texture), C.c_int32, _P, C.c_int32]),
     "rc_batch_create": (_S, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "rc_batch_destroy": (_S, [_P]),
     "rc_batch_scene_set": (_S, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int32]),

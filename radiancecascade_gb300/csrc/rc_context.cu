@@ -20,6 +20,7 @@
 #include "rc_level0.cuh"
 #include "rc_batch.cuh"
 #include "rc_mesh.cuh"
+#include "rc_shade.cuh"
 
 using namespace rcx;
 
@@ -869,6 +870,126 @@ rc_status rc_get_radiance(rc_context* c, int32_t level, void* out, int64_t bytes
     return RC_ERR_INVALID_ARG;
   }
   return copy_out(c, out, static_cast<char*>(c->rad) + c->rad_off[level], need, where, "rc_get_radiance");
+}
+
+rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertices, int64_t nverts,
+                   const uint32_t* indices, int64_t ntris, const uint16_t* tri_material,
+                   const rc_shade_material* materials, int32_t nmaterials, const rc_texture* textures,
+                   int32_t ntextures, float* out, int32_t where) {
+  if (check_ctx(c, "rc_shade") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!view || view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384 || nverts < 0 ||
+      ntris < 0 || ntris >= ((int64_t)1 << 32) || (nverts && !vertices) || (ntris && !indices) || nmaterials < 1 ||
+      !materials || ntextures < 0 || (ntextures && !textures) || !out ||
+      (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
+    rcx::set_error("rc_shade: invalid arguments (image 1..16384 px per side, >= 1 material, non-NULL arrays)");
+    return RC_ERR_INVALID_ARG;
+  }
+  for (int64_t i = 0; i < ntris * 3; ++i)
+    if (indices[i] >= (uint64_t)nverts) {
+      rcx::set_error("rc_shade: triangle %lld indexes vertex %u of %lld", (long long)(i / 3), indices[i],
+                     (long long)nverts);
+      return RC_ERR_INVALID_ARG;
+    }
+  for (int32_t m = 0; m < nmaterials; ++m) {
+    const rc_shade_material& mt = materials[m];
+    if (((mt.enable_bit & 1u) && (mt.color_texture < 0 || mt.color_texture >= ntextures)) ||
+        ((mt.enable_bit & 2u) && (mt.normal_texture < 0 || mt.normal_texture >= ntextures))) {
+      rcx::set_error("rc_shade: material %d names a missing texture", m);
+      return RC_ERR_INVALID_ARG;
+    }
+  }
+  if (tri_material)
+    for (int64_t t = 0; t < ntris; ++t)
+      if (tri_material[t] >= nmaterials) {
+        rcx::set_error("rc_shade: triangle %lld uses material %u of %d", (long long)t, tri_material[t], nmaterials);
+        return RC_ERR_INVALID_ARG;
+      }
+  for (int32_t k = 0; k < ntextures; ++k)
+    if (!textures[k].rgba || textures[k].width < 1 || textures[k].height < 1) {
+      rcx::set_error("rc_shade: texture %d is empty", k);
+      return RC_ERR_INVALID_ARG;
+    }
+  if (view->gi_scale > 0.f && !c->have_base) {
+    rcx::set_error("rc_shade: the GI term needs a solved scene");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  const int64_t npix = (int64_t)view->width * view->height;
+  std::vector<void*> owned;
+  auto done = [&](rc_status st) {
+    for (void* b : owned) cudaFree(b);
+    return st;
+  };
+  auto alloc = [&](void** p, size_t bytes, const char* what) {
+    rc_status st = dev_alloc(p, std::max<size_t>(bytes, 16), what);
+    if (st == RC_OK) owned.push_back(*p);
+    return st;
+  };
+  float* d_v = nullptr;
+  uint32_t* d_i = nullptr;
+  uint16_t* d_m = nullptr;
+  rc_shade_material* d_mat = nullptr;
+  ShadeTex* d_tex = nullptr;
+  unsigned long long* d_z = nullptr;
+  float* d_out = where == RC_MEM_DEVICE ? out : nullptr;
+  rc_status st;
+  if ((st = alloc((void**)&d_v, (size_t)nverts * kShadeVertexFloats * 4, "shade vertices")) != RC_OK) return done(st);
+  if ((st = alloc((void**)&d_i, (size_t)ntris * 12, "shade indices")) != RC_OK) return done(st);
+  if (tri_material && (st = alloc((void**)&d_m, (size_t)ntris * 2, "shade materials")) != RC_OK) return done(st);
+  if ((st = alloc((void**)&d_mat, (size_t)nmaterials * sizeof(rc_shade_material), "shade materials")) != RC_OK)
+    return done(st);
+  if ((st = alloc((void**)&d_z, (size_t)npix * 8, "depth buffer")) != RC_OK) return done(st);
+  if (!d_out && (st = alloc((void**)&d_out, (size_t)npix * 16, "image")) != RC_OK) return done(st);
+  std::vector<ShadeTex> tex((size_t)std::max(ntextures, 1));
+  for (int32_t k = 0; k < ntextures; ++k) {
+    uint8_t* d_t = nullptr;
+    const size_t bytes = (size_t)textures[k].width * textures[k].height * 4;
+    if ((st = alloc((void**)&d_t, bytes, "texture")) != RC_OK) return done(st);
+    RC_CUDA(cudaMemcpyAsync(d_t, textures[k].rgba, bytes, cudaMemcpyHostToDevice, c->stream), "rc_shade: upload");
+    tex[k] = ShadeTex{d_t, textures[k].width, textures[k].height, textures[k].srgb ? 1 : 0, 0};
+  }
+  if ((st = alloc((void**)&d_tex, tex.size() * sizeof(ShadeTex), "texture table")) != RC_OK) return done(st);
+  cudaStream_t s = c->stream;
+  RC_CUDA(cudaMemcpyAsync(d_tex, tex.data(), tex.size() * sizeof(ShadeTex), cudaMemcpyHostToDevice, s), "rc_shade");
+  if (nverts)
+    RC_CUDA(cudaMemcpyAsync(d_v, vertices, (size_t)nverts * kShadeVertexFloats * 4, cudaMemcpyHostToDevice, s),
+            "rc_shade: upload");
+  if (ntris) RC_CUDA(cudaMemcpyAsync(d_i, indices, (size_t)ntris * 12, cudaMemcpyHostToDevice, s), "rc_shade: upload");
+  if (d_m) RC_CUDA(cudaMemcpyAsync(d_m, tri_material, (size_t)ntris * 2, cudaMemcpyHostToDevice, s), "rc_shade: upload");
+  RC_CUDA(cudaMemcpyAsync(d_mat, materials, (size_t)nmaterials * sizeof(rc_shade_material), cudaMemcpyHostToDevice, s),
+          "rc_shade: upload");
+  RC_CUDA(cudaMemsetAsync(d_z, 0xFF, (size_t)npix * 8, s), "rc_shade: clear");
+  ShadeArgs a;
+  memset(&a, 0, sizeof a);
+  a.verts = d_v;
+  a.idx = d_i;
+  a.tmat = d_m;
+  a.mats = d_mat;
+  a.tex = d_tex;
+  a.ntris = ntris;
+  memcpy(a.vp, view->view_proj, sizeof a.vp);
+  memcpy(a.eye, view->eye, sizeof a.eye);
+  memcpy(a.light, view->light, sizeof a.light);
+  a.W = view->width;
+  a.H = view->height;
+  a.zbuf = d_z;
+  a.out = d_out;
+  a.fluence = c->fluence;
+  for (int k = 0; k < 3; ++k) a.M[k] = c->geom[0].M[k];
+  a.spacing = (float)c->geom[0].spacing;
+  memcpy(a.w2g, view->world_to_grid, sizeof a.w2g);
+  a.gi_scale = view->gi_scale;
+  a.ntex = ntextures;
+  if (ntris) {
+    const int64_t blocks = std::min<int64_t>((ntris * 32 + 255) / 256, 152 * 16);
+    k_shade_depth<<<(unsigned)blocks, 256, 0, s>>>(a);
+  }
+  k_shade_pixels<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(a);
+  RC_CUDA(cudaGetLastError(), "rc_shade: launch");
+  if (where == RC_MEM_HOST)
+    RC_CUDA(cudaMemcpyAsync(out, d_out, (size_t)npix * 16, cudaMemcpyDeviceToHost, s), "rc_shade: read back");
+  RC_CUDA(cudaStreamSynchronize(s), "rc_shade");
+  return done(RC_OK);
 }
 
 rc_status rc_get_volume(rc_context* c, rc_voxel* out, int64_t count, int32_t where) {

@@ -251,6 +251,122 @@ def room_mesh(grid: int, boxes: int = 6, seed: int = 7):
     return (np.concatenate(P).astype(np.float32), np.asarray(I, np.uint32), np.asarray(M, np.uint16), mats)
 
 
+# ---- shading pass helpers ----------------------------------------------------
+def perspective_rh(fovy_rad: float, aspect: float, znear: float, zfar: float) -> np.ndarray:
+    """Right-handed perspective with depth in [0, 1] (the reference's
+    Projection::calc_matrix, src/camera.rs:77-79), column-major 4x4."""
+    h = np.cos(0.5 * fovy_rad) / np.sin(0.5 * fovy_rad)
+    w = h / aspect
+    r = zfar / (znear - zfar)
+    m = np.zeros((4, 4))  # m[col][row]
+    m[0, 0], m[1, 1], m[2, 2], m[2, 3], m[3, 2] = w, h, r, -1.0, r * znear
+    return m
+
+
+def look_to_rh(eye, direction, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """Right-handed view matrix looking along `direction`, column-major 4x4."""
+    f = np.asarray(direction, np.float64)
+    f = f / np.linalg.norm(f)
+    s = np.cross(f, up)
+    s = s / np.linalg.norm(s)
+    u = np.cross(s, f)
+    e = np.asarray(eye, np.float64)
+    m = np.zeros((4, 4))
+    m[0] = (s[0], u[0], -f[0], 0.0)
+    m[1] = (s[1], u[1], -f[1], 0.0)
+    m[2] = (s[2], u[2], -f[2], 0.0)
+    m[3] = (-e.dot(s), -e.dot(u), e.dot(f), 1.0)
+    return m
+
+
+def camera_view_proj(eye, yaw: float, pitch: float, width: int, height: int, fovy_deg: float = 45.0,
+                     znear: float = 0.1, zfar: float = 100.0) -> np.ndarray:
+    """projection * view as the reference's camera builds it (src/camera.rs:20,
+    43-52: direction (cos pitch cos yaw, sin pitch, cos pitch sin yaw), up +Y);
+    -> 16 floats, column-major."""
+    d = (np.cos(pitch) * np.cos(yaw), np.sin(pitch), np.cos(pitch) * np.sin(yaw))
+    p = perspective_rh(np.radians(fovy_deg), width / height, znear, zfar)
+    v = look_to_rh(eye, d)
+    # column-major product: (P V)[col] = P applied to V's columns
+    pv = (p.T @ v.T).T
+    return pv.astype(np.float32).reshape(-1)
+
+
+def mesh_tbn(positions: np.ndarray, indices: np.ndarray, texcoords: Optional[np.ndarray]):
+    """Per-vertex tangent, bitangent and normal as the reference derives them
+    (src/primitives.rs:245-354): per triangle, the UV deltas scaled by 2^11,
+    T and B from the inverse of [duv1 duv2], N = B x T; accumulated over the
+    triangles without NaN, averaged and normalised (X, Y, Z where none)."""
+    p = np.asarray(positions, np.float32)
+    n = len(p)
+    uv = np.zeros((n, 2), np.float32) if texcoords is None or len(texcoords) != n else np.asarray(texcoords, np.float32)
+    T = np.zeros((n, 3), np.float32)
+    B = np.zeros((n, 3), np.float32)
+    N = np.zeros((n, 3), np.float32)
+    cnt = np.zeros(n, np.int64)
+    with np.errstate(all="ignore"):
+        for c in np.asarray(indices, np.int64).reshape(-1, 3):
+            dp1, dp2 = p[c[1]] - p[c[0]], p[c[2]] - p[c[0]]
+            d1 = (uv[c[1]] - uv[c[0]]) * np.float32(2.0 ** 11)
+            d2 = (uv[c[2]] - uv[c[0]]) * np.float32(2.0 ** 11)
+            det = np.float32(d1[0] * d2[1] - d2[0] * d1[1])
+            inv_det = np.float32(1.0) / det
+            col0 = np.array([d2[1], -d1[1]], np.float32) * inv_det
+            col1 = np.array([-d2[0], d1[0]], np.float32) * inv_det
+            t = col0[0] * dp1 - col0[1] * dp2
+            b = -col1[0] * dp1 + col1[1] * dp2
+            nn = np.cross(b, t)
+            nn = nn / np.linalg.norm(nn)
+            if np.isnan(t).any() or np.isnan(b).any() or np.isnan(nn).any():
+                continue
+            for k in c:
+                T[k] += t
+                B[k] += b
+                N[k] += nn
+                cnt[k] += 1
+    out = []
+    for acc, dflt in ((T, (1, 0, 0)), (B, (0, 1, 0)), (N, (0, 0, 1))):
+        r = np.tile(np.asarray(dflt, np.float32), (n, 1))
+        m = cnt > 0
+        with np.errstate(all="ignore"):
+            v = acc[m] / cnt[m, None]
+            r[m] = v / np.linalg.norm(v, axis=1, keepdims=True)
+        out.append(r)
+    return out
+
+
+def shade_vertices(positions, indices, colors=None, normals=None, texcoords=None) -> np.ndarray:
+    """The 17-float vertex records the reference builds (src/renderer.rs:
+    370-410): position, colour (default 1), normal (the mesh's, else the TBN
+    normal), tangent, bitangent, uv (default 0)."""
+    p = np.asarray(positions, np.float32)
+    n = len(p)
+    t, b, tn = mesh_tbn(p, indices, texcoords)
+    v = np.zeros((n, 17), np.float32)
+    v[:, 0:3] = p
+    v[:, 3:6] = 1.0 if colors is None else colors
+    v[:, 6:9] = tn if normals is None else normals
+    v[:, 9:12] = t
+    v[:, 12:15] = b
+    if texcoords is not None and len(texcoords) == n:
+        v[:, 15:17] = texcoords
+    return v
+
+
+def shade_material(ambient=None, diffuse=None, specular=None, shininess=None, color_texture=-1,
+                   normal_texture=-1) -> F.ShadeMaterial:
+    """UniformMaterial (src/primitives.rs:39-73): an absent component is (0, 0, 0, 0),
+    a present one (rgb, 1); shininess defaults to 1."""
+    m = F.ShadeMaterial()
+    for name, v in (("ambient", ambient), ("diffuse", diffuse), ("specular", specular)):
+        getattr(m, name)[:] = (0.0, 0.0, 0.0, 0.0) if v is None else (v[0], v[1], v[2], 1.0)
+    m.shininess = 1.0 if shininess is None else shininess
+    m.enable_bit = (1 if color_texture >= 0 else 0) | (2 if normal_texture >= 0 else 0)
+    m.color_texture = max(color_texture, 0)
+    m.normal_texture = max(normal_texture, 0)
+    return m
+
+
 # Batched workload: `count` cubic scenes, scene k seeded 2000 + k, edge drawn
 # uniformly from BATCH_EDGES by splitmix64(seed); the 64^3 workload's box and
 # sphere density per voxel (24 boxes and 4 spheres per 64^3, edges 4..20,
@@ -364,6 +480,24 @@ class Engine:
             out = np.empty(n, np.float32)
         F.check(self._lib.rc_get_fluence(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
         return out.reshape(-1, 3)
+
+    def shade(self, view: F.ShadeView, vertices: np.ndarray, indices: np.ndarray, materials,
+              tri_material: Optional[np.ndarray] = None, textures=()) -> np.ndarray:
+        """Raster + shade into an (H, W, 4) float32 image (see rc_shade)."""
+        v = np.ascontiguousarray(vertices, np.float32)
+        i = np.ascontiguousarray(indices, np.uint32)
+        tm = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint16)
+        mats = (F.ShadeMaterial * len(materials))(*materials)
+        keep = [np.ascontiguousarray(t["rgba"], np.uint8) for t in textures]
+        tex = (F.Texture * max(len(textures), 1))()
+        for k, t in enumerate(textures):
+            tex[k].rgba = keep[k].ctypes.data
+            tex[k].width, tex[k].height, tex[k].srgb = keep[k].shape[1], keep[k].shape[0], int(t.get("srgb", 1))
+        out = np.zeros((view.height, view.width, 4), np.float32)
+        F.check(self._lib.rc_shade(self.handle, C.byref(view), F.ptr(v), len(v), F.ptr(i), len(i),
+                                   None if tm is None else F.ptr(tm), mats, len(materials), tex, len(textures),
+                                   F.ptr(out), F.RC_MEM_HOST))
+        return out
 
     def volume(self) -> np.ndarray:
         """The composed scene volume (rc_voxel per voxel, x fastest)."""
