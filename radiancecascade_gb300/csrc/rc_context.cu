@@ -63,6 +63,8 @@ void release(rc_context* c) {
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   nrc_release(c);
   if (c->flu[1]) cudaFree(c->flu[1]);
+  for (void* b : c->scratch)
+    if (b) cudaFree(b);
   for (int k = 0; k < 2; ++k) {
     if (c->ev_solved[k]) cudaEventDestroy(c->ev_solved[k]);
     if (c->ev_copied[k]) cudaEventDestroy(c->ev_copied[k]);
@@ -915,41 +917,56 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
   }
   DeviceGuard g(c->device);
   const int64_t npix = (int64_t)view->width * view->height;
-  std::vector<void*> owned;
-  auto done = [&](rc_status st) {
-    for (void* b : owned) cudaFree(b);
-    return st;
-  };
-  auto alloc = [&](void** p, size_t bytes, const char* what) {
-    rc_status st = dev_alloc(p, std::max<size_t>(bytes, 16), what);
-    if (st == RC_OK) owned.push_back(*p);
-    return st;
+  // scratch slots: 0 vertices, 1 indices, 2 triangle materials, 3 materials, 4 texels, 5 texture table,
+  // 6 depth, 7 image, 8 bounds, 9 small list, 10 large list, 11 counts
+  auto scratch = [&](int slot, size_t bytes, void** p) -> rc_status {
+    bytes = std::max<size_t>(bytes, 16);
+    if (c->scratch_cap[slot] < bytes) {
+      if (c->scratch[slot]) cudaFree(c->scratch[slot]);
+      c->scratch[slot] = nullptr;
+      c->scratch_cap[slot] = 0;
+      rc_status st = dev_alloc(&c->scratch[slot], bytes, "shading scratch");
+      if (st != RC_OK) return st;
+      c->scratch_cap[slot] = bytes;
+    }
+    *p = c->scratch[slot];
+    return RC_OK;
   };
   float* d_v = nullptr;
-  uint32_t* d_i = nullptr;
+  uint32_t *d_i = nullptr, *d_small = nullptr, *d_big = nullptr;
   uint16_t* d_m = nullptr;
   rc_shade_material* d_mat = nullptr;
+  uint8_t* d_texels = nullptr;
   ShadeTex* d_tex = nullptr;
   unsigned long long* d_z = nullptr;
+  int4* d_bounds = nullptr;
+  unsigned* d_counts = nullptr;
   float* d_out = where == RC_MEM_DEVICE ? out : nullptr;
+  size_t texel_bytes = 0;
+  for (int32_t k = 0; k < ntextures; ++k) texel_bytes += ((size_t)textures[k].width * textures[k].height * 4 + 15) & ~(size_t)15;
   rc_status st;
-  if ((st = alloc((void**)&d_v, (size_t)nverts * kShadeVertexFloats * 4, "shade vertices")) != RC_OK) return done(st);
-  if ((st = alloc((void**)&d_i, (size_t)ntris * 12, "shade indices")) != RC_OK) return done(st);
-  if (tri_material && (st = alloc((void**)&d_m, (size_t)ntris * 2, "shade materials")) != RC_OK) return done(st);
-  if ((st = alloc((void**)&d_mat, (size_t)nmaterials * sizeof(rc_shade_material), "shade materials")) != RC_OK)
-    return done(st);
-  if ((st = alloc((void**)&d_z, (size_t)npix * 8, "depth buffer")) != RC_OK) return done(st);
-  if (!d_out && (st = alloc((void**)&d_out, (size_t)npix * 16, "image")) != RC_OK) return done(st);
-  std::vector<ShadeTex> tex((size_t)std::max(ntextures, 1));
-  for (int32_t k = 0; k < ntextures; ++k) {
-    uint8_t* d_t = nullptr;
-    const size_t bytes = (size_t)textures[k].width * textures[k].height * 4;
-    if ((st = alloc((void**)&d_t, bytes, "texture")) != RC_OK) return done(st);
-    RC_CUDA(cudaMemcpyAsync(d_t, textures[k].rgba, bytes, cudaMemcpyHostToDevice, c->stream), "rc_shade: upload");
-    tex[k] = ShadeTex{d_t, textures[k].width, textures[k].height, textures[k].srgb ? 1 : 0, 0};
-  }
-  if ((st = alloc((void**)&d_tex, tex.size() * sizeof(ShadeTex), "texture table")) != RC_OK) return done(st);
+  if ((st = scratch(0, (size_t)nverts * kShadeVertexFloats * 4, (void**)&d_v)) != RC_OK ||
+      (st = scratch(1, (size_t)ntris * 12, (void**)&d_i)) != RC_OK ||
+      (tri_material && (st = scratch(2, (size_t)ntris * 2, (void**)&d_m)) != RC_OK) ||
+      (st = scratch(3, (size_t)nmaterials * sizeof(rc_shade_material), (void**)&d_mat)) != RC_OK ||
+      (st = scratch(4, texel_bytes, (void**)&d_texels)) != RC_OK ||
+      (st = scratch(5, (size_t)std::max(ntextures, 1) * sizeof(ShadeTex), (void**)&d_tex)) != RC_OK ||
+      (st = scratch(6, (size_t)npix * 8, (void**)&d_z)) != RC_OK ||
+      (!d_out && (st = scratch(7, (size_t)npix * 16, (void**)&d_out)) != RC_OK) ||
+      (st = scratch(8, (size_t)ntris * sizeof(int4), (void**)&d_bounds)) != RC_OK ||
+      (st = scratch(9, (size_t)ntris * 4, (void**)&d_small)) != RC_OK ||
+      (st = scratch(10, (size_t)ntris * 4, (void**)&d_big)) != RC_OK ||
+      (st = scratch(11, 2 * sizeof(unsigned), (void**)&d_counts)) != RC_OK)
+    return st;
   cudaStream_t s = c->stream;
+  std::vector<ShadeTex> tex((size_t)std::max(ntextures, 1));
+  size_t off = 0;
+  for (int32_t k = 0; k < ntextures; ++k) {
+    const size_t bytes = (size_t)textures[k].width * textures[k].height * 4;
+    RC_CUDA(cudaMemcpyAsync(d_texels + off, textures[k].rgba, bytes, cudaMemcpyHostToDevice, s), "rc_shade: upload");
+    tex[k] = ShadeTex{d_texels + off, textures[k].width, textures[k].height, textures[k].srgb ? 1 : 0, 0};
+    off += (bytes + 15) & ~(size_t)15;
+  }
   RC_CUDA(cudaMemcpyAsync(d_tex, tex.data(), tex.size() * sizeof(ShadeTex), cudaMemcpyHostToDevice, s), "rc_shade");
   if (nverts)
     RC_CUDA(cudaMemcpyAsync(d_v, vertices, (size_t)nverts * kShadeVertexFloats * 4, cudaMemcpyHostToDevice, s),
@@ -959,6 +976,7 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
   RC_CUDA(cudaMemcpyAsync(d_mat, materials, (size_t)nmaterials * sizeof(rc_shade_material), cudaMemcpyHostToDevice, s),
           "rc_shade: upload");
   RC_CUDA(cudaMemsetAsync(d_z, 0xFF, (size_t)npix * 8, s), "rc_shade: clear");
+  RC_CUDA(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned), s), "rc_shade: clear");
   ShadeArgs a;
   memset(&a, 0, sizeof a);
   a.verts = d_v;
@@ -981,15 +999,25 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
   a.gi_scale = view->gi_scale;
   a.ntex = ntextures;
   if (ntris) {
-    const int64_t blocks = std::min<int64_t>((ntris * 32 + 255) / 256, 152 * 16);
-    k_shade_depth<<<(unsigned)blocks, 256, 0, s>>>(a);
+    k_shade_bin<<<(unsigned)((ntris + 255) / 256), 256, 0, s>>>(a, d_bounds, d_small, d_big, d_counts);
+    unsigned counts[2] = {0, 0};
+    RC_CUDA(cudaMemcpyAsync(counts, d_counts, sizeof counts, cudaMemcpyDeviceToHost, s), "rc_shade: bin");
+    RC_CUDA(cudaStreamSynchronize(s), "rc_shade: bin");
+    if (counts[0]) {
+      const int64_t blocks = std::min<int64_t>(((int64_t)counts[0] * 32 + 255) / 256, 152 * 32);
+      k_shade_depth_small<<<(unsigned)blocks, 256, 0, s>>>(a, d_bounds, d_small, d_counts);
+    }
+    if (counts[1]) {
+      const unsigned tiles = (unsigned)(((a.W + kShadeTile - 1) / kShadeTile) * ((a.H + kShadeTile - 1) / kShadeTile));
+      k_shade_depth_big<<<dim3(tiles, std::min(counts[1], 65535u)), 256, 0, s>>>(a, d_bounds, d_big, d_counts);
+    }
   }
   k_shade_pixels<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(a);
   RC_CUDA(cudaGetLastError(), "rc_shade: launch");
   if (where == RC_MEM_HOST)
     RC_CUDA(cudaMemcpyAsync(out, d_out, (size_t)npix * 16, cudaMemcpyDeviceToHost, s), "rc_shade: read back");
   RC_CUDA(cudaStreamSynchronize(s), "rc_shade");
-  return done(RC_OK);
+  return RC_OK;
 }
 
 rc_status rc_get_volume(rc_context* c, rc_voxel* out, int64_t count, int32_t where) {

@@ -76,6 +76,10 @@ struct rc_context {
   rcx::LevelArgs args[rcx::kMaxCascades]{};
 
   rcx::NrcState* nrc = nullptr;  // neural radiance cache (rc_nrc_enable), or null
+
+  // device scratch of the shading pass, grown on demand and kept
+  void* scratch[12] = {};
+  size_t scratch_cap[12] = {};
 };
 
 namespace rcx {

@@ -97,41 +97,96 @@ __device__ __forceinline__ void shade_load_tri(const ShadeArgs& a, int64_t t, fl
   }
 }
 
-// Pass 1: one warp per triangle, lanes over the pixels of its screen bounds.
-static __global__ void k_shade_depth(const __grid_constant__ ShadeArgs a) {
+// Screen bounds of triangle t (the whole image when a vertex is at or behind
+// the eye); false when it covers nothing.
+__device__ __forceinline__ bool shade_bounds(const ShadeArgs& a, const float c[3][4], int4& b) {
+  b = make_int4(0, 0, a.W - 1, a.H - 1);
+  if (c[0][3] > 0.f && c[1][3] > 0.f && c[2][3] > 0.f) {
+    float lx = 1e30f, hx = -1e30f, ly = 1e30f, hy = -1e30f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float sx = (c[k][0] / c[k][3] + 1.f) * 0.5f * a.W, sy = (1.f - c[k][1] / c[k][3]) * 0.5f * a.H;
+      lx = fminf(lx, sx); hx = fmaxf(hx, sx); ly = fminf(ly, sy); hy = fmaxf(hy, sy);
+    }
+    // clamp in float first: a vertex near the eye plane projects far away
+    lx = fmaxf(lx - 1.f, 0.f); ly = fmaxf(ly - 1.f, 0.f);
+    hx = fminf(hx + 1.f, (float)(a.W - 1)); hy = fminf(hy + 1.f, (float)(a.H - 1));
+    if (!(lx <= hx && ly <= hy)) return false;
+    b = make_int4((int)floorf(lx), (int)floorf(ly), (int)ceilf(hx), (int)ceilf(hy));
+  }
+  return true;
+}
+
+// Depth test of triangle t at pixel (x, y).
+__device__ __forceinline__ void shade_fragment(const ShadeArgs& a, int64_t t, const float c[3][4],
+                                               const float R[3][3], int x, int y) {
+  const float px = (2.f * ((float)x + 0.5f)) / (float)a.W - 1.f;
+  const float py = 1.f - (2.f * ((float)y + 0.5f)) / (float)a.H;
+  float g[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) g[k] = R[k][0] * px + R[k][1] * py + R[k][2];
+  if (!(g[0] >= 0.f && g[1] >= 0.f && g[2] >= 0.f) || g[0] + g[1] + g[2] <= 0.f) return;
+  const float z = g[0] * c[0][2] + g[1] * c[1][2] + g[2] * c[2][2];
+  if (!(z >= 0.f && z < 1.f)) return;
+  const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)t;
+  atomicMin(&a.zbuf[(int64_t)y * a.W + x], key);
+}
+
+constexpr int kShadeTile = 64;          // pixels per side of a large triangle's tile
+constexpr int kShadeSmallArea = 4096;   // bounds of at most this many pixels: one warp per triangle
+
+// Pass 0: bounds of every triangle, split into small ones (a warp each) and
+// large ones (a block per 64 x 64 tile of their bounds).
+static __global__ void k_shade_bin(const __grid_constant__ ShadeArgs a, int4* __restrict__ bounds,
+                                   uint32_t* __restrict__ small, uint32_t* __restrict__ big,
+                                   unsigned* __restrict__ counts) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= a.ntris) return;
+  float c[3][4], R[3][3];
+  shade_load_tri(a, t, c);
+  int4 b;
+  if (!shade_setup(c, R) || !shade_bounds(a, c, b)) return;
+  bounds[t] = b;
+  const int64_t area = (int64_t)(b.z - b.x + 1) * (b.w - b.y + 1);
+  if (area <= kShadeSmallArea) small[atomicAdd(&counts[0], 1u)] = (uint32_t)t;
+  else big[atomicAdd(&counts[1], 1u)] = (uint32_t)t;
+}
+
+// Pass 1a: one warp per small triangle, lanes over the pixels of its bounds.
+static __global__ void k_shade_depth_small(const __grid_constant__ ShadeArgs a, const int4* __restrict__ bounds,
+                                           const uint32_t* __restrict__ list, const unsigned* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < a.ntris; t += warps) {
+  const int64_t n = counts[0];
+  for (int64_t k = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < n; k += warps) {
+    const int64_t t = list[k];
     float c[3][4], R[3][3];
     shade_load_tri(a, t, c);
-    if (!shade_setup(c, R)) continue;
-    int x0 = 0, x1 = a.W - 1, y0 = 0, y1 = a.H - 1;
-    if (c[0][3] > 0.f && c[1][3] > 0.f && c[2][3] > 0.f) {
-      float lx = 1e30f, hx = -1e30f, ly = 1e30f, hy = -1e30f;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float sx = (c[k][0] / c[k][3] + 1.f) * 0.5f * a.W, sy = (1.f - c[k][1] / c[k][3]) * 0.5f * a.H;
-        lx = fminf(lx, sx); hx = fmaxf(hx, sx); ly = fminf(ly, sy); hy = fmaxf(hy, sy);
-      }
-      x0 = max(0, (int)floorf(lx - 1.f)); x1 = min(a.W - 1, (int)ceilf(hx + 1.f));
-      y0 = max(0, (int)floorf(ly - 1.f)); y1 = min(a.H - 1, (int)ceilf(hy + 1.f));
-      if (x0 > x1 || y0 > y1) continue;
-    }
+    shade_setup(c, R);
+    const int4 b = bounds[t];
+    const int nx = b.z - b.x + 1;
+    const int count = nx * (b.w - b.y + 1);
+    for (int q = lane; q < count; q += 32) shade_fragment(a, t, c, R, b.x + q % nx, b.y + q / nx);
+  }
+}
+
+// Pass 1b: block (tile, large triangle), threads over the tile's pixels.
+static __global__ void k_shade_depth_big(const __grid_constant__ ShadeArgs a, const int4* __restrict__ bounds,
+                                         const uint32_t* __restrict__ list, const unsigned* __restrict__ counts) {
+  const int tiles_x = (a.W + kShadeTile - 1) / kShadeTile;
+  const int tx = (int)(blockIdx.x % tiles_x), ty = (int)(blockIdx.x / tiles_x);
+  for (int64_t k = blockIdx.y; k < (int64_t)counts[1]; k += gridDim.y) {
+    const int64_t t = list[k];
+    const int4 b = bounds[t];
+    const int x0 = max(b.x, tx * kShadeTile), x1 = min(b.z, tx * kShadeTile + kShadeTile - 1);
+    const int y0 = max(b.y, ty * kShadeTile), y1 = min(b.w, ty * kShadeTile + kShadeTile - 1);
+    if (x0 > x1 || y0 > y1) continue;
+    float c[3][4], R[3][3];
+    shade_load_tri(a, t, c);
+    shade_setup(c, R);
     const int nx = x1 - x0 + 1;
-    const int64_t count = (int64_t)nx * (y1 - y0 + 1);
-    for (int64_t q = lane; q < count; q += 32) {
-      const int x = x0 + (int)(q % nx), y = y0 + (int)(q / nx);
-      const float px = (2.f * ((float)x + 0.5f)) / (float)a.W - 1.f;
-      const float py = 1.f - (2.f * ((float)y + 0.5f)) / (float)a.H;
-      float g[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) g[k] = R[k][0] * px + R[k][1] * py + R[k][2];
-      if (!(g[0] >= 0.f && g[1] >= 0.f && g[2] >= 0.f) || g[0] + g[1] + g[2] <= 0.f) continue;
-      const float z = g[0] * c[0][2] + g[1] * c[1][2] + g[2] * c[2][2];
-      if (!(z >= 0.f && z < 1.f)) continue;
-      const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)t;
-      atomicMin(&a.zbuf[(int64_t)y * a.W + x], key);
-    }
+    const int count = nx * (y1 - y0 + 1);
+    for (int q = threadIdx.x; q < count; q += blockDim.x) shade_fragment(a, t, c, R, x0 + q % nx, y0 + q / nx);
   }
 }
 
