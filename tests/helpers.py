@@ -1,4 +1,5 @@
 """Scene builders shared by the tests (numpy only)."""
+import os
 import numpy as np
 
 from oracle import oracle as O
@@ -26,3 +27,15 @@ def mirror_x(vox: np.ndarray, G: int) -> np.ndarray:
 
 def mirror_y(vox: np.ndarray, G: int) -> np.ndarray:
     return vox.reshape(G, G, G)[:, ::-1, :].reshape(-1).copy()
+
+
+def build_abi_driver(tmpdir):
+    """Compile tests/abi_driver.cpp against include/rc.h and librc.so; -> path of the binary."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.join(root, "radiancecascade_gb300")
+    exe = os.path.join(str(tmpdir), "abi_driver")
+    subprocess.run(["g++", "-std=c++17", "-O1", os.path.join(root, "tests", "abi_driver.cpp"),
+                    "-I", os.path.join(root, "include"), "-L", libdir, "-lrc", "-Wl,-rpath," + libdir,
+                    "-o", exe], check=True, capture_output=True, text=True)
+    return exe

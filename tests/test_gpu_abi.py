@@ -114,3 +114,23 @@ def test_async_fluence_readback_matches_sync_per_frame():
             assert np.array_equal(outs[f], want[f]), f
         with pytest.raises(ValueError):
             e.fluence_async(np.zeros(10, np.float32))
+
+
+
+def test_cpp_driver_solve_matches_python_binding(tmp_path):
+    """The same solve through the C++ driver and through ctypes is bit-identical."""
+    import subprocess
+    from tests.helpers import build_abi_driver
+    exe = build_abi_driver(tmp_path)
+    out = str(tmp_path / "flu.bin")
+    r = subprocess.run([exe, "gpu", out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(out, np.float32)
+    spec = R.scene_spec(32, 6, (3, 10), 3, (1.5, 4.0), (1.0, 20.0))
+    boxes, spheres = R.generate_scene(spec, 77)
+    with R.Engine(R.make_params(32, 4)) as e:
+        e.set_boxes(boxes)
+        e.set_spheres(spheres)
+        e.solve()
+        want = e.fluence().reshape(-1)
+    assert np.array_equal(got, want)

@@ -162,6 +162,26 @@ def test_c256_frame0_matches_fp64_oracle(walk):
     _check(gflu, gL, oflu, oL)
 
 
+@pytest.mark.parametrize("frame", [1, 239])
+def test_c256_later_frames_match_fp64_oracle(frame):
+    """Frames 1 and 239 of the moving-emitter workload, reached by incremental
+    emitter updates frame after frame, against the oracle's fresh solve."""
+    boxes, spheres = R.workload_scene("c256")
+    with R.Engine(R.make_params(256, 6)) as e:
+        e.set_boxes(boxes)
+        sph = spheres.copy()
+        for _ in range(frame):
+            e.set_spheres(sph)
+            R.advance_spheres(sph, 256, 1)
+        e.set_spheres(sph)
+        e.solve()
+        gflu = e.fluence().astype(np.float64)
+    ob, os_ = O.config_scene("c256", frame=frame)
+    oflu, _ = O.solve(O.params(256, 6), O.voxelise(256, ob, os_), jump=True)
+    assert rel_l2(gflu, oflu) <= FP32_REL_L2
+    assert np.abs(gflu - oflu).max() <= FP32_MAX_REL * oflu.max()
+
+
 def test_c256_size_independent_properties():
     """Full size: energy bounds, furnace and FP16 error."""
     boxes, spheres = R.workload_scene("c256", frame=120)

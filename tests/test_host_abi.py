@@ -148,3 +148,14 @@ def test_nrc_defaults_and_argument_checks():
     assert F.lib().rc_nrc_enable(None, C.byref(p)) == F.RC_ERR_INVALID_ARG
     assert F.lib().rc_nrc_disable(None) == F.RC_ERR_INVALID_ARG
     assert F.lib().rc_nrc_params_default(None) == F.RC_ERR_INVALID_ARG
+
+
+
+def test_cpp_driver_host_calls(tmp_path):
+    """The C ABI driven from C++ (as a native renderer would), host-only calls."""
+    import subprocess
+    from tests.helpers import build_abi_driver
+    exe = build_abi_driver(tmp_path)
+    r = subprocess.run([exe, "host"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "host ok" in r.stdout
