@@ -244,6 +244,15 @@ bool setup_tma0(rc_context* c) {
                          const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return false;
+  // kL0Stages 128-byte aligned stages, their barriers and up to 127 bytes to align the base
+  const size_t stage = 3 * (((size_t)3 * py * UMx * es + 127) & ~(size_t)127);
+  const int smem = (int)(kL0Stages * stage + 8 * kL0Stages + 128);
+  cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                          : cudaFuncSetAttribute(k_level0_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
   c->tma0_py = py;
   c->mode[0] = kModeTma0;
   return true;
@@ -279,8 +288,10 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
         const int yblocks = (a.M[1] + kL0TmaRows - 1) / kL0TmaRows;
         const unsigned blocks = (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + 1) / 2));
         // two 128-byte aligned stages, two mbarriers, and up to 127 bytes to align the base
-        const size_t stage = ((size_t)3 * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127;
-        k_level0_tma<T><<<blocks, kL0Threads, 2 * stage + 16 + 128, s>>>(a, c->tma0, c->tma0_py, c->err);
+        // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
+        const size_t stage = 3 * (((size_t)3 * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
+        k_level0_tma<T><<<blocks, kL0Threads, kL0Stages * stage + 8 * kL0Stages + 128, s>>>(a, c->tma0, c->tma0_py,
+                                                                                           c->err);
       }
       break;
     }

@@ -238,17 +238,19 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 }
 
 // TMA-staged form of k_level0_direct.  Block = 8 child rows (one per warp) x
-// 2 planes of one 128-probe chunk.  For every (channel, direction) the parent
-// tile of cascade 1's child-averaged radiance -- the full parent row width x
-// PY rows x 3 planes -- is brought into shared memory by one
-// cp.async.bulk.tensor while the previous tile is consumed (two stages, one
-// mbarrier each).  Lanes read their 4 parent columns from shared memory.
+// 2 planes of one 128-probe chunk.  For every direction the parent tiles of
+// cascade 1's child-averaged radiance -- per channel the full parent row width
+// x PY rows x 3 planes -- are brought into shared memory by three
+// cp.async.bulk.tensor copies while the previous direction's tiles are
+// consumed (two stages, one mbarrier each); one iteration serves all three
+// channels.  Lanes read their 4 parent columns from shared memory.
 // Every barrier wait is bounded: on timeout the block records *err = 1, waits
 // (bounded) for the copy it may still have in flight, and returns.
 constexpr int kL0TmaRows = 8;
+constexpr int kL0Stages = 2;  // parent tiles in flight: the copy for iteration it + 1 starts at iteration it
 
 template <typename T>
-__global__ void __launch_bounds__(kL0Threads, 4)
+__global__ void __launch_bounds__(kL0Threads, 2)
     k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int PY, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -258,11 +260,13 @@ __global__ void __launch_bounds__(kL0Threads, 4)
   // start at multiples of 128 from a 128-byte aligned base.
   const int tile_elems = 3 * PY * UMx;
   const uint32_t tile_bytes = (uint32_t)tile_elems * (uint32_t)sizeof(T);
-  const uint32_t stage_bytes = (tile_bytes + 127u) & ~127u;
+  const uint32_t tile_stride = (tile_bytes + 127u) & ~127u;  // one channel's tile, 128-byte aligned
+  const uint32_t stage_bytes = 3u * tile_stride;              // the three channels of one direction
   unsigned char* base = smem + ((128u - (smem_u32(smem) & 127u)) & 127u);
   T* tiles = reinterpret_cast<T*>(base);
   const int stage_elems = (int)(stage_bytes / sizeof(T));
-  uint64_t* bar = reinterpret_cast<uint64_t*>(base + 2 * stage_bytes);
+  const int tile_stride_elems = (int)(tile_stride / sizeof(T));
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base + kL0Stages * stage_bytes);
 
   const int chunks = (Mx + 127) >> 7, yblocks = (My + kL0TmaRows - 1) / kL0TmaRows;
   int bid = blockIdx.x;
@@ -325,116 +329,134 @@ __global__ void __launch_bounds__(kL0Threads, 4)
   T* L = static_cast<T*>(a.L);
   const int64_t plane = (int64_t)My * Mx;
   const int64_t p0 = ((int64_t)z0 * My + y) * Mx + x0;
-  const int total = 3 * a.ndirs;
+  const int64_t chstride = (int64_t)a.ndirs * a.P;  // one channel of L_0
+  const int total = a.ndirs;
 
+  // the three channel tiles of direction dd into stage st
+  auto issue = [&](int dd, int st) {
+    mbar_arrive_expect_tx(&bar[st], 3u * tile_bytes);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+      tma_load_3d(tiles + st * stage_elems + ch * tile_stride_elems, &tmap, 0, ys, (ch * a.ndirs + dd) * UMz + zs,
+                  &bar[st]);
+  };
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+#pragma unroll
+    for (int k = 0; k < kL0Stages; ++k) mbar_init(&bar[k], 1);
     mbar_fence_init();
   }
   __syncthreads();
   // a destination off its 128-byte boundary is reported and never copied to
-  const bool aligned = ((smem_u32(tiles) | stage_bytes) & 127u) == 0u;
+  const bool aligned = ((smem_u32(tiles) | tile_stride) & 127u) == 0u;
   if (threadIdx.x == 0) {
     if (aligned) {
-      mbar_arrive_expect_tx(&bar[0], tile_bytes);
-      tma_load_3d(tiles, &tmap, 0, ys, zs, &bar[0]);
+      for (int k = 0; k < kL0Stages - 1 && k < total; ++k) issue(k, k);
     } else {
       atomicExch(err, 2);
     }
   }
-  float flu[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+  float flu[3][2][4];
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) flu[ch][zc][0] = flu[ch][zc][1] = flu[ch][zc][2] = flu[ch][zc][3] = 0.f;
   int it = 0;
   bool failed = false;
 #pragma unroll 1
   for (; it < total; ++it) {
-    const int ch = it / a.ndirs, d = it - ch * a.ndirs;
-    const int st = it & 1;
-    if (threadIdx.x == 0 && it + 1 < total && aligned) {
-      // the other stage was released by the barrier at the end of the previous iteration
+    const int d = it;
+    const int st = it % kL0Stages;
+    const int nx_ = it + kL0Stages - 1;
+    // stage nx_ % S was last read in iteration it - 1 and released by its closing barrier
+    if (threadIdx.x == 0 && nx_ < total && aligned) {
       fence_proxy_async();
-      mbar_arrive_expect_tx(&bar[st ^ 1], tile_bytes);
-      tma_load_3d(tiles + (st ^ 1) * stage_elems, &tmap, 0, ys, (it + 1) * UMz + zs, &bar[st ^ 1]);
+      issue(nx_, nx_ % kL0Stages);
     }
-    const bool ok = mbar_wait_bounded(&bar[st], (it >> 1) & 1);
+    const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)(it / kL0Stages) & 1u);
     if (__syncthreads_or(!ok)) {
       failed = true;
       break;
     }
-    const T* tile = tiles + st * stage_elems;
     const DirInfo& di = a.dirs[d];
     const int ox = di.start_off[0] + 1, oy = di.start_off[1] + 1, oz = di.start_off[2] + 1;
     const int oct = ox + 2 * oy + 4 * oz;
     const bool hi_oct = oct >= 4;
     const unsigned opq = ((hi_oct ? oct_opq[1] : oct_opq[0]) >> (8 * (oct & 3))) & 0xFFu;
     const unsigned ems = ((hi_oct ? oct_ems[1] : oct_ems[0]) >> (8 * (oct & 3))) & 0xFFu;
-    float mv[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-    if (__any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u)) {
-      float zr[2][2][4];
-#pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        float cv[3][4];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const T* row = tile + rowoff[r][k];
-          cv[k][0] = to_float(row[lcol]);
-          cv[k][1] = to_float(row[c0]);
-          cv[k][2] = to_float(row[c0 + 1]);
-          cv[k][3] = to_float(row[rcol]);
-        }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          zr[0][r][c] = fmaf(0.25f, cv[0][c], 0.75f * cv[1][c]);
-          zr[1][r][c] = fmaf(0.75f, cv[1][c], 0.25f * cv[2][c]);
-        }
-      }
-#pragma unroll
-      for (int zc = 0; zc < 2; ++zc) {
-        float v[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) v[c] = fmaf(wy_lo, zr[zc][0][c], wy_hi * zr[zc][1][c]);
-        mv[zc][0] = fmaf(0.25f, v[0], 0.75f * v[1]);
-        mv[zc][1] = fmaf(0.75f, v[1], 0.25f * v[2]);
-        mv[zc][2] = fmaf(0.25f, v[1], 0.75f * v[2]);
-        mv[zc][3] = fmaf(0.75f, v[2], 0.25f * v[3]);
-      }
-    }
+    const bool merge = __any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u);
     const float om = di.omega;
-    T* lrow = L + (int64_t)(ch * a.ndirs + d) * a.P + p0;
+    T* lrow = L + (int64_t)d * a.P + p0;
 #pragma unroll
-    for (int zc = 0; zc < 2; ++zc) {
-      float o[4];
+    for (int ch = 0; ch < 3; ++ch) {
+      const T* tile = tiles + st * stage_elems + ch * tile_stride_elems;
+      float mv[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+      if (merge) {
+        float zr[2][2][4];
 #pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const int bit = zc * 4 + e;
-        o[e] = ((opq >> bit) & 1u) ? 0.f : mv[zc][e];
-        if ((ems >> bit) & 1u) {  // emissive start voxel (rare)
-          const int64_t vidx =
-              ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + 2 * (x0 + e) + ox;
-          o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
+        for (int r = 0; r < 2; ++r) {
+          float cv[3][4];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            const T* row = tile + rowoff[r][k];
+            cv[k][0] = to_float(row[lcol]);
+            cv[k][1] = to_float(row[c0]);
+            cv[k][2] = to_float(row[c0 + 1]);
+            cv[k][3] = to_float(row[rcol]);
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            zr[0][r][c] = fmaf(0.25f, cv[0][c], 0.75f * cv[1][c]);
+            zr[1][r][c] = fmaf(0.75f, cv[1][c], 0.25f * cv[2][c]);
+          }
         }
-        flu[zc][e] = fmaf(om, o[e], flu[zc][e]);
+#pragma unroll
+        for (int zc = 0; zc < 2; ++zc) {
+          float v[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) v[c] = fmaf(wy_lo, zr[zc][0][c], wy_hi * zr[zc][1][c]);
+          mv[zc][0] = fmaf(0.25f, v[0], 0.75f * v[1]);
+          mv[zc][1] = fmaf(0.75f, v[1], 0.25f * v[2]);
+          mv[zc][2] = fmaf(0.25f, v[1], 0.75f * v[2]);
+          mv[zc][3] = fmaf(0.75f, v[2], 0.25f * v[3]);
+        }
       }
-      if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + zc * plane, o[0], o[1], o[2], o[3]);
-    }
-    if (d == a.ndirs - 1) {
 #pragma unroll
       for (int zc = 0; zc < 2; ++zc) {
-        if ((valid >> (zc * 4)) & 1u) {
-          float* f = a.fluence + (p0 + zc * plane) * 3 + ch;
+        float o[4];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) f[3 * e] = flu[zc][e];
+        for (int e = 0; e < 4; ++e) {
+          const int bit = zc * 4 + e;
+          o[e] = ((opq >> bit) & 1u) ? 0.f : mv[zc][e];
+          if ((ems >> bit) & 1u) {  // emissive start voxel (rare)
+            const int64_t vidx =
+                ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + 2 * (x0 + e) + ox;
+            o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
+          }
+          flu[ch][zc][e] = fmaf(om, o[e], flu[ch][zc][e]);
         }
-        flu[zc][0] = flu[zc][1] = flu[zc][2] = flu[zc][3] = 0.f;
+        if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + ch * chstride + zc * plane, o[0], o[1], o[2], o[3]);
       }
     }
     __syncthreads();  // this stage may be refilled from the next iteration on
   }
+  if (!failed) {
+#pragma unroll
+    for (int zc = 0; zc < 2; ++zc) {
+      if (!((valid >> (zc * 4)) & 1u)) continue;
+      float* f = a.fluence + (p0 + zc * plane) * 3;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        f[3 * e] = flu[0][zc][e];
+        f[3 * e + 1] = flu[1][zc][e];
+        f[3 * e + 2] = flu[2][zc][e];
+      }
+    }
+  }
   if (failed && threadIdx.x == 0) {
     atomicExch(err, 1);
-    // the copies for iterations it and it + 1 may still be in flight: let them land first
-    (void)mbar_wait_bounded(&bar[it & 1], (it >> 1) & 1);
-    if (it + 1 < total) (void)mbar_wait_bounded(&bar[(it + 1) & 1], ((it + 1) >> 1) & 1);
+    // the copies for iterations it .. it + S - 1 may still be in flight: let them land first
+    for (int j = it; j < it + kL0Stages && j < total; ++j)
+      (void)mbar_wait_bounded(&bar[j % kL0Stages], (uint32_t)(j / kL0Stages) & 1u);
   }
 }
 

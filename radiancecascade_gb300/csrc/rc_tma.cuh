@@ -37,13 +37,30 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
+// try_wait that lets the hardware suspend the thread until the phase
+// completes or `ns` nanoseconds pass, instead of spinning.
+__device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t parity, uint32_t ns) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(ns)
+      : "memory");
+  return done != 0;
+}
+
 // Waits for the barrier phase with a time limit (about one second of SM
-// clocks); returns false when the limit ran out.
+// clocks); returns false when the limit ran out.  The thread is suspended
+// between checks (up to 20 us each), so waiting warps take no issue slots.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long start = clock64();
   while (clock64() - start < 2000000000ll)
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_suspend(bar, parity, 20000u)) return true;
   return false;
 }
 
