@@ -244,8 +244,12 @@ bool setup_tma0(rc_context* c) {
                          const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return false;
-  // kL0Stages 128-byte aligned stages, their barriers and up to 127 bytes to align the base
-  const size_t stage = 3 * (((size_t)3 * py * UMx * es + 127) & ~(size_t)127);
+  // The shared-memory limit is a property of the kernel, not of this context:
+  // set it to the largest any context needs (parent rows of up to 256 FP32
+  // values; kL0Stages stages of three 128-byte aligned channel tiles, their
+  // barriers and up to 127 bytes to align the base), so that a later context
+  // never lowers it under an earlier one.
+  const size_t stage = 3 * (((size_t)3 * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
   const int smem = (int)(kL0Stages * stage + 8 * kL0Stages + 128);
   cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
                           : cudaFuncSetAttribute(k_level0_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -44,7 +44,12 @@ struct QueueArgs {
   QueueLevel lv[kMaxCascades];
 };
 
-// One lane's walk of one queue item, advanced kWalkBatch steps at a time.
+// One lane's walk of one queue item, advanced kBatch steps at a time.  The
+// voxel offset a = (cell c, phase ph) per axis is kept split (a = c s + ph):
+// a step moves one phase by +-1 and only when it wraps does the coarse cell
+// change -- and with it the set of probes still inside the grid in x and y
+// (inr) and whether the z plane exists (zin), which are therefore recomputed
+// only then.
 struct Walker {
   const uint32_t* mask;
   uint32_t* rec;
@@ -54,7 +59,21 @@ struct Walker {
   uint32_t valid, done, hits;
   int ax, ay, az, tx, ty, tz, k;
   int sx, sy, sz, dx, dy, dz;
+  int px, py, pz, cx, cy, cz;  // phase and coarse cell of the current offset
+  uint32_t inr;                // probes whose current voxel is inside the grid in x and y
+  bool zin;                    // the current z plane lies inside the grid
   bool first;
+
+  __device__ __forceinline__ void cell_changed() {
+    const int Px = 1 << l2px;
+    if (l2px >= 5) {
+      inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+    } else {
+      inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * rep;
+      inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+    }
+    zin = (unsigned)(zl + cz) < (unsigned)Mz;
+  }
 
   // Returns false when the item holds no probe.
   __device__ __forceinline__ bool init(const QueueArgs& q, int64_t item) {
@@ -103,17 +122,24 @@ struct Walker {
     dz = di.step_T[2];
     k = di.steps;
     first = L.test_start != 0;
+    const int sm = (1 << l2s) - 1;
+    px = ax & sm;
+    py = ay & sm;
+    pz = az & sm;
+    cx = ax >> l2s;
+    cy = ay >> l2s;
+    cz = az >> l2s;
+    cell_changed();
     return true;
   }
 
   // Walks up to kBatch steps; returns true when the item is finished.
   template <int kBatch>
   __device__ __forceinline__ bool batch(const QueueArgs& q) {
-    const int s = 1 << l2s, Px = 1 << l2px;
-    const int64_t phase_stride = (int64_t)Mz * wpp;
-    const uint32_t* zbase = mask + (int64_t)zl * wpp;
-    int bx_[kBatch], by_[kBatch], bz_[kBatch];
-    uint32_t lo_[kBatch], hi_[kBatch];
+    const int sm = (1 << l2s) - 1, Px = 1 << l2px;
+    const int mzw = Mz * wpp;  // words per phase
+    int bx_[kBatch], by_[kBatch], bz_[kBatch], gs_[kBatch];
+    uint32_t lo_[kBatch], hi_[kBatch], inr_[kBatch];
     bool ok_[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -126,12 +152,24 @@ struct Walker {
         const bool px_ = (tx <= ty) & (tx <= tz);
         const bool py_ = !px_ & (ty <= tz);
         const bool pz_ = !px_ & !py_;
-        ax += px_ ? sx : 0;
+        const int ex = px_ ? sx : 0, ey = py_ ? sy : 0, ez = pz_ ? sz : 0;
+        ax += ex;
+        ay += ey;
+        az += ez;
         tx += px_ ? dx : 0;
-        ay += py_ ? sy : 0;
         ty += py_ ? dy : 0;
-        az += pz_ ? sz : 0;
         tz += pz_ ? dz : 0;
+        const int nx = px + ex, ny = py + ey, nz = pz + ez;
+        const int wx = nx >> l2s, wy = ny >> l2s, wz = nz >> l2s;  // -1, 0 or +1
+        px = nx & sm;
+        py = ny & sm;
+        pz = nz & sm;
+        if ((wx | wy | wz) != 0) {  // crossed into another coarse cell (every s-th step on an axis)
+          cx += wx;
+          cy += wy;
+          cz += wz;
+          cell_changed();
+        }
         step_ok = true;
       } else {
         step_ok = false;
@@ -139,30 +177,20 @@ struct Walker {
       bx_[u] = ax;
       by_[u] = ay;
       bz_[u] = az;
-      ok_[u] = step_ok;
-      const int zc = zl + (az >> l2s);
-      const bool zin = step_ok && (unsigned)zc < (unsigned)Mz;
-      const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
-      const uint32_t* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * wpp;
-      const int q0 = (g0 + (ay >> l2s) * Px + (ax >> l2s)) >> 5;
-      lo_[u] = (zin && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
-      hi_[u] = (zin && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
+      ok_[u] = step_ok && zin;
+      inr_[u] = step_ok ? inr : 0u;
+      const int gs = g0 + cy * Px + cx;
+      gs_[u] = gs;
+      const int q0 = gs >> 5;
+      const uint32_t* plane = mask + ((((pz << l2s) + py) << l2s) + px) * mzw + (zl + cz) * wpp;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
+      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (!ok_[u]) return true;
-      const int cz = bz_[u] >> l2s, cy = by_[u] >> l2s, cx = bx_[u] >> l2s;
-      if ((unsigned)(zl + cz) >= (unsigned)Mz) return true;
-      uint32_t inr;
-      if (l2px >= 5) {
-        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
-      } else {
-        inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * rep;
-        inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
-      }
-      done |= ~inr;
-      const int gs = g0 + cy * Px + cx;
-      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs & 31) & ~done;
+      if (!ok_[u]) return true;  // interval finished, or the walk left the grid in z
+      done |= ~inr_[u];
+      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs_[u] & 31) & ~done;
       if (nw) {
         done |= nw;
         hits |= nw;

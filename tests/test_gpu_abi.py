@@ -134,3 +134,24 @@ def test_cpp_driver_solve_matches_python_binding(tmp_path):
         e.solve()
         want = e.fluence().reshape(-1)
     assert np.array_equal(got, want)
+
+
+def test_contexts_of_different_sizes_coexist():
+    """A context created after a larger one must not break the larger one's
+    kernels (per-kernel launch limits are shared by all contexts)."""
+    spec = R.scene_spec(96, 10, (3, 12), 3, (1.5, 4.0), (1.0, 20.0))
+    boxes, spheres = R.generate_scene(spec, 3)
+    big = R.Engine(R.make_params(96, 5))
+    small = R.Engine(R.make_params(32, 3))
+    try:
+        big.set_boxes(boxes)
+        big.set_spheres(spheres)
+        small.upload(O.voxelise(32, np.zeros(0, R.BOX_DT), np.zeros(0, R.SPHERE_DT)))
+        small.solve()
+        big.solve()
+        got = big.fluence().astype(np.float64)
+        want, _ = O.solve(O.params(96, 5), O.voxelise(96, boxes, spheres), jump=True)
+        assert rel_l2(got, want) <= 1e-4
+    finally:
+        small.close()
+        big.close()
