@@ -46,6 +46,33 @@ WORKLOAD_DESC = ("256^3 voxels, 400 seeded opaque boxes (edges 4-48), 32 emissiv
                  "x4 dirs and /2 probes per axis per level, intervals 0,1,5,21,85,341,1365")
 
 
+def init_replicas(world: int, local: int):
+    """One process per GPU: the process group (NCCL on GPUs, gloo on CPU) when
+    world > 1, else None.  Rendezvous from MASTER_ADDR / MASTER_PORT."""
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return dist
+
+
+def max_over_ranks(value: float, dist) -> float:
+    """The slowest rank's figure (wall or event time): the job is done when it is."""
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_first_frame(rank: int, steps: int, warmup: int) -> int:
+    """Replicas solve disjoint frame ranges of the moving-emitter workload."""
+    return rank * (steps + warmup)
+
+
 def _env_int(name, default):
     try:
         return int(os.environ.get(name, default))
@@ -274,11 +301,8 @@ def run_batch(args, rank, world):
     import torch
     import radiancecascade_gb300 as R
 
-    dist = None
     local = _env_int("LOCAL_RANK", 0)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dist = init_replicas(world, local)
     torch.cuda.set_device(local)
     items = R.batch_workload()
     prec = args.precision
@@ -305,11 +329,7 @@ def run_batch(args, rank, world):
     b.synchronize()
     torch.cuda.synchronize()
     clock_info = clocks.stop()
-    ms = t0.elapsed_time(t1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(t0.elapsed_time(t1), dist)
     value = world * len(items) * args.steps / (ms / 1000.0)
 
     # the same scenes as separate contexts (fastest per-level kernels), one after another
@@ -348,11 +368,7 @@ def run_batch(args, rank, world):
         b.solve()
         for k in range(len(items)):
             outs[k][:] = b.fluence(k).reshape(-1)
-    e2e_s = time.perf_counter() - w0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - w0, dist)
     e2e_value = world * len(items) * e2e_steps / e2e_s
 
     elem = 2 if prec == "fp16" else 4
@@ -504,10 +520,7 @@ def main():
     import torch
     import radiancecascade_gb300 as R
 
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dist = init_replicas(world, local)
     torch.cuda.set_device(local)
 
     boxes, spheres = R.workload_scene(WORKLOAD)
@@ -518,7 +531,7 @@ def main():
     # replicas: rank r starts at frame r * steps so the ranks solve different frames
     sph = spheres.copy()
     if rank:
-        R.advance_spheres(sph, 256, rank * (args.steps + args.warmup))
+        R.advance_spheres(sph, 256, replica_first_frame(rank, args.steps, args.warmup))
     stream = torch.cuda.ExternalStream(eng.stream(), device=local)
 
     for _ in range(args.warmup):
@@ -543,11 +556,8 @@ def main():
     t_end.synchronize()
     torch.cuda.synchronize()
     clock_info = clocks.stop()
-    ms = t_start.elapsed_time(t_end)
+    ms = max_over_ranks(t_start.elapsed_time(t_end), dist)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     value = world * args.steps / (ms / 1000.0)
     # recompose + one kernel per cascade + the shared walk of the narrow levels
@@ -572,11 +582,7 @@ def main():
         eng.fluence_async(host_out[f & 1])
         R.advance_spheres(sph, 256, 1)
     eng.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
     e2e_value = world * args.steps / e2e_s
 
     # ---- roofline of the level kernels (CUDA events around every launch)
