@@ -200,6 +200,8 @@ def learned_form(args, R, local, boxes, spheres, plain_fps):
     cascades 2-5 from the neural radiance cache, refit every frame on a 1/16
     slice of walked probes, per-8^3-tile fallback at 1% held-out error.  The
     cache first learns for `learned_warmup` frames; the timed frames follow."""
+    import torch
+
     from oracle import oracle as O
     out = {}
     eng = R.Engine(R.make_params(256, 6, precision="fp16"), device=local)
@@ -211,13 +213,16 @@ def learned_form(args, R, local, boxes, spheres, plain_fps):
     eng.synchronize()
     ms, _ = timed_frames(eng, R, sph.copy(), args.steps, local)
     out["plain_fp16_frames_per_s"] = round(args.steps / (ms / 1000.0), 3)
-    eng.nrc_enable()
+    eng.nrc_enable(first_level=args.learned_first_level, fallback_threshold=args.learned_threshold,
+                   plain_level_fraction=args.learned_plain_fraction)
     for _ in range(args.learned_warmup):
         eng.set_spheres(sph)
         eng.solve()
         R.advance_spheres(sph, 256, 1)
     eng.synchronize()
+    torch.cuda.nvtx.range_push("learned_timed")  # launch lists of the learned frames select this range
     ms, last = timed_frames(eng, R, sph, args.steps, local)
+    torch.cuda.nvtx.range_pop()
     fps = args.steps / (ms / 1000.0)
     g = eng.fluence().astype(np.float64)
     st = eng.nrc_stats()
@@ -230,6 +235,8 @@ def learned_form(args, R, local, boxes, spheres, plain_fps):
         "fallback_tiles": int(st["fallback_tiles"]), "tiles": int(st["tiles"]),
         "cascades_from_network": [i for i in range(6) if (st["served_levels"] >> i) & 1],
         "frames_learned_before_timing": args.learned_warmup, "frames_timed": args.steps,
+        "first_level": args.learned_first_level, "fallback_threshold": args.learned_threshold,
+        "plain_level_fraction": args.learned_plain_fraction,
         "storage": "radiance f16, network bf16 with f32 accumulation",
     })
     return out
@@ -504,6 +511,11 @@ def main():
     ap.add_argument("--learned-warmup", type=int, default=48,
                     help="frames the radiance cache learns before the learned form is timed")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned+FP16 form")
+    ap.add_argument("--learned-first-level", type=int, default=2, help="first cascade the radiance cache serves")
+    ap.add_argument("--learned-threshold", type=float, default=0.01,
+                    help="held-out relative error above which a tile falls back to the plain walk")
+    ap.add_argument("--learned-plain-fraction", type=float, default=0.5,
+                    help="a cascade runs its plain kernels when this fraction of its probes is in fallback tiles")
     ap.add_argument("--workload", default="c256", choices=["c256", "batch64", "render"],
                     help="c256: the 256^3 moving-emitter frame (default); batch64: 64 uneven scenes")
     args = ap.parse_args()

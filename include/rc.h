@@ -347,8 +347,8 @@ typedef struct rc_nrc_stats {
   float last_loss;         /* mean squared error of the last step            */
   int32_t served_levels;   /* bit i: cascade i came from the network in the
                               last solve (else its plain kernels ran)       */
-  int64_t fallback_tiles;  /* tiles on the plain walk now                    */
-  int64_t tiles;           /* all tiles                                      */
+  int64_t fallback_tiles;  /* of `tiles`, those on the plain walk now       */
+  int64_t tiles;           /* fallback tiles that hold a far-cascade probe  */
 } rc_nrc_stats;
 
 rc_status rc_nrc_params_default(rc_nrc_params* out);

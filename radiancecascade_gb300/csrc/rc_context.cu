@@ -331,10 +331,34 @@ void launch_level(const rc_context* c, int level, cudaStream_t s) {
 }
 
 // The walks of every queue level, in one launch (they depend only on the scene).
-void launch_queue_walk(const rc_context* c, cudaStream_t s) {
+// Walks of the queued levels, except the cascades set in `skip` (bit i =
+// cascade i).  Each level's records have their own place, so a subset of the
+// levels walks in a launch of its own with the items renumbered.
+void launch_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip = 0) {
   if (!c->queue_blocks) return;
+  const QueueArgs* q = &c->qargs;
+  QueueArgs sub;
+  bool subset = false;
+  for (int k = 0; k < c->qargs.n; ++k) subset |= ((skip >> c->qargs.lv[k].level) & 1u) != 0;
+  if (subset) {
+    sub = c->qargs;
+    sub.n = 0;
+    sub.total = 0;
+    for (int k = 0; k < c->qargs.n; ++k) {
+      const QueueLevel& L = c->qargs.lv[k];
+      if ((skip >> L.level) & 1u) continue;
+      sub.lv[sub.n] = L;
+      sub.lv[sub.n].item_begin = sub.total;
+      sub.total += (int64_t)L.slots * c->geom[L.level].ndirs;
+      ++sub.n;
+    }
+    if (!sub.n) return;
+    q = &sub;
+  }
+  // queue_blocks is already capped at one resident wave
+  const int64_t blocks = std::min<int64_t>((q->total + kQueueThreads - 1) / kQueueThreads, c->queue_blocks);
   cudaMemsetAsync(c->qcounter, 0, sizeof(unsigned long long), s);
-  k_walk_queue<<<(unsigned)c->queue_blocks, kQueueThreads, 0, s>>>(c->qargs);
+  k_walk_queue<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
 }
 
 }  // namespace
@@ -344,7 +368,7 @@ void plain_level(const rc_context* c, int level, cudaStream_t s) {
   if (c->elem == 2) launch_level<__half>(c, level, s);
   else launch_level<float>(c, level, s);
 }
-void plain_queue_walk(const rc_context* c, cudaStream_t s) { launch_queue_walk(c, s); }
+void plain_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip) { launch_queue_walk(c, s, skip); }
 bool level_uses_queue(const rc_context* c, int level) { return c->mode[level] == kModeQueue; }
 }  // namespace rcx
 
@@ -359,7 +383,8 @@ rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
     near = nrc_first_level(c);
     bool queue_near = false;
     for (int i = 0; i < near; ++i) queue_near |= c->mode[i] == kModeQueue;
-    if (queue_near) launch_queue_walk(c, s);
+    // the far levels' walks, where they run at all, are launched by the cache
+    if (queue_near) launch_queue_walk(c, s, ~((1u << near) - 1u));
     rc_status st = nrc_enqueue_far(c, s);
     if (st != RC_OK) return st;
   } else {
@@ -430,6 +455,7 @@ void setup_queue(rc_context* c, uint32_t* recs, unsigned long long* counter) {
     for (int ax = 0; ax < 3; ++ax) L.M[ax] = a.M[ax];
     L.rep = a.rep;
     L.test_start = (i == 0);
+    L.level = i;
   }
   q.n = n;
   q.total = items;

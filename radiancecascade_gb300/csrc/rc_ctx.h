@@ -108,7 +108,8 @@ struct DeviceGuard {
 // Plain solve of one level (its usual kernel), the walk queue of the narrow
 // levels, and whether a level reads walk records (rc_context.cu).
 void plain_level(const rc_context* c, int level, cudaStream_t s);
-void plain_queue_walk(const rc_context* c, cudaStream_t s);
+// Walks of the queued levels except those set in `skip` (bit i = cascade i).
+void plain_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip);
 bool level_uses_queue(const rc_context* c, int level);
 
 // Neural radiance cache hooks (rc_nrc.cu).

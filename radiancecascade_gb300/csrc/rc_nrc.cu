@@ -33,6 +33,7 @@ struct NrcState {
   // tiles of the sample probes (all their directions), grouped by phase
   NrcTile* tiles = nullptr;
   std::vector<NrcTile> h_tiles;
+  std::vector<uint8_t> probe_tile;  // tiles that hold a far probe
   std::vector<int64_t> tile_begin;
   int64_t max_tiles2 = 0, max_held = 0;
   float* target = nullptr;
@@ -104,8 +105,10 @@ rc_status check(const rc_context* c, const char* fn, bool need_nrc) {
 unsigned blocks_for(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads); }
 
 void launch_adam(float* p, float* g, float* m, float* v, __half* half_out, int64_t count, const rc_nrc_params& prm,
-                 int64_t t, cudaStream_t s) {
+                 int64_t t, bool lazy, cudaStream_t s) {
   AdamArgs a;
+  a.lazy = lazy ? 1 : 0;
+  a.pad = 0;
   a.p = p;
   a.g = g;
   a.m = m;
@@ -253,8 +256,9 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
       a.inv_batch = 1.f / (float)std::max<int64_t>(rows, 1);
       k_nrc_train<<<(unsigned)std::min<int64_t>(a1 - a0, n->train_blocks), kNrcThreads, kTrainSmem, s>>>(a);
       ++n->steps;
-      launch_adam(n->mlp, n->mlp_g, n->mlp_m, n->mlp_v, nullptr, kNrcParams, n->prm, n->steps, s);
-      launch_adam(n->hash_master, n->hash_g, n->hash_m, n->hash_v, n->hash_half, n->hash_n, n->prm, n->steps, s);
+      launch_adam(n->mlp, n->mlp_g, n->mlp_m, n->mlp_v, nullptr, kNrcParams, n->prm, n->steps, false, s);
+      launch_adam(n->hash_master, n->hash_g, n->hash_m, n->hash_v, n->hash_half, n->hash_n, n->prm, n->steps, true,
+                  s);
       launch_pack(n, s);
     }
     RC_CUDA(cudaMemcpyAsync(n->h_loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "cache loss");
@@ -277,7 +281,13 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     }
   }
   inf.tile0[c->nlev] = t0;
-  if (queue_plain) plain_queue_walk(c, s);
+  if (queue_plain) {
+    // near levels walked before the cache ran; served levels need no walk
+    uint32_t skip = (1u << n->first) - 1u;
+    for (int i = n->first; i < c->nlev; ++i)
+      if (n->served[i]) skip |= 1u << i;
+    plain_queue_walk(c, s, skip);
+  }
   if (any_served) {
     k_nrc_forward<true><<<(unsigned)std::min<int64_t>(t0, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(inf, t0);
     NrcFallbackArgs f;
@@ -504,6 +514,17 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   RC_CUDA(cudaMemset(n->tnum, 0, cells * 4), "rc_nrc_enable: memset");
   RC_CUDA(cudaMemset(n->tden, 0, cells * 4), "rc_nrc_enable: memset");
   RC_CUDA(cudaMemset(n->flag, 1, cells), "rc_nrc_enable: memset");
+  n->probe_tile.assign((size_t)cells, 0);
+  for (int i = n->first; i < c->nlev; ++i) {
+    const LevelGeom& gm = c->geom[i];
+    const int h = gm.spacing >> 1;
+    for (int z = 0; z < gm.M[2]; ++z)
+      for (int y = 0; y < gm.M[1]; ++y)
+        for (int x = 0; x < gm.M[0]; ++x)
+          n->probe_tile[((size_t)((z * gm.spacing + h) >> n->tile_shift) * n->TY + ((y * gm.spacing + h) >> n->tile_shift)) *
+                            n->TX +
+                        ((x * gm.spacing + h) >> n->tile_shift)] = 1;
+  }
   // kernels: shared memory and resident blocks
   RC_CUDA(cudaFuncSetAttribute(k_nrc_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem),
           "rc_nrc_enable: attribute");
@@ -624,10 +645,13 @@ rc_status rc_nrc_get_stats(rc_context* c, rc_nrc_stats* out) {
   out->solves = n->solves;
   out->steps = n->steps;
   out->last_loss = n->loss_rows ? *n->h_loss / (float)n->loss_rows : 0.f;
-  out->fallback_tiles = std::count(f.begin(), f.end(), (uint8_t)1);
+  for (int64_t t = 0; t < cells; ++t)
+    if (n->probe_tile[(size_t)t]) {
+      ++out->tiles;
+      out->fallback_tiles += f[(size_t)t] ? 1 : 0;
+    }
   for (int i = n->first; i < c->nlev; ++i)
     if (n->served[i]) out->served_levels |= 1 << i;
-  out->tiles = cells;
   return RC_OK;
 }
 

@@ -594,11 +594,17 @@ struct AdamArgs {
   int64_t n;
   float lr, beta1, beta2, eps;
   float c1, c2;  // bias corrections 1 - beta^t
+  int32_t lazy;  // skip entries whose gradient is exactly zero (hash table)
+  int32_t pad;
 };
 
+// Adam step.  With `lazy`, an entry no training sample touched this step
+// (gradient exactly 0) keeps its value and moments, as Mueller et al. 2022 do
+// for the hash table: a step then writes only the touched entries.
 __global__ void k_nrc_adam(const __grid_constant__ AdamArgs a) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
     const float g = a.g[i];
+    if (a.lazy && g == 0.f) continue;
     const float m = fmaf(a.beta1, a.m[i], (1.f - a.beta1) * g);
     const float v = fmaf(a.beta2, a.v[i], (1.f - a.beta2) * g * g);
     a.m[i] = m;

@@ -30,7 +30,7 @@ struct QueueLevel {
   int32_t M[3];
   uint32_t rep;
   int32_t test_start;  // level 0: the probe's own voxel belongs to the interval
-  int32_t pad;
+  int32_t level;       // cascade index
 };
 
 struct QueueArgs {
