@@ -71,7 +71,7 @@ void release(rc_context* c) {
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg};
+  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg, c->d_slist};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -92,6 +92,10 @@ rc_status check_ctx(const rc_context* c, const char* fn) {
   return RC_OK;
 }
 
+// Sphere-list entries per sphere of capacity: the lists of one update hold at
+// most this many entries per sphere, else every region tests all spheres.
+constexpr int kSphereListCap = 8;
+
 // Grow the sphere/region device buffers and the pinned staging area.
 rc_status ensure_sphere_capacity(rc_context* c, int n) {
   if (n <= c->sph_cap) return RC_OK;
@@ -104,16 +108,20 @@ rc_status ensure_sphere_capacity(rc_context* c, int n) {
     }
   if (c->d_sph) cudaFree(c->d_sph);
   if (c->d_reg) cudaFree(c->d_reg);
+  if (c->d_slist) cudaFree(c->d_slist);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   c->d_sph = nullptr;
   c->d_reg = nullptr;
+  c->d_slist = nullptr;
   c->h_stage = nullptr;
   c->sph_cap = 0;
   rc_status s = dev_alloc((void**)&c->d_sph, sizeof(QSphere) * cap, "sphere buffer");
   if (s != RC_OK) return s;
   s = dev_alloc((void**)&c->d_reg, sizeof(Region) * (2 * cap + 1), "region buffer");
   if (s != RC_OK) return s;
-  c->slot_bytes = sizeof(QSphere) * cap + sizeof(Region) * (2 * cap + 1);
+  s = dev_alloc((void**)&c->d_slist, sizeof(int32_t) * kSphereListCap * cap, "sphere list buffer");
+  if (s != RC_OK) return s;
+  c->slot_bytes = sizeof(QSphere) * cap + sizeof(Region) * (2 * cap + 1) + sizeof(int32_t) * kSphereListCap * cap;
   RC_CUDA(cudaMallocHost(&c->h_stage, 2 * c->slot_bytes), "pinned staging buffer");
   c->sph_cap = cap;
   return RC_OK;
@@ -133,7 +141,7 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
     RC_CUDA(cudaEventSynchronize(c->ev_stage[k]), "staging wait");
     c->stage_pending[k] = false;
   }
-  Region whole{0, c->W, 0, c->p.grid[1], 0, c->p.grid[2], {0, 0}};
+  Region whole{0, c->W, 0, c->p.grid[1], 0, c->p.grid[2], 0, -1};
   if (!regions) {
     regions = &whole;
     nreg = 1;
@@ -141,11 +149,48 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
   if (nreg == 0) return RC_OK;
   char* st = static_cast<char*>(c->h_stage) + k * c->slot_bytes;
   if (n) memcpy(st, c->cur.data(), sizeof(QSphere) * n);
-  memcpy(st + sizeof(QSphere) * c->sph_cap, regions, sizeof(Region) * nreg);
+  Region* sreg = reinterpret_cast<Region*>(st + sizeof(QSphere) * c->sph_cap);
+  int32_t* slist = reinterpret_cast<int32_t*>(st + sizeof(QSphere) * c->sph_cap + sizeof(Region) * (2 * c->sph_cap + 1));
+  memcpy(sreg, regions, sizeof(Region) * nreg);
+  // per-region lists of the spheres whose extent meets the region (a region
+  // of the whole grid, or an update whose lists would not fit, tests them all)
+  int64_t listed = 0;
+  const int64_t list_cap = (int64_t)kSphereListCap * c->sph_cap;
+  bool lists = n > 0 && (int64_t)nreg * n <= (int64_t)1 << 22;
+  std::vector<Region> ext;
+  if (lists) {
+    ext.resize(n);
+    for (int i = 0; i < n; ++i)
+      if (!sphere_region(c->cur[i], c->p.grid, &ext[i])) ext[i].w1 = ext[i].w0;  // empty: meets nothing
+  }
+  for (int r = 0; r < nreg && lists; ++r) {
+    Region& g = sreg[r];
+    g.s0 = (int32_t)listed;
+    g.sn = 0;
+    for (int i = 0; i < n; ++i) {
+      const Region& e = ext[i];
+      if (e.w0 < g.w1 && g.w0 < e.w1 && e.y0 < g.y1 && g.y0 < e.y1 && e.z0 < g.z1 && g.z0 < e.z1) {
+        if (listed == list_cap) {
+          lists = false;
+          break;
+        }
+        slist[listed++] = i;
+        ++g.sn;
+      }
+    }
+  }
+  if (!lists) {
+    listed = 0;
+    for (int r = 0; r < nreg; ++r) {
+      sreg[r].s0 = 0;
+      sreg[r].sn = -1;
+    }
+  }
   RC_CUDA(cudaMemcpyAsync(c->d_sph, st, sizeof(QSphere) * n, cudaMemcpyHostToDevice, c->stream), "sphere upload");
-  RC_CUDA(cudaMemcpyAsync(c->d_reg, st + sizeof(QSphere) * c->sph_cap, sizeof(Region) * nreg,
-                          cudaMemcpyHostToDevice, c->stream),
-          "region upload");
+  RC_CUDA(cudaMemcpyAsync(c->d_reg, sreg, sizeof(Region) * nreg, cudaMemcpyHostToDevice, c->stream), "region upload");
+  if (listed)
+    RC_CUDA(cudaMemcpyAsync(c->d_slist, slist, sizeof(int32_t) * listed, cudaMemcpyHostToDevice, c->stream),
+            "sphere list upload");
   RC_CUDA(cudaEventRecord(c->ev_stage[k], c->stream), "event record");
   c->stage_pending[k] = true;
   int64_t words = 0;
@@ -157,7 +202,7 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
   blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
   k_compose_masks<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
       c->base, c->vol, c->occ, c->emis, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, c->d_sph, n, c->d_reg,
-      c->mset);
+      c->d_slist, c->mset);
   RC_CUDA(cudaGetLastError(), "compose launch");
   return RC_OK;
 }
@@ -291,7 +336,6 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
       if (L0 && !TOP) {
         const int yblocks = (a.M[1] + kL0TmaRows - 1) / kL0TmaRows;
         const unsigned blocks = (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + 1) / 2));
-        // two 128-byte aligned stages, two mbarriers, and up to 127 bytes to align the base
         // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
         const size_t stage = 3 * (((size_t)3 * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
         k_level0_tma<T><<<blocks, kL0Threads, kL0Stages * stage + 8 * kL0Stages + 128, s>>>(a, c->tma0, c->tma0_py,
@@ -330,10 +374,10 @@ void launch_level(const rc_context* c, int level, cudaStream_t s) {
   }
 }
 
-// The walks of every queue level, in one launch (they depend only on the scene).
 // Walks of the queued levels, except the cascades set in `skip` (bit i =
-// cascade i).  Each level's records have their own place, so a subset of the
-// levels walks in a launch of its own with the items renumbered.
+// cascade i), in one launch (they depend only on the scene).  Each level's
+// records have their own place, so a subset of the levels walks in a launch
+// of its own with the items renumbered.
 void launch_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip = 0) {
   if (!c->queue_blocks) return;
   const QueueArgs* q = &c->qargs;
@@ -357,7 +401,7 @@ void launch_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip = 0) {
   }
   // queue_blocks is already capped at one resident wave
   const int64_t blocks = std::min<int64_t>((q->total + kQueueThreads - 1) / kQueueThreads, c->queue_blocks);
-  cudaMemsetAsync(c->qcounter, 0, sizeof(unsigned long long), s);
+  cudaMemsetAsync(q->counter, 0, sizeof(unsigned long long), s);
   k_walk_queue<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
 }
 
@@ -390,10 +434,7 @@ rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
   } else {
     launch_queue_walk(c, s);
   }
-  for (int i = near - 1; i >= 0; --i) {
-    if (c->elem == 2) launch_level<__half>(c, i, s);
-    else launch_level<float>(c, i, s);
-  }
+  for (int i = near - 1; i >= 0; --i) plain_level(c, i, s);
   return RC_OK;
 }
 
@@ -824,10 +865,32 @@ rc_status rc_scene_set_spheres(rc_context* c, const rc_sphere* spheres, int32_t 
   std::vector<Region> regs;
   bool full = (int)c->cur.size() != n;
   if (!full) {
+    // A sphere's old and new extents become one region (their bounding box)
+    // when that box is no larger than the two apart -- the usual case of a
+    // sphere moving a voxel or less per frame, which overlaps itself.
+    auto words = [](const Region& r) { return (int64_t)(r.w1 - r.w0) * (r.y1 - r.y0) * (r.z1 - r.z0); };
     for (int i = 0; i < n; ++i) {
-      Region r;
-      if (sphere_region(c->cur[i], c->p.grid, &r)) regs.push_back(r);
-      if (sphere_region(next[i], c->p.grid, &r)) regs.push_back(r);
+      Region a, b;
+      const bool ha = sphere_region(c->cur[i], c->p.grid, &a), hb = sphere_region(next[i], c->p.grid, &b);
+      if (ha && hb) {
+        Region u = a;
+        u.w0 = std::min(a.w0, b.w0);
+        u.w1 = std::max(a.w1, b.w1);
+        u.y0 = std::min(a.y0, b.y0);
+        u.y1 = std::max(a.y1, b.y1);
+        u.z0 = std::min(a.z0, b.z0);
+        u.z1 = std::max(a.z1, b.z1);
+        if (words(u) <= words(a) + words(b)) {
+          regs.push_back(u);
+        } else {
+          regs.push_back(a);
+          regs.push_back(b);
+        }
+      } else if (ha) {
+        regs.push_back(a);
+      } else if (hb) {
+        regs.push_back(b);
+      }
     }
   }
   c->cur.swap(next);

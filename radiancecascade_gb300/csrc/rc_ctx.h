@@ -66,6 +66,7 @@ struct rc_context {
   // dynamic spheres
   rcx::QSphere* d_sph = nullptr;
   rcx::Region* d_reg = nullptr;
+  int32_t* d_slist = nullptr;  // per-region sphere lists
   int sph_cap = 0;
   void* h_stage = nullptr;  // pinned, two slots of (spheres, regions)
   size_t slot_bytes = 0;

@@ -186,7 +186,8 @@ bool sphere_region(const QSphere& q, const int32_t grid[3], Region* r) {
   r->y1 = (int32_t)hi[1];
   r->z0 = (int32_t)lo[2];
   r->z1 = (int32_t)hi[2];
-  r->pad[0] = r->pad[1] = 0;
+  r->s0 = 0;
+  r->sn = -1;
   return true;
 }
 

@@ -63,7 +63,7 @@ struct Region {
   int32_t w0, w1;  // x words
   int32_t y0, y1;
   int32_t z0, z1;
-  int32_t pad[2];
+  int32_t s0, sn;  // spheres that may cover the region: list[s0 .. s0 + sn), or all when sn < 0
 };
 
 }  // namespace rcx

@@ -103,13 +103,16 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
 }
 
 // Composed volume, full-resolution opacity and emissive bits, and every
-// level's decimated opacity over a list of regions (composition rule as in
-// k_compose).
+// level's decimated opacity over a list of regions.  A voxel whose centre is
+// inside a sphere takes the value of the last such sphere of the list, else
+// its base value.  Each region tests only its own list of spheres (ascending
+// indices), or all of them.
 static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ,
                                 uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W,
                                 const QSphere* __restrict__ sph, int ns, const Region* __restrict__ regs,
-                                const MaskSet ms) {
+                                const int32_t* __restrict__ slist, const MaskSet ms) {
   const Region r = regs[blockIdx.y];
+  const int nt = r.sn < 0 ? ns : r.sn;
   const int64_t nw = r.w1 - r.w0, ny = r.y1 - r.y0, nz = r.z1 - r.z0;
   const int64_t words = nw * ny * nz;
   const int lane = threadIdx.x & 31;
@@ -125,8 +128,8 @@ static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __
       const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
       uint2 v = base[idx];
       const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
-      for (int s = 0; s < ns; ++s) {
-        const QSphere& S = sph[s];
+      for (int k = 0; k < nt; ++k) {
+        const QSphere& S = sph[r.sn < 0 ? k : __ldg(slist + r.s0 + k)];
         const int64_t dx = px - S.c[0], dy = py - S.c[1], dz = pz - S.c[2];
         if (dx > S.r || -dx > S.r || dy > S.r || -dy > S.r || dz > S.r || -dz > S.r) continue;
         if (dx * dx + dy * dy + dz * dz <= S.r * S.r) {
