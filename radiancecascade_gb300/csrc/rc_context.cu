@@ -307,6 +307,42 @@ bool setup_tma0(rc_context* c) {
   return true;
 }
 
+// Wide levels between cascade 0 and the top: stage the next level's
+// child-averaged radiance by TMA where the box fits the copy rules (row pitch
+// a multiple of 16 bytes, at most 256 values per row, a box inside the level).
+void setup_tma_up(rc_context* c) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+  for (int i = 1; i + 1 < c->nlev; ++i) {
+    if (c->mode[i] != kModeFused) continue;
+    LevelArgs& a = c->args[i];
+    const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
+    const int BY = (512 >> a.l2px) / 2 + 2;  // a block tile holds 512 / Px rows of each of its two planes
+    const size_t es = c->elem;
+    if (UMx < 2 || UMx > 256 || (UMx * es) % 16 != 0 || UMy < BY || UMz < 3) continue;
+    if (!enc && !(enc = tensor_map_encoder())) return;
+    cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
+    cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
+    cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)BY, 3};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(&c->tmap_up[i], es == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                           3, const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) continue;
+    // the kernel's shared-memory limit: the largest box any level can need
+    // (512 / Px rows / 2 + 2 rows of Px / 2 FP32 values; largest at Px = 256)
+    const int smem = (int)bits_up_smem(up_tile_stride((512 >> 8) / 2 + 2, 128, 4));
+    cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level_bits_up<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                            : cudaFuncSetAttribute(k_level_bits_up<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      return;
+    }
+    a.up_rows = BY;
+    c->tma_up[i] = true;
+  }
+}
+
 // Reads and clears the device error flag; a bounded wait that ran out
 // becomes RC_ERR_TIMEOUT.
 rc_status check_device_error(rc_context* c, const char* fn) {
@@ -329,7 +365,12 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
   switch (c->mode[level]) {
     case kModeFused: {
       const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2);  // two parent texels per block
-      k_level_bits<T, L0, TOP><<<(unsigned)a.tiles * groups, kBitsThreads, kBitsSmem, s>>>(a);
+      if (!L0 && !TOP && c->tma_up[level]) {
+        const size_t smem = bits_up_smem(up_tile_stride(a.up_rows, a.UM[0], (int)sizeof(T)));
+        k_level_bits_up<T><<<(unsigned)a.tiles * groups, kBitsThreads, smem, s>>>(a, c->tmap_up[level], c->err);
+      } else {
+        k_level_bits<T, L0, TOP><<<(unsigned)a.tiles * groups, kBitsThreads, kBitsSmem, s>>>(a);
+      }
       break;
     }
     case kModeTma0: {
@@ -687,7 +728,10 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
   }
   if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);
   if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
-  if (!minimal && !(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) setup_tma0(c);
+  if (!minimal && !(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) {
+    setup_tma0(c);
+    setup_tma_up(c);
+  }
   *out = c;
   return RC_OK;
 }

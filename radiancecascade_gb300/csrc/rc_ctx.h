@@ -45,6 +45,10 @@ struct rc_context {
   int rec_slots[rcx::kMaxCascades]{};
   const uint32_t* rec_level[rcx::kMaxCascades]{};
   CUtensorMap tma0{};                // cascade 1's child-averaged radiance, for k_level0_tma
+  // wide levels between cascade 0 and the top: the next level's child-averaged
+  // radiance staged by TMA (k_level_bits_up)
+  bool tma_up[rcx::kMaxCascades]{};
+  CUtensorMap tmap_up[rcx::kMaxCascades]{};
   int tma0_py = 0;
   int* err = nullptr;                // device error flag set by bounded waits
   rcx::DirInfo* dirs = nullptr;      // all levels, concatenated

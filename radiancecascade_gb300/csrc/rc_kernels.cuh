@@ -65,7 +65,7 @@ struct LevelArgs {
   int32_t wpp;           // words per decimated plane
   uint32_t rep;          // narrow levels: 1 bit at the start of every row of a word
   int32_t tiles;         // block tiles per direction group
-  int32_t pad0;
+  int32_t up_rows;       // rows of the next level's probes one block stages (k_level_bits_up)
   const uint32_t* occ;
   const uint2* vol;
   int32_t G[3];

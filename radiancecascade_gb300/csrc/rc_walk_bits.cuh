@@ -20,6 +20,7 @@
 #pragma once
 
 #include "rc_kernels.cuh"
+#include "rc_tma.cuh"
 
 namespace rcx {
 
@@ -306,6 +307,19 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
   return (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
 }
 
+// Directions staged ahead in k_level_bits_up: the first kUpStages copies are
+// issued before the walk phase, so the walks hide them.
+constexpr int kUpStages = 4;
+
+// Bytes of one channel tile of the next level's box staged per direction
+// (3 planes x up_rows rows x UM[0] values), and its 128-byte aligned stride.
+__host__ __device__ __forceinline__ uint32_t up_tile_bytes(int up_rows, int umx, int elem) {
+  return 3u * (uint32_t)up_rows * (uint32_t)umx * (uint32_t)elem;
+}
+__host__ __device__ __forceinline__ uint32_t up_tile_stride(int up_rows, int umx, int elem) {
+  return (up_tile_bytes(up_rows, umx, elem) + 127u) & ~127u;
+}
+
 // Bit-parallel cascade level for wide levels (>= 32 probes per row).  Block =
 // one tile of 32 probe words x 8 directions (256 threads).
 // Phase 1: warp = direction, lane = word: walk 32 probes per lane, record the
@@ -319,8 +333,15 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
 // level_bits_block is one block's share (block index `bid`, shared memory
 // s_hit of kBitsSmem bytes); CG: the next level was written during the same
 // launch (see load_up).
-template <typename T, bool L0, bool TOP, bool CG>
-__device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, uint32_t* s_hit) {
+// TM: the next level's values come from shared memory instead: per direction
+// one TMA copy per channel of the block's parent box (all UM[0] columns,
+// up_rows rows, 3 planes) through `tmap` into s_up (128-byte aligned,
+// kUpStages stages of three channel tiles, then kUpStages mbarriers).
+template <typename T, bool L0, bool TOP, bool CG, bool TM = false>
+__device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, uint32_t* s_hit,
+                                                 const CUtensorMap* tmap = nullptr, unsigned char* s_up = nullptr,
+                                                 int* err = nullptr) {
+  static_assert(!TM || (!L0 && !TOP), "the staged merge serves levels between cascade 0 and the top");
   constexpr bool WIDE = true;  // narrow levels walk through the work queue (rc_walk_queue.cuh)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int tile_id = bid % a.tiles;
@@ -363,6 +384,45 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
   const int src_lo = (lane + 1) >> 1;
   const float wlo = (lane & 1) ? 0.75f : 0.25f, whi = 1.0f - wlo;
 
+  // TM: the block's parent box starts at (0, ys, zs); the clamped rows and
+  // planes above fall inside it (up_rows = rows of the tile / 2 + 2)
+  int soff[9];
+  T* up_tiles = nullptr;
+  uint64_t* ubar = nullptr;
+  uint32_t tstride = 0;
+  if (TM) {
+    const int BY = a.up_rows;
+    const int y0min = (t.w0 << 5) >> a.l2px;
+    const int ys = max(0, min(y0min / 2 - 1, a.UM[1] - BY));
+    const int zs = max(0, min(t.z0 / 2 - 1, a.UM[2] - 3));
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int jj = 0; jj < 3; ++jj)
+        soff[k * 3 + jj] = ((min(max(t.z0 / 2 - 1 + k, 0), a.UM[2] - 1) - zs) * BY +
+                            (min(max(y0 / 2 - 1 + jj, 0), a.UM[1] - 1) - ys)) * a.UM[0] + qx;
+    const uint32_t tbytes = up_tile_bytes(BY, a.UM[0], (int)sizeof(T));
+    tstride = up_tile_stride(BY, a.UM[0], (int)sizeof(T));
+    up_tiles = reinterpret_cast<T*>(s_up);
+    ubar = reinterpret_cast<uint64_t*>(s_up + kUpStages * 3 * tstride);
+    if (tid == 0) {
+#pragma unroll
+      for (int st = 0; st < kUpStages; ++st) mbar_init(&ubar[st], 1);
+      mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+      for (int k = 0; k < kUpStages && k < 8; ++k) {
+        const int d = block_dir<L0>(a, 0, dgroup, k);
+        mbar_arrive_expect_tx(&ubar[k], 3u * tbytes);
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch)
+          tma_load_3d(reinterpret_cast<unsigned char*>(up_tiles) + (k * 3 + ch) * tstride, tmap, 0, ys,
+                      (ch * a.ndirs + d) * a.UM[2] + zs, &ubar[k]);
+      }
+    }
+  }
+
   float acc[4][3];
 #pragma unroll
   for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
@@ -388,6 +448,8 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         const int dl = k;
         const int d = block_dir<L0>(a, pass, dgroup, dl);
         if (d < 0) break;
+        const int ust = k % kUpStages;
+        if (TM && !mbar_wait_bounded(&ubar[ust], (uint32_t)(k / kUpStages) & 1u) && lane == 0) atomicExch(err, 3);
         uint32_t rec[4];
         unsigned missm = 0, emism = 0;
         const uint32_t* hrow = s_hit + (dl * kTileSlots + slot0) * kHitStride + lane;
@@ -404,10 +466,17 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         for (int ch = 0; ch < 3; ++ch) {
           float mv[4] = {0.f, 0.f, 0.f, 0.f};
           if (merge) {
-            const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
             float av[9];
+            if (TM) {
+              const T* tile = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(up_tiles) +
+                                                         (ust * 3 + ch) * tstride);
 #pragma unroll
-            for (int q = 0; q < 9; ++q) av[q] = ploader ? load_up<T, CG>(src + aoff[q]) : 0.f;
+              for (int q = 0; q < 9; ++q) av[q] = ploader ? to_float(tile[soff[q]]) : 0.f;
+            } else {
+              const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
+#pragma unroll
+              for (int q = 0; q < 9; ++q) av[q] = ploader ? load_up<T, CG>(src + aoff[q]) : 0.f;
+            }
 #pragma unroll
             for (int ez = 0; ez < 2; ++ez) {
               float zv[3];
@@ -452,9 +521,29 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
             }
           }
         }
+        if (TM) {
+          __syncthreads();  // every warp is done with stage ust: refill it with direction k + kUpStages
+          if (tid == 0 && k + kUpStages < 8) {
+            const int kn = k + kUpStages, dn = block_dir<L0>(a, pass, dgroup, kn);
+            const int BY = a.up_rows;
+            const int ys = max(0, min(((t.w0 << 5) >> a.l2px) / 2 - 1, a.UM[1] - BY));
+            const int zs = max(0, min(t.z0 / 2 - 1, a.UM[2] - 3));
+            fence_proxy_async();
+            mbar_arrive_expect_tx(&ubar[ust], 3u * up_tile_bytes(BY, a.UM[0], (int)sizeof(T)));
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch)
+              tma_load_3d(reinterpret_cast<unsigned char*>(up_tiles) + (ust * 3 + ch) * tstride, tmap, 0, ys,
+                          (ch * a.ndirs + dn) * a.UM[2] + zs, &ubar[ust]);
+          }
+        }
       }
     }
     __syncthreads();
+  }
+  if (TM && tid == 0) {
+    // every copy was waited for above unless a wait ran out: wait (bounded)
+    // for the last phase of each stage before the block's shared memory goes
+    for (int st = 0; st < kUpStages && st < 8; ++st) mbar_wait_bounded(&ubar[st], (uint32_t)((7 - st) / kUpStages) & 1u);
   }
 
   if (L0) {
@@ -474,6 +563,24 @@ template <typename T, bool L0, bool TOP>
 __global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const __grid_constant__ LevelArgs a) {
   extern __shared__ uint32_t s_hit[];
   level_bits_block<T, L0, TOP, false>(a, blockIdx.x, s_hit);
+}
+
+// A wide level between cascade 0 and the top with the next level's values
+// staged by TMA (tmap: 3D map over A_up, x = UM[0], y = UM[1], z = channel x
+// direction x UM[2]; box UM[0] x up_rows x 3).  Shared memory: up to 127
+// bytes to align, the hit records, then the stages and their barriers.
+constexpr size_t kBitsHitBytes = (kBitsSmem + 127) & ~(size_t)127;
+__host__ __device__ constexpr size_t bits_up_smem(uint32_t tile_stride) {
+  return 128 + kBitsHitBytes + (size_t)kUpStages * 3 * tile_stride + 8 * kUpStages;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBitsThreads, 3)
+    k_level_bits_up(const __grid_constant__ LevelArgs a, const __grid_constant__ CUtensorMap tmap, int* err) {
+  extern __shared__ __align__(128) unsigned char smem_bits_up[];
+  unsigned char* base = smem_bits_up + ((128u - (smem_u32(smem_bits_up) & 127u)) & 127u);
+  level_bits_block<T, false, false, false, true>(a, blockIdx.x, reinterpret_cast<uint32_t*>(base), &tmap,
+                                                 base + kBitsHitBytes, err);
 }
 
 }  // namespace rcx

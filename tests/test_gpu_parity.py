@@ -99,6 +99,21 @@ def test_other_shapes_match_oracle(grid, N, kw, walk):
     _check(gflu, gL, oflu, oL)
 
 
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_c128_staged_merge_matches_oracle(precision):
+    """128^3: cascade 1 (32^3 probes) is a wide bit-parallel level whose merge
+    reads cascade 2 through TMA-staged shared-memory tiles."""
+    spec = R.scene_spec(128, 100, (4, 24), 12, (2.0, 6.0), (1.0, 20.0))
+    boxes, spheres = R.generate_scene(spec, 31)
+    vox = O.voxelise(128, boxes, spheres)
+    oflu, oL = O.solve(O.params(128, 5), vox, jump=True)
+    gflu, gL = _solve_gpu(R.make_params(128, 5, precision=precision), vox=vox)
+    if precision == "fp32":
+        _check(gflu, gL, oflu, oL)
+    else:
+        _check(gflu, gL, oflu, oL, rel=FP16_REL_L2, max_rel=None)
+
+
 def test_moving_emitters_incremental_update_matches_fresh_solve():
     boxes, spheres = R.workload_scene("c64")
     p = R.make_params(64, 5)
