@@ -621,7 +621,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": traffic,
-                     "kernel": "cascade levels: k_level_bits (wide) + k_walk_queue / k_level_merge (narrow)",
+                     "kernel": "cascade levels: k_level0_tma + k_level_bits_up (wide) + k_walk_queue / k_level_merge (narrow)",
                      "algorithmic_bytes_per_frame": B,
                      "level_ms_per_frame": round(level_ms, 4),
                      "per_level_ms": [round(float(x), 4) for x in per_level_ms[1:]],
