@@ -71,7 +71,7 @@ void release(rc_context* c) {
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg, c->d_slist};
+  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg, c->d_slist, c->qsteps, c->qstep_begin};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -443,7 +443,10 @@ void launch_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip = 0) {
   // queue_blocks is already capped at one resident wave
   const int64_t blocks = std::min<int64_t>((q->total + kQueueThreads - 1) / kQueueThreads, c->queue_blocks);
   cudaMemsetAsync(q->counter, 0, sizeof(unsigned long long), s);
-  k_walk_queue<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
+  if (c->qtab)
+    k_walk_queue_tab<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
+  else
+    k_walk_queue<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
 }
 
 }  // namespace
@@ -489,11 +492,62 @@ size_t queue_records_bytes(const rc_context* c) {
   return total;
 }
 
+// Step tables of the queue levels: each direction's walk replayed on the host
+// with the device's rule (the axis with the smallest next T; x before y
+// before z on ties), one entry per visited offset, cut where every probe of
+// the level has left the grid on some axis (the offset moves monotonically
+// on each axis, so no later step comes back).  Returns false, leaving the
+// queue on its own DDA, when a coarse cell does not fit a signed byte.
+bool build_step_tables(rc_context* c, const std::vector<DirInfo>& tab, std::vector<uint2>& steps,
+                       std::vector<int32_t>& begin, int32_t begin_off[kMaxCascades]) {
+  for (int i = 0; i < c->nlev; ++i) {
+    if (c->mode[i] != kModeQueue) continue;
+    const LevelGeom& g = c->geom[i];
+    int l2s = 0;
+    while ((1 << l2s) < g.spacing) ++l2s;
+    const int s = 1 << l2s, h = s >> 1;
+    begin_off[i] = (int32_t)begin.size();
+    for (int d = 0; d < g.ndirs; ++d) {
+      if (steps.size() > (size_t)INT32_MAX / 2) return false;
+      begin.push_back((int32_t)steps.size());
+      const DirInfo& di = tab[c->dir_off[i] + d];
+      int64_t a[3], t[3];
+      for (int ax = 0; ax < 3; ++ax) {
+        a[ax] = h + di.start_off[ax];
+        t[ax] = di.first_T[ax];
+      }
+      auto push = [&]() -> int {  // 1 pushed, 0 every probe out of the grid, -1 cell out of range
+        uint32_t ph = 0, pc = 0;
+        for (int ax = 2; ax >= 0; --ax) {
+          if (a[ax] >= c->p.grid[ax] || a[ax] + (int64_t)(g.M[ax] - 1) * s < 0) return 0;
+          const int64_t cell = a[ax] >> l2s;  // floor division
+          if (cell < -127 || cell > 127) return -1;
+          ph = (ph << l2s) | (uint32_t)(a[ax] & (s - 1));
+          pc |= ((uint32_t)cell & 0xFFu) << (8 * ax);
+        }
+        steps.push_back(make_uint2(ph, pc));
+        return 1;
+      };
+      int r = i == 0 ? push() : 1;  // cascade 0 tests the probe's own voxel first
+      for (int k = 0; k < di.steps && r == 1; ++k) {
+        const int ax = (t[0] <= t[1] && t[0] <= t[2]) ? 0 : (t[1] <= t[2] ? 1 : 2);
+        a[ax] += di.sgn[ax];
+        t[ax] += di.step_T[ax];
+        r = push();
+      }
+      if (r < 0) return false;
+    }
+    begin.push_back((int32_t)steps.size());
+  }
+  return true;
+}
+
 // Resident blocks of the walk kernel on the current device (SMs x blocks per SM).
-int queue_resident_blocks() {
+int queue_resident_blocks(bool tables = false) {
   int dev = 0, sms = 0, per_sm = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue, kQueueThreads, 0) != cudaSuccess) {
+      (tables ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue_tab, kQueueThreads, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue, kQueueThreads, 0)) != cudaSuccess) {
     (void)cudaGetLastError();
     return 152 * 2;
   }
@@ -725,6 +779,28 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
         return fail(s);
     }
     setup_queue(c, c->recs, c->qcounter);
+  }
+  if (!minimal && c->qargs.n > 0 && !(getenv("RC_WALK_TABLES") && strcmp(getenv("RC_WALK_TABLES"), "0") == 0)) {
+    std::vector<uint2> st;
+    std::vector<int32_t> begin;
+    int32_t boff[kMaxCascades] = {};
+    if (build_step_tables(c, tab, st, begin, boff) && !st.empty()) {
+      if ((s = dev_alloc((void**)&c->qsteps, st.size() * sizeof(uint2), "walk step tables")) != RC_OK) return fail(s);
+      if ((s = dev_alloc((void**)&c->qstep_begin, begin.size() * sizeof(int32_t), "walk step tables")) != RC_OK)
+        return fail(s);
+      if ((e = cudaMemcpy(c->qsteps, st.data(), st.size() * sizeof(uint2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+          (e = cudaMemcpy(c->qstep_begin, begin.data(), begin.size() * sizeof(int32_t), cudaMemcpyHostToDevice)) !=
+              cudaSuccess)
+        return fail(cuda_fail(e, "rc_create: step table upload"));
+      for (int k = 0; k < c->qargs.n; ++k) {
+        QueueLevel& L = c->qargs.lv[k];
+        L.steps = c->qsteps;
+        L.step_begin = c->qstep_begin + boff[L.level];
+      }
+      c->qtab = true;
+      c->queue_blocks = (int)std::min<int64_t>((c->qargs.total + kQueueThreads - 1) / kQueueThreads,
+                                               queue_resident_blocks(true));
+    }
   }
   if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);
   if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));

@@ -40,6 +40,10 @@ struct rc_context {
   int mode[rcx::kMaxCascades]{};          // how the level is solved (kMode*)
   uint32_t* recs = nullptr;               // walk records of the queue-walked levels
   unsigned long long* qcounter = nullptr;
+  // step tables of the queue levels (k_walk_queue_tab); qtab: every queue level has one
+  uint2* qsteps = nullptr;
+  int32_t* qstep_begin = nullptr;
+  bool qtab = false;
   rcx::QueueArgs qargs{};
   int queue_blocks = 0;
   int rec_slots[rcx::kMaxCascades]{};

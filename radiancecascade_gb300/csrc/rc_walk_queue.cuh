@@ -31,6 +31,13 @@ struct QueueLevel {
   uint32_t rep;
   int32_t test_start;  // level 0: the probe's own voxel belongs to the interval
   int32_t level;       // cascade index
+  // Step tables (or null: the walk runs its own DDA): for direction d the
+  // steps step_begin[d] .. step_begin[d + 1] - 1 of `steps`, each the voxel
+  // offset of one walk step split as x = phase index ((pz << l2s) + py) << l2s
+  // + px and y = the coarse cell (cx, cy, cz) as three signed bytes.  A table
+  // ends where every probe of the level has left the grid on some axis.
+  const uint2* steps;
+  const int32_t* step_begin;
 };
 
 struct QueueArgs {
@@ -220,15 +227,152 @@ struct Walker {
   }
 };
 
+// The same walk driven by a level's step table instead of its own DDA: a step
+// is one 8-byte load (shared by the lanes on the same direction) and the
+// per-cell state changes only when the table's coarse cell does.
+struct TableWalker {
+  const uint32_t* mask;
+  uint32_t* rec;
+  const uint2* st;  // next step
+  int n;            // steps left
+  int l2s, l2px, wpp, Mx, My, Mz, mzw;
+  uint32_t rep;
+  int zl, g0, wy0, wx0;
+  uint32_t valid, done, hits;
+  uint32_t cell;   // packed coarse cell of the current step
+  int gcell;       // cy * Px + cx
+  int64_t zoff;    // (zl + cz) * wpp
+  uint32_t inr;
+  bool zin;
+
+  __device__ __forceinline__ void set_cell(uint32_t packed) {
+    cell = packed;
+    const int cx = (int)(int8_t)(packed & 0xFFu), cy = (int)(int8_t)((packed >> 8) & 0xFFu),
+              cz = (int)(int8_t)((packed >> 16) & 0xFFu);
+    const int Px = 1 << l2px;
+    if (l2px >= 5) {
+      inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+    } else {
+      inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * rep;
+      inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+    }
+    zin = (unsigned)(zl + cz) < (unsigned)Mz;
+    gcell = cy * Px + cx;
+    zoff = (int64_t)(zl + cz) * wpp;
+  }
+
+  // Returns false when the item holds no probe.
+  __device__ __forceinline__ bool init(const QueueArgs& q, int64_t item) {
+    int li = 0;
+    while (li + 1 < q.n && item >= q.lv[li + 1].item_begin) ++li;
+    const QueueLevel& L = q.lv[li];
+    const int64_t r = item - L.item_begin;
+    const int d = (int)(r / L.slots), slot = (int)(r - (int64_t)d * L.slots);
+    mask = L.mask;
+    l2s = L.l2s;
+    l2px = L.l2px;
+    wpp = L.wpp;
+    Mx = L.M[0];
+    My = L.M[1];
+    Mz = L.M[2];
+    mzw = Mz * wpp;
+    rep = L.rep;
+    zl = slot / wpp;
+    const int wl = slot - zl * wpp;
+    g0 = wl << 5;
+    const int Px = 1 << l2px;
+    wy0 = g0 >> l2px;
+    wx0 = g0 & (Px - 1);
+    if (l2px >= 5) {
+      valid = wy0 < My ? range_bits(0, Mx - wx0) : 0u;
+    } else {
+      valid = range_bits(0, Mx) * rep;
+      valid &= range_bits(0, (My - wy0) * Px);
+    }
+    if (valid == 0u) return false;
+    rec = L.rec + ((int64_t)d * L.slots + slot) * 32;
+    done = ~valid;
+    hits = 0u;
+    const int b0 = __ldg(L.step_begin + d);
+    st = L.steps + b0;
+    n = __ldg(L.step_begin + d + 1) - b0;
+    set_cell(0x80808080u);  // no real cell: the first step sets it
+    return true;
+  }
+
+  // Walks up to kBatch steps; returns true when the item is finished.
+  template <int kBatch>
+  __device__ __forceinline__ bool batch(const QueueArgs& q) {
+    const int sm = (1 << l2s) - 1, Px = 1 << l2px;
+    uint2 e[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) e[u] = u < n ? __ldg(st + u) : make_uint2(0u, 0u);
+    int gs_[kBatch];
+    uint32_t lo_[kBatch], hi_[kBatch], inr_[kBatch];
+    bool ok_[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const bool step_ok = u < n;
+      if (step_ok && e[u].y != cell) set_cell(e[u].y);
+      ok_[u] = step_ok && zin;
+      inr_[u] = step_ok ? inr : 0u;
+      const int gs = g0 + gcell;
+      gs_[u] = gs;
+      const int q0 = gs >> 5;
+      const uint32_t* plane = mask + (int64_t)e[u].x * mzw + zoff;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
+      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
+    }
+    st += kBatch;
+    n -= kBatch;
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      if (!ok_[u]) return true;  // table finished, or the walk left the grid in z
+      done |= ~inr_[u];
+      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs_[u] & 31) & ~done;
+      if (nw) {
+        done |= nw;
+        hits |= nw;
+        // the step's voxel offset from its table entry
+        const uint32_t ph = e[u].x, pc = e[u].y;
+        const int bx = ((int)(int8_t)(pc & 0xFFu) << l2s) + (int)(ph & sm);
+        const int by = ((int)(int8_t)((pc >> 8) & 0xFFu) << l2s) + (int)((ph >> l2s) & sm);
+        const int bz = ((int)(int8_t)((pc >> 16) & 0xFFu) << l2s) + (int)(ph >> (2 * l2s));
+        const int vz = (zl << l2s) + bz;
+        do {
+          const int b = __ffs(nw) - 1;
+          nw &= nw - 1;
+          const int g = g0 + b;
+          const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
+          const int64_t row = (int64_t)vz * q.G[1] + vy;
+          const uint32_t ev = __ldg(&q.emis[row * q.W + (vx >> 5)]);
+          rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+        } while (nw);
+      }
+      if (done == 0xFFFFFFFFu) return true;
+    }
+    return n <= 0;
+  }
+
+  __device__ __forceinline__ void finish() {
+    uint32_t m = valid & ~hits;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      rec[b] = kMiss;
+    }
+  }
+};
+
 constexpr int kQueueThreads = 256;
 
 // Every warp walks queue items taken from *counter (a global or shared
 // counter) until the items up to `end` are gone; lanes refill one by one.
 // kBatch steps are issued per lane between refills.
-template <int kBatch>
+template <int kBatch, typename W = Walker>
 __device__ __forceinline__ void walk_tasks(const QueueArgs& q, unsigned long long* counter, int64_t end) {
   const int lane = threadIdx.x & 31;
-  Walker w;
+  W w;
   bool active = false, exhausted = false;
   for (;;) {
     const unsigned need = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
@@ -256,6 +400,12 @@ __device__ __forceinline__ void walk_tasks(const QueueArgs& q, unsigned long lon
 
 static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
   walk_tasks<4>(q, q.counter, q.total);
+}
+
+// The walks of levels that all have step tables (4 blocks/SM: 64 registers,
+// no spills; the extra resident warps hide the mask loads' latency).
+static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
+  walk_tasks<4, TableWalker>(q, q.counter, q.total);
 }
 
 // Merge of a narrow level from its walk records, probe p: parent texels
