@@ -315,13 +315,17 @@ __global__ void __launch_bounds__(kL0Threads, 2)
   const int zs = max(0, min(z0 / 2 - 1, UMz - 3));
   // inactive warps and lanes still read the tile: keep their rows and columns inside it
   const int ylo = (min(y, My - 1) - 1) >> 1;
-  const float wy_lo = (y & 1) ? 0.75f : 0.25f, wy_hi = 1.0f - wy_lo;
+  // Row 0 of rowoff is the parent row of weight 3/4 (ylo + 1 for even y,
+  // ylo for odd y), row 1 the one of weight 1/4.  Every 1D blend below is
+  // a + 3 b = 4 (a/4 + 3b/4); the three blends' factor 64 is divided out
+  // once per value (exact: a power of two).
+  const int yfar = (y & 1) ^ 1;
   int rowoff[2][3];
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const int qy = min(max(ylo + r, 0), UMy - 1), qz = min(max(z0 / 2 - 1 + k, 0), UMz - 1);
+      const int qy = min(max(ylo + (r ^ yfar), 0), UMy - 1), qz = min(max(z0 / 2 - 1 + k, 0), UMz - 1);
       rowoff[r][k] = ((qz - zs) * PY + (qy - ys)) * UMx;
     }
   const int c0 = min(2 * lq, UMx - 2), lcol = min(max(2 * lq - 1, 0), UMx - 1), rcol = min(2 * lq + 2, UMx - 1);
@@ -405,19 +409,19 @@ __global__ void __launch_bounds__(kL0Threads, 2)
           }
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
-            zr[0][r][c] = fmaf(0.25f, cv[0][c], 0.75f * cv[1][c]);
-            zr[1][r][c] = fmaf(0.75f, cv[1][c], 0.25f * cv[2][c]);
+            zr[0][r][c] = fmaf(3.f, cv[1][c], cv[0][c]);
+            zr[1][r][c] = fmaf(3.f, cv[1][c], cv[2][c]);
           }
         }
 #pragma unroll
         for (int zc = 0; zc < 2; ++zc) {
           float v[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) v[c] = fmaf(wy_lo, zr[zc][0][c], wy_hi * zr[zc][1][c]);
-          mv[zc][0] = fmaf(0.25f, v[0], 0.75f * v[1]);
-          mv[zc][1] = fmaf(0.75f, v[1], 0.25f * v[2]);
-          mv[zc][2] = fmaf(0.25f, v[1], 0.75f * v[2]);
-          mv[zc][3] = fmaf(0.75f, v[2], 0.25f * v[3]);
+          for (int c = 0; c < 4; ++c) v[c] = fmaf(3.f, zr[zc][0][c], zr[zc][1][c]);
+          mv[zc][0] = fmaf(3.f, v[1], v[0]) * (1.f / 64.f);
+          mv[zc][1] = fmaf(3.f, v[1], v[2]) * (1.f / 64.f);
+          mv[zc][2] = fmaf(3.f, v[2], v[1]) * (1.f / 64.f);
+          mv[zc][3] = fmaf(3.f, v[2], v[3]) * (1.f / 64.f);
         }
       }
 #pragma unroll
