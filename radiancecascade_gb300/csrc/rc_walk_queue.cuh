@@ -448,7 +448,8 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
   const int64_t npar = (int64_t)hn * hn;
   const int ndl = L0 ? a.ndirs : 8;
   float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
+  // two directions per pass: their parent taps are in flight together
+#pragma unroll 2
   for (int dl = 0; dl < ndl; ++dl) {
     int d;
     if (L0) {
