@@ -283,7 +283,7 @@ bool setup_tma0(rc_context* c) {
   const int py = std::min(6, UMy);
   cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
   cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
-  cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)py, 3};
+  cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)py, (cuuint32_t)(kL0Planes + 1)};
   cuuint32_t estr[3] = {1, 1, 1};
   const CUresult r = enc(&c->tma0, es == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                          const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -294,10 +294,12 @@ bool setup_tma0(rc_context* c) {
   // values; kL0Stages stages of three 128-byte aligned channel tiles, their
   // barriers and up to 127 bytes to align the base), so that a later context
   // never lowers it under an earlier one.
-  const size_t stage = 3 * (((size_t)3 * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
+  const size_t stage = 3 * (((size_t)(kL0Planes + 1) * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
   const int smem = (int)(kL0Stages * stage + 8 * kL0Stages + 128);
-  cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-                          : cudaFuncSetAttribute(k_level0_tma<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half, kL0Planes>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
+                          : cudaFuncSetAttribute(k_level0_tma<float, kL0Planes>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
@@ -376,11 +378,13 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
     case kModeTma0: {
       if (L0 && !TOP) {
         const int yblocks = (a.M[1] + kL0TmaRows - 1) / kL0TmaRows;
-        const unsigned blocks = (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + 1) / 2));
+        const unsigned blocks =
+            (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + kL0Planes - 1) / kL0Planes));
         // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
-        const size_t stage = 3 * (((size_t)3 * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
-        k_level0_tma<T><<<blocks, kL0Threads, kL0Stages * stage + 8 * kL0Stages + 128, s>>>(a, c->tma0, c->tma0_py,
-                                                                                           c->err);
+        const size_t stage =
+            3 * (((size_t)(kL0Planes + 1) * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
+        k_level0_tma<T, kL0Planes><<<blocks, kL0Threads, kL0Stages * stage + 8 * kL0Stages + 128, s>>>(
+            a, c->tma0, c->tma0_py, c->err);
       }
       break;
     }

@@ -238,9 +238,9 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 }
 
 // TMA-staged form of k_level0_direct.  Block = 8 child rows (one per warp) x
-// 2 planes of one 128-probe chunk.  For every direction the parent tiles of
+// ZC planes of one 128-probe chunk.  For every direction the parent tiles of
 // cascade 1's child-averaged radiance -- per channel the full parent row width
-// x PY rows x 3 planes -- are brought into shared memory by three
+// x PY rows x (ZC + 1) planes -- are brought into shared memory by three
 // cp.async.bulk.tensor copies while the previous direction's tiles are
 // consumed (two stages, one mbarrier each); one iteration serves all three
 // channels.  Lanes read their 4 parent columns from shared memory.
@@ -248,17 +248,23 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 // (bounded) for the copy it may still have in flight, and returns.
 constexpr int kL0TmaRows = 8;
 constexpr int kL0Stages = 2;  // parent tiles in flight: the copy for iteration it + 1 starts at iteration it
+// Child planes per block (ZC).  ZC = 1 halves the per-lane accumulators (80
+// registers, 3 blocks/SM) but reads 4 parent values per output instead of 3;
+// at 256^3 it measured 160 us against 153 us for ZC = 2 (128 registers, 2 blocks/SM).
+constexpr int kL0Planes = 2;
 
-template <typename T>
-__global__ void __launch_bounds__(kL0Threads, 2)
+template <typename T, int ZC>
+__global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
     k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int PY, int* err) {
+  static_assert(ZC == 1 || ZC == 2, "one or two child planes per block");
+  constexpr int PZ = ZC + 1;  // parent planes in a tile
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
   // TMA writes to shared memory must start on a 128-byte boundary: both stages
   // start at multiples of 128 from a 128-byte aligned base.
-  const int tile_elems = 3 * PY * UMx;
+  const int tile_elems = PZ * PY * UMx;
   const uint32_t tile_bytes = (uint32_t)tile_elems * (uint32_t)sizeof(T);
   const uint32_t tile_stride = (tile_bytes + 127u) & ~127u;  // one channel's tile, 128-byte aligned
   const uint32_t stage_bytes = 3u * tile_stride;              // the three channels of one direction
@@ -273,11 +279,11 @@ __global__ void __launch_bounds__(kL0Threads, 2)
   const int cw = bid % chunks;
   bid /= chunks;
   const int yb = (bid % yblocks) * kL0TmaRows;
-  const int z0 = 2 * (bid / yblocks);
+  const int z0 = ZC * (bid / yblocks);
   const int y = yb + warp;
   const int lq = 32 * cw + lane, x0 = 4 * lq;
   const bool active = y < My && x0 < Mx && z0 < Mz;
-  const bool zok1 = z0 + 1 < Mz;
+  const bool zok1 = ZC == 2 && z0 + 1 < Mz;
 
   // opacity / emissive masks per octant, as in k_level0_direct
   uint32_t ow[2] = {0u, 0u}, ew[2] = {0u, 0u};
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(kL0Threads, 2)
     const int ox = o & 1, oy = (o >> 1) & 1, oz = o >> 2;
     uint32_t mo = 0, me = 0;
 #pragma unroll
-    for (int zc = 0; zc < 2; ++zc) {
+    for (int zc = 0; zc < ZC; ++zc) {
       const uint32_t ob = (ow[zc] >> (8 * (oz * 2 + oy))) & 0xFFu, eb = (ew[zc] >> (8 * (oz * 2 + oy))) & 0xFFu;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -312,20 +318,22 @@ __global__ void __launch_bounds__(kL0Threads, 2)
 
   // tile origin and this warp's parent rows inside it
   const int ys = max(0, min(yb / 2 - 1, UMy - PY));
-  const int zs = max(0, min(z0 / 2 - 1, UMz - 3));
+  const int zs = max(0, min((z0 - 1) >> 1, UMz - PZ));
   // inactive warps and lanes still read the tile: keep their rows and columns inside it
   const int ylo = (min(y, My - 1) - 1) >> 1;
   // Row 0 of rowoff is the parent row of weight 3/4 (ylo + 1 for even y,
-  // ylo for odd y), row 1 the one of weight 1/4.  Every 1D blend below is
+  // ylo for odd y), row 1 the one of weight 1/4; with one child plane
+  // (ZC = 1) the planes are ordered the same way.  Every 1D blend below is
   // a + 3 b = 4 (a/4 + 3b/4); the three blends' factor 64 is divided out
   // once per value (exact: a power of two).
-  const int yfar = (y & 1) ^ 1;
-  int rowoff[2][3];
+  const int yfar = (y & 1) ^ 1, zfar = ZC == 1 ? (z0 & 1) ^ 1 : 0;
+  int rowoff[2][PZ];
 #pragma unroll
   for (int r = 0; r < 2; ++r)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int qy = min(max(ylo + (r ^ yfar), 0), UMy - 1), qz = min(max(z0 / 2 - 1 + k, 0), UMz - 1);
+    for (int k = 0; k < PZ; ++k) {
+      const int qy = min(max(ylo + (r ^ yfar), 0), UMy - 1);
+      const int qz = min(max(((z0 - 1) >> 1) + (ZC == 1 ? (k ^ zfar) : k), 0), UMz - 1);
       rowoff[r][k] = ((qz - zs) * PY + (qy - ys)) * UMx;
     }
   const int c0 = min(2 * lq, UMx - 2), lcol = min(max(2 * lq - 1, 0), UMx - 1), rcol = min(2 * lq + 2, UMx - 1);
@@ -359,11 +367,11 @@ __global__ void __launch_bounds__(kL0Threads, 2)
       atomicExch(err, 2);
     }
   }
-  float flu[3][2][4];
+  float flu[3][ZC][4];
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch)
 #pragma unroll
-    for (int zc = 0; zc < 2; ++zc) flu[ch][zc][0] = flu[ch][zc][1] = flu[ch][zc][2] = flu[ch][zc][3] = 0.f;
+    for (int zc = 0; zc < ZC; ++zc) flu[ch][zc][0] = flu[ch][zc][1] = flu[ch][zc][2] = flu[ch][zc][3] = 0.f;
   int it = 0;
   bool failed = false;
 #pragma unroll 1
@@ -393,14 +401,16 @@ __global__ void __launch_bounds__(kL0Threads, 2)
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
       const T* tile = tiles + st * stage_elems + ch * tile_stride_elems;
-      float mv[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+      float mv[ZC][4];
+#pragma unroll
+      for (int zc = 0; zc < ZC; ++zc) mv[zc][0] = mv[zc][1] = mv[zc][2] = mv[zc][3] = 0.f;
       if (merge) {
-        float zr[2][2][4];
+        float zr[ZC][2][4];
 #pragma unroll
         for (int r = 0; r < 2; ++r) {
-          float cv[3][4];
+          float cv[PZ][4];
 #pragma unroll
-          for (int k = 0; k < 3; ++k) {
+          for (int k = 0; k < PZ; ++k) {
             const T* row = tile + rowoff[r][k];
             cv[k][0] = to_float(row[lcol]);
             cv[k][1] = to_float(row[c0]);
@@ -409,12 +419,16 @@ __global__ void __launch_bounds__(kL0Threads, 2)
           }
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
-            zr[0][r][c] = fmaf(3.f, cv[1][c], cv[0][c]);
-            zr[1][r][c] = fmaf(3.f, cv[1][c], cv[2][c]);
+            if (ZC == 1) {
+              zr[0][r][c] = fmaf(3.f, cv[0][c], cv[PZ - 1][c]);  // plane 0 has weight 3/4
+            } else {
+              zr[0][r][c] = fmaf(3.f, cv[1][c], cv[0][c]);
+              zr[ZC - 1][r][c] = fmaf(3.f, cv[1][c], cv[PZ - 1][c]);
+            }
           }
         }
 #pragma unroll
-        for (int zc = 0; zc < 2; ++zc) {
+        for (int zc = 0; zc < ZC; ++zc) {
           float v[4];
 #pragma unroll
           for (int c = 0; c < 4; ++c) v[c] = fmaf(3.f, zr[zc][0][c], zr[zc][1][c]);
@@ -425,7 +439,7 @@ __global__ void __launch_bounds__(kL0Threads, 2)
         }
       }
 #pragma unroll
-      for (int zc = 0; zc < 2; ++zc) {
+      for (int zc = 0; zc < ZC; ++zc) {
         float o[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -445,7 +459,7 @@ __global__ void __launch_bounds__(kL0Threads, 2)
   }
   if (!failed) {
 #pragma unroll
-    for (int zc = 0; zc < 2; ++zc) {
+    for (int zc = 0; zc < ZC; ++zc) {
       if (!((valid >> (zc * 4)) & 1u)) continue;
       float* f = a.fluence + (p0 + zc * plane) * 3;
 #pragma unroll
