@@ -312,6 +312,22 @@ rc_status rc_shade(rc_context* ctx, const rc_shade_view* view,
                    const rc_texture* textures, int32_t ntextures,
                    float* out, int32_t where);
 
+/* rc_shade in two parts, as the reference builds its vertex, index and
+ * material buffers once (src/renderer.rs:411-490) and renders every frame
+ * from them (src/renderer.rs:559, src/app.rs:4-6): rc_shade_set_mesh
+ * uploads the mesh, materials and textures (same arguments and checks as
+ * rc_shade; the host arrays may be freed on return); rc_shade_draw shades
+ * one view of the last uploaded mesh with the context's current fluence.
+ * With where = RC_MEM_HOST the draw returns when the image is in `out`; with
+ * RC_MEM_DEVICE it returns once the work is queued on the context's stream
+ * (rc_synchronize waits for it).  rc_shade = set_mesh + draw + synchronize. */
+rc_status rc_shade_set_mesh(rc_context* ctx, const float* vertices, int64_t nverts,
+                            const uint32_t* indices, int64_t ntris,
+                            const uint16_t* tri_material,
+                            const rc_shade_material* materials, int32_t nmaterials,
+                            const rc_texture* textures, int32_t ntextures);
+rc_status rc_shade_draw(rc_context* ctx, const rc_shade_view* view, float* out, int32_t where);
+
 /* ---- neural radiance cache ------------------------------------------ */
 /* With the cache enabled, rc_solve serves the far cascades (first_level and
  * up) from a small network instead of walking their intervals: it predicts

@@ -115,6 +115,9 @@ SIGNATURES = {
     "rc_get_volume": (_S, [_P, _P, C.c_int64, C.c_int32]),
     "rc_shade": (_S, [_P, C.POINTER(ShadeView), _P, C.c_int64, _P, C.c_int64, _P, C.POINTER(ShadeMaterial),
                       C.c_int32, C.POINTER(Texture), C.c_int32, _P, C.c_int32]),
+    "rc_shade_set_mesh": (_S, [_P, _P, C.c_int64, _P, C.c_int64, _P, C.POINTER(ShadeMaterial), C.c_int32,
+                               C.POINTER(Texture), C.c_int32]),
+    "rc_shade_draw": (_S, [_P, C.POINTER(ShadeView), _P, C.c_int32]),
     "rc_batch_create": (_S, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "rc_batch_destroy": (_S, [_P]),
     "rc_batch_scene_set": (_S, [_P, C.c_int32, _P, C.c_int32, _P, C.c_int32]),

@@ -1102,16 +1102,30 @@ rc_status rc_get_radiance(rc_context* c, int32_t level, void* out, int64_t bytes
   return copy_out(c, out, static_cast<char*>(c->rad) + c->rad_off[level], need, where, "rc_get_radiance");
 }
 
-rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertices, int64_t nverts,
-                   const uint32_t* indices, int64_t ntris, const uint16_t* tri_material,
-                   const rc_shade_material* materials, int32_t nmaterials, const rc_texture* textures,
-                   int32_t ntextures, float* out, int32_t where) {
-  if (check_ctx(c, "rc_shade") != RC_OK) return RC_ERR_INVALID_ARG;
-  if (!view || view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384 || nverts < 0 ||
-      ntris < 0 || ntris >= ((int64_t)1 << 32) || (nverts && !vertices) || (ntris && !indices) || nmaterials < 1 ||
-      !materials || ntextures < 0 || (ntextures && !textures) || !out ||
-      (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
-    rcx::set_error("rc_shade: invalid arguments (image 1..16384 px per side, >= 1 material, non-NULL arrays)");
+// Shading scratch slots of a context: 0 vertices, 1 indices, 2 triangle
+// materials, 3 materials, 4 texels, 5 texture table (the mesh); 6 depth,
+// 7 image, 8 bounds, 9 small list, 10 large list, 11 counts (per draw).
+static rc_status shade_scratch(rc_context* c, int slot, size_t bytes, void** p) {
+  bytes = std::max<size_t>(bytes, 16);
+  if (c->scratch_cap[slot] < bytes) {
+    if (c->scratch[slot]) cudaFree(c->scratch[slot]);
+    c->scratch[slot] = nullptr;
+    c->scratch_cap[slot] = 0;
+    rc_status st = dev_alloc(&c->scratch[slot], bytes, "shading scratch");
+    if (st != RC_OK) return st;
+    c->scratch_cap[slot] = bytes;
+  }
+  *p = c->scratch[slot];
+  return RC_OK;
+}
+
+rc_status rc_shade_set_mesh(rc_context* c, const float* vertices, int64_t nverts, const uint32_t* indices,
+                            int64_t ntris, const uint16_t* tri_material, const rc_shade_material* materials,
+                            int32_t nmaterials, const rc_texture* textures, int32_t ntextures) {
+  if (check_ctx(c, "rc_shade_set_mesh") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (nverts < 0 || ntris < 0 || ntris >= ((int64_t)1 << 32) || (nverts && !vertices) || (ntris && !indices) ||
+      nmaterials < 1 || !materials || ntextures < 0 || (ntextures && !textures)) {
+    rcx::set_error("rc_shade_set_mesh: invalid arguments (>= 1 material, non-NULL arrays)");
     return RC_ERR_INVALID_ARG;
   }
   for (int64_t i = 0; i < ntris * 3; ++i)
@@ -1139,52 +1153,27 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
       rcx::set_error("rc_shade: texture %d is empty", k);
       return RC_ERR_INVALID_ARG;
     }
-  if (view->gi_scale > 0.f && !c->have_base) {
-    rcx::set_error("rc_shade: the GI term needs a solved scene");
-    return RC_ERR_STATE;
-  }
   DeviceGuard g(c->device);
-  const int64_t npix = (int64_t)view->width * view->height;
-  // scratch slots: 0 vertices, 1 indices, 2 triangle materials, 3 materials, 4 texels, 5 texture table,
-  // 6 depth, 7 image, 8 bounds, 9 small list, 10 large list, 11 counts
-  auto scratch = [&](int slot, size_t bytes, void** p) -> rc_status {
-    bytes = std::max<size_t>(bytes, 16);
-    if (c->scratch_cap[slot] < bytes) {
-      if (c->scratch[slot]) cudaFree(c->scratch[slot]);
-      c->scratch[slot] = nullptr;
-      c->scratch_cap[slot] = 0;
-      rc_status st = dev_alloc(&c->scratch[slot], bytes, "shading scratch");
-      if (st != RC_OK) return st;
-      c->scratch_cap[slot] = bytes;
-    }
-    *p = c->scratch[slot];
-    return RC_OK;
-  };
+  c->shade_mesh = false;
   float* d_v = nullptr;
   uint32_t *d_i = nullptr, *d_small = nullptr, *d_big = nullptr;
   uint16_t* d_m = nullptr;
   rc_shade_material* d_mat = nullptr;
   uint8_t* d_texels = nullptr;
   ShadeTex* d_tex = nullptr;
-  unsigned long long* d_z = nullptr;
   int4* d_bounds = nullptr;
-  unsigned* d_counts = nullptr;
-  float* d_out = where == RC_MEM_DEVICE ? out : nullptr;
   size_t texel_bytes = 0;
   for (int32_t k = 0; k < ntextures; ++k) texel_bytes += ((size_t)textures[k].width * textures[k].height * 4 + 15) & ~(size_t)15;
   rc_status st;
-  if ((st = scratch(0, (size_t)nverts * kShadeVertexFloats * 4, (void**)&d_v)) != RC_OK ||
-      (st = scratch(1, (size_t)ntris * 12, (void**)&d_i)) != RC_OK ||
-      (tri_material && (st = scratch(2, (size_t)ntris * 2, (void**)&d_m)) != RC_OK) ||
-      (st = scratch(3, (size_t)nmaterials * sizeof(rc_shade_material), (void**)&d_mat)) != RC_OK ||
-      (st = scratch(4, texel_bytes, (void**)&d_texels)) != RC_OK ||
-      (st = scratch(5, (size_t)std::max(ntextures, 1) * sizeof(ShadeTex), (void**)&d_tex)) != RC_OK ||
-      (st = scratch(6, (size_t)npix * 8, (void**)&d_z)) != RC_OK ||
-      (!d_out && (st = scratch(7, (size_t)npix * 16, (void**)&d_out)) != RC_OK) ||
-      (st = scratch(8, (size_t)ntris * sizeof(int4), (void**)&d_bounds)) != RC_OK ||
-      (st = scratch(9, (size_t)ntris * 4, (void**)&d_small)) != RC_OK ||
-      (st = scratch(10, (size_t)ntris * 4, (void**)&d_big)) != RC_OK ||
-      (st = scratch(11, 2 * sizeof(unsigned), (void**)&d_counts)) != RC_OK)
+  if ((st = shade_scratch(c, 0, (size_t)nverts * kShadeVertexFloats * 4, (void**)&d_v)) != RC_OK ||
+      (st = shade_scratch(c, 1, (size_t)ntris * 12, (void**)&d_i)) != RC_OK ||
+      (tri_material && (st = shade_scratch(c, 2, (size_t)ntris * 2, (void**)&d_m)) != RC_OK) ||
+      (st = shade_scratch(c, 3, (size_t)nmaterials * sizeof(rc_shade_material), (void**)&d_mat)) != RC_OK ||
+      (st = shade_scratch(c, 4, texel_bytes, (void**)&d_texels)) != RC_OK ||
+      (st = shade_scratch(c, 5, (size_t)std::max(ntextures, 1) * sizeof(ShadeTex), (void**)&d_tex)) != RC_OK ||
+      (st = shade_scratch(c, 8, (size_t)ntris * sizeof(int4), (void**)&d_bounds)) != RC_OK ||
+      (st = shade_scratch(c, 9, (size_t)ntris * 4, (void**)&d_small)) != RC_OK ||
+      (st = shade_scratch(c, 10, (size_t)ntris * 4, (void**)&d_big)) != RC_OK)
     return st;
   cudaStream_t s = c->stream;
   std::vector<ShadeTex> tex((size_t)std::max(ntextures, 1));
@@ -1203,15 +1192,51 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
   if (d_m) RC_CUDA(cudaMemcpyAsync(d_m, tri_material, (size_t)ntris * 2, cudaMemcpyHostToDevice, s), "rc_shade: upload");
   RC_CUDA(cudaMemcpyAsync(d_mat, materials, (size_t)nmaterials * sizeof(rc_shade_material), cudaMemcpyHostToDevice, s),
           "rc_shade: upload");
+  // the host arrays (and the texture table above) may go once this returns
+  RC_CUDA(cudaStreamSynchronize(s), "rc_shade_set_mesh");
+  c->shade_ntris = ntris;
+  c->shade_ntex = ntextures;
+  c->shade_tmat = tri_material != nullptr;
+  c->shade_mesh = true;
+  return RC_OK;
+}
+
+rc_status rc_shade_draw(rc_context* c, const rc_shade_view* view, float* out, int32_t where) {
+  if (check_ctx(c, "rc_shade_draw") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!view || view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384 || !out ||
+      (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
+    rcx::set_error("rc_shade_draw: invalid arguments (image 1..16384 px per side, non-NULL output)");
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!c->shade_mesh) {
+    rcx::set_error("rc_shade_draw: no mesh (rc_shade_set_mesh first)");
+    return RC_ERR_STATE;
+  }
+  if (view->gi_scale > 0.f && !c->have_base) {
+    rcx::set_error("rc_shade: the GI term needs a solved scene");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  const int64_t npix = (int64_t)view->width * view->height;
+  const int64_t ntris = c->shade_ntris;
+  unsigned long long* d_z = nullptr;
+  unsigned* d_counts = nullptr;
+  float* d_out = where == RC_MEM_DEVICE ? out : nullptr;
+  rc_status st;
+  if ((st = shade_scratch(c, 6, (size_t)npix * 8, (void**)&d_z)) != RC_OK ||
+      (!d_out && (st = shade_scratch(c, 7, (size_t)npix * 16, (void**)&d_out)) != RC_OK) ||
+      (st = shade_scratch(c, 11, 2 * sizeof(unsigned), (void**)&d_counts)) != RC_OK)
+    return st;
+  cudaStream_t s = c->stream;
   RC_CUDA(cudaMemsetAsync(d_z, 0xFF, (size_t)npix * 8, s), "rc_shade: clear");
   RC_CUDA(cudaMemsetAsync(d_counts, 0, 2 * sizeof(unsigned), s), "rc_shade: clear");
   ShadeArgs a;
   memset(&a, 0, sizeof a);
-  a.verts = d_v;
-  a.idx = d_i;
-  a.tmat = d_m;
-  a.mats = d_mat;
-  a.tex = d_tex;
+  a.verts = static_cast<const float*>(c->scratch[0]);
+  a.idx = static_cast<const uint32_t*>(c->scratch[1]);
+  a.tmat = c->shade_tmat ? static_cast<const uint16_t*>(c->scratch[2]) : nullptr;
+  a.mats = static_cast<const rc_shade_material*>(c->scratch[3]);
+  a.tex = static_cast<const ShadeTex*>(c->scratch[5]);
   a.ntris = ntris;
   memcpy(a.vp, view->view_proj, sizeof a.vp);
   memcpy(a.eye, view->eye, sizeof a.eye);
@@ -1225,26 +1250,53 @@ rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertic
   a.spacing = (float)c->geom[0].spacing;
   memcpy(a.w2g, view->world_to_grid, sizeof a.w2g);
   a.gi_scale = view->gi_scale;
-  a.ntex = ntextures;
+  a.ntex = c->shade_ntex;
   if (ntris) {
+    int4* d_bounds = static_cast<int4*>(c->scratch[8]);
+    uint32_t* d_small = static_cast<uint32_t*>(c->scratch[9]);
+    uint32_t* d_big = static_cast<uint32_t*>(c->scratch[10]);
     k_shade_bin<<<(unsigned)((ntris + 255) / 256), 256, 0, s>>>(a, d_bounds, d_small, d_big, d_counts);
-    unsigned counts[2] = {0, 0};
-    RC_CUDA(cudaMemcpyAsync(counts, d_counts, sizeof counts, cudaMemcpyDeviceToHost, s), "rc_shade: bin");
-    RC_CUDA(cudaStreamSynchronize(s), "rc_shade: bin");
-    if (counts[0]) {
-      const int64_t blocks = std::min<int64_t>(((int64_t)counts[0] * 32 + 255) / 256, 152 * 32);
-      k_shade_depth_small<<<(unsigned)blocks, 256, 0, s>>>(a, d_bounds, d_small, d_counts);
-    }
-    if (counts[1]) {
-      const unsigned tiles = (unsigned)(((a.W + kShadeTile - 1) / kShadeTile) * ((a.H + kShadeTile - 1) / kShadeTile));
-      k_shade_depth_big<<<dim3(tiles, std::min(counts[1], 65535u)), 256, 0, s>>>(a, d_bounds, d_big, d_counts);
-    }
+    // Both depth passes loop over the binned lists' lengths as the device
+    // counted them; their grids are sized for the worst case, so the host
+    // never waits between the passes.
+    const int64_t blocks = std::min<int64_t>((ntris * 32 + 255) / 256, 152 * 32);
+    k_shade_depth_small<<<(unsigned)blocks, 256, 0, s>>>(a, d_bounds, d_small, d_counts);
+    const unsigned tiles = (unsigned)(((a.W + kShadeTile - 1) / kShadeTile) * ((a.H + kShadeTile - 1) / kShadeTile));
+    k_shade_depth_big<<<dim3(tiles, (unsigned)std::min<int64_t>(ntris, kShadeBigRows)), 256, 0, s>>>(a, d_bounds,
+                                                                                                    d_big, d_counts);
   }
   k_shade_pixels<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(a);
   RC_CUDA(cudaGetLastError(), "rc_shade: launch");
-  if (where == RC_MEM_HOST)
+  if (where == RC_MEM_HOST) {
     RC_CUDA(cudaMemcpyAsync(out, d_out, (size_t)npix * 16, cudaMemcpyDeviceToHost, s), "rc_shade: read back");
-  RC_CUDA(cudaStreamSynchronize(s), "rc_shade");
+    RC_CUDA(cudaStreamSynchronize(s), "rc_shade");
+  }
+  return RC_OK;
+}
+
+rc_status rc_shade(rc_context* c, const rc_shade_view* view, const float* vertices, int64_t nverts,
+                   const uint32_t* indices, int64_t ntris, const uint16_t* tri_material,
+                   const rc_shade_material* materials, int32_t nmaterials, const rc_texture* textures,
+                   int32_t ntextures, float* out, int32_t where) {
+  if (check_ctx(c, "rc_shade") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!view || view->width < 1 || view->height < 1 || view->width > 16384 || view->height > 16384 || nverts < 0 ||
+      ntris < 0 || ntris >= ((int64_t)1 << 32) || (nverts && !vertices) || (ntris && !indices) || nmaterials < 1 ||
+      !materials || ntextures < 0 || (ntextures && !textures) || !out ||
+      (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
+    rcx::set_error("rc_shade: invalid arguments (image 1..16384 px per side, >= 1 material, non-NULL arrays)");
+    return RC_ERR_INVALID_ARG;
+  }
+  if (view->gi_scale > 0.f && !c->have_base) {
+    rcx::set_error("rc_shade: the GI term needs a solved scene");
+    return RC_ERR_STATE;
+  }
+  rc_status st = rc_shade_set_mesh(c, vertices, nverts, indices, ntris, tri_material, materials, nmaterials, textures,
+                                   ntextures);
+  if (st != RC_OK) return st;
+  st = rc_shade_draw(c, view, out, where);
+  if (st != RC_OK) return st;
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaStreamSynchronize(c->stream), "rc_shade");
   return RC_OK;
 }
 

@@ -89,6 +89,11 @@ struct rc_context {
   // device scratch of the shading pass, grown on demand and kept
   void* scratch[12] = {};
   size_t scratch_cap[12] = {};
+  // the mesh rc_shade_set_mesh left on the device for rc_shade_draw
+  bool shade_mesh = false;
+  int64_t shade_ntris = 0;
+  int32_t shade_ntex = 0;
+  bool shade_tmat = false;
 };
 
 namespace rcx {

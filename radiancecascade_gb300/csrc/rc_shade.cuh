@@ -133,6 +133,7 @@ __device__ __forceinline__ void shade_fragment(const ShadeArgs& a, int64_t t, co
 }
 
 constexpr int kShadeTile = 64;          // pixels per side of a large triangle's tile
+constexpr int kShadeBigRows = 32;       // blocks per tile that share the large triangles
 constexpr int kShadeSmallArea = 4096;   // bounds of at most this many pixels: one warp per triangle
 
 // Pass 0: bounds of every triangle, split into small ones (a warp each) and

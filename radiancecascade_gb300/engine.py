@@ -481,9 +481,8 @@ class Engine:
         F.check(self._lib.rc_get_fluence(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
         return out.reshape(-1, 3)
 
-    def shade(self, view: F.ShadeView, vertices: np.ndarray, indices: np.ndarray, materials,
-              tri_material: Optional[np.ndarray] = None, textures=()) -> np.ndarray:
-        """Raster + shade into an (H, W, 4) float32 image (see rc_shade)."""
+    @staticmethod
+    def _shade_mesh_args(vertices, indices, materials, tri_material, textures):
         v = np.ascontiguousarray(vertices, np.float32)
         i = np.ascontiguousarray(indices, np.uint32)
         tm = None if tri_material is None else np.ascontiguousarray(tri_material, np.uint16)
@@ -493,10 +492,39 @@ class Engine:
         for k, t in enumerate(textures):
             tex[k].rgba = keep[k].ctypes.data
             tex[k].width, tex[k].height, tex[k].srgb = keep[k].shape[1], keep[k].shape[0], int(t.get("srgb", 1))
+        return (F.ptr(v), len(v), F.ptr(i), len(i), None if tm is None else F.ptr(tm), mats, len(materials), tex,
+                len(textures)), (v, i, tm, keep)
+
+    def shade(self, view: F.ShadeView, vertices: np.ndarray, indices: np.ndarray, materials,
+              tri_material: Optional[np.ndarray] = None, textures=()) -> np.ndarray:
+        """Raster + shade into an (H, W, 4) float32 image (see rc_shade)."""
+        args, _keep = self._shade_mesh_args(vertices, indices, materials, tri_material, textures)
         out = np.zeros((view.height, view.width, 4), np.float32)
-        F.check(self._lib.rc_shade(self.handle, C.byref(view), F.ptr(v), len(v), F.ptr(i), len(i),
-                                   None if tm is None else F.ptr(tm), mats, len(materials), tex, len(textures),
-                                   F.ptr(out), F.RC_MEM_HOST))
+        F.check(self._lib.rc_shade(self.handle, C.byref(view), *args, F.ptr(out), F.RC_MEM_HOST))
+        return out
+
+    def shade_set_mesh(self, vertices: np.ndarray, indices: np.ndarray, materials,
+                       tri_material: Optional[np.ndarray] = None, textures=()) -> None:
+        """Uploads the mesh that shade_draw renders (rc_shade_set_mesh)."""
+        args, _keep = self._shade_mesh_args(vertices, indices, materials, tri_material, textures)
+        F.check(self._lib.rc_shade_set_mesh(self.handle, *args))
+
+    def shade_draw(self, view: F.ShadeView, out=None):
+        """Shades one view of the uploaded mesh (rc_shade_draw).  `out`: None
+        (a new host array), a C-contiguous (H, W, 4) float32 host array, or a
+        CUDA tensor of that shape (the draw is then only queued on the
+        context's stream)."""
+        if out is None:
+            out = np.zeros((view.height, view.width, 4), np.float32)
+        if isinstance(out, np.ndarray):
+            if out.dtype != np.float32 or out.shape != (view.height, view.width, 4) or not out.flags.c_contiguous:
+                raise ValueError("shade_draw: out must be a C-contiguous (H, W, 4) float32 array")
+            F.check(self._lib.rc_shade_draw(self.handle, C.byref(view), F.ptr(out), F.RC_MEM_HOST))
+            return out
+        if tuple(out.shape) != (view.height, view.width, 4) or not out.is_cuda or not out.is_contiguous() \
+                or str(out.dtype) != "torch.float32":
+            raise ValueError("shade_draw: out must be a contiguous (H, W, 4) float32 CUDA tensor")
+        F.check(self._lib.rc_shade_draw(self.handle, C.byref(view), C.c_void_p(out.data_ptr()), F.RC_MEM_DEVICE))
         return out
 
     def volume(self) -> np.ndarray:

@@ -91,3 +91,29 @@ def test_shading_argument_checks():
             e.shade(v, verts, np.array([[0, 1, 2]], np.uint32), [R.shade_material(color_texture=0)])
         img = e.shade(v, verts, np.array([[0, 1, 2]], np.uint32), [R.shade_material()])
         assert np.array_equal(img[..., 3], np.ones((8, 8))) and not img[..., :3].any()
+
+
+def test_set_mesh_then_draw_matches_one_call_shading():
+    """rc_shade_set_mesh + rc_shade_draw give rc_shade's image bit for bit, for
+    several views of one upload, into host memory and into a device buffer."""
+    torch = pytest.importorskip("torch")
+    g, W, H = 32, 96, 72
+    pos, idx, tm, vox_mats, verts, mats, tex = _scene(g)
+    with R.Engine(R.make_params(g, 4)) as e:
+        e.set_mesh(pos, idx, vox_mats, tm)
+        e.solve()
+        views = [_view(g, W, H, 1.0), _view(g, W, H, 0.0)]
+        views[1].eye[:] = (g / 3, g / 2, 3.0)
+        views[1].view_proj[:] = R.camera_view_proj((g / 3, g / 2, 3.0), np.pi / 3, 0.0, W, H, fovy_deg=60,
+                                                   znear=0.1, zfar=4.0 * g)
+        want = [e.shade(v, verts, idx, mats, tm, tex) for v in views]
+        with pytest.raises(R.RCError):  # a fresh context has no mesh to draw
+            with R.Engine(R.make_params(16, 2)) as e2:
+                e2.shade_draw(_view(16, 8, 8, 0.0))
+        e.shade_set_mesh(verts, idx, mats, tm, tex)
+        for v, w in zip(views, want):
+            assert np.array_equal(e.shade_draw(v), w)
+            d = torch.empty((H, W, 4), dtype=torch.float32, device="cuda")
+            e.shade_draw(v, d)
+            e.synchronize()
+            assert np.array_equal(d.cpu().numpy(), w)
