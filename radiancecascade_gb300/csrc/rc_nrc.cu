@@ -208,6 +208,11 @@ void nrc_release(rc_context* c) {
 //   4. per level: served by the network when less than plain_level_fraction
 //      of its probes is in fallback tiles (inference for the level, plain walk
 //      for its fallback probes, merge from (R, T)), else its plain kernels.
+// Inference grid: one resident wave at most, kFwdGroups tiles per block at a time.
+unsigned fwd_grid(const NrcState* n, int64_t ntiles) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((ntiles + kFwdGroups - 1) / kFwdGroups, n->fwd_blocks));
+}
+
 rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   NrcState* n = c->nrc;
   const int ph = (int)(n->solves % n->nph), hp = (ph + n->nph / 2) % n->nph;
@@ -222,7 +227,7 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     a.tiles = n->tiles + ho0;
     a.ntiles = nho;
     a.out = n->pred;
-    k_nrc_forward<false><<<(unsigned)std::min<int64_t>(nho, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(a, nho);
+    k_nrc_forward<false><<<fwd_grid(n, nho), kFwdThreads, kFwdSmem, s>>>(a, nho);
     k_nrc_tile_error<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(n->tiles + ho0, nho, n->pred, tho, n->base,
                                                                         n->tile_shift, n->TX, n->TY, n->tnum, n->tden);
     const float thr = n->prm.fallback_threshold;
@@ -289,7 +294,7 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     plain_queue_walk(c, s, skip);
   }
   if (any_served) {
-    k_nrc_forward<true><<<(unsigned)std::min<int64_t>(t0, n->fwd_blocks), kNrcThreads, kFwdSmem, s>>>(inf, t0);
+    k_nrc_forward<true><<<fwd_grid(n, t0), kFwdThreads, kFwdSmem, s>>>(inf, t0);
     NrcFallbackArgs f;
     memset(&f, 0, sizeof f);
     for (int i = 0; i < c->nlev; ++i) f.lv[i] = c->args[i];
@@ -416,6 +421,10 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   n->base.nlev = c->nlev;
   int64_t queries = 0, dirs = 0;
   for (int i = n->first; i < c->nlev; ++i) {
+    if (c->geom[i].probes() * c->geom[i].ndirs >= ((int64_t)1 << 31)) {
+      set_error("rc_nrc_enable: cascade %d has 2^31 or more (probe, direction) queries", i);
+      return fail(RC_ERR_UNSUPPORTED);
+    }
     queries += c->geom[i].probes() * c->geom[i].ndirs;
     dirs += c->geom[i].ndirs;
     n->total_probes += c->geom[i].probes();
@@ -533,7 +542,7 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   RC_CUDA(cudaFuncSetAttribute(k_nrc_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem),
           "rc_nrc_enable: attribute");
   // Resident blocks: shared memory and registers per SM, and the tensor-memory
-  // budget of 512 columns per SM (64 per inference block, 512 per training
+  // budget of 512 columns per SM (64 per inference warpgroup, 512 per training
   // block) -- so that no allocation ever waits.
   int sms = 0, smem_sm = 0, regs_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -544,8 +553,9 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   if (cudaFuncGetAttributes(&fa, k_nrc_forward<true>) == cudaSuccess) fwd_regs = std::max(fa.numRegs, 1);
   (void)cudaGetLastError();
   const int by_smem = smem_sm / (kFwdSmem + 1024);
-  const int by_regs = regs_sm / (((fwd_regs + 7) & ~7) * kNrcThreads);
-  n->fwd_blocks = std::max(1, sms * std::max(1, std::min(std::min(by_smem, by_regs), 8)));
+  const int by_regs = regs_sm / (((fwd_regs + 7) & ~7) * kFwdThreads);
+  const int by_tmem = 512 / (64 * kFwdGroups);
+  n->fwd_blocks = std::max(1, sms * std::max(1, std::min(std::min(by_smem, by_regs), by_tmem)));
   n->train_blocks = std::max(1, sms);
   {
     std::vector<float> mlp, hash;
@@ -681,7 +691,7 @@ rc_status rc_nrc_query(rc_context* c, int32_t level, const int32_t* probes, cons
   a.tiles = n->qtiles;
   a.ntiles = count;
   a.out = n->qout;
-  k_nrc_forward<false><<<(unsigned)std::min<int64_t>(count, n->fwd_blocks), kNrcThreads, kFwdSmem, st>>>(a, count);
+  k_nrc_forward<false><<<fwd_grid(n, count), kFwdThreads, kFwdSmem, st>>>(a, count);
   RC_CUDA(cudaGetLastError(), "rc_nrc_query: launch");
   std::vector<float> raw((size_t)count * kNrcThreads * 4);
   RC_CUDA(cudaMemcpyAsync(raw.data(), n->qout, raw.size() * 4, cudaMemcpyDeviceToHost, st), "rc_nrc_query");

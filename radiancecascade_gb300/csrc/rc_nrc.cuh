@@ -125,19 +125,22 @@ __device__ __forceinline__ bool nrc_query(const NrcArgs& a, int64_t t, int r, in
   li = a.first;
   while (li + 1 < a.nlev && t >= a.tile0[li + 1]) ++li;
   const NrcLevel& L = a.lv[li];
-  const int64_t q = (t - a.tile0[li]) * kNrcThreads + r;
+  // a level's queries number below 2^31 (checked when the cache is enabled)
+  const uint32_t q = (uint32_t)(t - a.tile0[li]) * (uint32_t)kNrcThreads + (uint32_t)r;
+  const uint32_t P = (uint32_t)L.P;
   slot = -1;
-  if (q >= L.P * L.ndirs) return false;
-  d = (int)(q / L.P);
-  p = q - (int64_t)d * L.P;
+  if (q >= P * (uint32_t)L.ndirs) return false;
+  const uint32_t dq = q / P;
+  d = (int)dq;
+  p = (int64_t)(q - dq * P);
   return true;
 }
 
 // Probe centre (voxel units) of probe p of level L, scaled to [0, 1].
 __device__ __forceinline__ void nrc_probe_pos(const NrcLevel& L, int64_t p, float inv_extent, float* u) {
-  const int mx = (int)(p % L.M[0]);
-  const int my = (int)((p / L.M[0]) % L.M[1]);
-  const int mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
+  const uint32_t pp = (uint32_t)p, M0 = (uint32_t)L.M[0], M1 = (uint32_t)L.M[1];
+  const uint32_t row = pp / M0, mz_ = row / M1;
+  const int mx = (int)(pp - row * M0), my = (int)(row - mz_ * M1), mz = (int)mz_;
   const float h = 0.5f * (float)L.spacing;
   u[0] = ((float)mx * L.spacing + h) * inv_extent;
   u[1] = ((float)my * L.spacing + h) * inv_extent;
@@ -225,71 +228,183 @@ __device__ __host__ __forceinline__ void nrc_serve(const float* o, float scale, 
   for (int c = 0; c < 3; ++c) sv[c] = through ? 0.f : fmaxf(o[c] / scale, 0.f);
 }
 
+// The input row of a query written straight into row `row` of the K-major
+// activation operand, 8 columns (16 bytes) at a time: the 32 hash features
+// (16 gathers issued together), the 16 direction features (stored BF16
+// already), 16 zeros.  Same values as nrc_input + store_row64_bf16.
+__device__ __forceinline__ void nrc_encode_row(const NrcArgs& a, bool valid, int li, int64_t p, int d,
+                                               unsigned char* XA, int row) {
+  const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+  if (!valid) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(XA + core_off(row, 8 * c, 64)) = zero;
+    return;
+  }
+  const NrcQuery q = nrc_make_query(a, li, p, d);
+  __half2 f[kNrcHashLevels];
+#pragma unroll
+  for (int l = 0; l < kNrcHashLevels; ++l)
+    f[l] = __ldg(reinterpret_cast<const __half2*>(a.hash.table) + nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc));
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float2 v = __half22float2(f[4 * c + j]);
+      h[j] = __floats2bfloat162_rn(v.x, v.y);
+    }
+    *reinterpret_cast<uint4*>(XA + core_off(row, 8 * c, 64)) = *reinterpret_cast<const uint4*>(h);
+  }
+  const uint4* dp = reinterpret_cast<const uint4*>(a.lv[li].denc + (int64_t)d * kNrcDirFeat);
+  *reinterpret_cast<uint4*>(XA + core_off(row, 32, 64)) = __ldg(dp);
+  *reinterpret_cast<uint4*>(XA + core_off(row, 40, 64)) = __ldg(dp + 1);
+  *reinterpret_cast<uint4*>(XA + core_off(row, 48, 64)) = zero;
+  *reinterpret_cast<uint4*>(XA + core_off(row, 56, 64)) = zero;
+}
+
+constexpr int kFwdGroupsMax = 2;
+
+// Bias add and ReLU of 32 accumulator columns (c0 .. c0 + 31 of row `row`),
+// stored as BF16 into the K-major operand: per column pair one packed FP32
+// add and one converting ReLU (relu(round(x)) = round(relu(x)), so the values
+// equal fmaxf(v + b, 0) rounded to BF16).
+__device__ __forceinline__ void bias_relu_store32(unsigned char* XA, int row, int c0, const float* v,
+                                                  const float* bias) {
+  uint32_t hb[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const float2 b = reinterpret_cast<const float2*>(bias)[j];
+    asm("{\n"
+        ".reg .b64 x, y, z;\n"
+        ".reg .f32 lo, hi;\n"
+        "mov.b64 x, {%1, %2};\n"
+        "mov.b64 y, {%3, %4};\n"
+        "add.rn.f32x2 z, x, y;\n"
+        "mov.b64 {lo, hi}, z;\n"
+        "cvt.rn.relu.bf16x2.f32 %0, hi, lo;\n"
+        "}\n"
+        : "=r"(hb[j])
+        : "f"(v[2 * j]), "f"(v[2 * j + 1]), "f"(b.x), "f"(b.y));
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c)
+    *reinterpret_cast<uint4*>(XA + core_off(row, c0 + 8 * c, 64)) =
+        make_uint4(hb[4 * c], hb[4 * c + 1], hb[4 * c + 2], hb[4 * c + 3]);
+}
+
+// Barrier of one warpgroup (128 threads, named barrier 1 + wg; immediate ids
+// so that the kernel reserves only the barriers it uses).
+__device__ __forceinline__ void wg_sync(int wg) {
+  if (wg == 0) asm volatile("bar.sync 1, 128;" ::: "memory");
+  else asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+// The same barrier, returning whether any of its threads passed `v`.
+__device__ __forceinline__ bool wg_sync_or(int wg, bool v) {
+  uint32_t r;
+  if (wg == 0)
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.u32 p, %1, 0;\n"
+        "barrier.cta.red.or.pred q, 1, 128, p;\n"
+        "selp.u32 %0, 1, 0, q;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+  else
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.u32 p, %1, 0;\n"
+        "barrier.cta.red.or.pred q, 2, 128, p;\n"
+        "selp.u32 %0, 1, 0, q;\n"
+        "}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+  return r != 0;
+}
+static_assert(kFwdGroupsMax == 2, "named barriers 1 and 2 serve the two warpgroups");
+
 // ---------------------------------------------------------------------------
-// Inference.  Block = 128 threads, persistent over tiles; shared memory: the
-// activation operand (16 KB), the forward weights (34 KB), biases.
+// Inference.  Block = kFwdGroups warpgroups, persistent over tiles: each
+// warpgroup takes its own tiles (128 queries, one per thread) through the
+// five layers with its own activation operand (16 KB), tensor-memory columns
+// (64) and mbarrier, so one warpgroup's epilogue runs while the other's MMAs
+// and gathers are in flight; the weights (34 KB) and biases are shared.
+// Epilogues read tensor memory 32 columns at a time (3 blocks/SM).
 // RT: write (R, T) planes of the enumerated far levels; else raw outputs.
 // ---------------------------------------------------------------------------
-constexpr int kFwdSmem = 16384 + 4 * 8192 + 2048 + 272 * 4 + 64 + 128;
+constexpr int kFwdGroups = kFwdGroupsMax;
+constexpr int kFwdThreads = 128 * kFwdGroups;
+constexpr int kFwdXA = 36864;  // activation operands start here (1024-byte aligned, after weights and biases)
+constexpr int kFwdSmem = kFwdXA + kFwdGroups * 16384 + 8 * kFwdGroups + 16 + 128;
+static_assert(4 * 8192 + 2048 + 272 * 4 <= kFwdXA, "weights and biases fit before the operands");
 
 template <bool RT>
-__global__ void __launch_bounds__(kNrcThreads) k_nrc_forward(const __grid_constant__ NrcArgs a, int64_t ntiles) {
+__global__ void __launch_bounds__(kFwdThreads, 3) k_nrc_forward(const __grid_constant__ NrcArgs a, int64_t ntiles) {
   extern __shared__ unsigned char sm_raw[];
   unsigned char* sm = align128(sm_raw);
-  unsigned char* XA = sm;
-  unsigned char* WF = sm + 16384;
+  unsigned char* WF = sm;
   unsigned char* W4F = WF + 4 * 8192;
   float* sb = reinterpret_cast<float*>(W4F + 2048);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sb + 272);
-  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bar + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kFwdXA + kFwdGroups * 16384);
+  uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bars + kFwdGroups);
+  const int tid = threadIdx.x, wg = tid >> 7, row = tid & 127, warp = tid >> 5;
 
   for (int l = 0; l < 4; ++l) copy_smem(WF + 8192 * l, a.img + 16384 * l, 8192);
   copy_smem(W4F, a.img + kImgW4F, 2048);
   for (int j = tid; j < 272; j += blockDim.x)
     sb[j] = j < 256 ? a.params[(j >> 6) * kNrcLayerStride + 4096 + (j & 63)] : a.params[kNrcB4 + j - 256];
   if (tid == 0) {
-    mbar_init(bar, 1);
+#pragma unroll
+    for (int g = 0; g < kFwdGroups; ++g) mbar_init(&bars[g], 1);
     mbar_fence_init();
   }
-  if (warp == 0) tmem_alloc(s_taddr, 64);
+  if (warp == 0) tmem_alloc(s_taddr, 64 * kFwdGroups);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tmem = *s_taddr;
-  const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t tmem = *s_taddr + 64u * (uint32_t)wg;            // this warpgroup's columns
+  const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's lane quarter
+  unsigned char* XA = sm + kFwdXA + wg * 16384;
+  uint64_t* bar = &bars[wg];
   uint32_t phase = 0;
   bool ok = true;
 
-  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+  for (int64_t t = (int64_t)blockIdx.x * kFwdGroups + wg; t < ntiles && ok; t += (int64_t)gridDim.x * kFwdGroups) {
     int li, d, slot;
     int64_t p;
-    const bool valid = nrc_query(a, t, tid, li, p, d, slot);
-    {
-      float x[64];
-      nrc_input(a, valid, li, p, d, x);
-      store_row64_bf16(XA, tid, x);
-    }
+    const bool valid = nrc_query(a, t, row, li, p, d, slot);
+    nrc_encode_row(a, valid, li, p, d, XA, row);
     fence_proxy_async();
-    __syncthreads();
+    wg_sync(wg);
     float o[16];
-    for (int l = 0; l < 5 && ok; ++l) {
-      if (tid == 0) {
+    for (int l = 0; l < 5; ++l) {
+      if (row == 0) {
         tc_fence_after();
         umma_gemm(tmem, smem_u32(XA), smem_u32(l < 4 ? WF + 8192 * l : W4F), 128, l < 4 ? 64 : 16, 64, false);
         umma_commit(bar);
       }
-      if (!(ok = nrc_wait(bar, phase, a.err))) break;
+      const bool got = mbar_wait_bounded(bar, phase);
+      phase ^= 1u;
+      if (wg_sync_or(wg, !got)) {
+        if (row == 0) atomicExch(a.err, 3);
+        ok = false;
+        break;
+      }
       tc_fence_after();
       if (l < 4) {
-        float v[64];
-        tmem_ld64(tl, v);
 #pragma unroll
-        for (int j = 0; j < 64; ++j) v[j] = fmaxf(v[j] + sb[64 * l + j], 0.f);
-        store_row64_bf16(XA, tid, v);
+        for (int hf = 0; hf < 2; ++hf) {
+          float v[32];
+          tmem_ld32(tl + 32u * hf, v);
+          bias_relu_store32(XA, row, 32 * hf, v, sb + 64 * l + 32 * hf);
+        }
         tc_fence_before();
         fence_proxy_async();
-        __syncthreads();
+        wg_sync(wg);
       } else {
         tmem_ld16(tl, o);
         tc_fence_before();
@@ -308,13 +423,13 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_forward(const __grid_consta
       for (int c = 0; c < 4; ++c) L.rt[c * plane + off] = __float2half_rn(sv[c]);
     } else {
       float4 r4 = make_float4(o[0], o[1], o[2], o[3]);
-      *reinterpret_cast<float4*>(a.out + (t * kNrcThreads + tid) * 4) = r4;
+      *reinterpret_cast<float4*>(a.out + (t * kNrcThreads + row) * 4) = r4;
     }
   }
   if (!ok) mbar_wait_bounded(bar, phase ^ 1u);  // the group that timed out, if it still runs
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, 64);
+  if (warp == 0) tmem_dealloc(*s_taddr, 64 * kFwdGroups);
 }
 
 // ---------------------------------------------------------------------------
