@@ -264,15 +264,15 @@ __device__ __forceinline__ void nrc_encode_row(const NrcArgs& a, bool valid, int
 
 constexpr int kFwdGroupsMax = 2;
 
-// Bias add and ReLU of 32 accumulator columns (c0 .. c0 + 31 of row `row`),
+// Bias add and ReLU of 16 accumulator columns (c0 .. c0 + 15 of row `row`),
 // stored as BF16 into the K-major operand: per column pair one packed FP32
 // add and one converting ReLU (relu(round(x)) = round(relu(x)), so the values
 // equal fmaxf(v + b, 0) rounded to BF16).
-__device__ __forceinline__ void bias_relu_store32(unsigned char* XA, int row, int c0, const float* v,
+__device__ __forceinline__ void bias_relu_store16(unsigned char* XA, int row, int c0, const float* v,
                                                   const float* bias) {
-  uint32_t hb[16];
+  uint32_t hb[8];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) {
+  for (int j = 0; j < 8; ++j) {
     const float2 b = reinterpret_cast<const float2*>(bias)[j];
     asm("{\n"
         ".reg .b64 x, y, z;\n"
@@ -287,7 +287,7 @@ __device__ __forceinline__ void bias_relu_store32(unsigned char* XA, int row, in
         : "f"(v[2 * j]), "f"(v[2 * j + 1]), "f"(b.x), "f"(b.y));
   }
 #pragma unroll
-  for (int c = 0; c < 4; ++c)
+  for (int c = 0; c < 2; ++c)
     *reinterpret_cast<uint4*>(XA + core_off(row, c0 + 8 * c, 64)) =
         make_uint4(hb[4 * c], hb[4 * c + 1], hb[4 * c + 2], hb[4 * c + 3]);
 }
@@ -333,7 +333,7 @@ static_assert(kFwdGroupsMax == 2, "named barriers 1 and 2 serve the two warpgrou
 // five layers with its own activation operand (16 KB), tensor-memory columns
 // (64) and mbarrier, so one warpgroup's epilogue runs while the other's MMAs
 // and gathers are in flight; the weights (34 KB) and biases are shared.
-// Epilogues read tensor memory 32 columns at a time (3 blocks/SM).
+// Epilogues read tensor memory 16 columns at a time (3 blocks/SM).
 // RT: write (R, T) planes of the enumerated far levels; else raw outputs.
 // ---------------------------------------------------------------------------
 constexpr int kFwdGroups = kFwdGroupsMax;
@@ -397,10 +397,10 @@ __global__ void __launch_bounds__(kFwdThreads, 3) k_nrc_forward(const __grid_con
       tc_fence_after();
       if (l < 4) {
 #pragma unroll
-        for (int hf = 0; hf < 2; ++hf) {
-          float v[32];
-          tmem_ld32(tl + 32u * hf, v);
-          bias_relu_store32(XA, row, 32 * hf, v, sb + 64 * l + 32 * hf);
+        for (int q = 0; q < 4; ++q) {
+          float v[16];
+          tmem_ld16(tl + 16u * q, v);
+          bias_relu_store16(XA, row, 16 * q, v, sb + 64 * l + 16 * q);
         }
         tc_fence_before();
         fence_proxy_async();
