@@ -381,8 +381,11 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
       aoff[k * 3 + jj] = (min(max(t.z0 / 2 - 1 + k, 0), a.UM[2] - 1) * a.UM[1] +
                           min(max(y0 / 2 - 1 + jj, 0), a.UM[1] - 1)) * a.UM[0] + qx;
   const bool ploader = lane < 18;
+  // x blend from the parent columns (lane + 1) / 2 and the next one: the
+  // weight-3/4 column first (the lower one for odd lanes).  Every 1D blend is
+  // a + 3 b = 4 (a/4 + 3b/4); the factor 64 of the three is divided out once.
   const int src_lo = (lane + 1) >> 1;
-  const float wlo = (lane & 1) ? 0.75f : 0.25f, whi = 1.0f - wlo;
+  const int src_near = (lane & 1) ? src_lo : src_lo + 1, src_far = (lane & 1) ? src_lo + 1 : src_lo;
 
   // TM: the block's parent box starts at (0, ys, zs); the clamped rows and
   // planes above fall inside it (up_rows = rows of the tile / 2 + 2)
@@ -482,13 +485,13 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
               float zv[3];
 #pragma unroll
               for (int jy = 0; jy < 3; ++jy)
-                zv[jy] = ez == 0 ? fmaf(0.25f, av[jy], 0.75f * av[3 + jy]) : fmaf(0.75f, av[3 + jy], 0.25f * av[6 + jy]);
-              const float v0 = fmaf(0.25f, zv[0], 0.75f * zv[1]);
-              const float v1 = fmaf(0.75f, zv[1], 0.25f * zv[2]);
-              const float l0 = __shfl_sync(0xFFFFFFFFu, v0, src_lo), h0 = __shfl_sync(0xFFFFFFFFu, v0, src_lo + 1);
-              const float l1 = __shfl_sync(0xFFFFFFFFu, v1, src_lo), h1 = __shfl_sync(0xFFFFFFFFu, v1, src_lo + 1);
-              mv[ez * 2 + 0] = fmaf(wlo, l0, whi * h0);
-              mv[ez * 2 + 1] = fmaf(wlo, l1, whi * h1);
+                zv[jy] = fmaf(3.f, av[3 + jy], ez == 0 ? av[jy] : av[6 + jy]);
+              const float v0 = fmaf(3.f, zv[1], zv[0]);
+              const float v1 = fmaf(3.f, zv[1], zv[2]);
+              const float n0 = __shfl_sync(0xFFFFFFFFu, v0, src_near), f0 = __shfl_sync(0xFFFFFFFFu, v0, src_far);
+              const float n1 = __shfl_sync(0xFFFFFFFFu, v1, src_near), f1 = __shfl_sync(0xFFFFFFFFu, v1, src_far);
+              mv[ez * 2 + 0] = fmaf(3.f, n0, f0) * (1.f / 64.f);
+              mv[ez * 2 + 1] = fmaf(3.f, n1, f1) * (1.f / 64.f);
             }
           }
 #pragma unroll
