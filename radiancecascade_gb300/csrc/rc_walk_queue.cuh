@@ -365,6 +365,7 @@ struct TableWalker {
 };
 
 constexpr int kQueueThreads = 256;
+constexpr bool kWalkGroups = true;  // warps walk 32 consecutive items in step (else lanes refill one by one)
 
 // Every warp walks queue items taken from *counter (a global or shared
 // counter) until the items up to `end` are gone; lanes refill one by one.
@@ -402,10 +403,35 @@ static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __gri
   walk_tasks<4>(q, q.counter, q.total);
 }
 
+// Every warp takes 32 consecutive queue items at a time and walks them in
+// step: lanes of one direction share the table entries and load neighbouring
+// words; the warp takes its next 32 items when all of its lanes are done.
+template <int kBatch, typename W>
+__device__ __forceinline__ void walk_groups(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+  const int lane = threadIdx.x & 31;
+  W w;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32ull);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if ((int64_t)base >= end) break;
+    const int64_t item = (int64_t)base + lane;
+    bool active = item < end && w.init(q, item);
+    while (__any_sync(0xFFFFFFFFu, active))
+      if (active && w.template batch<kBatch>(q)) {
+        w.finish();
+        active = false;
+      }
+  }
+}
+
 // The walks of levels that all have step tables (4 blocks/SM: 64 registers,
 // no spills; the extra resident warps hide the mask loads' latency).
 static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
-  walk_tasks<4, TableWalker>(q, q.counter, q.total);
+  if (kWalkGroups)
+    walk_groups<4, TableWalker>(q, q.counter, q.total);
+  else
+    walk_tasks<4, TableWalker>(q, q.counter, q.total);
 }
 
 // Merge of a narrow level from its walk records, probe p: parent texels
