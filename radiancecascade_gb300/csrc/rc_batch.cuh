@@ -127,7 +127,7 @@ __device__ __forceinline__ void batch_item(const BatchLevel& lv, int tile, const
 }
 
 __device__ __forceinline__ void batch_walk(const QueueArgs& q, unsigned long long* counter, int64_t end) {
-  walk_tasks<kBatchWalkSteps>(q, counter, end);
+  walk_groups<kBatchWalkSteps, Walker>(q, counter, end);
 }
 
 // Bounded wait (about one second of SM clocks) until entry `e` has finished
