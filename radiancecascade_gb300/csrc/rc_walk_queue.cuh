@@ -365,47 +365,12 @@ struct TableWalker {
 };
 
 constexpr int kQueueThreads = 256;
-constexpr bool kWalkGroups = true;  // warps walk 32 consecutive items in step (else lanes refill one by one)
 
-// Every warp walks queue items taken from *counter (a global or shared
-// counter) until the items up to `end` are gone; lanes refill one by one.
-// kBatch steps are issued per lane between refills.
-template <int kBatch, typename W = Walker>
-__device__ __forceinline__ void walk_tasks(const QueueArgs& q, unsigned long long* counter, int64_t end) {
-  const int lane = threadIdx.x & 31;
-  W w;
-  bool active = false, exhausted = false;
-  for (;;) {
-    const unsigned need = __ballot_sync(0xFFFFFFFFu, !active && !exhausted);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
-      base = __shfl_sync(0xFFFFFFFFu, base, leader);
-      if (!active && !exhausted) {
-        const int64_t item = (int64_t)base + __popc(need & ((1u << lane) - 1u));
-        if (item >= end) exhausted = true;
-        else active = w.init(q, item);
-      }
-    }
-    if (!__any_sync(0xFFFFFFFFu, active)) {
-      if (!__any_sync(0xFFFFFFFFu, !exhausted)) break;
-      continue;
-    }
-    if (active && w.batch<kBatch>(q)) {
-      w.finish();
-      active = false;
-    }
-  }
-}
-
-static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
-  walk_tasks<4>(q, q.counter, q.total);
-}
-
-// Every warp takes 32 consecutive queue items at a time and walks them in
-// step: lanes of one direction share the table entries and load neighbouring
-// words; the warp takes its next 32 items when all of its lanes are done.
+// Every warp takes 32 consecutive queue items at a time (from *counter, a
+// global or shared counter, up to `end`) and walks them in step: lanes of one
+// direction share the table entries and load neighbouring words; the warp
+// takes its next 32 items when all of its lanes are done.  (Refilling lanes
+// one by one instead left two thirds of the lanes idle per instruction.)
 template <int kBatch, typename W>
 __device__ __forceinline__ void walk_groups(const QueueArgs& q, unsigned long long* counter, int64_t end) {
   const int lane = threadIdx.x & 31;
@@ -425,13 +390,14 @@ __device__ __forceinline__ void walk_groups(const QueueArgs& q, unsigned long lo
   }
 }
 
+static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __grid_constant__ QueueArgs q) {
+  walk_groups<4, Walker>(q, q.counter, q.total);
+}
+
 // The walks of levels that all have step tables (4 blocks/SM: 64 registers,
 // no spills; the extra resident warps hide the mask loads' latency).
 static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
-  if (kWalkGroups)
-    walk_groups<4, TableWalker>(q, q.counter, q.total);
-  else
-    walk_tasks<4, TableWalker>(q, q.counter, q.total);
+  walk_groups<4, TableWalker>(q, q.counter, q.total);
 }
 
 // Merge of a narrow level from its walk records, probe p: parent texels
