@@ -71,7 +71,7 @@ void release(rc_context* c) {
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
-  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->d_reg, c->d_slist, c->qsteps, c->qstep_begin};
+  void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->qsteps, c->qstep_begin};  // d_reg, d_slist point into d_sph
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -107,21 +107,19 @@ rc_status ensure_sphere_capacity(rc_context* c, int n) {
       c->stage_pending[k] = false;
     }
   if (c->d_sph) cudaFree(c->d_sph);
-  if (c->d_reg) cudaFree(c->d_reg);
-  if (c->d_slist) cudaFree(c->d_slist);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   c->d_sph = nullptr;
   c->d_reg = nullptr;
   c->d_slist = nullptr;
   c->h_stage = nullptr;
   c->sph_cap = 0;
-  rc_status s = dev_alloc((void**)&c->d_sph, sizeof(QSphere) * cap, "sphere buffer");
-  if (s != RC_OK) return s;
-  s = dev_alloc((void**)&c->d_reg, sizeof(Region) * (2 * cap + 1), "region buffer");
-  if (s != RC_OK) return s;
-  s = dev_alloc((void**)&c->d_slist, sizeof(int32_t) * kSphereListCap * cap, "sphere list buffer");
-  if (s != RC_OK) return s;
+  // one device buffer laid out as a staging slot (spheres, regions, sphere
+  // lists), so that an update is one host-to-device copy
   c->slot_bytes = sizeof(QSphere) * cap + sizeof(Region) * (2 * cap + 1) + sizeof(int32_t) * kSphereListCap * cap;
+  rc_status s = dev_alloc((void**)&c->d_sph, c->slot_bytes, "sphere buffer");
+  if (s != RC_OK) return s;
+  c->d_reg = reinterpret_cast<Region*>(reinterpret_cast<char*>(c->d_sph) + sizeof(QSphere) * cap);
+  c->d_slist = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(c->d_reg) + sizeof(Region) * (2 * cap + 1));
   RC_CUDA(cudaMallocHost(&c->h_stage, 2 * c->slot_bytes), "pinned staging buffer");
   c->sph_cap = cap;
   return RC_OK;
@@ -186,11 +184,10 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
       sreg[r].sn = -1;
     }
   }
-  RC_CUDA(cudaMemcpyAsync(c->d_sph, st, sizeof(QSphere) * n, cudaMemcpyHostToDevice, c->stream), "sphere upload");
-  RC_CUDA(cudaMemcpyAsync(c->d_reg, sreg, sizeof(Region) * nreg, cudaMemcpyHostToDevice, c->stream), "region upload");
-  if (listed)
-    RC_CUDA(cudaMemcpyAsync(c->d_slist, slist, sizeof(int32_t) * listed, cudaMemcpyHostToDevice, c->stream),
-            "sphere list upload");
+  // spheres, regions and lists in one copy (the slot's layout is the buffer's)
+  const size_t used = listed ? (size_t)(reinterpret_cast<char*>(slist + listed) - st)
+                             : (size_t)(reinterpret_cast<char*>(sreg + nreg) - st);
+  RC_CUDA(cudaMemcpyAsync(c->d_sph, st, used, cudaMemcpyHostToDevice, c->stream), "sphere upload");
   RC_CUDA(cudaEventRecord(c->ev_stage[k], c->stream), "event record");
   c->stage_pending[k] = true;
   int64_t words = 0;
