@@ -493,50 +493,25 @@ size_t queue_records_bytes(const rc_context* c) {
   return total;
 }
 
-// Step tables of the queue levels: each direction's walk replayed on the host
-// with the device's rule (the axis with the smallest next T; x before y
-// before z on ties), one entry per visited offset, cut where every probe of
-// the level has left the grid on some axis (the offset moves monotonically
-// on each axis, so no later step comes back).  Returns false, leaving the
-// queue on its own DDA, when a coarse cell does not fit a signed byte.
+// Step tables of the queue levels (walk_steps per direction).  Returns
+// false, leaving the queue on its own DDA, when a coarse cell does not fit a
+// signed byte.
 bool build_step_tables(rc_context* c, const std::vector<DirInfo>& tab, std::vector<uint2>& steps,
                        std::vector<int32_t>& begin, int32_t begin_off[kMaxCascades]) {
+  static_assert(sizeof(WalkStep) == sizeof(uint2), "a step table entry is a uint2 on the device");
   for (int i = 0; i < c->nlev; ++i) {
     if (c->mode[i] != kModeQueue) continue;
     const LevelGeom& g = c->geom[i];
-    int l2s = 0;
-    while ((1 << l2s) < g.spacing) ++l2s;
-    const int s = 1 << l2s, h = s >> 1;
     begin_off[i] = (int32_t)begin.size();
     for (int d = 0; d < g.ndirs; ++d) {
       if (steps.size() > (size_t)INT32_MAX / 2) return false;
       begin.push_back((int32_t)steps.size());
       const DirInfo& di = tab[c->dir_off[i] + d];
-      int64_t a[3], t[3];
-      for (int ax = 0; ax < 3; ++ax) {
-        a[ax] = h + di.start_off[ax];
-        t[ax] = di.first_T[ax];
-      }
-      auto push = [&]() -> int {  // 1 pushed, 0 every probe out of the grid, -1 cell out of range
-        uint32_t ph = 0, pc = 0;
-        for (int ax = 2; ax >= 0; --ax) {
-          if (a[ax] >= c->p.grid[ax] || a[ax] + (int64_t)(g.M[ax] - 1) * s < 0) return 0;
-          const int64_t cell = a[ax] >> l2s;  // floor division
-          if (cell < -127 || cell > 127) return -1;
-          ph = (ph << l2s) | (uint32_t)(a[ax] & (s - 1));
-          pc |= ((uint32_t)cell & 0xFFu) << (8 * ax);
-        }
-        steps.push_back(make_uint2(ph, pc));
-        return 1;
-      };
-      int r = i == 0 ? push() : 1;  // cascade 0 tests the probe's own voxel first
-      for (int k = 0; k < di.steps && r == 1; ++k) {
-        const int ax = (t[0] <= t[1] && t[0] <= t[2]) ? 0 : (t[1] <= t[2] ? 1 : 2);
-        a[ax] += di.sgn[ax];
-        t[ax] += di.step_T[ax];
-        r = push();
-      }
-      if (r < 0) return false;
+      const int64_t n = walk_steps(g, c->p.grid, di, i == 0, nullptr, 0);  // count first
+      if (n < 0) return false;
+      const size_t at = steps.size();
+      steps.resize(at + (size_t)n);
+      walk_steps(g, c->p.grid, di, i == 0, reinterpret_cast<WalkStep*>(steps.data() + at), n);
     }
     begin.push_back((int32_t)steps.size());
   }

@@ -102,6 +102,40 @@ static int64_t crossings(int64_t b, int64_t Da, int64_t S) {
   return k;
 }
 
+int64_t walk_steps(const LevelGeom& g, const int32_t grid[3], const DirInfo& di, bool test_start, WalkStep* out,
+                   int64_t cap) {
+  int l2s = 0;
+  while ((1 << l2s) < g.spacing) ++l2s;
+  const int s = 1 << l2s, h = s >> 1;
+  int64_t a[3], t[3], n = 0;
+  for (int ax = 0; ax < 3; ++ax) {
+    a[ax] = h + di.start_off[ax];
+    t[ax] = di.first_T[ax];
+  }
+  // 1 stored, 0 every probe out of the grid, -1 cell out of range
+  auto push = [&]() -> int {
+    uint32_t ph = 0, pc = 0;
+    for (int ax = 2; ax >= 0; --ax) {
+      if (a[ax] >= grid[ax] || a[ax] + (int64_t)(g.M[ax] - 1) * s < 0) return 0;
+      const int64_t cell = a[ax] >> l2s;  // floor division
+      if (cell < -127 || cell > 127) return -1;
+      ph = (ph << l2s) | (uint32_t)(a[ax] & (s - 1));
+      pc |= ((uint32_t)cell & 0xFFu) << (8 * ax);
+    }
+    if (n < cap) out[n] = WalkStep{ph, pc};
+    ++n;
+    return 1;
+  };
+  int r = test_start ? push() : 1;
+  for (int k = 0; k < di.steps && r == 1; ++k) {
+    const int ax = (t[0] <= t[1] && t[0] <= t[2]) ? 0 : (t[1] <= t[2] ? 1 : 2);
+    a[ax] += di.sgn[ax];
+    t[ax] += di.step_T[ax];
+    r = push();
+  }
+  return r < 0 ? -1 : n;
+}
+
 bool build_dir_table(const LevelGeom& g, const int32_t grid[3], DirInfo* out, char* msg, size_t cap) {
   // A ray from a probe inside the grid is outside it beyond the grid diagonal,
   // so the walk never needs crossings farther away than that.

@@ -75,6 +75,22 @@ void level_geometry(const rc_params& p, LevelGeom* out);  // out[num_cascades]
 // Fills the direction table of one level; returns false (with msg) when the
 // integer walk would leave the exact 32-bit range.
 bool build_dir_table(const LevelGeom& g, const int32_t grid[3], DirInfo* out, char* msg, size_t cap);
+
+// One step of a walk as the queue kernel replays it: the voxel offset from
+// the probe's cell origin split into the decimated-plane phase index
+// ((pz << l2s) + py) << l2s + px and the coarse cell (cx, cy, cz) as three
+// signed bytes (cx in bits 0-7).  Same layout as the device's uint2.
+struct WalkStep {
+  uint32_t phase;
+  uint32_t cell;
+};
+// Appends to `out` the steps of direction `di` of level `g` (the start voxel
+// first when `test_start`), replayed with the walk's own rule (the axis with
+// the smallest next T; x before y before z on ties) and cut where every probe
+// of the level has left the grid on some axis.  Returns the number of steps,
+// or -1 when a coarse cell does not fit a signed byte.
+int64_t walk_steps(const LevelGeom& g, const int32_t grid[3], const DirInfo& di, bool test_start, WalkStep* out,
+                   int64_t cap);
 // Largest number of voxel crossings any direction of the level takes.
 int64_t max_level_steps(const LevelGeom& g, const int32_t grid[3]);
 void quantise_sphere(const rc_sphere& s, QSphere* q);
