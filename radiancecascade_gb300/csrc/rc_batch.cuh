@@ -126,8 +126,20 @@ __device__ __forceinline__ void batch_item(const BatchLevel& lv, int tile, const
   }
 }
 
-__device__ __forceinline__ void batch_walk(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+// A scene's walks replay its step tables when it has them (every level of a
+// scene has them or none does), else run their own DDA.  Separate functions,
+// so that each walker gets its own register allocation.
+__device__ __noinline__ void batch_walk_tables(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+  walk_groups<kBatchWalkSteps, TableWalker>(q, counter, end);
+}
+__device__ __noinline__ void batch_walk_dda(const QueueArgs& q, unsigned long long* counter, int64_t end) {
   walk_groups<kBatchWalkSteps, Walker>(q, counter, end);
+}
+__device__ __forceinline__ void batch_walk(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+  if (q.lv[0].steps)
+    batch_walk_tables(q, counter, end);
+  else
+    batch_walk_dda(q, counter, end);
 }
 
 // Bounded wait (about one second of SM clocks) until entry `e` has finished

@@ -756,7 +756,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
     }
     setup_queue(c, c->recs, c->qcounter);
   }
-  if (!minimal && c->qargs.n > 0 && !(getenv("RC_WALK_TABLES") && strcmp(getenv("RC_WALK_TABLES"), "0") == 0)) {
+  if (c->qargs.n > 0 && !(getenv("RC_WALK_TABLES") && strcmp(getenv("RC_WALK_TABLES"), "0") == 0)) {
     std::vector<uint2> st;
     std::vector<int32_t> begin;
     int32_t boff[kMaxCascades] = {};
