@@ -152,38 +152,8 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
   memcpy(sreg, regions, sizeof(Region) * nreg);
   // per-region lists of the spheres whose extent meets the region (a region
   // of the whole grid, or an update whose lists would not fit, tests them all)
-  int64_t listed = 0;
-  const int64_t list_cap = (int64_t)kSphereListCap * c->sph_cap;
-  bool lists = n > 0 && (int64_t)nreg * n <= (int64_t)1 << 22;
-  std::vector<Region> ext;
-  if (lists) {
-    ext.resize(n);
-    for (int i = 0; i < n; ++i)
-      if (!sphere_region(c->cur[i], c->p.grid, &ext[i])) ext[i].w1 = ext[i].w0;  // empty: meets nothing
-  }
-  for (int r = 0; r < nreg && lists; ++r) {
-    Region& g = sreg[r];
-    g.s0 = (int32_t)listed;
-    g.sn = 0;
-    for (int i = 0; i < n; ++i) {
-      const Region& e = ext[i];
-      if (e.w0 < g.w1 && g.w0 < e.w1 && e.y0 < g.y1 && g.y0 < e.y1 && e.z0 < g.z1 && g.z0 < e.z1) {
-        if (listed == list_cap) {
-          lists = false;
-          break;
-        }
-        slist[listed++] = i;
-        ++g.sn;
-      }
-    }
-  }
-  if (!lists) {
-    listed = 0;
-    for (int r = 0; r < nreg; ++r) {
-      sreg[r].s0 = 0;
-      sreg[r].sn = -1;
-    }
-  }
+  const int64_t listed = sphere_lists(c->cur.data(), n, c->p.grid, sreg, nreg, slist,
+                                      (int64_t)kSphereListCap * c->sph_cap);
   // spheres, regions and lists in one copy (the slot's layout is the buffer's)
   const size_t used = listed ? (size_t)(reinterpret_cast<char*>(slist + listed) - st)
                              : (size_t)(reinterpret_cast<char*>(sreg + nreg) - st);
@@ -961,33 +931,10 @@ rc_status rc_scene_set_spheres(rc_context* c, const rc_sphere* spheres, int32_t 
   std::vector<Region> regs;
   bool full = (int)c->cur.size() != n;
   if (!full) {
-    // A sphere's old and new extents become one region (their bounding box)
-    // when that box is no larger than the two apart -- the usual case of a
-    // sphere moving a voxel or less per frame, which overlaps itself.
-    auto words = [](const Region& r) { return (int64_t)(r.w1 - r.w0) * (r.y1 - r.y0) * (r.z1 - r.z0); };
-    for (int i = 0; i < n; ++i) {
-      Region a, b;
-      const bool ha = sphere_region(c->cur[i], c->p.grid, &a), hb = sphere_region(next[i], c->p.grid, &b);
-      if (ha && hb) {
-        Region u = a;
-        u.w0 = std::min(a.w0, b.w0);
-        u.w1 = std::max(a.w1, b.w1);
-        u.y0 = std::min(a.y0, b.y0);
-        u.y1 = std::max(a.y1, b.y1);
-        u.z0 = std::min(a.z0, b.z0);
-        u.z1 = std::max(a.z1, b.z1);
-        if (words(u) <= words(a) + words(b)) {
-          regs.push_back(u);
-        } else {
-          regs.push_back(a);
-          regs.push_back(b);
-        }
-      } else if (ha) {
-        regs.push_back(a);
-      } else if (hb) {
-        regs.push_back(b);
-      }
-    }
+    // a sphere moving a voxel or less per frame overlaps itself: its old and
+    // new extents usually become one region
+    regs.resize((size_t)2 * n);
+    regs.resize((size_t)update_regions(c->cur.data(), next.data(), n, c->p.grid, regs.data()));
   }
   c->cur.swap(next);
   rc_status s = ensure_sphere_capacity(c, std::max(n, 1));

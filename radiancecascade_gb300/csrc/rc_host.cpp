@@ -225,6 +225,71 @@ bool sphere_region(const QSphere& q, const int32_t grid[3], Region* r) {
   return true;
 }
 
+int update_regions(const QSphere* old_sph, const QSphere* new_sph, int n, const int32_t grid[3], Region* out) {
+  auto words = [](const Region& r) { return (int64_t)(r.w1 - r.w0) * (r.y1 - r.y0) * (r.z1 - r.z0); };
+  int k = 0;
+  for (int i = 0; i < n; ++i) {
+    Region a, b;
+    const bool ha = sphere_region(old_sph[i], grid, &a), hb = sphere_region(new_sph[i], grid, &b);
+    if (ha && hb) {
+      Region u = a;
+      u.w0 = std::min(a.w0, b.w0);
+      u.w1 = std::max(a.w1, b.w1);
+      u.y0 = std::min(a.y0, b.y0);
+      u.y1 = std::max(a.y1, b.y1);
+      u.z0 = std::min(a.z0, b.z0);
+      u.z1 = std::max(a.z1, b.z1);
+      if (words(u) <= words(a) + words(b)) {
+        out[k++] = u;
+      } else {
+        out[k++] = a;
+        out[k++] = b;
+      }
+    } else if (ha) {
+      out[k++] = a;
+    } else if (hb) {
+      out[k++] = b;
+    }
+  }
+  return k;
+}
+
+int64_t sphere_lists(const QSphere* sph, int n, const int32_t grid[3], Region* regs, int nreg, int32_t* list,
+                     int64_t cap) {
+  int64_t listed = 0;
+  bool ok = n > 0 && (int64_t)nreg * n <= (int64_t)1 << 22;
+  std::vector<Region> ext;
+  if (ok) {
+    ext.resize((size_t)n);
+    for (int i = 0; i < n; ++i)
+      if (!sphere_region(sph[i], grid, &ext[(size_t)i])) ext[(size_t)i].w1 = ext[(size_t)i].w0;  // meets nothing
+  }
+  for (int r = 0; r < nreg && ok; ++r) {
+    Region& g = regs[r];
+    g.s0 = (int32_t)listed;
+    g.sn = 0;
+    for (int i = 0; i < n; ++i) {
+      const Region& e = ext[(size_t)i];
+      if (e.w0 < g.w1 && g.w0 < e.w1 && e.y0 < g.y1 && g.y0 < e.y1 && e.z0 < g.z1 && g.z0 < e.z1) {
+        if (listed == cap) {
+          ok = false;
+          break;
+        }
+        list[listed++] = i;
+        ++g.sn;
+      }
+    }
+  }
+  if (!ok) {
+    listed = 0;
+    for (int r = 0; r < nreg; ++r) {
+      regs[r].s0 = 0;
+      regs[r].sn = -1;
+    }
+  }
+  return listed;
+}
+
 // ---------------------------------------------------------------------------
 // Solid angle of an octahedral texel.  Each texel is a square in (|u|,|v|);
 // the line |u|+|v| = 1 splits it into an upper and a lower planar piece on

@@ -96,5 +96,15 @@ int64_t max_level_steps(const LevelGeom& g, const int32_t grid[3]);
 void quantise_sphere(const rc_sphere& s, QSphere* q);
 // Bounding region (whole x-words, clipped to the grid) of a quantised sphere.
 bool sphere_region(const QSphere& q, const int32_t grid[3], Region* r);
+// Regions an emitter update recomposes, appended to `out` (at most 2 per
+// sphere): for each sphere the box around its old and new extents when that
+// box is no larger than the two apart, else both.  Returns the count added.
+int update_regions(const QSphere* old_sph, const QSphere* new_sph, int n, const int32_t grid[3], Region* out);
+// For each region, the spheres whose extent meets it (ascending indices)
+// into list[regs[r].s0 .. + regs[r].sn).  When the lists would exceed `cap`
+// entries or `nreg * n` tests exceed 2^22, every region gets sn = -1 (test all
+// spheres).  Returns the number of list entries.
+int64_t sphere_lists(const QSphere* sph, int n, const int32_t grid[3], Region* regs, int nreg, int32_t* list,
+                     int64_t cap);
 void set_error(const char* fmt, ...);
 }  // namespace rcx
