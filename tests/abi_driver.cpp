@@ -72,6 +72,13 @@ static int host_checks() {
   CHECK(rc_get_fluence(nullptr, nullptr, 0, RC_MEM_HOST) == RC_ERR_INVALID_ARG);
   CHECK(rc_create(&p, 0, nullptr) == RC_ERR_INVALID_ARG);
   CHECK(rc_batch_destroy(nullptr) == RC_OK);
+  CHECK(rc_batch_solve(nullptr, nullptr) == RC_ERR_INVALID_ARG);
+  CHECK(rc_get_fluence_async(nullptr, nullptr, 0) == RC_ERR_INVALID_ARG);
+  CHECK(rc_shade_set_mesh(nullptr, nullptr, 0, nullptr, 0, nullptr, nullptr, 0, nullptr, 0) == RC_ERR_INVALID_ARG);
+  rc_shade_view view;
+  std::memset(&view, 0, sizeof view);
+  CHECK(rc_shade_draw(nullptr, &view, nullptr, RC_MEM_HOST) == RC_ERR_INVALID_ARG);
+  CHECK(rc_nrc_enable(nullptr, nullptr) == RC_ERR_INVALID_ARG);
   std::printf("host ok\n");
   return 0;
 }
