@@ -409,6 +409,10 @@ int32_t rc_nrc_param_count(void);
  *             (sum of rc_level_info.radiance_bytes)
  *   stream    cudaStream_t or NULL (legacy default stream)
  *
+ * All three buffers must be 16-byte aligned (cudaMalloc's 256-byte alignment
+ * is ample); a misaligned pointer returns RC_ERR_INVALID_ARG before any GPU
+ * work.
+ *
  * Its working memory (opacity bits, the per-level decimated opacity, the
  * child-averaged radiance and the walk tables) lives in one statically sized
  * device array of RC_NOALLOC_SCRATCH_BYTES (8 MiB, enough for grids up to 64^3

@@ -1355,11 +1355,24 @@ constexpr int kNoallocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 void* g_noalloc_scratch_ptr[kNoallocMaxDevices] = {};
 
-// Host staging of the walk tables.  A pageable cudaMemcpyAsync has copied
-// its source by the time it returns, so one static buffer serves all calls.
+// Host staging of the walk tables (built under the mutex below).
 constexpr size_t kNoallocMaxDirs = RC_NOALLOC_SCRATCH_BYTES / sizeof(DirInfo);
 DirInfo g_noalloc_tab[kNoallocMaxDirs];
 double g_noalloc_omega[kNoallocMaxDirs];
+
+// The tables reach the scratch as kernel arguments, in chunks of 640 entries
+// (30,720 bytes; kernel arguments may take up to 32,764 bytes).  A launch
+// copies its arguments when it is made, so no work left on the stream reads
+// the host staging above, which the next call rewrites.
+constexpr int kTabChunk = 640;
+struct DirChunk {
+  DirInfo d[kTabChunk];
+};
+static_assert(sizeof(DirChunk) + 16 <= 32764, "walk-table chunk fits the kernel-argument limit");
+
+__global__ void k_put_dirs(DirInfo* __restrict__ dst, int n, const __grid_constant__ DirChunk c) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = c.d[i];
+}
 
 // Opacity bits and decimated opacity of a caller-owned volume (the volume is
 // only read).
@@ -1407,6 +1420,12 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   }
   if (!voxels || !fluence || !radiance) {
     rcx::set_error("rc_solve_noalloc: voxels, fluence and radiance must be device pointers, not NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  // The kernels read and write these buffers with 16-byte vector accesses.
+  if ((reinterpret_cast<uintptr_t>(voxels) | reinterpret_cast<uintptr_t>(fluence) |
+       reinterpret_cast<uintptr_t>(radiance)) & 15u) {
+    rcx::set_error("rc_solve_noalloc: voxels, fluence and radiance must be 16-byte aligned");
     return RC_ERR_INVALID_ARG;
   }
   int dev = 0;
@@ -1483,8 +1502,13 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   rc_solid_angles(v.geom[0].n, g_noalloc_omega);
   for (int d = 0; d < v.geom[0].ndirs; ++d) g_noalloc_tab[d].omega = (float)g_noalloc_omega[d];
   DirInfo* dirs = reinterpret_cast<DirInfo*>(scratch + dirs_off);
-  RC_CUDA(cudaMemcpyAsync(dirs, g_noalloc_tab, ndirs_total * sizeof(DirInfo), cudaMemcpyHostToDevice, st),
-          "rc_solve_noalloc: table upload");
+  for (size_t c0 = 0; c0 < ndirs_total; c0 += kTabChunk) {
+    const int cnt = (int)std::min<size_t>(kTabChunk, ndirs_total - c0);
+    DirChunk chunk;
+    memcpy(chunk.d, g_noalloc_tab + c0, (size_t)cnt * sizeof(DirInfo));
+    k_put_dirs<<<1, 256, 0, st>>>(dirs + c0, cnt, chunk);
+    RC_CUDA(cudaGetLastError(), "rc_solve_noalloc: table upload");
+  }
   // Decimated opacity keeps unused padding bits at zero; the previous call's
   // contents are cleared.  Everything else is fully rewritten below.
   if (mask_bytes) RC_CUDA(cudaMemsetAsync(scratch + mask_begin, 0, mask_bytes, st), "rc_solve_noalloc: clear");

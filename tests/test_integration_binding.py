@@ -1,31 +1,36 @@
-"""The Rust binding a maintainer adds to the reference crate (INTEGRATION.md,
-section 2) cannot be compiled in this image (no cargo).  This checks it
-against the C header without Rust: every `#[repr(C)]` struct's size and
-field offsets, computed with C layout rules from the Rust field types, must
-equal what gcc reports for the same struct of `include/rc.h`, and every
-`extern "C"` function must be declared in the header with the same number
-of parameters."""
+"""The Rust binding a maintainer adds to the reference crate
+(integration/rust/src/gi/ffi.rs and the GiStage in mod.rs) cannot be compiled
+in this image (no cargo).  This checks it against the C header without Rust:
+every `#[repr(C)]` struct's size and field offsets, computed with C layout
+rules from the Rust field types, must equal what gcc reports for the same
+struct of `include/rc.h`; every `extern "C"` function must be declared in the
+header with the same number of parameters, and every function of the header
+must be bound."""
 import os
 import re
 import subprocess
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-DOC = os.path.join(ROOT, "INTEGRATION.md")
+FFI = os.path.join(ROOT, "integration", "rust", "src", "gi", "ffi.rs")
+STAGE = os.path.join(ROOT, "integration", "rust", "src", "gi", "mod.rs")
 HDR = os.path.join(ROOT, "include", "rc.h")
 SCALARS = {"i8": 1, "u8": 1, "i16": 2, "u16": 2, "i32": 4, "u32": 4, "f32": 4, "i64": 8, "u64": 8, "f64": 8,
            "c_int": 4, "c_char": 1}
 
 
 def _rust_block():
-    text = open(DOC).read()
-    m = re.search(r"## 2\. `extern \"C\"` block.*?```rust\n(.*?)```", text, re.S)
-    assert m, "INTEGRATION.md has no extern block"
-    return m.group(1)
+    text = open(FFI).read()
+    return re.sub(r"//[^\n]*", "", text)
+
+
+def _header_functions():
+    hdr = re.sub(r"/\*.*?\*/", "", open(HDR).read(), flags=re.S)
+    return hdr, set(re.findall(r"\b(rc_\w+)\s*\([^)]*\)\s*;", hdr))
 
 
 def _rust_structs(block):
     out = {}
-    for name, body in re.findall(r"#\[repr\(C\)\][^\n]*\n?\s*pub struct (\w+)\s*\{(.*?)\}", block, re.S):
+    for name, body in re.findall(r"#\[repr\(C\)\](?:\s*#\[[^\]]*\])*\s*pub struct (\w+)\s*\{(.*?)\}", block, re.S):
         fields = re.findall(r"(?:pub\s+)?(\w+)\s*:\s*([^,]+?)\s*(?:,|$)", body.strip())
         out[name] = [(f, t.strip()) for f, t in fields]
     return out
@@ -82,7 +87,8 @@ def _c_layouts(structs, tmp_path):
 
 def test_rust_structs_match_the_c_layout(tmp_path):
     structs = {k: v for k, v in _rust_structs(_rust_block()).items() if not all(f.startswith("_") for f, _ in v)}
-    assert {"rc_params", "rc_voxel", "rc_sphere", "rc_nrc_params", "rc_shade_view"} <= set(structs)
+    assert {"rc_params", "rc_voxel", "rc_box", "rc_sphere", "rc_scene_spec", "rc_level_info", "rc_batch_tiles",
+            "rc_nrc_params", "rc_nrc_stats", "rc_shade_material", "rc_texture", "rc_shade_view"} <= set(structs)
     c = _c_layouts(structs, tmp_path)
     memo = {}
     for name in structs:
@@ -95,8 +101,8 @@ def test_rust_structs_match_the_c_layout(tmp_path):
 def test_rust_functions_are_declared_in_the_header():
     block = _rust_block()
     fns = re.findall(r"pub fn (\w+)\((.*?)\)\s*(?:->\s*[^;]+)?;", block, re.S)
-    assert len(fns) >= 20
-    hdr = re.sub(r"/\*.*?\*/", "", open(HDR).read(), flags=re.S)
+    hdr, declared = _header_functions()
+    assert declared == {name for name, _ in fns}, declared ^ {name for name, _ in fns}
     for name, params in fns:
         m = re.search(r"\b%s\s*\(([^)]*)\)\s*;" % name, hdr, re.S)
         assert m, "%s is not declared in include/rc.h" % name
@@ -104,3 +110,15 @@ def test_rust_functions_are_declared_in_the_header():
         n_c = 0 if cp in ("", "void") else cp.count(",") + 1
         n_r = 0 if not params.strip() else params.count(",") + 1
         assert n_c == n_r, (name, n_c, n_r)
+
+
+def test_stage_implements_the_render_stage_trait():
+    """GiStage provides the three methods of RenderStage<T> (reference:
+    src/app.rs:3-7) and calls only functions the binding declares."""
+    text = open(STAGE).read()
+    assert re.search(r"impl RenderStage<AppState> for GiStage", text)
+    for method in ("update", "render", "resize"):
+        assert re.search(r"fn %s\(" % method, text), method
+    bound = set(re.findall(r"pub fn (\w+)\(", _rust_block()))
+    used = set(re.findall(r"\b(rc_\w+)\(", text))
+    assert used and used <= bound, used - bound
