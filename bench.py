@@ -202,9 +202,10 @@ def timed_frames(eng, R, sph, frames, local):
 
 def learned_form(args, R, local, boxes, spheres, plain_fps):
     """The learned+FP16 form of the same moving-emitter workload: FP16 radiance,
-    cascades 2-5 from the neural radiance cache, refit every frame on a 1/16
-    slice of walked probes, per-8^3-tile fallback at 1% held-out error.  The
-    cache first learns for `learned_warmup` frames; the timed frames follow."""
+    the far cascades (from --learned-first-level, default 4) from the neural
+    radiance cache, refit every frame on 1/16 of the walked directions of every
+    far probe, per-8^3-tile fallback at 1% held-out error.  The cache first
+    learns for `learned_warmup` frames; the timed frames follow."""
     import torch
 
     from oracle import oracle as O
@@ -225,20 +226,24 @@ def learned_form(args, R, local, boxes, spheres, plain_fps):
         eng.solve()
         R.advance_spheres(sph, 256, 1)
     eng.synchronize()
+    before = eng.nrc_stats()["served_solves"]
     torch.cuda.nvtx.range_push("learned_timed")  # launch lists of the learned frames select this range
     ms, last = timed_frames(eng, R, sph, args.steps, local)
     torch.cuda.nvtx.range_pop()
     fps = args.steps / (ms / 1000.0)
     g = eng.fluence().astype(np.float64)
     st = eng.nrc_stats()
+    served = [(st["served_solves"][i] - before[i]) / args.steps for i in range(6)]
     eng.close()
     ref, _ = O.solve(O.params(256, 6), O.voxelise(256, boxes, last), jump=True)
     out.update({
         "frames_per_s": round(fps, 3), "ms_per_frame": round(ms / args.steps, 4),
         "speedup_vs_plain_fp32": round(fps / plain_fps, 4),
         "fluence_rel_l2_vs_fp64": float(np.linalg.norm(g - ref) / np.linalg.norm(ref)),
+        "fluence_max_abs_vs_fp64": float(np.abs(g - ref).max()),
         "fallback_tiles": int(st["fallback_tiles"]), "tiles": int(st["tiles"]),
         "cascades_from_network": [i for i in range(6) if (st["served_levels"] >> i) & 1],
+        "served_fraction_of_timed_frames": {str(i): round(served[i], 4) for i in range(args.learned_first_level, 6)},
         "frames_learned_before_timing": args.learned_warmup, "frames_timed": args.steps,
         "first_level": args.learned_first_level, "fallback_threshold": args.learned_threshold,
         "plain_level_fraction": args.learned_plain_fraction,
@@ -543,7 +548,7 @@ def main():
     ap.add_argument("--learned-warmup", type=int, default=48,
                     help="frames the radiance cache learns before the learned form is timed")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned+FP16 form")
-    ap.add_argument("--learned-first-level", type=int, default=2, help="first cascade the radiance cache serves")
+    ap.add_argument("--learned-first-level", type=int, default=4, help="first cascade the radiance cache serves")
     ap.add_argument("--learned-threshold", type=float, default=0.01,
                     help="held-out relative error above which a tile falls back to the plain walk")
     ap.add_argument("--learned-plain-fraction", type=float, default=0.5,

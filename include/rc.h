@@ -333,12 +333,19 @@ rc_status rc_shade_draw(rc_context* ctx, const rc_shade_view* view, float* out, 
  * up) from a small network instead of walking their intervals: it predicts
  * each (probe, direction)'s interval result (R = radiance of the first
  * opaque voxel, T = 1 when the ray got through) from a multiresolution hash
- * grid of the probe position and the direction.  Every solve it first walks
- * 1/2^train_fraction_log2 of the far probes (all their directions) to refit
- * the network (Adam), and a second such slice, held out, to measure its
- * error per voxel tile of fallback_tile^3; tiles whose relative L2 error of
- * (R, T) exceeds fallback_threshold use the plain walk for their probes;
- * a far cascade mostly in such tiles runs its plain kernels instead. */
+ * grid of the probe position and the direction.  Every solve walks
+ * 1/2^train_fraction_log2 of the directions of every far probe (a regular
+ * sub-lattice of the octahedral map, another one each solve) as training
+ * samples and a second such slice as held-out samples.  The held-out samples
+ * score the network per voxel tile of fallback_tile^3: the solid-angle
+ * weighted relative L2 error of the merged radiance (R + T x the next
+ * cascade's radiance) the tile's far probes hand to the cascades below, over
+ * this solve and over the last 2^train_fraction_log2 solves.  A tile above
+ * fallback_threshold on either walks its probes instead of serving them; a
+ * far cascade with at least plain_level_fraction of its probes in such tiles
+ * walks entirely.  The network then serves the other probes with the weights
+ * just scored, and one Adam step on the training samples prepares the next
+ * solve.  Every decision is taken on the device: rc_solve does not wait. */
 typedef struct rc_nrc_params {
   int32_t first_level;          /* first cascade served (default 2)          */
   int32_t hash_log2_entries;    /* entries per hash level, log2 (19)        */
@@ -346,29 +353,36 @@ typedef struct rc_nrc_params {
   int32_t max_resolution;       /* finest hash grid (512)                   */
   float learning_rate;          /* Adam step (1e-2)                         */
   float beta1, beta2, epsilon;  /* Adam (0.9, 0.99, 1e-10)                  */
-  int32_t train_fraction_log2;  /* training slice 1/2^k of the far probes (4) */
+  int32_t train_fraction_log2;  /* samples: 1/2^k of the far directions (4)  */
   int32_t steps_per_solve;      /* Adam steps per solve (1)                 */
   float fallback_threshold;     /* held-out relative L2 error (0.01)        */
   int32_t fallback_tile;        /* voxel tile edge, power of two (8)        */
   float radiance_scale;         /* network predicts R * scale (1/4)         */
   float plain_level_fraction;   /* a far cascade with at least this share of
-                                   its probes in fallback tiles runs the plain
-                                   walk for the whole cascade (0.5)         */
+                                   its probes in fallback tiles walks
+                                   entirely (0.5)                           */
   uint64_t seed;                /* initial weights                          */
 } rc_nrc_params;
+
+#define RC_MAX_CASCADES 10
 
 typedef struct rc_nrc_stats {
   int64_t solves;          /* solves served by the cache                     */
   int64_t steps;           /* Adam steps taken                               */
   float last_loss;         /* mean squared error of the last step            */
-  int32_t served_levels;   /* bit i: cascade i came from the network in the
-                              last solve (else its plain kernels ran)       */
+  int32_t served_levels;   /* bit i: the network served cascade i (its
+                              probes outside flagged tiles) in the last
+                              solve; else the whole cascade walked          */
   int64_t fallback_tiles;  /* of `tiles`, those on the plain walk now       */
   int64_t tiles;           /* fallback tiles that hold a far-cascade probe  */
+  int64_t served_solves[RC_MAX_CASCADES]; /* per cascade: solves since
+                              rc_nrc_enable in which the network served it  */
 } rc_nrc_stats;
 
 rc_status rc_nrc_params_default(rc_nrc_params* out);
-/* Allocates and initialises the cache (all tiles start on the plain walk). */
+/* Allocates and initialises the cache (all tiles start on the plain walk).
+ * Every far cascade must have the bit-parallel walk (RC_ERR_UNSUPPORTED
+ * otherwise, e.g. with RC_WALK=scalar). */
 rc_status rc_nrc_enable(rc_context* ctx, const rc_nrc_params* params);
 rc_status rc_nrc_disable(rc_context* ctx);
 /* Serialises the parameters (MLP and hash grid, FP32).  With out == NULL or

@@ -22,6 +22,7 @@ pub const RC_MEM_HOST: i32 = 0;
 pub const RC_MEM_DEVICE: i32 = 1;
 pub const RC_VOXEL_OPAQUE: u16 = 0x8000;
 pub const RC_NOALLOC_SCRATCH_BYTES: usize = 8 << 20;
+pub const RC_MAX_CASCADES: usize = 10;
 
 #[repr(C)]
 #[derive(Clone, Copy, Default, Debug)]
@@ -177,6 +178,7 @@ pub struct rc_nrc_stats {
     pub served_levels: i32,
     pub fallback_tiles: i64,
     pub tiles: i64,
+    pub served_solves: [i64; RC_MAX_CASCADES],
 }
 
 #[link(name = "rc")]

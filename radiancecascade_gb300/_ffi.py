@@ -53,7 +53,7 @@ class NrcParams(C.Structure):
 
 class NrcStats(C.Structure):
     _fields_ = [("solves", C.c_int64), ("steps", C.c_int64), ("last_loss", C.c_float), ("served_levels", C.c_int32),
-                ("fallback_tiles", C.c_int64), ("tiles", C.c_int64)]
+                ("fallback_tiles", C.c_int64), ("tiles", C.c_int64), ("served_solves", C.c_int64 * 10)]
 
 
 class ShadeMaterial(C.Structure):

@@ -16,6 +16,8 @@
 #include "rc_ctx.h"
 #include "rc_nrc.cuh"
 
+static_assert(RC_MAX_CASCADES == rcx::kMaxCascades, "rc_nrc_stats.served_solves covers every cascade");
+
 namespace rcx {
 
 struct NrcState {
@@ -30,28 +32,40 @@ struct NrcState {
   __nv_bfloat16* denc = nullptr;
   __half* rt = nullptr;
   int64_t total_queries = 0, enum_tiles = 0;
-  // tiles of the sample probes (all their directions), grouped by phase
+  // tiles of the sample probes (all their directions), grouped by phase; a
+  // tile's slot is its probe's index in the phase
   NrcTile* tiles = nullptr;
   std::vector<NrcTile> h_tiles;
   std::vector<uint8_t> probe_tile;  // tiles that hold a far probe
   std::vector<int64_t> tile_begin;
+  int32_t* dlist = nullptr;  // directions of the sample tiles, per level and phase
   int64_t max_tiles2 = 0, max_held = 0;
   float* target = nullptr;
   float* pred = nullptr;
   float* epos_grad = nullptr;
   float* loss = nullptr;
-  float* h_loss = nullptr;  // pinned
-  unsigned* count = nullptr;    // probes in fallback tiles per far level
-  unsigned* h_count = nullptr;  // pinned copy
-  cudaEvent_t ev_count = nullptr;
+  float* h_loss = nullptr;    // pinned
+  unsigned* count = nullptr;  // probes in fallback tiles per far level
+  int32_t* plain = nullptr;   // per level: 1 = the level runs on its walks this solve
+  unsigned long long* served_solves = nullptr;  // per level: solves the network served it
   int64_t total_probes = 0;
-  int served[kMaxCascades]{};  // levels served by the network in the last solve
   NrcTile* qtiles = nullptr;  // rc_nrc_query / rc_nrc_tile_gradient scratch
   float* qout = nullptr;
   int64_t qcap = 0;
+  // the far levels' own walk queue: records, step tables, per-word switches
+  QueueArgs fq{};
+  uint32_t* frec = nullptr;
+  unsigned long long* fcounter = nullptr;
+  uint2* fsteps = nullptr;
+  int32_t* fstep_begin = nullptr;
+  bool ftab = false;
+  int fq_blocks = 0;
+  uint8_t* word_on = nullptr;
+  float* omega = nullptr;
+  NrcWordArgs words{};
   // fallback tiles
   int tile_shift = 3, TX = 0, TY = 0, TZ = 0;
-  float *tnum = nullptr, *tden = nullptr;
+  float *tnum = nullptr, *tden = nullptr, *tring = nullptr;
   uint8_t* flag = nullptr;
   NrcArgs base{};
   int64_t solves = 0, steps = 0;
@@ -71,22 +85,16 @@ float uniform(uint64_t& s, float lo, float hi) {
   return lo + (hi - lo) * (float)((splitmix(s) >> 11) * (1.0 / 9007199254740992.0));
 }
 
-int nrc_phase(uint64_t seed, int level, int64_t probe, int nph) {
-  uint64_t s = seed ^ ((uint64_t)level << 40) ^ (uint64_t)probe;
-  return (int)(splitmix(s) >> 40) & (nph - 1);
-}
-
 void free_state(NrcState* n) {
   if (!n) return;
-  void* bufs[] = {n->hash_master, n->hash_m, n->hash_v, n->hash_g, n->hash_half, n->mlp, n->mlp_m, n->mlp_v,
-                  n->mlp_g, n->dbg_g, n->img, n->denc, n->rt, n->tiles, n->target, n->pred,
-                  n->epos_grad, n->loss, n->qtiles, n->qout, n->tnum, n->tden, n->flag};
+  void* bufs[] = {n->hash_master, n->hash_m, n->hash_v, n->hash_g, n->hash_half, n->mlp,   n->mlp_m,
+                  n->mlp_v,       n->mlp_g,  n->dbg_g,  n->img,    n->denc,      n->rt,    n->tiles,
+                  n->dlist, n->target, n->pred,   n->epos_grad, n->loss,  n->qtiles,
+                  n->qout,        n->tnum,   n->tden,   n->tring,   n->flag,   n->count,     n->plain, n->served_solves, n->frec,
+                  n->fcounter,    n->fsteps, n->fstep_begin, n->word_on, n->omega};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (n->h_loss) cudaFreeHost(n->h_loss);
-  if (n->count) cudaFree(n->count);
-  if (n->h_count) cudaFreeHost(n->h_count);
-  if (n->ev_count) cudaEventDestroy(n->ev_count);
   delete n;
 }
 
@@ -104,6 +112,7 @@ rc_status check(const rc_context* c, const char* fn, bool need_nrc) {
 
 unsigned blocks_for(int64_t n, int threads) { return (unsigned)std::max<int64_t>(1, (n + threads - 1) / threads); }
 
+// count is a multiple of 4 (the MLP's 17,680 parameters, the hash table's 32 T).
 void launch_adam(float* p, float* g, float* m, float* v, __half* half_out, int64_t count, const rc_nrc_params& prm,
                  int64_t t, bool lazy, cudaStream_t s) {
   AdamArgs a;
@@ -121,21 +130,11 @@ void launch_adam(float* p, float* g, float* m, float* v, __half* half_out, int64
   a.eps = prm.epsilon;
   a.c1 = (float)(1.0 - pow((double)prm.beta1, (double)t));
   a.c2 = (float)(1.0 - pow((double)prm.beta2, (double)t));
-  k_nrc_adam<<<(unsigned)std::min<int64_t>(blocks_for(count, 256), 152 * 8), 256, 0, s>>>(a);
+  k_nrc_adam<<<(unsigned)std::min<int64_t>(blocks_for(count / 4, 256), 152 * 8), 256, 0, s>>>(a);
 }
 
 void launch_pack(NrcState* n, cudaStream_t s) {
   k_nrc_pack<<<blocks_for(kImgBytes / 2, 256), 256, 0, s>>>(n->mlp, n->img);
-}
-
-NrcWalkArgs walk_args(const rc_context* c, const NrcTile* tiles, int64_t ntiles, float* target) {
-  NrcWalkArgs w;
-  memset(&w, 0, sizeof w);
-  for (int i = 0; i < c->nlev; ++i) w.lv[i] = c->args[i];
-  w.tiles = tiles;
-  w.ntiles = ntiles;
-  w.target = target;
-  return w;
 }
 
 rc_status ensure_query(NrcState* n, int64_t count) {
@@ -200,18 +199,55 @@ void nrc_release(rc_context* c) {
   c->nrc = nullptr;
 }
 
-// One solve's far cascades:
-//   1. plain (R, T) of this solve's training slice and held-out slice;
-//   2. held-out error of the current network -> fallback flags -> probes in
-//      fallback tiles per level (copied to the host);
-//   3. refit (Adam) on the training slice;
-//   4. per level: served by the network when less than plain_level_fraction
-//      of its probes is in fallback tiles (inference for the level, plain walk
-//      for its fallback probes, merge from (R, T)), else its plain kernels.
+// One solve's far cascades, all on the stream with no host wait:
+//   1. walk this solve's training and held-out directions of every far probe
+//      (the far levels' own walk queue), and read their targets;
+//   2. refit (Adam) on the training samples;
+//   3. held-out error of the refitted network per fallback tile -> flags ->
+//      per level the serve decision (a level with at least
+//      plain_level_fraction of its probes in flagged tiles runs on its walks);
+//   4. walk what is still needed: the other directions of every word of a
+//      level on its walks and of the words holding a probe of a flagged tile;
+//   5. inference of the served probes with the network just scored, then per
+//      level, top down, the merge from the network or from the walk records.
 // Inference grid: one resident wave at most, kFwdGroups tiles per block at a time.
 unsigned fwd_grid(const NrcState* n, int64_t ntiles) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>((ntiles + kFwdGroups - 1) / kFwdGroups, n->fwd_blocks));
 }
+
+namespace {
+
+void far_walk(NrcState* n, cudaStream_t s, int mode, int ph, int hp) {
+  NrcWordArgs w = n->words;
+  w.mode = mode;
+  w.ph = ph;
+  w.hp = hp;
+  k_nrc_words<<<blocks_for(w.slot0[w.nlev] + w.dir0[w.nlev], 128), 128, 0, s>>>(w);
+  cudaMemsetAsync(n->fcounter, 0, sizeof(unsigned long long), s);
+  if (n->ftab)
+    k_walk_queue_tab<<<(unsigned)n->fq_blocks, kQueueThreads, 0, s>>>(n->fq);
+  else
+    k_walk_queue<<<(unsigned)n->fq_blocks, kQueueThreads, 0, s>>>(n->fq);
+}
+
+template <typename T>
+void launch_heldout(const rc_context* c, NrcState* n, const NrcArgs& a, int64_t nho, const float* tho,
+                    cudaStream_t s) {
+  NrcLevelArgs la;
+  memset(&la, 0, sizeof la);
+  for (int i = 0; i < c->nlev; ++i) la.lv[i] = c->args[i];
+  k_nrc_heldout<T><<<(unsigned)nho, kNrcThreads, 0, s>>>(a, la, n->pred, tho, n->tnum, n->tden);
+}
+
+template <typename T>
+void launch_merge(const rc_context* c, const NrcState* n, int i, cudaStream_t s) {
+  const LevelArgs& a = c->args[i];
+  dim3 grid(blocks_for(a.P, 128), (unsigned)((a.n / 2) * (a.n / 2) / 2));
+  if (i == c->nlev - 1) k_level_merge_nrc<T, true><<<grid, 128, 0, s>>>(a, n->base, i);
+  else k_level_merge_nrc<T, false><<<grid, 128, 0, s>>>(a, n->base, i);
+}
+
+}  // namespace
 
 rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   NrcState* n = c->nrc;
@@ -220,27 +256,18 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   const int64_t ho0 = n->tile_begin[hp], nho = n->tile_begin[hp + 1] - ho0;
   float* ttr = n->target;
   float* tho = n->target + ntr * kNrcThreads * 4;
-  if (ntr) k_nrc_targets<<<blocks_for(ntr * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + tr0, ntr, ttr));
-  if (nho) k_nrc_targets<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(walk_args(c, n->tiles + ho0, nho, tho));
-  if (nho) {
-    NrcArgs a = n->base;
-    a.tiles = n->tiles + ho0;
-    a.ntiles = nho;
-    a.out = n->pred;
-    k_nrc_forward<false><<<fwd_grid(n, nho), kFwdThreads, kFwdSmem, s>>>(a, nho);
-    k_nrc_tile_error<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(n->tiles + ho0, nho, n->pred, tho, n->base,
-                                                                        n->tile_shift, n->TX, n->TY, n->tnum, n->tden);
-    const float thr = n->prm.fallback_threshold;
-    const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
-    k_nrc_flags<<<blocks_for(cells, 256), 256, 0, s>>>(n->tnum, n->tden, n->flag, cells, thr * thr);
+  // 1. the sample directions and their targets
+  far_walk(n, s, 0, ph, hp);
+  NrcArgs a = n->base;
+  if (ntr) {
+    a.tiles = n->tiles + tr0;
+    k_nrc_targets<<<blocks_for(ntr * kNrcThreads, 256), 256, 0, s>>>(a, c->vol, ntr, ttr);
   }
-  RC_CUDA(cudaMemsetAsync(n->count, 0, kMaxCascades * sizeof(unsigned), s), "cache count reset");
-  k_nrc_count<<<blocks_for(n->total_probes, 256), 256, 0, s>>>(n->base, n->flag, n->tile_shift, n->TX, n->TY,
-                                                                n->total_probes, n->count);
-  RC_CUDA(cudaMemcpyAsync(n->h_count, n->count, kMaxCascades * sizeof(unsigned), cudaMemcpyDeviceToHost, s),
-          "cache count");
-  RC_CUDA(cudaEventRecord(n->ev_count, s), "cache count");
-  // refit on the training slice (enqueued before the host waits for the counts)
+  if (nho) {
+    a.tiles = n->tiles + ho0;
+    k_nrc_targets<<<blocks_for(nho * kNrcThreads, 256), 256, 0, s>>>(a, c->vol, nho, tho);
+  }
+  // 2. refit on the training samples
   const int steps = std::max(1, n->prm.steps_per_solve);
   if (ntr) {
     RC_CUDA(cudaMemsetAsync(n->loss, 0, sizeof(float), s), "cache loss reset");
@@ -251,15 +278,15 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
       int64_t rows = 0;
       for (int64_t t = a0; t < a1; ++t) rows += n->h_tiles[tr0 + t].n;
       n->loss_rows += rows;
-      NrcArgs a = n->base;
-      a.tiles = n->tiles + tr0 + a0;
-      a.ntiles = a1 - a0;
-      a.target = ttr + a0 * kNrcThreads * 4;
-      a.grad = n->mlp_g;
-      a.epos_grad = nullptr;
-      a.loss = n->loss;
-      a.inv_batch = 1.f / (float)std::max<int64_t>(rows, 1);
-      k_nrc_train<<<(unsigned)std::min<int64_t>(a1 - a0, n->train_blocks), kNrcThreads, kTrainSmem, s>>>(a);
+      NrcArgs ta = n->base;
+      ta.tiles = n->tiles + tr0 + a0;
+      ta.ntiles = a1 - a0;
+      ta.target = ttr + a0 * kNrcThreads * 4;
+      ta.grad = n->mlp_g;
+      ta.epos_grad = nullptr;
+      ta.loss = n->loss;
+      ta.inv_batch = 1.f / (float)std::max<int64_t>(rows, 1);
+      k_nrc_train<<<(unsigned)std::min<int64_t>(a1 - a0, n->train_blocks), kNrcThreads, kTrainSmem, s>>>(ta);
       ++n->steps;
       launch_adam(n->mlp, n->mlp_g, n->mlp_m, n->mlp_v, nullptr, kNrcParams, n->prm, n->steps, false, s);
       launch_adam(n->hash_master, n->hash_g, n->hash_m, n->hash_v, n->hash_half, n->hash_n, n->prm, n->steps, true,
@@ -268,63 +295,30 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
     }
     RC_CUDA(cudaMemcpyAsync(n->h_loss, n->loss, sizeof(float), cudaMemcpyDeviceToHost, s), "cache loss");
   }
-  // which levels the network serves this solve
-  RC_CUDA(cudaEventSynchronize(n->ev_count), "cache count wait");
-  NrcArgs inf = n->base;
-  int64_t t0 = 0, served_queries = 0;
-  bool any_served = false, queue_plain = false;
-  for (int i = n->first; i < c->nlev; ++i) {
-    const int64_t P = c->geom[i].probes();
-    n->served[i] = (double)n->h_count[i] < (double)n->prm.plain_level_fraction * (double)P;
-    inf.tile0[i] = t0;
-    if (n->served[i]) {
-      t0 += (P * c->geom[i].ndirs + kNrcThreads - 1) / kNrcThreads;
-      served_queries += P * c->geom[i].ndirs;
-      any_served = true;
-    } else {
-      queue_plain |= level_uses_queue(c, i);
-    }
+  // 3. held-out error of the refitted network -> flags -> serve decisions
+  if (nho) {
+    a.ntiles = nho;
+    a.out = n->pred;
+    k_nrc_forward<false><<<fwd_grid(n, nho), kFwdThreads, kFwdSmem, s>>>(a, nho);
+    if (c->elem == 2) launch_heldout<__half>(c, n, a, nho, tho, s);
+    else launch_heldout<float>(c, n, a, nho, tho, s);
+    const float thr = n->prm.fallback_threshold;
+    const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
+    k_nrc_flags<<<blocks_for(cells, 256), 256, 0, s>>>(n->tnum, n->tden, n->tring, n->nph, ph, n->flag, cells,
+                                                       thr * thr);
   }
-  inf.tile0[c->nlev] = t0;
-  if (queue_plain) {
-    // near levels walked before the cache ran; served levels need no walk
-    uint32_t skip = (1u << n->first) - 1u;
-    for (int i = n->first; i < c->nlev; ++i)
-      if (n->served[i]) skip |= 1u << i;
-    plain_queue_walk(c, s, skip);
-  }
-  if (any_served) {
-    k_nrc_forward<true><<<fwd_grid(n, t0), kFwdThreads, kFwdSmem, s>>>(inf, t0);
-    NrcFallbackArgs f;
-    memset(&f, 0, sizeof f);
-    for (int i = 0; i < c->nlev; ++i) f.lv[i] = c->args[i];
-    f.n = n->base;
-    f.flag = n->flag;
-    f.tile_shift = n->tile_shift;
-    f.TX = n->TX;
-    f.TY = n->TY;
-    for (int i = 0; i < kMaxCascades; ++i) f.served[i] = n->served[i];
-    f.total = n->total_queries;
-    k_nrc_fallback<<<blocks_for(n->total_queries, 256), 256, 0, s>>>(f);
-  }
-  (void)served_queries;
-  // far levels, top down
+  k_nrc_count<<<blocks_for(n->total_probes, 256), 256, 0, s>>>(n->base, n->flag, n->tile_shift, n->TX, n->TY,
+                                                                n->total_probes, n->count);
+  k_nrc_decide<<<1, kMaxCascades, 0, s>>>(n->base, n->count, n->plain, n->served_solves,
+                                          n->prm.plain_level_fraction);
+  // 4. the walks still needed
+  far_walk(n, s, 1, ph, hp);
+  // 5. inference of the served probes with the network just scored, merges
+  // top down
+  k_nrc_forward<true><<<fwd_grid(n, n->enum_tiles), kFwdThreads, kFwdSmem, s>>>(n->base, n->enum_tiles);
   for (int i = c->nlev - 1; i >= n->first; --i) {
-    if (!n->served[i]) {
-      plain_level(c, i, s);
-      continue;
-    }
-    const LevelArgs& a = c->args[i];
-    const __half* rt = n->base.lv[i].rt;
-    dim3 grid(blocks_for(a.P, 128), (unsigned)((a.n / 2) * (a.n / 2) / 2));
-    const bool top = i == c->nlev - 1;
-    if (c->elem == 2) {
-      if (top) k_level_merge_rt<__half, true><<<grid, 128, 0, s>>>(a, rt);
-      else k_level_merge_rt<__half, false><<<grid, 128, 0, s>>>(a, rt);
-    } else {
-      if (top) k_level_merge_rt<float, true><<<grid, 128, 0, s>>>(a, rt);
-      else k_level_merge_rt<float, false><<<grid, 128, 0, s>>>(a, rt);
-    }
+    if (c->elem == 2) launch_merge<__half>(c, n, i, s);
+    else launch_merge<float>(c, n, i, s);
   }
   RC_CUDA(cudaGetLastError(), "cache launch");
   ++n->solves;
@@ -468,27 +462,71 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   n->base.params = n->mlp;
   n->base.scale = q.radiance_scale;
   n->base.err = c->err;
-  // sample probes by phase and their tiles of up to 128 directions
+  // Far levels' walk geometry (the decimated-opacity words of the bit-parallel
+  // walk).
+  int64_t slot_total = 0, dir_total = 0;
+  for (int i = n->first; i < c->nlev; ++i) {
+    const LevelArgs& la = c->args[i];
+    if (!c->bits_level[i] || !la.mask) {
+      set_error("rc_nrc_enable: cascade %d has no bit-parallel walk (the learned form walks its words)", i);
+      return fail(RC_ERR_UNSUPPORTED);
+    }
+    NrcLevel& L = n->base.lv[i];
+    L.slots = c->rec_slots[i];
+    L.wpp = la.wpp;
+    L.l2px = la.l2px;
+    n->words.slot0[i] = slot_total;
+    slot_total += L.slots;
+    n->words.dir0[i] = dir_total;
+    dir_total += c->geom[i].ndirs;
+  }
+  n->words.slot0[c->nlev] = slot_total;
+  n->words.dir0[c->nlev] = dir_total;
+  // Sample tiles by phase: every far probe with the directions of the phase
+  // (nrc_dir_phase), up to 128 per tile; a tile's slot is its probe's index.
   {
-    std::vector<std::vector<std::pair<int, int32_t>>> sp(n->nph);
+    std::vector<int32_t> dlist;
+    std::vector<std::vector<int64_t>> list_at(kMaxCascades, std::vector<int64_t>(n->nph + 1, 0));
     for (int i = n->first; i < c->nlev; ++i)
-      for (int64_t p = 0; p < c->geom[i].probes(); ++p)
-        sp[nrc_phase(q.seed ^ 0xA5A5A5A5ull, i, p, n->nph)].push_back({i, (int32_t)p});
+      for (int ph = 0; ph < n->nph; ++ph) {
+        list_at[i][ph] = (int64_t)dlist.size();
+        for (int d = 0; d < c->geom[i].ndirs; ++d)
+          if (nrc_dir_phase(d, c->geom[i].n, n->nph) == ph) dlist.push_back(d);
+        list_at[i][ph + 1] = (int64_t)dlist.size();
+      }
+    if ((int64_t)dlist.size() >= ((int64_t)1 << 31)) {
+      set_error("rc_nrc_enable: too many far directions");
+      return fail(RC_ERR_UNSUPPORTED);
+    }
     n->tile_begin.assign(n->nph + 1, 0);
     for (int ph = 0; ph < n->nph; ++ph) {
       n->tile_begin[ph] = (int64_t)n->h_tiles.size();
-      for (const auto& smp : sp[ph]) {
-        const int nd = c->geom[smp.first].ndirs;
-        for (int d0 = 0; d0 < nd; d0 += kNrcThreads)
-          n->h_tiles.push_back(NrcTile{smp.first, smp.second, d0, std::min(kNrcThreads, nd - d0), 0, 0});
+      int32_t k = 0;
+      for (int i = n->first; i < c->nlev; ++i) {
+        const int64_t l0 = list_at[i][ph], len = list_at[i][ph + 1] - l0;
+        if (len == 0) continue;
+        const int64_t P = c->geom[i].probes();
+        if (len >= kNrcThreads) {  // tiles of one probe, 128 of its directions each
+          for (int64_t p = 0; p < P; ++p, ++k)
+            for (int64_t r0 = 0; r0 < len; r0 += kNrcThreads)
+              n->h_tiles.push_back(NrcTile{i, (int32_t)p, (int32_t)(l0 + r0),
+                                           (int32_t)std::min<int64_t>(kNrcThreads, len - r0), k, kNrcThreads});
+        } else {  // tiles of 128 / len probes, all of their directions
+          const int64_t per = kNrcThreads / len;
+          for (int64_t p = 0; p < P; p += per) {
+            const int64_t np = std::min<int64_t>(per, P - p);
+            n->h_tiles.push_back(NrcTile{i, (int32_t)p, (int32_t)l0, (int32_t)(np * len), k, (int32_t)len});
+            k += (int32_t)np;
+          }
+        }
       }
     }
     n->tile_begin[n->nph] = (int64_t)n->h_tiles.size();
     for (int ph = 0; ph < n->nph; ++ph) {
       const int hp = (ph + n->nph / 2) % n->nph;
-      const int64_t a = n->tile_begin[ph + 1] - n->tile_begin[ph], b = n->tile_begin[hp + 1] - n->tile_begin[hp];
-      n->max_tiles2 = std::max(n->max_tiles2, a + b);
-      n->max_held = std::max(n->max_held, b);
+      const int64_t ta = n->tile_begin[ph + 1] - n->tile_begin[ph], tb = n->tile_begin[hp + 1] - n->tile_begin[hp];
+      n->max_tiles2 = std::max(n->max_tiles2, ta + tb);
+      n->max_held = std::max(n->max_held, tb);
     }
     if ((s = dev_alloc((void**)&n->tiles, std::max<size_t>(1, n->h_tiles.size()) * sizeof(NrcTile), "cache tiles")) !=
         RC_OK)
@@ -496,6 +534,13 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
     if (!n->h_tiles.empty())
       RC_CUDA(cudaMemcpy(n->tiles, n->h_tiles.data(), n->h_tiles.size() * sizeof(NrcTile), cudaMemcpyHostToDevice),
               "rc_nrc_enable: upload");
+    if ((s = dev_alloc((void**)&n->dlist, std::max<size_t>(1, dlist.size()) * sizeof(int32_t),
+                       "cache sample directions")) != RC_OK)
+      return fail(s);
+    if (!dlist.empty())
+      RC_CUDA(cudaMemcpy(n->dlist, dlist.data(), dlist.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
+              "rc_nrc_enable: upload");
+    n->base.dlist = n->dlist;
   }
   if ((s = dev_alloc((void**)&n->target, std::max<int64_t>(1, n->max_tiles2) * kNrcThreads * 16, "cache targets")) !=
       RC_OK)
@@ -508,8 +553,33 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   RC_CUDA(cudaMallocHost((void**)&n->h_loss, sizeof(float)), "rc_nrc_enable: pinned");
   *n->h_loss = 0.f;
   if ((s = dev_alloc((void**)&n->count, kMaxCascades * sizeof(unsigned), "cache counts")) != RC_OK) return fail(s);
-  RC_CUDA(cudaMallocHost((void**)&n->h_count, kMaxCascades * sizeof(unsigned)), "rc_nrc_enable: pinned");
-  RC_CUDA(cudaEventCreateWithFlags(&n->ev_count, cudaEventDisableTiming), "rc_nrc_enable: event");
+  RC_CUDA(cudaMemset(n->count, 0, kMaxCascades * sizeof(unsigned)), "rc_nrc_enable: memset");
+  if ((s = dev_alloc((void**)&n->plain, kMaxCascades * sizeof(int32_t), "cache serve decisions")) != RC_OK)
+    return fail(s);
+  if ((s = dev_alloc((void**)&n->served_solves, kMaxCascades * sizeof(unsigned long long), "cache serve counts")) !=
+      RC_OK)
+    return fail(s);
+  RC_CUDA(cudaMemset(n->served_solves, 0, kMaxCascades * sizeof(unsigned long long)), "rc_nrc_enable: memset");
+  {
+    const std::vector<int32_t> all_plain(kMaxCascades, 1);  // every tile starts on the walk
+    RC_CUDA(cudaMemcpy(n->plain, all_plain.data(), kMaxCascades * sizeof(int32_t), cudaMemcpyHostToDevice),
+            "rc_nrc_enable: upload");
+  }
+  // exact texel solid angles of the far levels
+  {
+    std::vector<float> om;
+    std::vector<int64_t> at(kMaxCascades, 0);
+    for (int i = n->first; i < c->nlev; ++i) {
+      at[i] = (int64_t)om.size();
+      std::vector<double> w((size_t)c->geom[i].ndirs);
+      rc_solid_angles(c->geom[i].n, w.data());
+      for (double x : w) om.push_back((float)x);
+    }
+    if ((s = dev_alloc((void**)&n->omega, om.size() * sizeof(float), "far solid angles")) != RC_OK) return fail(s);
+    RC_CUDA(cudaMemcpy(n->omega, om.data(), om.size() * sizeof(float), cudaMemcpyHostToDevice),
+            "rc_nrc_enable: upload");
+    for (int i = n->first; i < c->nlev; ++i) n->base.lv[i].omega = n->omega + at[i];
+  }
   // fallback tiles: all start on the plain walk
   n->tile_shift = 0;
   while ((1 << n->tile_shift) < q.fallback_tile) ++n->tile_shift;
@@ -517,8 +587,11 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   n->TY = (c->p.grid[1] + q.fallback_tile - 1) / q.fallback_tile;
   n->TZ = (c->p.grid[2] + q.fallback_tile - 1) / q.fallback_tile;
   const int64_t cells = (int64_t)n->TX * n->TY * n->TZ;
+  // per cell: this solve's held-out sums, and those of the last nph solves
   if ((s = dev_alloc((void**)&n->tnum, cells * 4, "tile errors")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->tden, cells * 4, "tile errors")) != RC_OK) return fail(s);
+  if ((s = dev_alloc((void**)&n->tring, (size_t)n->nph * 2 * cells * 4, "tile error window")) != RC_OK) return fail(s);
+  RC_CUDA(cudaMemset(n->tring, 0, (size_t)n->nph * 2 * cells * 4), "rc_nrc_enable: memset");
   if ((s = dev_alloc((void**)&n->flag, cells, "tile flags")) != RC_OK) return fail(s);
   RC_CUDA(cudaMemset(n->tnum, 0, cells * 4), "rc_nrc_enable: memset");
   RC_CUDA(cudaMemset(n->tden, 0, cells * 4), "rc_nrc_enable: memset");
@@ -533,6 +606,117 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
           n->probe_tile[((size_t)((z * gm.spacing + h) >> n->tile_shift) * n->TY + ((y * gm.spacing + h) >> n->tile_shift)) *
                             n->TX +
                         ((x * gm.spacing + h) >> n->tile_shift)] = 1;
+  }
+  n->base.plain = n->plain;
+  n->base.flag = n->flag;
+  n->base.tile_shift = n->tile_shift;
+  n->base.TX = n->TX;
+  n->base.TY = n->TY;
+  // The far levels' own walk queue: records of every far level, step tables
+  // where every far level has one (else the walk's own DDA), and one switch
+  // per word that the schedule sets before each walk.
+  {
+    if ((s = dev_alloc((void**)&n->word_on, std::max<int64_t>(1, slot_total + dir_total), "far walk switches")) !=
+        RC_OK)
+      return fail(s);
+    RC_CUDA(cudaMemset(n->word_on, 0, std::max<int64_t>(1, slot_total + dir_total)), "rc_nrc_enable: memset");
+    uint8_t* dir_on = n->word_on + slot_total;
+    size_t rec_words = 0;
+    for (int i = n->first; i < c->nlev; ++i) rec_words += (size_t)c->geom[i].ndirs * n->base.lv[i].slots * 32;
+    if ((s = dev_alloc((void**)&n->frec, rec_words * sizeof(uint32_t), "far walk records")) != RC_OK) return fail(s);
+    if ((s = dev_alloc((void**)&n->fcounter, sizeof(unsigned long long), "far walk counter")) != RC_OK)
+      return fail(s);
+    QueueArgs& fq = n->fq;
+    memset(&fq, 0, sizeof fq);
+    fq.emis = c->emis;
+    fq.counter = n->fcounter;
+    for (int a3 = 0; a3 < 3; ++a3) fq.G[a3] = c->p.grid[a3];
+    fq.W = c->W;
+    std::vector<uint2> steps;
+    std::vector<int32_t> begin;
+    std::vector<size_t> boff;
+    bool tab_ok = !(getenv("RC_WALK_TABLES") && strcmp(getenv("RC_WALK_TABLES"), "0") == 0);
+    size_t roff = 0;
+    int64_t items = 0;
+    char msg[256];
+    for (int i = c->nlev - 1; i >= n->first; --i) {  // longest intervals first
+      const LevelArgs& la = c->args[i];
+      const LevelGeom& gm = c->geom[i];
+      NrcLevel& NL = n->base.lv[i];
+      QueueLevel& L = fq.lv[fq.n++];
+      L.mask = la.mask;
+      L.dirs = la.dirs;
+      L.rec = n->frec + roff;
+      NL.rec = L.rec;
+      roff += (size_t)gm.ndirs * NL.slots * 32;
+      L.item_begin = items;
+      items += (int64_t)gm.ndirs * NL.slots;
+      L.slots = NL.slots;
+      L.l2s = la.l2s;
+      L.l2px = la.l2px;
+      L.wpp = la.wpp;
+      for (int ax = 0; ax < 3; ++ax) L.M[ax] = la.M[ax];
+      L.rep = la.rep;
+      L.test_start = 0;
+      L.level = i;
+      L.word_on = n->word_on + n->words.slot0[i];
+      NL.word_on = n->word_on + n->words.slot0[i];
+      L.dir_on = dir_on + n->words.dir0[i];
+      NL.dir_on = dir_on + n->words.dir0[i];
+      if (tab_ok) {
+        std::vector<DirInfo> tab((size_t)gm.ndirs);
+        if (!build_dir_table(gm, c->p.grid, tab.data(), msg, sizeof msg)) return fail(RC_ERR_UNSUPPORTED);
+        boff.push_back(begin.size());
+        for (int d = 0; d < gm.ndirs && tab_ok; ++d) {
+          begin.push_back((int32_t)steps.size());
+          const int64_t cnt = walk_steps(gm, c->p.grid, tab[d], false, nullptr, 0);
+          if (cnt < 0 || steps.size() + (size_t)cnt > (size_t)INT32_MAX / 2) {
+            tab_ok = false;
+            break;
+          }
+          const size_t at = steps.size();
+          steps.resize(at + (size_t)cnt);
+          walk_steps(gm, c->p.grid, tab[d], false, reinterpret_cast<WalkStep*>(steps.data() + at), cnt);
+        }
+        begin.push_back((int32_t)steps.size());
+      }
+    }
+    fq.total = items;
+    if (tab_ok && !steps.empty()) {
+      if ((s = dev_alloc((void**)&n->fsteps, steps.size() * sizeof(uint2), "far walk step tables")) != RC_OK)
+        return fail(s);
+      if ((s = dev_alloc((void**)&n->fstep_begin, begin.size() * sizeof(int32_t), "far walk step tables")) != RC_OK)
+        return fail(s);
+      RC_CUDA(cudaMemcpy(n->fsteps, steps.data(), steps.size() * sizeof(uint2), cudaMemcpyHostToDevice),
+              "rc_nrc_enable: upload");
+      RC_CUDA(cudaMemcpy(n->fstep_begin, begin.data(), begin.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
+              "rc_nrc_enable: upload");
+      for (int k = 0; k < fq.n; ++k) {
+        fq.lv[k].steps = n->fsteps;
+        fq.lv[k].step_begin = n->fstep_begin + boff[(size_t)k];
+      }
+      n->ftab = true;
+    }
+    int per_sm = 0, sms0 = 0;
+    cudaDeviceGetAttribute(&sms0, cudaDevAttrMultiProcessorCount, c->device);
+    if ((n->ftab ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue_tab, kQueueThreads, 0)
+                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue, kQueueThreads, 0)) !=
+        cudaSuccess) {
+      (void)cudaGetLastError();
+      per_sm = 2;
+    }
+    n->fq_blocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>((items + kQueueThreads - 1) / kQueueThreads, (int64_t)std::max(1, sms0 * per_sm)));
+    NrcWordArgs& w = n->words;
+    for (int i = 0; i < kMaxCascades; ++i) w.lv[i] = n->base.lv[i];
+    w.first = n->first;
+    w.nlev = c->nlev;
+    w.nph = n->nph;
+    w.plain = n->plain;
+    w.flag = n->flag;
+    w.tile_shift = n->tile_shift;
+    w.TX = n->TX;
+    w.TY = n->TY;
   }
   // kernels: shared memory and resident blocks
   RC_CUDA(cudaFuncSetAttribute(k_nrc_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem),
@@ -660,8 +844,13 @@ rc_status rc_nrc_get_stats(rc_context* c, rc_nrc_stats* out) {
       ++out->tiles;
       out->fallback_tiles += f[(size_t)t] ? 1 : 0;
     }
+  int32_t plain[kMaxCascades] = {};
+  RC_CUDA(cudaMemcpy(plain, n->plain, sizeof plain, cudaMemcpyDeviceToHost), "rc_nrc_get_stats");
   for (int i = n->first; i < c->nlev; ++i)
-    if (n->served[i]) out->served_levels |= 1 << i;
+    if (n->solves && !plain[i]) out->served_levels |= 1 << i;
+  unsigned long long served[kMaxCascades] = {};
+  RC_CUDA(cudaMemcpy(served, n->served_solves, sizeof served, cudaMemcpyDeviceToHost), "rc_nrc_get_stats");
+  for (int i = 0; i < kMaxCascades; ++i) out->served_solves[i] = (int64_t)served[i];
   return RC_OK;
 }
 

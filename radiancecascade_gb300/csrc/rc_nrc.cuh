@@ -34,6 +34,7 @@
 
 #include "rc_kernels.cuh"
 #include "rc_umma.cuh"
+#include "rc_walk_queue.cuh"
 
 namespace rcx {
 
@@ -49,6 +50,7 @@ constexpr int kNrcLayerStride = 64 * 64 + 64;
 constexpr int kNrcW4 = 4 * kNrcLayerStride;
 constexpr int kNrcB4 = kNrcW4 + 16 * 64;
 constexpr int kNrcParams = kNrcB4 + 16;  // 17680
+static_assert(kNrcParams % 4 == 0, "Adam takes the parameters four at a time");
 
 // BF16 weight image (byte offsets), already in the K-major core layout:
 //   l = 0..3:  F_l = W_l as [64 n = out][64 k = in]     at 16384 l
@@ -58,14 +60,18 @@ constexpr int kImgW4F = 65536;
 constexpr int kImgW4B = 67584;
 constexpr int kImgBytes = 69632;
 
-// One tile of up to 128 queries: directions d0 .. d0 + n - 1 of one probe.
+// One tile of up to 128 queries.  list = 0: directions d0 .. d0 + n - 1 of
+// one probe.  list = k > 0: row r is probe `probe + r / k` with direction
+// dlist[d0 + r % k] (NrcArgs.dlist), so a tile packs 128 / k probes when
+// their direction lists are short; slot + r / k is the row's probe index in
+// its sample phase.
 struct NrcTile {
   int32_t level;
   int32_t probe;
   int32_t d0;
   int32_t n;
   int32_t slot;
-  int32_t pad;
+  int32_t list;
 };
 
 struct NrcLevel {
@@ -76,6 +82,13 @@ struct NrcLevel {
   int32_t n;                  // direction resolution (n x n texels)
   int32_t M[3];
   int32_t spacing;
+  // The level's own walk records (rc_walk_queue.cuh layout rec[d][slot][32],
+  // slot = z * wpp + word, bit g = y * 2^l2px + x of the probe's plane).
+  const uint32_t* rec;
+  int32_t slots, wpp, l2px;
+  uint8_t* word_on;           // [slots] walk switch of the level's words
+  uint8_t* dir_on;            // [ndirs] walk switch of the level's directions
+  const float* omega;         // [ndirs] exact texel solid angles
 };
 
 struct NrcHash {
@@ -96,6 +109,7 @@ struct NrcArgs {
   int32_t nlev;
   int64_t tile0[kMaxCascades + 1];  // enumeration: first tile of each far level
   const NrcTile* tiles;      // explicit tile list (or null: enumerate the far levels)
+  const int32_t* dlist;      // direction lists of the sample tiles
   int64_t ntiles;
   float* out;                // explicit tiles: raw outputs [tile][128][4]
   const float* target;       // training: [tile][128][4] (R, G, B, T)
@@ -105,6 +119,12 @@ struct NrcArgs {
   float scale;               // radiance scale of the outputs
   float inv_batch;           // training: 1 / (queries in the step)
   int* err;
+  // Serving (enumerated inference only): plain[level] != 0 means the level
+  // runs on its walks this solve; probes whose fallback tile is flagged are
+  // walked too, so their rows are not stored.
+  const int32_t* plain;
+  const uint8_t* flag;
+  int32_t tile_shift, TX, TY;
 };
 
 __device__ __forceinline__ unsigned char* align128(unsigned char* p) {
@@ -118,9 +138,19 @@ __device__ __forceinline__ bool nrc_query(const NrcArgs& a, int64_t t, int r, in
     const NrcTile tl = a.tiles[t];
     li = tl.level;
     p = tl.probe;
-    d = tl.d0 + r;
     slot = tl.slot;
-    return r < tl.n;
+    if (r >= tl.n) {
+      d = 0;
+      return false;
+    }
+    if (tl.list) {
+      p += r / tl.list;
+      slot += r / tl.list;
+      d = __ldg(a.dlist + tl.d0 + r % tl.list);
+    } else {
+      d = tl.d0 + r;
+    }
+    return true;
   }
   li = a.first;
   while (li + 1 < a.nlev && t >= a.tile0[li + 1]) ++li;
@@ -145,6 +175,33 @@ __device__ __forceinline__ void nrc_probe_pos(const NrcLevel& L, int64_t p, floa
   u[0] = ((float)mx * L.spacing + h) * inv_extent;
   u[1] = ((float)my * L.spacing + h) * inv_extent;
   u[2] = ((float)mz * L.spacing + h) * inv_extent;
+}
+
+// Fallback tile (voxel cell of 2^shift edge) of probe p's centre.
+__device__ __forceinline__ int64_t nrc_cell(const NrcLevel& L, int64_t p, int shift, int TX, int TY) {
+  const uint32_t pp = (uint32_t)p, M0 = (uint32_t)L.M[0], M1 = (uint32_t)L.M[1];
+  const uint32_t row = pp / M0, mz = row / M1;
+  const int mx = (int)(pp - row * M0), my = (int)(row - mz * M1);
+  const int h = L.spacing >> 1;
+  return ((int64_t)(((int)mz * L.spacing + h) >> shift) * TY + ((my * L.spacing + h) >> shift)) * TX +
+         ((mx * L.spacing + h) >> shift);
+}
+
+// Record index of probe p's entry for direction d: ((d * slots + slot) * 32 + bit).
+__device__ __forceinline__ int64_t nrc_rec_index(const NrcLevel& L, int64_t p, int d) {
+  const uint32_t pp = (uint32_t)p, M0 = (uint32_t)L.M[0], M1 = (uint32_t)L.M[1];
+  const uint32_t row = pp / M0, mz = row / M1;
+  const int mx = (int)(pp - row * M0), my = (int)(row - mz * M1);
+  const int g = (my << L.l2px) + mx;
+  return ((int64_t)d * L.slots + (int)mz * L.wpp + (g >> 5)) * 32 + (g & 31);
+}
+
+// Walk result (R, G, B, T) of one record entry: first-hit voxel (emissive),
+// kBlack (opaque, no emission) or kMiss (the ray got through).
+__device__ __forceinline__ void nrc_record_rt(const uint2* __restrict__ vol, uint32_t r, float* rt) {
+  rt[0] = rt[1] = rt[2] = 0.f;
+  rt[3] = r == kMiss ? 1.f : 0.f;
+  if (r != kMiss && r != kBlack) voxel_emission(vol, r, rt);
 }
 
 // Table row of hash level l for a query (see the file comment).
@@ -376,7 +433,14 @@ __global__ void __launch_bounds__(kFwdThreads, 3) k_nrc_forward(const __grid_con
   for (int64_t t = (int64_t)blockIdx.x * kFwdGroups + wg; t < ntiles && ok; t += (int64_t)gridDim.x * kFwdGroups) {
     int li, d, slot;
     int64_t p;
-    const bool valid = nrc_query(a, t, row, li, p, d, slot);
+    bool valid = nrc_query(a, t, row, li, p, d, slot);
+    if (RT) {
+      // rows on the walk (the level runs plain, or the probe's tile is
+      // flagged) are not served; a tile with no served row is skipped
+      valid = valid && !__ldg(a.plain + li) &&
+              !__ldg(a.flag + nrc_cell(a.lv[li], p, a.tile_shift, a.TX, a.TY));
+      if (!wg_sync_or(wg, valid)) continue;
+    }
     nrc_encode_row(a, valid, li, p, d, XA, row);
     fence_proxy_async();
     wg_sync(wg);
@@ -716,19 +780,39 @@ struct AdamArgs {
 // Adam step.  With `lazy`, an entry no training sample touched this step
 // (gradient exactly 0) keeps its value and moments, as Mueller et al. 2022 do
 // for the hash table: a step then writes only the touched entries.
+__device__ __forceinline__ float adam_one(const AdamArgs& a, float g, float& m, float& v, float p) {
+  m = fmaf(a.beta1, m, (1.f - a.beta1) * g);
+  v = fmaf(a.beta2, v, (1.f - a.beta2) * g * g);
+  return p - a.lr * (m / a.c1) / (sqrtf(v / a.c2) + a.eps);
+}
+
+// Four entries per thread and step (16-byte loads; a.n is a multiple of 4 for
+// both parameter sets, checked by the host); a lazy step skips a group whose
+// four gradients are all zero without touching its moments.
 __global__ void k_nrc_adam(const __grid_constant__ AdamArgs a) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float g = a.g[i];
-    if (a.lazy && g == 0.f) continue;
-    const float m = fmaf(a.beta1, a.m[i], (1.f - a.beta1) * g);
-    const float v = fmaf(a.beta2, a.v[i], (1.f - a.beta2) * g * g);
-    a.m[i] = m;
-    a.v[i] = v;
-    a.g[i] = 0.f;
-    const float step = a.lr * (m / a.c1) / (sqrtf(v / a.c2) + a.eps);
-    const float p = a.p[i] - step;
-    a.p[i] = p;
-    if (a.half_out) a.half_out[i] = __float2half_rn(p);
+  const int64_t n4 = a.n >> 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 g = reinterpret_cast<const float4*>(a.g)[i];
+    if (a.lazy && g.x == 0.f && g.y == 0.f && g.z == 0.f && g.w == 0.f) continue;
+    float4 m = reinterpret_cast<const float4*>(a.m)[i];
+    float4 v = reinterpret_cast<const float4*>(a.v)[i];
+    float4 p = reinterpret_cast<const float4*>(a.p)[i];
+    // with `lazy`, an entry of the group whose own gradient is zero keeps its state
+    if (!a.lazy || g.x != 0.f) p.x = adam_one(a, g.x, m.x, v.x, p.x);
+    if (!a.lazy || g.y != 0.f) p.y = adam_one(a, g.y, m.y, v.y, p.y);
+    if (!a.lazy || g.z != 0.f) p.z = adam_one(a, g.z, m.z, v.z, p.z);
+    if (!a.lazy || g.w != 0.f) p.w = adam_one(a, g.w, m.w, v.w, p.w);
+    reinterpret_cast<float4*>(a.m)[i] = m;
+    reinterpret_cast<float4*>(a.v)[i] = v;
+    reinterpret_cast<float4*>(a.p)[i] = p;
+    reinterpret_cast<float4*>(a.g)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.half_out) {
+      const __half2 lo = __floats2half2_rn(p.x, p.y), hi = __floats2half2_rn(p.z, p.w);
+      uint2 h;
+      h.x = *reinterpret_cast<const uint32_t*>(&lo);
+      h.y = *reinterpret_cast<const uint32_t*>(&hi);
+      reinterpret_cast<uint2*>(a.half_out)[i] = h;
+    }
   }
 }
 
@@ -757,89 +841,221 @@ __global__ void k_nrc_pack(const float* __restrict__ params, unsigned char* __re
 }
 
 // ---------------------------------------------------------------------------
-// Plain (R, T) of queries: training targets and the fallback.
+// Per-solve schedule kernels: which words the far levels walk, training
+// targets from the walk records, the held-out error per fallback tile, the
+// serve decision per level, and the merge from the network or the records.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void nrc_walk(const LevelArgs& a, int64_t p, int d, float* rt) {
-  const int mx = (int)(p % a.M[0]);
-  const int my = (int)((p / a.M[0]) % a.M[1]);
-  const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
-  const int h = a.spacing >> 1;
-  const DirInfo di = a.dirs[d];
-  const int64_t hit = walk_interval(a.occ, a.G, a.W, mx * a.spacing + h + di.start_off[0],
-                                    my * a.spacing + h + di.start_off[1], mz * a.spacing + h + di.start_off[2], di,
-                                    false);
-  rt[0] = rt[1] = rt[2] = 0.f;
-  rt[3] = hit < 0 ? 1.f : 0.f;
-  if (hit >= 0) voxel_emission(a.vol, hit, rt);
+
+// Sample phase of direction texel (j, k): the phases tile the octahedral map
+// in a pattern of a x b texels (a * b = nph), so a phase's directions are a
+// regular sub-lattice spread over the whole sphere.  Training and held-out
+// samples are every probe of the far levels with the directions of phase ph
+// and of phase ph + nph/2 respectively.
+__host__ __device__ __forceinline__ int nrc_dir_phase(int d, int n, int nph) {
+  int t = 0;
+  while ((1 << t) < nph) ++t;
+  const int a = 1 << ((t + 1) / 2), b = nph / a;
+  const int j = d % n, k = d / n;
+  return (j % a) + a * (k % b);
 }
 
-struct NrcWalkArgs {
-  LevelArgs lv[kMaxCascades];
-  const NrcTile* tiles;
-  int64_t ntiles;
-  float* target;  // [tile][128][4]
+// Probe of bit b of slot `slot`, or -1 when the bit holds no probe.
+__host__ __device__ __forceinline__ int64_t nrc_slot_probe(const int32_t M[3], int wpp, int l2px, int slot, int b) {
+  const int z = slot / wpp, g = (slot - z * wpp) * 32 + b;
+  const int x = g & ((1 << l2px) - 1), y = g >> l2px;
+  if (x >= M[0] || y >= M[1] || z >= M[2]) return -1;
+  return ((int64_t)z * M[1] + y) * M[0] + x;
+}
+
+struct NrcWordArgs {
+  NrcLevel lv[kMaxCascades];
+  int32_t first, nlev;
+  int32_t mode;    // 0: the sample directions of phases ph, hp; 1: what the solve still needs
+  int32_t ph, hp, nph;
+  const int32_t* plain;
+  const uint8_t* flag;
+  int32_t tile_shift, TX, TY;
+  int64_t slot0[kMaxCascades + 1];  // first global slot of each far level
+  int64_t dir0[kMaxCascades + 1];   // first global direction of each far level
 };
 
-__global__ void k_nrc_targets(const __grid_constant__ NrcWalkArgs w) {
+// Walk switches of the far levels' queue, one thread per (level, slot) and
+// per (level, direction).  Mode 0: every word, the sample directions.  Mode 1:
+// the other directions, of every word of a level on its walks and of the
+// words holding a probe of a flagged tile.
+__global__ void k_nrc_words(const __grid_constant__ NrcWordArgs w) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= w.ntiles * kNrcThreads) return;
-  const NrcTile t = w.tiles[i / kNrcThreads];
-  const int r = (int)(i % kNrcThreads);
-  float rt[4] = {0.f, 0.f, 0.f, 0.f};
-  if (r < t.n) nrc_walk(w.lv[t.level], t.probe, t.d0 + r, rt);
-  *reinterpret_cast<float4*>(w.target + i * 4) = make_float4(rt[0], rt[1], rt[2], rt[3]);
+  const int64_t nslots = w.slot0[w.nlev];
+  if (i < nslots) {
+    int li = w.first;
+    while (li + 1 < w.nlev && i >= w.slot0[li + 1]) ++li;
+    const NrcLevel& L = w.lv[li];
+    const int slot = (int)(i - w.slot0[li]);
+    bool on = true;
+    if (w.mode == 1 && !__ldg(w.plain + li)) {
+      on = false;
+      for (int b = 0; b < 32 && !on; ++b) {
+        const int64_t p = nrc_slot_probe(L.M, L.wpp, L.l2px, slot, b);
+        if (p >= 0) on = __ldg(w.flag + nrc_cell(L, p, w.tile_shift, w.TX, w.TY)) != 0;
+      }
+    }
+    L.word_on[slot] = on;
+    return;
+  }
+  const int64_t j = i - nslots;
+  if (j >= w.dir0[w.nlev]) return;
+  int li = w.first;
+  while (li + 1 < w.nlev && j >= w.dir0[li + 1]) ++li;
+  const NrcLevel& L = w.lv[li];
+  const int d = (int)(j - w.dir0[li]);
+  const int ph = nrc_dir_phase(d, L.n, w.nph);
+  const bool sample = ph == w.ph || ph == w.hp;
+  L.dir_on[d] = w.mode == 0 ? sample : !sample;
 }
 
-// Held-out error of the cache per fallback tile (voxel tile of the probe
-// centre): sum of squared errors and of squared targets.
-__global__ void k_nrc_tile_error(const NrcTile* __restrict__ tiles, int64_t ntiles, const float* __restrict__ pred,
-                                 const float* __restrict__ target, const __grid_constant__ NrcArgs a, int tile_shift,
-                                 int TX, int TY, float* __restrict__ num, float* __restrict__ den) {
+// Training / held-out targets: row r of tile t is the tile's r-th direction
+// of its probe, read from the level's walk records.
+__global__ void k_nrc_targets(const __grid_constant__ NrcArgs a, const uint2* __restrict__ vol, int64_t ntiles,
+                              float* __restrict__ target) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ntiles * kNrcThreads) return;
-  const NrcTile t = tiles[i / kNrcThreads];
+  const NrcTile t = a.tiles[i / kNrcThreads];
   const int r = (int)(i % kNrcThreads);
-  if (r >= t.n) return;
-  const float4 pr = *reinterpret_cast<const float4*>(pred + i * 4);
-  const float4 y = *reinterpret_cast<const float4*>(target + i * 4);
-  const float po[4] = {pr.x, pr.y, pr.z, pr.w};
-  float R[4];
-  nrc_serve(po, a.scale, R);
-  const float Y[4] = {y.x, y.y, y.z, y.w};
-  float e = 0.f, s = 0.f;
-#pragma unroll
-  for (int c = 0; c < 4; ++c) {
-    e = fmaf(R[c] - Y[c], R[c] - Y[c], e);
-    s = fmaf(Y[c], Y[c], s);
+  float rt[4] = {0.f, 0.f, 0.f, 0.f};
+  if (r < t.n) {
+    const NrcLevel& L = a.lv[t.level];
+    const int64_t p = t.list ? t.probe + r / t.list : t.probe;
+    const int d = t.list ? __ldg(a.dlist + t.d0 + r % t.list) : t.d0 + r;
+    nrc_record_rt(vol, __ldg(L.rec + nrc_rec_index(L, p, d)), rt);
   }
-  const NrcLevel& L = a.lv[t.level];
-  const int64_t p = t.probe;
-  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
-  const int h = L.spacing >> 1;
-  const int tx = (mx * L.spacing + h) >> tile_shift, ty = (my * L.spacing + h) >> tile_shift,
-            tz = (mz * L.spacing + h) >> tile_shift;
-  const int64_t cell = ((int64_t)tz * TY + ty) * TX + tx;
-  atomicAdd(&num[cell], e);
-  atomicAdd(&den[cell], s);
+  *reinterpret_cast<float4*>(target + i * 4) = make_float4(rt[0], rt[1], rt[2], rt[3]);
 }
 
-// Fallback flags from the accumulated errors; cells without held-out samples
-// this frame keep their flag.  Clears the accumulators.
-__global__ void k_nrc_flags(float* __restrict__ num, float* __restrict__ den, uint8_t* __restrict__ flag, int64_t n,
-                            float thr2) {
+// Trilinear taps of probe p of a level into the next level's probes (child
+// index m sits at parent coordinate m/2 - 1/4, clamped): offsets and weights.
+__device__ __forceinline__ void merge_taps(const LevelArgs& a, int64_t p, int tap_off[8], float tap_w[8]) {
+  const int Mx = a.M[0], My = a.M[1];
+  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  int qq[3][2];
+  float wt[3][2];
+  const int m[3] = {mx, my, mz};
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    const int lo = (m[ax] - 1) >> 1;
+    wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
+    wt[ax][1] = 1.0f - wt[ax][0];
+    qq[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
+    qq[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
+  }
+#pragma unroll
+  for (int tp = 0; tp < 8; ++tp) {
+    const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
+    tap_off[tp] = (qq[2][iz] * a.UM[1] + qq[1][iy]) * a.UM[0] + qq[0][ix];
+    tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
+  }
+}
+
+// Held-out error per fallback tile.  A held-out query (p, d) of far level i
+// enters the merged radiance L_c = R_c + T M_c(p, d), M = the trilinear blend
+// of the next level's child-averaged radiance (the values of the previous
+// solve, which this solve's merges overwrite later; zero at the top level).
+// The tile of p accumulates sum Omega_d |L^ - L|^2 (L^ from the served
+// network output) and sum Omega_d |L|^2 over its held-out queries: the
+// solid-angle-weighted relative L2 error of the radiance the level hands to
+// the merges below.  One block = one tile; rows of one probe are contiguous,
+// so a segmented warp scan sums them and the last lane of each segment adds
+// the sums to the probe's cell.
+struct NrcLevelArgs {
+  LevelArgs lv[kMaxCascades];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kNrcThreads) k_nrc_heldout(const __grid_constant__ NrcArgs a,
+                                                            const __grid_constant__ NrcLevelArgs lv,
+                                                            const float* __restrict__ pred,
+                                                            const float* __restrict__ target,
+                                                            float* __restrict__ num, float* __restrict__ den) {
+  const NrcTile t = a.tiles[blockIdx.x];
+  const int r = threadIdx.x, lane = r & 31;
+  const int seg = t.list ? r / t.list : 0;  // row's probe within the tile
+  const int64_t p = t.probe + seg;
+  float e2 = 0.f, s2 = 0.f;
+  if (r < t.n) {
+    const int64_t i = (int64_t)blockIdx.x * kNrcThreads + r;
+    const float4 pr = *reinterpret_cast<const float4*>(pred + i * 4);
+    const float4 y = *reinterpret_cast<const float4*>(target + i * 4);
+    const float po[4] = {pr.x, pr.y, pr.z, pr.w};
+    float sv[4];
+    nrc_serve(po, a.scale, sv);
+    const int d = t.list ? __ldg(a.dlist + t.d0 + r % t.list) : t.d0 + r;
+    const NrcLevel& L = a.lv[t.level];
+    const LevelArgs& la = lv.lv[t.level];
+    float M[3] = {0.f, 0.f, 0.f};
+    if (t.level + 1 < a.nlev) {
+      int tap_off[8];
+      float tap_w[8];
+      merge_taps(la, p, tap_off, tap_w);
+      const T* Au = static_cast<const T*>(la.A_up);
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const T* src = Au + ((int64_t)ch * la.ndirs + d) * la.P_up;
+#pragma unroll
+        for (int tp = 0; tp < 8; ++tp) M[ch] = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), M[ch]);
+      }
+    }
+    const float om = __ldg(L.omega + d);
+    const float Y[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      const float lw = fmaf(Y[3], M[ch], Y[ch]), ls = fmaf(sv[3], M[ch], sv[ch]);
+      e2 = fmaf(om * (ls - lw), ls - lw, e2);
+      s2 = fmaf(om * lw, lw, s2);
+    }
+  }
+  // rows past t.n belong to no probe: give them a key of their own
+  const int key = r < t.n ? seg : -1 - r;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int k2 = __shfl_up_sync(0xFFFFFFFFu, key, off);
+    const float ea = __shfl_up_sync(0xFFFFFFFFu, e2, off), sa = __shfl_up_sync(0xFFFFFFFFu, s2, off);
+    if (lane >= off && k2 == key) {
+      e2 += ea;
+      s2 += sa;
+    }
+  }
+  const int next = __shfl_down_sync(0xFFFFFFFFu, key, 1);
+  if (r < t.n && (lane == 31 || next != key)) {
+    const int64_t cell = nrc_cell(a.lv[t.level], p, a.tile_shift, a.TX, a.TY);
+    atomicAdd(&num[cell], e2);
+    // the smallest normal float marks the cell as scored this solve even where
+    // no light reaches its probes
+    atomicAdd(&den[cell], s2 + 1.17549435e-38f);
+  }
+}
+
+// Fallback flags from the held-out sums of this solve (num, den) and of the
+// last `window` solves (ring[window][2][n], this solve's sums go to row
+// `slot`).  Each solve scores another sub-lattice of directions, so the
+// window covers every direction of the cell.  A cell scored this solve is
+// flagged when the relative error of this solve or of the window exceeds the
+// threshold; cells not scored this solve keep their flag.  Clears num, den.
+__global__ void k_nrc_flags(float* __restrict__ num, float* __restrict__ den, float* __restrict__ ring, int window,
+                            int slot, uint8_t* __restrict__ flag, int64_t n, float thr2) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float e = num[i], s = den[i];
-  if (e > 0.f || s > 0.f) flag[i] = (e > thr2 * fmaxf(s, 1e-6f)) ? 1 : 0;
+  ring[((int64_t)slot * 2) * n + i] = e;
+  ring[((int64_t)slot * 2 + 1) * n + i] = s;
+  if (e > 0.f || s > 0.f) {
+    float we = 0.f, ws = 0.f;
+    for (int k = 0; k < window; ++k) {
+      we += ring[((int64_t)k * 2) * n + i];
+      ws += ring[((int64_t)k * 2 + 1) * n + i];
+    }
+    flag[i] = (e > thr2 * fmaxf(s, 1e-6f) || we > thr2 * fmaxf(ws, 1e-6f)) ? 1 : 0;
+  }
   num[i] = 0.f;
   den[i] = 0.f;
-}
-
-__device__ __forceinline__ int64_t nrc_cell(const NrcLevel& L, int64_t p, int shift, int TX, int TY) {
-  const int mx = (int)(p % L.M[0]), my = (int)((p / L.M[0]) % L.M[1]), mz = (int)(p / ((int64_t)L.M[0] * L.M[1]));
-  const int h = L.spacing >> 1;
-  return ((int64_t)((mz * L.spacing + h) >> shift) * TY + ((my * L.spacing + h) >> shift)) * TX +
-         ((mx * L.spacing + h) >> shift);
 }
 
 // Probes of each far level that sit in fallback tiles.
@@ -854,90 +1070,64 @@ __global__ void k_nrc_count(const __grid_constant__ NrcArgs a, const uint8_t* __
   if (flag[nrc_cell(a.lv[li], p, shift, TX, TY)]) atomicAdd(&count[li], 1u);
 }
 
-// Fallback: plain (R, T) for every query of probes in flagged tiles of the
-// levels the network serves (served[level]).
-struct NrcFallbackArgs {
-  LevelArgs lv[kMaxCascades];
-  NrcArgs n;
-  const uint8_t* flag;
-  int tile_shift, TX, TY;
-  int32_t served[kMaxCascades];
-  int64_t total;  // queries over all far levels
-};
-
-__global__ void k_nrc_fallback(const __grid_constant__ NrcFallbackArgs f) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= f.total) return;
-  int li = f.n.first;
-  int64_t q = i;
-  while (li < f.n.nlev && q >= f.n.lv[li].P * f.n.lv[li].ndirs) q -= f.n.lv[li].P * f.n.lv[li++].ndirs;
-  if (li >= f.n.nlev || !f.served[li]) return;
-  const NrcLevel& L = f.n.lv[li];
-  const int d = (int)(q / L.P);
-  const int64_t p = q - (int64_t)d * L.P;
-  if (!f.flag[nrc_cell(L, p, f.tile_shift, f.TX, f.TY)]) return;
-  float rt[4];
-  nrc_walk(f.lv[li], p, d, rt);
-  const int64_t plane = (int64_t)L.ndirs * L.P;
-#pragma unroll
-  for (int c = 0; c < 4; ++c) L.rt[c * plane + q] = __float2half_rn(rt[c]);
+// Serve decision per far level: a level with at least `fraction` of its
+// probes in flagged tiles runs entirely on its walks (plain[level] = 1);
+// served[level] counts the solves the network served the level.  Clears the
+// counts for the next solve.
+__global__ void k_nrc_decide(const __grid_constant__ NrcArgs a, unsigned* __restrict__ count,
+                             int32_t* __restrict__ plain, unsigned long long* __restrict__ served, float fraction) {
+  const int li = a.first + (int)threadIdx.x;
+  if (li >= a.nlev) return;
+  const int walk = (double)count[li] >= (double)fraction * (double)a.lv[li].P ? 1 : 0;
+  plain[li] = walk;
+  if (!walk) ++served[li];
+  count[li] = 0u;
 }
 
 // ---------------------------------------------------------------------------
-// Merge of a far level from (R, T): L = R + T * trilinear(A_{i+1}); one thread
-// per probe, block row = a pair of parent texels (eight child directions).
+// Merge of a far level: per probe the interval results come from the network
+// (R, T), or from the walk records when the level runs plain or the probe's
+// tile is flagged; then L = R + T * trilinear(A_{i+1}) as in the plain merge.
+// One thread per probe, block row = a pair of parent texels (eight child
+// directions).
 // ---------------------------------------------------------------------------
 template <typename T, bool TOP>
-__global__ void __launch_bounds__(128) k_level_merge_rt(const __grid_constant__ LevelArgs a,
-                                                        const __half* __restrict__ rt) {
+__global__ void __launch_bounds__(128) k_level_merge_nrc(const __grid_constant__ LevelArgs a,
+                                                         const __grid_constant__ NrcArgs n, int level) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.P) return;
-  const int Mx = a.M[0], My = a.M[1];
-  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  const NrcLevel& NL = n.lv[level];
+  const bool walked = __ldg(n.plain + level) != 0 || __ldg(n.flag + nrc_cell(NL, p, n.tile_shift, n.TX, n.TY)) != 0;
   int tap_off[8];
   float tap_w[8];
-  if (!TOP) {
-    int qq[3][2];
-    float wt[3][2];
-    const int m[3] = {mx, my, mz};
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-      const int lo = (m[ax] - 1) >> 1;
-      wt[ax][0] = (m[ax] & 1) ? 0.75f : 0.25f;
-      wt[ax][1] = 1.0f - wt[ax][0];
-      qq[ax][0] = min(max(lo, 0), a.UM[ax] - 1);
-      qq[ax][1] = min(max(lo + 1, 0), a.UM[ax] - 1);
-    }
-#pragma unroll
-    for (int tp = 0; tp < 8; ++tp) {
-      const int ix = tp & 1, iy = (tp >> 1) & 1, iz = tp >> 2;
-      tap_off[tp] = (qq[2][iz] * a.UM[1] + qq[1][iy]) * a.UM[0] + qq[0][ix];
-      tap_w[tp] = wt[2][iz] * wt[1][iy] * wt[0][ix];
-    }
-  }
+  if (!TOP) merge_taps(a, p, tap_off, tap_w);
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
   const int hn = a.n >> 1;
   const int64_t npar = (int64_t)hn * hn;
   const int64_t plane = (int64_t)a.ndirs * a.P;
+  const __half* rt = NL.rt;
   float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll 1
   for (int dl = 0; dl < 8; ++dl) {
     const int dp = blockIdx.y * 2 + (dl >> 2), c = dl & 3;
     const int d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
     const int64_t off = (int64_t)d * a.P + p;
-    float rv[3];
+    float rv[4];
+    if (walked) {
+      nrc_record_rt(a.vol, __ldg(NL.rec + nrc_rec_index(NL, p, d)), rv);
+    } else {
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) rv[ch] = __half2float(rt[ch * plane + off]);
-    const float tr = __half2float(rt[3 * plane + off]);
-    if (!TOP && tr > 0.f) {
+      for (int ch = 0; ch < 4; ++ch) rv[ch] = __half2float(rt[ch * plane + off]);
+    }
+    if (!TOP && rv[3] > 0.f) {
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) {
         const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
         float sum = 0.f;
 #pragma unroll
         for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
-        rv[ch] = fmaf(tr, sum, rv[ch]);
+        rv[ch] = fmaf(rv[3], sum, rv[ch]);
       }
     }
 #pragma unroll

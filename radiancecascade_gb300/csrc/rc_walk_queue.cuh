@@ -38,6 +38,11 @@ struct QueueLevel {
   // ends where every probe of the level has left the grid on some axis.
   const uint2* steps;
   const int32_t* step_begin;
+  // Optional per-slot and per-direction switches (null: all on): item
+  // (d, slot) walks only when both bytes are nonzero.  The learned form walks
+  // only the words and directions it needs.
+  const uint8_t* word_on;
+  const uint8_t* dir_on;
 };
 
 struct QueueArgs {
@@ -97,6 +102,7 @@ struct Walker {
     My = L.M[1];
     Mz = L.M[2];
     rep = L.rep;
+    if ((L.word_on && !__ldg(L.word_on + slot)) || (L.dir_on && !__ldg(L.dir_on + d))) return false;
     zl = slot / wpp;
     const int wl = slot - zl * wpp;
     g0 = wl << 5;
@@ -277,6 +283,7 @@ struct TableWalker {
     Mz = L.M[2];
     mzw = Mz * wpp;
     rep = L.rep;
+    if ((L.word_on && !__ldg(L.word_on + slot)) || (L.dir_on && !__ldg(L.dir_on + d))) return false;
     zl = slot / wpp;
     const int wl = slot - zl * wpp;
     g0 = wl << 5;

@@ -590,7 +590,9 @@ class Engine:
     def nrc_stats(self) -> dict:
         st = F.NrcStats()
         F.check(self._lib.rc_nrc_get_stats(self.handle, C.byref(st)))
-        return {k: getattr(st, k) for k, _ in st._fields_ if k != "pad"}
+        out = {k: getattr(st, k) for k, _ in st._fields_ if k != "pad"}
+        out["served_solves"] = list(st.served_solves)
+        return out
 
     def nrc_save(self) -> bytes:
         need = C.c_int64()

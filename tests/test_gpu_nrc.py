@@ -3,8 +3,9 @@ training, the learned solve against the FP64 oracle, save / load.
 
 Tolerances: served (R, G, B, T) within 2e-3 absolute (radiance units after
 1/scale) of the BF16-emulating NumPy forward, away from the T threshold; the tile gradient within 3e-2
-relative L2 (BF16 rounding of the backward operands); the learned solve's
-fluence within 1% relative L2 of the FP64 oracle (with the per-tile fallback).
+relative L2 (BF16 rounding of the backward operands); the learned solve,
+with the network serving at least one far cascade, within 1% relative L2 of
+the FP64 oracle with the per-tile fallback and within 2% with no fallback.
 """
 import numpy as np
 import pytest
@@ -88,7 +89,7 @@ def test_tile_gradient_matches_numpy():
         e.close()
 
 
-def test_training_lowers_loss_and_learned_solve_within_one_percent():
+def test_training_lowers_loss():
     e, boxes, spheres = _engine()
     try:
         losses = []
@@ -99,24 +100,72 @@ def test_training_lowers_loss_and_learned_solve_within_one_percent():
         st = e.nrc_stats()
         assert st["solves"] == 48 and st["steps"] == 48
         assert losses[-1] < losses[0]
-        g = e.fluence().astype(np.float64)
-        ref, _ = O.solve(O.params(64, 5), O.voxelise(64, boxes, spheres))
-        assert rel_l2(g, ref) <= 1e-2, rel_l2(g, ref)
     finally:
         e.close()
 
 
-def test_no_fallback_serves_every_tile_from_the_network():
-    """Threshold above any error: after the first held-out pass every tile is
-    served by the network; the fluence stays finite and non-negative."""
-    e, boxes, spheres = _engine(fallback_threshold=1e9)
+def _served(st, level):
+    return (st["served_levels"] >> level) & 1
+
+
+@pytest.mark.parametrize("first,plain_fraction", [(3, 0.5), (2, 1.0)])
+def test_learned_solve_serves_from_the_network_within_one_percent(first, plain_fraction):
+    """64^3: after 48 solves the network serves at least one far cascade (in
+    whole, or per tile next to walked fallback tiles) and the fluence stays
+    within 1% relative L2 of the FP64 oracle."""
+    e, boxes, spheres = _engine(first_level=first, plain_level_fraction=plain_fraction)
     try:
-        for _ in range(20):
+        for _ in range(48):
             e.solve()
         st = e.nrc_stats()
-        assert st["fallback_tiles"] == 0 and st["tiles"] == 8 ** 3
         g = e.fluence().astype(np.float64)
-        assert np.isfinite(g).all() and g.min() >= 0.0
+    finally:
+        e.close()
+    assert st["served_levels"] != 0, st
+    assert st["fallback_tiles"] < st["tiles"], st
+    ref, _ = O.solve(O.params(64, 5), O.voxelise(64, boxes, spheres))
+    err, max_abs = rel_l2(g, ref), float(np.abs(g - ref).max())
+    print("64^3 learned (first %d): served %s, fallback %d/%d tiles, rel-L2 %.3e, max-abs %.3e"
+          % (first, bin(st["served_levels"]), st["fallback_tiles"], st["tiles"], err, max_abs))
+    assert err <= 1e-2, err
+    assert np.isfinite(max_abs)
+
+
+def _scene_256(frame):
+    boxes, sph = R.workload_scene("c256")
+    sph = sph.copy()
+    R.advance_spheres(sph, 256, frame)
+    return boxes, sph
+
+
+@pytest.mark.parametrize("threshold,bound", [(0.01, 1e-2), (1e9, 2e-2)])
+def test_learned_256_frames_0_1_239(threshold, bound):
+    """256^3 FP16, the cache on cascades 4 and 5: it learns for 48 solves on
+    frame 0, then solves frame 1, then jumps to frame 239 (8 solves).  With
+    the 1% per-tile fallback the cache serves cascade 5 and the fluence is
+    within 1% of the FP64 oracle on every frame; with no fallback at all (the
+    network serves every tile of both cascades) within 2%."""
+    e = R.Engine(R.make_params(256, 6, precision="fp16"))
+    boxes, _ = _scene_256(0)
+    e.set_boxes(boxes)
+    e.nrc_enable(first_level=4, fallback_threshold=threshold)
+    try:
+        for frame, solves in ((0, 48), (1, 1), (239, 8)):
+            _, sph = _scene_256(frame)
+            e.set_spheres(sph)
+            for _ in range(solves):
+                e.solve()
+            st = e.nrc_stats()
+            g = e.fluence().astype(np.float64)
+            ref, _ = O.solve(O.params(256, 6), O.voxelise(256, boxes, sph), jump=True)
+            err, max_abs = rel_l2(g, ref), float(np.abs(g - ref).max())
+            print("256^3 frame %d: served %s, fallback %d/%d, rel-L2 %.3e, max-abs %.3e"
+                  % (frame, bin(st["served_levels"]), st["fallback_tiles"], st["tiles"], err, max_abs))
+            assert _served(st, 5), st
+            assert st["fallback_tiles"] < st["tiles"], st
+            if threshold > 1.0:
+                assert st["fallback_tiles"] == 0 and _served(st, 4), st
+            assert err <= bound, (frame, err)
     finally:
         e.close()
 

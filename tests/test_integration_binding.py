@@ -36,13 +36,19 @@ def _rust_structs(block):
     return out
 
 
+def _consts():
+    """usize constants of the binding (array lengths)."""
+    return {k: int(v) for k, v in re.findall(r"pub const (\w+): usize = (\d+);", _rust_block())}
+
+
 def _layout(ty, structs, memo):
     """(size, align) of a Rust field type under C layout rules."""
     ty = ty.strip()
-    m = re.fullmatch(r"\[(.+);\s*(\d+)\]", ty)
+    m = re.fullmatch(r"\[(.+);\s*(\w+)\]", ty)
     if m:
         s, a = _layout(m.group(1), structs, memo)
-        return s * int(m.group(2)), a
+        count = m.group(2)
+        return s * (int(count) if count.isdigit() else _consts()[count]), a
     if ty.startswith("*"):
         return 8, 8
     if ty in SCALARS:
