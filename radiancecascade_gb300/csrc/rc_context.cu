@@ -415,7 +415,7 @@ void launch_queue_walk(const rc_context* c, cudaStream_t s, uint32_t skip = 0) {
   const int64_t blocks = std::min<int64_t>((q->total + kQueueThreads - 1) / kQueueThreads, c->queue_blocks);
   cudaMemsetAsync(q->counter, 0, sizeof(unsigned long long), s);
   if (c->qtab)
-    k_walk_queue_tab<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
+    launch_table_walk(*q, c->queue_resident, s);
   else
     k_walk_queue<<<(unsigned)blocks, kQueueThreads, 0, s>>>(*q);
 }
@@ -443,7 +443,9 @@ rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
     bool queue_near = false;
     for (int i = 0; i < near; ++i) queue_near |= c->mode[i] == kModeQueue;
     // the far levels' walks, where they run at all, are launched by the cache
-    if (queue_near) launch_queue_walk(c, s, ~((1u << near) - 1u));
+    // (the cache's second far walk takes the near levels' walks along when
+    // both use step tables: one launch balances them together)
+    if (queue_near && !nrc_walks_near(c)) launch_queue_walk(c, s, ~((1u << near) - 1u));
     rc_status st = nrc_enqueue_far(c, s);
     if (st != RC_OK) return st;
   } else {
@@ -744,8 +746,9 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
         L.step_begin = c->qstep_begin + boff[L.level];
       }
       c->qtab = true;
+      c->queue_resident = queue_resident_blocks(true);
       c->queue_blocks = (int)std::min<int64_t>((c->qargs.total + kQueueThreads - 1) / kQueueThreads,
-                                               queue_resident_blocks(true));
+                                               c->queue_resident);
     }
   }
   if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);

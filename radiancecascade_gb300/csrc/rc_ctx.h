@@ -46,6 +46,7 @@ struct rc_context {
   bool qtab = false;
   rcx::QueueArgs qargs{};
   int queue_blocks = 0;
+  int queue_resident = 0;  // blocks of the step-table walk that fit the GPU at once
   int rec_slots[rcx::kMaxCascades]{};
   const uint32_t* rec_level[rcx::kMaxCascades]{};
   CUtensorMap tma0{};                // cascade 1's child-averaged radiance, for k_level0_tma
@@ -129,6 +130,9 @@ bool level_uses_queue(const rc_context* c, int level);
 // Neural radiance cache hooks (rc_nrc.cu).
 bool nrc_active(const rc_context* c);
 int nrc_first_level(const rc_context* c);  // first cascade the cache serves
+// Whether the cache's far walk also walks the near levels that use the walk
+// queue (both use step tables); then the solve launches no near walk.
+bool nrc_walks_near(const rc_context* c);
 // Enqueues the cache's per-frame work for the far cascades (training-sample
 // walks, refit, inference, fallback walks) and their merges, top level down to
 // the first far level.  Called from the solve before the near levels.

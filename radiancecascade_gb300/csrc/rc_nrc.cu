@@ -39,6 +39,9 @@ struct NrcState {
   std::vector<uint8_t> probe_tile;  // tiles that hold a far probe
   std::vector<int64_t> tile_begin;
   int32_t* dlist = nullptr;  // directions of the sample tiles, per level and phase
+  int64_t dlist_base[kMaxCascades]{};  // a level's directions in dlist
+  std::vector<std::vector<int64_t>> pair_start = std::vector<std::vector<int64_t>>(kMaxCascades),
+                                    pair_len = std::vector<std::vector<int64_t>>(kMaxCascades);
   int64_t max_tiles2 = 0, max_held = 0;
   float* target = nullptr;
   float* pred = nullptr;
@@ -59,9 +62,10 @@ struct NrcState {
   uint2* fsteps = nullptr;
   int32_t* fstep_begin = nullptr;
   bool ftab = false;
-  int fq_blocks = 0;
+  int fq_resident = 0;  // walk blocks that fit the GPU at once
   uint8_t* word_on = nullptr;
   float* omega = nullptr;
+  uint32_t* hparts = nullptr;  // hash parts of the far probes, then of the far directions
   NrcWordArgs words{};
   // fallback tiles
   int tile_shift = 3, TX = 0, TY = 0, TZ = 0;
@@ -91,7 +95,7 @@ void free_state(NrcState* n) {
                   n->mlp_v,       n->mlp_g,  n->dbg_g,  n->img,    n->denc,      n->rt,    n->tiles,
                   n->dlist, n->target, n->pred,   n->epos_grad, n->loss,  n->qtiles,
                   n->qout,        n->tnum,   n->tden,   n->tring,   n->flag,   n->count,     n->plain, n->served_solves, n->frec,
-                  n->fcounter,    n->fsteps, n->fstep_begin, n->word_on, n->omega};
+                  n->fcounter,    n->fsteps, n->fstep_begin, n->word_on, n->omega, n->hparts};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (n->h_loss) cudaFreeHost(n->h_loss);
@@ -192,6 +196,7 @@ rc_status upload_params(NrcState* n, const std::vector<float>& mlp, const std::v
 
 bool nrc_active(const rc_context* c) { return c && c->nrc; }
 int nrc_first_level(const rc_context* c) { return c->nrc ? c->nrc->first : c->nlev; }
+bool nrc_walks_near(const rc_context* c) { return c->nrc && c->nrc->ftab && c->qtab; }
 
 void nrc_release(rc_context* c) {
   if (!c || !c->nrc) return;
@@ -217,17 +222,45 @@ unsigned fwd_grid(const NrcState* n, int64_t ntiles) {
 
 namespace {
 
-void far_walk(NrcState* n, cudaStream_t s, int mode, int ph, int hp) {
-  NrcWordArgs w = n->words;
-  w.mode = mode;
-  w.ph = ph;
-  w.hp = hp;
-  k_nrc_words<<<blocks_for(w.slot0[w.nlev] + w.dir0[w.nlev], 128), 128, 0, s>>>(w);
+// Walk of the far levels' queue.  Mode 0: the training and held-out
+// directions (phase pair ph, ph + nph/2) of every word.  Mode 1: every other
+// direction of the words k_nrc_words switches on, and every walk of the near
+// levels that use the walk queue (nrc_walks_near).  The items of a far level
+// are its selected directions x its slots, so skipped walks cost no lanes.
+void far_walk(const rc_context* c, NrcState* n, cudaStream_t s, int mode, int ph) {
+  QueueArgs q = n->fq;
+  const int pair = ph % (n->nph / 2);
+  int64_t items = 0;
+  for (int k = 0; k < q.n; ++k) {
+    QueueLevel& L = q.lv[k];
+    const int i = L.level;
+    const int64_t st = n->pair_start[i][pair], len = n->pair_len[i][pair];
+    L.dsel_start = (int32_t)(mode == 0 ? st : (st + len) % L.dsel_len);
+    L.dsel_n = (int32_t)(mode == 0 ? len : L.dsel_len - len);
+    if (mode == 0) L.word_on = nullptr;
+    L.item_begin = items;
+    items += (int64_t)L.dsel_n * L.slots;
+  }
+  if (mode == 1 && nrc_walks_near(c))
+    for (int k = 0; k < c->qargs.n; ++k) {
+      const QueueLevel& nl = c->qargs.lv[k];
+      if (nl.level >= n->first) continue;
+      QueueLevel& L = q.lv[q.n++];
+      L = nl;
+      L.item_begin = items;
+      items += (int64_t)L.slots * c->geom[L.level].ndirs;
+    }
+  q.total = items;
+  if (!items) return;
+  if (mode == 1) k_nrc_words<<<blocks_for(n->words.slot0[n->words.nlev], 128), 128, 0, s>>>(n->words);
   cudaMemsetAsync(n->fcounter, 0, sizeof(unsigned long long), s);
-  if (n->ftab)
-    k_walk_queue_tab<<<(unsigned)n->fq_blocks, kQueueThreads, 0, s>>>(n->fq);
-  else
-    k_walk_queue<<<(unsigned)n->fq_blocks, kQueueThreads, 0, s>>>(n->fq);
+  if (n->ftab) {
+    launch_table_walk(q, n->fq_resident, s);
+  } else {
+    const unsigned blocks = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((items + kQueueThreads - 1) / kQueueThreads, (int64_t)n->fq_resident));
+    k_walk_queue<<<blocks, kQueueThreads, 0, s>>>(q);
+  }
 }
 
 template <typename T>
@@ -257,7 +290,7 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   float* ttr = n->target;
   float* tho = n->target + ntr * kNrcThreads * 4;
   // 1. the sample directions and their targets
-  far_walk(n, s, 0, ph, hp);
+  far_walk(c, n, s, 0, ph);
   NrcArgs a = n->base;
   if (ntr) {
     a.tiles = n->tiles + tr0;
@@ -312,7 +345,7 @@ rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
   k_nrc_decide<<<1, kMaxCascades, 0, s>>>(n->base, n->count, n->plain, n->served_solves,
                                           n->prm.plain_level_fraction);
   // 4. the walks still needed
-  far_walk(n, s, 1, ph, hp);
+  far_walk(c, n, s, 1, ph);
   // 5. inference of the served probes with the network just scored, merges
   // top down
   k_nrc_forward<true><<<fwd_grid(n, n->enum_tiles), kFwdThreads, kFwdSmem, s>>>(n->base, n->enum_tiles);
@@ -464,7 +497,7 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   n->base.err = c->err;
   // Far levels' walk geometry (the decimated-opacity words of the bit-parallel
   // walk).
-  int64_t slot_total = 0, dir_total = 0;
+  int64_t slot_total = 0;
   for (int i = n->first; i < c->nlev; ++i) {
     const LevelArgs& la = c->args[i];
     if (!c->bits_level[i] || !la.mask) {
@@ -477,23 +510,33 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
     L.l2px = la.l2px;
     n->words.slot0[i] = slot_total;
     slot_total += L.slots;
-    n->words.dir0[i] = dir_total;
-    dir_total += c->geom[i].ndirs;
   }
   n->words.slot0[c->nlev] = slot_total;
-  n->words.dir0[c->nlev] = dir_total;
   // Sample tiles by phase: every far probe with the directions of the phase
   // (nrc_dir_phase), up to 128 per tile; a tile's slot is its probe's index.
   {
+    // Per level the directions ordered by phase pair (q, q + nph/2): the
+    // training and held-out directions of a solve are one contiguous run,
+    // the rest of the level the run after it (cyclically).
     std::vector<int32_t> dlist;
-    std::vector<std::vector<int64_t>> list_at(kMaxCascades, std::vector<int64_t>(n->nph + 1, 0));
-    for (int i = n->first; i < c->nlev; ++i)
-      for (int ph = 0; ph < n->nph; ++ph) {
-        list_at[i][ph] = (int64_t)dlist.size();
-        for (int d = 0; d < c->geom[i].ndirs; ++d)
-          if (nrc_dir_phase(d, c->geom[i].n, n->nph) == ph) dlist.push_back(d);
-        list_at[i][ph + 1] = (int64_t)dlist.size();
+    std::vector<std::vector<int64_t>> list_b(kMaxCascades, std::vector<int64_t>(n->nph, 0)),
+        list_e(kMaxCascades, std::vector<int64_t>(n->nph, 0));
+    for (int i = n->first; i < c->nlev; ++i) {
+      n->pair_start[i].assign(n->nph / 2, 0);
+      n->pair_len[i].assign(n->nph / 2, 0);
+      n->dlist_base[i] = (int64_t)dlist.size();
+      for (int q = 0; q < n->nph / 2; ++q)
+        for (int ph : {q, q + n->nph / 2}) {
+          list_b[i][ph] = (int64_t)dlist.size();
+          for (int d = 0; d < c->geom[i].ndirs; ++d)
+            if (nrc_dir_phase(d, c->geom[i].n, n->nph) == ph) dlist.push_back(d);
+          list_e[i][ph] = (int64_t)dlist.size();
+        }
+      for (int q = 0; q < n->nph / 2; ++q) {
+        n->pair_start[i][q] = list_b[i][q] - n->dlist_base[i];
+        n->pair_len[i][q] = list_e[i][q + n->nph / 2] - list_b[i][q];
       }
+    }
     if ((int64_t)dlist.size() >= ((int64_t)1 << 31)) {
       set_error("rc_nrc_enable: too many far directions");
       return fail(RC_ERR_UNSUPPORTED);
@@ -503,7 +546,7 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
       n->tile_begin[ph] = (int64_t)n->h_tiles.size();
       int32_t k = 0;
       for (int i = n->first; i < c->nlev; ++i) {
-        const int64_t l0 = list_at[i][ph], len = list_at[i][ph + 1] - l0;
+        const int64_t l0 = list_b[i][ph], len = list_e[i][ph] - l0;
         if (len == 0) continue;
         const int64_t P = c->geom[i].probes();
         if (len >= kNrcThreads) {  // tiles of one probe, 128 of its directions each
@@ -580,6 +623,28 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
             "rc_nrc_enable: upload");
     for (int i = n->first; i < c->nlev; ++i) n->base.lv[i].omega = n->omega + at[i];
   }
+  // the position and direction parts of every far query's hash
+  {
+    int64_t np = 0, nd = 0;
+    for (int i = n->first; i < c->nlev; ++i) {
+      np += c->geom[i].probes();
+      nd += c->geom[i].ndirs;
+    }
+    if ((s = dev_alloc((void**)&n->hparts, (size_t)(np + nd) * kNrcHashLevels * sizeof(uint32_t),
+                       "hash parts")) != RC_OK)
+      return fail(s);
+    int64_t po = 0, dof = np;
+    for (int i = n->first; i < c->nlev; ++i) {
+      NrcLevel& L = n->base.lv[i];
+      L.hpos = n->hparts + po * kNrcHashLevels;
+      L.hdir = n->hparts + dof * kNrcHashLevels;
+      po += c->geom[i].probes();
+      dof += c->geom[i].ndirs;
+      const int64_t m = std::max<int64_t>(c->geom[i].probes(), c->geom[i].ndirs);
+      k_nrc_hash_parts<<<blocks_for(m, 128), 128>>>(n->base, i);
+    }
+    RC_CUDA(cudaGetLastError(), "rc_nrc_enable: hash parts");
+  }
   // fallback tiles: all start on the plain walk
   n->tile_shift = 0;
   while ((1 << n->tile_shift) < q.fallback_tile) ++n->tile_shift;
@@ -616,11 +681,9 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
   // where every far level has one (else the walk's own DDA), and one switch
   // per word that the schedule sets before each walk.
   {
-    if ((s = dev_alloc((void**)&n->word_on, std::max<int64_t>(1, slot_total + dir_total), "far walk switches")) !=
-        RC_OK)
+    if ((s = dev_alloc((void**)&n->word_on, std::max<int64_t>(1, slot_total), "far walk switches")) != RC_OK)
       return fail(s);
-    RC_CUDA(cudaMemset(n->word_on, 0, std::max<int64_t>(1, slot_total + dir_total)), "rc_nrc_enable: memset");
-    uint8_t* dir_on = n->word_on + slot_total;
+    RC_CUDA(cudaMemset(n->word_on, 0, std::max<int64_t>(1, slot_total)), "rc_nrc_enable: memset");
     size_t rec_words = 0;
     for (int i = n->first; i < c->nlev; ++i) rec_words += (size_t)c->geom[i].ndirs * n->base.lv[i].slots * 32;
     if ((s = dev_alloc((void**)&n->frec, rec_words * sizeof(uint32_t), "far walk records")) != RC_OK) return fail(s);
@@ -661,8 +724,8 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
       L.level = i;
       L.word_on = n->word_on + n->words.slot0[i];
       NL.word_on = n->word_on + n->words.slot0[i];
-      L.dir_on = dir_on + n->words.dir0[i];
-      NL.dir_on = dir_on + n->words.dir0[i];
+      L.dsel = n->dlist + n->dlist_base[i];
+      L.dsel_len = gm.ndirs;
       if (tab_ok) {
         std::vector<DirInfo> tab((size_t)gm.ndirs);
         if (!build_dir_table(gm, c->p.grid, tab.data(), msg, sizeof msg)) return fail(RC_ERR_UNSUPPORTED);
@@ -705,13 +768,11 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
       (void)cudaGetLastError();
       per_sm = 2;
     }
-    n->fq_blocks = (int)std::max<int64_t>(
-        1, std::min<int64_t>((items + kQueueThreads - 1) / kQueueThreads, (int64_t)std::max(1, sms0 * per_sm)));
+    n->fq_resident = std::max(1, sms0 * per_sm);
     NrcWordArgs& w = n->words;
     for (int i = 0; i < kMaxCascades; ++i) w.lv[i] = n->base.lv[i];
     w.first = n->first;
     w.nlev = c->nlev;
-    w.nph = n->nph;
     w.plain = n->plain;
     w.flag = n->flag;
     w.tile_shift = n->tile_shift;

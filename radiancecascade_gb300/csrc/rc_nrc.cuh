@@ -87,8 +87,9 @@ struct NrcLevel {
   const uint32_t* rec;
   int32_t slots, wpp, l2px;
   uint8_t* word_on;           // [slots] walk switch of the level's words
-  uint8_t* dir_on;            // [ndirs] walk switch of the level's directions
   const float* omega;         // [ndirs] exact texel solid angles
+  uint32_t* hpos;             // [P][16] position part of the hash per hash level
+  uint32_t* hdir;             // [ndirs][16] direction part of the hash per hash level
 };
 
 struct NrcHash {
@@ -204,34 +205,57 @@ __device__ __forceinline__ void nrc_record_rt(const uint2* __restrict__ vol, uin
   if (r != kMiss && r != kBlack) voxel_emission(vol, r, rt);
 }
 
-// Table row of hash level l for a query (see the file comment).
-__device__ __forceinline__ uint32_t nrc_hash_row(const NrcHash& h, int l, const float* u, float du, float dv,
-                                                 int casc) {
-  const int r = h.res[l], q = h.dres[l];
+// The hash of a query (see the file comment) is the XOR of a part that
+// depends only on the probe's cell, x ^ y K1 ^ z K2, and a part that depends
+// only on the direction texel's cell and the cascade, a K3 ^ b K4 ^ c K5.
+__device__ __forceinline__ uint32_t nrc_hash_pos(const NrcHash& h, int l, const float* u) {
+  const int r = h.res[l];
   const uint32_t x = (uint32_t)min((int)(u[0] * (float)r), r - 1);
   const uint32_t y = (uint32_t)min((int)(u[1] * (float)r), r - 1);
   const uint32_t z = (uint32_t)min((int)(u[2] * (float)r), r - 1);
+  return x ^ (y * 2654435761u) ^ (z * 805459861u);
+}
+__device__ __forceinline__ uint32_t nrc_hash_dir(const NrcHash& h, int l, float du, float dv, int casc) {
+  const int q = h.dres[l];
   const uint32_t a = (uint32_t)min((int)(du * (float)q), q - 1);
   const uint32_t b = (uint32_t)min((int)(dv * (float)q), q - 1);
-  const uint32_t hv = x ^ (y * 2654435761u) ^ (z * 805459861u) ^ (a * 0x85EBCA77u) ^ (b * 0xC2B2AE3Du) ^
-                      ((uint32_t)casc * 0x27D4EB2Fu);
-  return (uint32_t)l * (1u << h.log2T) + (hv & ((1u << h.log2T) - 1u));
+  return (a * 0x85EBCA77u) ^ (b * 0xC2B2AE3Du) ^ ((uint32_t)casc * 0x27D4EB2Fu);
 }
 
-struct NrcQuery {
-  float u[3];   // probe centre in [0, 1]
-  float du, dv; // texel centre in [0, 1]
-  int casc;
-};
-
-__device__ __forceinline__ NrcQuery nrc_make_query(const NrcArgs& a, int li, int64_t p, int d) {
-  NrcQuery q;
+// Both parts for every probe and every direction of far level li, written
+// once when the cache is enabled (NrcLevel.hpos, .hdir).
+__global__ void k_nrc_hash_parts(const __grid_constant__ NrcArgs a, int li) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const NrcLevel& L = a.lv[li];
-  nrc_probe_pos(L, p, a.hash.inv_extent, q.u);
-  q.du = ((float)(d % L.n) + 0.5f) / (float)L.n;
-  q.dv = ((float)(d / L.n) + 0.5f) / (float)L.n;
-  q.casc = li;
-  return q;
+  if (i < L.P) {
+    float u[3];
+    nrc_probe_pos(L, i, a.hash.inv_extent, u);
+#pragma unroll
+    for (int l = 0; l < kNrcHashLevels; ++l) L.hpos[i * kNrcHashLevels + l] = nrc_hash_pos(a.hash, l, u);
+  }
+  if (i < L.ndirs) {
+    const int d = (int)i;
+    const float du = ((float)(d % L.n) + 0.5f) / (float)L.n, dv = ((float)(d / L.n) + 0.5f) / (float)L.n;
+#pragma unroll
+    for (int l = 0; l < kNrcHashLevels; ++l) L.hdir[i * kNrcHashLevels + l] = nrc_hash_dir(a.hash, l, du, dv, li);
+  }
+}
+
+// Table rows of the 16 hash levels of query (p, d) of far level li:
+// row_l = l 2^log2T + ((hpos_l ^ hdir_l) mod 2^log2T), two 64-byte loads.
+__device__ __forceinline__ void nrc_rows(const NrcArgs& a, int li, int64_t p, int d, uint32_t* rows) {
+  const NrcLevel& L = a.lv[li];
+  const uint4* hp = reinterpret_cast<const uint4*>(L.hpos + p * kNrcHashLevels);
+  const uint4* hd = reinterpret_cast<const uint4*>(L.hdir + (int64_t)d * kNrcHashLevels);
+  const uint32_t T = 1u << a.hash.log2T, mask = T - 1u;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint4 P = __ldg(hp + j), D = __ldg(hd + j);
+    rows[4 * j + 0] = (4 * j + 0) * T + ((P.x ^ D.x) & mask);
+    rows[4 * j + 1] = (4 * j + 1) * T + ((P.y ^ D.y) & mask);
+    rows[4 * j + 2] = (4 * j + 2) * T + ((P.z ^ D.z) & mask);
+    rows[4 * j + 3] = (4 * j + 3) * T + ((P.w ^ D.w) & mask);
+  }
 }
 
 // Input row: 32 hash features, 16 direction features, 16 zeros.
@@ -240,11 +264,11 @@ __device__ __forceinline__ void nrc_input(const NrcArgs& a, bool valid, int li, 
   for (int j = 0; j < 64; ++j) x[j] = 0.f;
   if (!valid) return;
   const NrcLevel& L = a.lv[li];
-  const NrcQuery q = nrc_make_query(a, li, p, d);
+  uint32_t rows[kNrcHashLevels];
+  nrc_rows(a, li, p, d, rows);
 #pragma unroll
   for (int l = 0; l < kNrcHashLevels; ++l) {
-    const uint32_t row = nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc);
-    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(a.hash.table) + row));
+    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(a.hash.table) + rows[l]));
     x[2 * l] = f.x;
     x[2 * l + 1] = f.y;
   }
@@ -297,11 +321,11 @@ __device__ __forceinline__ void nrc_encode_row(const NrcArgs& a, bool valid, int
     for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(XA + core_off(row, 8 * c, 64)) = zero;
     return;
   }
-  const NrcQuery q = nrc_make_query(a, li, p, d);
+  uint32_t rows[kNrcHashLevels];
+  nrc_rows(a, li, p, d, rows);
   __half2 f[kNrcHashLevels];
 #pragma unroll
-  for (int l = 0; l < kNrcHashLevels; ++l)
-    f[l] = __ldg(reinterpret_cast<const __half2*>(a.hash.table) + nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc));
+  for (int l = 0; l < kNrcHashLevels; ++l) f[l] = __ldg(reinterpret_cast<const __half2*>(a.hash.table) + rows[l]);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     __nv_bfloat162 h[4];
@@ -704,10 +728,11 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant
       tmem_ld64(tl, v);
       tc_fence_before();
       if (valid && a.hash.grad) {
-        const NrcQuery q = nrc_make_query(a, li, p, d);
+        uint32_t rows[kNrcHashLevels];
+        nrc_rows(a, li, p, d, rows);
 #pragma unroll
         for (int l = 0; l < kNrcHashLevels; ++l) {
-          const uint32_t row = nrc_hash_row(a.hash, l, q.u, q.du, q.dv, q.casc);
+          const uint32_t row = rows[l];
           if (v[2 * l] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row, v[2 * l]);
           if (v[2 * l + 1] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row + 1, v[2 * l + 1]);
         }
@@ -870,47 +895,28 @@ __host__ __device__ __forceinline__ int64_t nrc_slot_probe(const int32_t M[3], i
 struct NrcWordArgs {
   NrcLevel lv[kMaxCascades];
   int32_t first, nlev;
-  int32_t mode;    // 0: the sample directions of phases ph, hp; 1: what the solve still needs
-  int32_t ph, hp, nph;
   const int32_t* plain;
   const uint8_t* flag;
   int32_t tile_shift, TX, TY;
   int64_t slot0[kMaxCascades + 1];  // first global slot of each far level
-  int64_t dir0[kMaxCascades + 1];   // first global direction of each far level
 };
 
-// Walk switches of the far levels' queue, one thread per (level, slot) and
-// per (level, direction).  Mode 0: every word, the sample directions.  Mode 1:
-// the other directions, of every word of a level on its walks and of the
-// words holding a probe of a flagged tile.
+// Walk switch of every word of the far levels (one thread per level and
+// slot) for the walk that follows the serve decisions: on for every word of
+// a level on its walks and for the words holding a probe of a flagged tile.
 __global__ void k_nrc_words(const __grid_constant__ NrcWordArgs w) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t nslots = w.slot0[w.nlev];
-  if (i < nslots) {
-    int li = w.first;
-    while (li + 1 < w.nlev && i >= w.slot0[li + 1]) ++li;
-    const NrcLevel& L = w.lv[li];
-    const int slot = (int)(i - w.slot0[li]);
-    bool on = true;
-    if (w.mode == 1 && !__ldg(w.plain + li)) {
-      on = false;
-      for (int b = 0; b < 32 && !on; ++b) {
-        const int64_t p = nrc_slot_probe(L.M, L.wpp, L.l2px, slot, b);
-        if (p >= 0) on = __ldg(w.flag + nrc_cell(L, p, w.tile_shift, w.TX, w.TY)) != 0;
-      }
-    }
-    L.word_on[slot] = on;
-    return;
-  }
-  const int64_t j = i - nslots;
-  if (j >= w.dir0[w.nlev]) return;
+  if (i >= w.slot0[w.nlev]) return;
   int li = w.first;
-  while (li + 1 < w.nlev && j >= w.dir0[li + 1]) ++li;
+  while (li + 1 < w.nlev && i >= w.slot0[li + 1]) ++li;
   const NrcLevel& L = w.lv[li];
-  const int d = (int)(j - w.dir0[li]);
-  const int ph = nrc_dir_phase(d, L.n, w.nph);
-  const bool sample = ph == w.ph || ph == w.hp;
-  L.dir_on[d] = w.mode == 0 ? sample : !sample;
+  const int slot = (int)(i - w.slot0[li]);
+  bool on = __ldg(w.plain + li) != 0;
+  for (int b = 0; b < 32 && !on; ++b) {
+    const int64_t p = nrc_slot_probe(L.M, L.wpp, L.l2px, slot, b);
+    if (p >= 0) on = __ldg(w.flag + nrc_cell(L, p, w.tile_shift, w.TX, w.TY)) != 0;
+  }
+  L.word_on[slot] = on;
 }
 
 // Training / held-out targets: row r of tile t is the tile's r-th direction

@@ -16,6 +16,10 @@
 // (opaque voxel without emission) or kMiss.
 #pragma once
 
+#include <stdlib.h>
+
+#include <algorithm>
+
 #include "rc_walk_bits.cuh"
 
 namespace rcx {
@@ -38,12 +42,29 @@ struct QueueLevel {
   // ends where every probe of the level has left the grid on some axis.
   const uint2* steps;
   const int32_t* step_begin;
-  // Optional per-slot and per-direction switches (null: all on): item
-  // (d, slot) walks only when both bytes are nonzero.  The learned form walks
-  // only the words and directions it needs.
+  // Optional selections (the learned form walks only what it needs):
+  // word_on (null: every slot) -- a slot whose byte is 0 holds no walk;
+  // dsel (null: every direction, items d * slots + slot) -- the level's items
+  // are slot * dsel_n + k for the dsel_n directions
+  // dsel[(dsel_start + k) mod dsel_len], so a warp's 32 items share a word.
   const uint8_t* word_on;
-  const uint8_t* dir_on;
+  const int32_t* dsel;
+  int32_t dsel_len, dsel_start, dsel_n;
+  int32_t pad;
 };
+
+// Direction and slot of item r (counted from the level's first item).
+__device__ __forceinline__ void queue_item(const QueueLevel& L, int64_t r, int& d, int& slot) {
+  if (L.dsel) {
+    slot = (int)(r / L.dsel_n);
+    int j = L.dsel_start + (int)(r - (int64_t)slot * L.dsel_n);
+    if (j >= L.dsel_len) j -= L.dsel_len;
+    d = __ldg(L.dsel + j);
+  } else {
+    d = (int)(r / L.slots);
+    slot = (int)(r - (int64_t)d * L.slots);
+  }
+}
 
 struct QueueArgs {
   const uint32_t* emis;
@@ -92,8 +113,8 @@ struct Walker {
     int li = 0;
     while (li + 1 < q.n && item >= q.lv[li + 1].item_begin) ++li;
     const QueueLevel& L = q.lv[li];
-    const int64_t r = item - L.item_begin;
-    const int d = (int)(r / L.slots), slot = (int)(r - (int64_t)d * L.slots);
+    int d, slot;
+    queue_item(L, item - L.item_begin, d, slot);
     mask = L.mask;
     l2s = L.l2s;
     l2px = L.l2px;
@@ -102,7 +123,7 @@ struct Walker {
     My = L.M[1];
     Mz = L.M[2];
     rep = L.rep;
-    if ((L.word_on && !__ldg(L.word_on + slot)) || (L.dir_on && !__ldg(L.dir_on + d))) return false;
+    if (L.word_on && !__ldg(L.word_on + slot)) return false;
     zl = slot / wpp;
     const int wl = slot - zl * wpp;
     g0 = wl << 5;
@@ -272,8 +293,8 @@ struct TableWalker {
     int li = 0;
     while (li + 1 < q.n && item >= q.lv[li + 1].item_begin) ++li;
     const QueueLevel& L = q.lv[li];
-    const int64_t r = item - L.item_begin;
-    const int d = (int)(r / L.slots), slot = (int)(r - (int64_t)d * L.slots);
+    int d, slot;
+    queue_item(L, item - L.item_begin, d, slot);
     mask = L.mask;
     l2s = L.l2s;
     l2px = L.l2px;
@@ -283,7 +304,7 @@ struct TableWalker {
     Mz = L.M[2];
     mzw = Mz * wpp;
     rep = L.rep;
-    if ((L.word_on && !__ldg(L.word_on + slot)) || (L.dir_on && !__ldg(L.dir_on + d))) return false;
+    if (L.word_on && !__ldg(L.word_on + slot)) return false;
     zl = slot / wpp;
     const int wl = slot - zl * wpp;
     g0 = wl << 5;
@@ -373,6 +394,179 @@ struct TableWalker {
 
 constexpr int kQueueThreads = 256;
 
+// ---------------------------------------------------------------------------
+// Cooperative table walk: a group of G lanes walks ONE item, lane j taking
+// step j of every G consecutive steps of the direction's table, so a walk of
+// k steps takes k / G dependent rounds instead of k.  Along a ray a probe
+// that has left the grid never comes back (the grid is convex), so the steps
+// of a round can be tested independently: a probe's first hit is the lowest
+// lane whose step hits it (exclusive OR-scan over the group), a probe outside
+// the grid at a step has no hit at any later step, and a step outside the
+// grid in z or past the table's end ends the walk.  Same records as
+// TableWalker, bit for bit.
+// ---------------------------------------------------------------------------
+template <int G>
+struct CoopWalker {
+  const uint32_t* mask;
+  uint32_t* rec;
+  const uint2* st;
+  int n;  // steps left
+  int l2s, l2px, wpp, Mx, My, Mz, mzw;
+  uint32_t rep;
+  int zl, g0, wy0, wx0;
+  uint32_t valid, done, hits;
+
+  __device__ __forceinline__ bool init(const QueueArgs& q, int64_t item) {
+    int li = 0;
+    while (li + 1 < q.n && item >= q.lv[li + 1].item_begin) ++li;
+    const QueueLevel& L = q.lv[li];
+    int d, slot;
+    queue_item(L, item - L.item_begin, d, slot);
+    mask = L.mask;
+    l2s = L.l2s;
+    l2px = L.l2px;
+    wpp = L.wpp;
+    Mx = L.M[0];
+    My = L.M[1];
+    Mz = L.M[2];
+    mzw = Mz * wpp;
+    rep = L.rep;
+    if (L.word_on && !__ldg(L.word_on + slot)) return false;
+    zl = slot / wpp;
+    const int wl = slot - zl * wpp;
+    g0 = wl << 5;
+    const int Px = 1 << l2px;
+    wy0 = g0 >> l2px;
+    wx0 = g0 & (Px - 1);
+    if (l2px >= 5) {
+      valid = wy0 < My ? range_bits(0, Mx - wx0) : 0u;
+    } else {
+      valid = range_bits(0, Mx) * rep;
+      valid &= range_bits(0, (My - wy0) * Px);
+    }
+    if (valid == 0u) return false;
+    rec = L.rec + ((int64_t)d * L.slots + slot) * 32;
+    done = ~valid;
+    hits = 0u;
+    const int b0 = __ldg(L.step_begin + d);
+    st = L.steps + b0;
+    n = __ldg(L.step_begin + d + 1) - b0;
+    return true;
+  }
+
+  // One round of G steps; every lane of the warp calls it (inactive groups
+  // with active = false).  Returns true when this group's item is finished.
+  __device__ __forceinline__ bool round(const QueueArgs& q, bool active, int sub) {
+    uint32_t h = 0u, out = 0u;
+    bool stop = false;
+    uint32_t ph = 0u, pc = 0u;
+    if (active) {
+      const bool step_ok = sub < n;
+      const uint2 e = step_ok ? __ldg(st + sub) : make_uint2(0u, 0u);
+      ph = e.x;
+      pc = e.y;
+      const int cx = (int)(int8_t)(pc & 0xFFu), cy = (int)(int8_t)((pc >> 8) & 0xFFu),
+                cz = (int)(int8_t)((pc >> 16) & 0xFFu);
+      const int Px = 1 << l2px;
+      uint32_t inr;
+      if (l2px >= 5) {
+        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+      } else {
+        inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * rep;
+        inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
+      }
+      const bool ok = step_ok && (unsigned)(zl + cz) < (unsigned)Mz;
+      stop = !ok;
+      if (ok) {
+        const int gs = g0 + cy * Px + cx;
+        const int q0 = gs >> 5;
+        const uint32_t* plane = mask + (int64_t)ph * mzw + (int64_t)(zl + cz) * wpp;
+        const uint32_t lo = (unsigned)q0 < (unsigned)wpp ? __ldg(plane + q0) : 0u;
+        const uint32_t hi = (unsigned)(q0 + 1) < (unsigned)wpp ? __ldg(plane + q0 + 1) : 0u;
+        h = __funnelshift_r(lo, hi, gs & 31) & inr & ~done;
+        out = ~inr;
+      }
+    }
+    // first hit per probe: the lowest lane of the group whose step hits it
+    uint32_t incl = h;
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o, G);
+      if (sub >= o) incl |= y;
+    }
+    uint32_t before = __shfl_up_sync(0xFFFFFFFFu, incl, 1, G);
+    if (sub == 0) before = 0u;
+    uint32_t nw = h & ~before;
+    if (nw) {
+      const int sm = (1 << l2s) - 1, Px = 1 << l2px;
+      const int bx = ((int)(int8_t)(pc & 0xFFu) << l2s) + (int)(ph & sm);
+      const int by = ((int)(int8_t)((pc >> 8) & 0xFFu) << l2s) + (int)((ph >> l2s) & sm);
+      const int bz = ((int)(int8_t)((pc >> 16) & 0xFFu) << l2s) + (int)(ph >> (2 * l2s));
+      const int vz = (zl << l2s) + bz;
+      do {
+        const int b = __ffs(nw) - 1;
+        nw &= nw - 1;
+        const int g = g0 + b;
+        const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
+        const int64_t row = (int64_t)vz * q.G[1] + vy;
+        const uint32_t ev = __ldg(&q.emis[row * q.W + (vx >> 5)]);
+        rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+      } while (nw);
+    }
+    // group totals: probes hit, probes out of the grid, walk ended
+    uint32_t all = incl, gone = out;
+    int ended = stop ? 1 : 0;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      all |= __shfl_xor_sync(0xFFFFFFFFu, all, o, G);
+      gone |= __shfl_xor_sync(0xFFFFFFFFu, gone, o, G);
+      ended |= __shfl_xor_sync(0xFFFFFFFFu, ended, o, G);
+    }
+    if (!active) return true;
+    hits |= all;
+    done |= all | gone;
+    st += G;
+    n -= G;
+    return ended || n <= 0 || done == 0xFFFFFFFFu;
+  }
+
+  // Records of the probes without a hit; the group's lanes share the writes.
+  __device__ __forceinline__ void finish(int sub) {
+    const uint32_t m = valid & ~hits;
+    for (int b = sub; b < 32; b += G)
+      if ((m >> b) & 1u) rec[b] = kMiss;
+  }
+};
+
+// Groups of G lanes per item, 32 / G items per warp at a time from *counter.
+template <int G>
+__device__ __forceinline__ void walk_groups_coop(const QueueArgs& q, unsigned long long* counter, int64_t end) {
+  static_assert(G == 2 || G == 4 || G == 8 || G == 16 || G == 32, "group of 2, 4, 8, 16 or 32 lanes");
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+  CoopWalker<G> w;
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(counter, (unsigned long long)(32 / G));
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if ((int64_t)base >= end) break;
+    const int64_t item = (int64_t)base + grp;
+    bool active = item < end && w.init(q, item);
+    while (__any_sync(0xFFFFFFFFu, active)) {
+      const bool fin = w.round(q, active, sub);
+      if (active && fin) {
+        w.finish(sub);
+        active = false;
+      }
+    }
+  }
+}
+
+template <int G>
+static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_coop(const __grid_constant__ QueueArgs q) {
+  walk_groups_coop<G>(q, q.counter, q.total);
+}
+
+
 // Every warp takes 32 consecutive queue items at a time (from *counter, a
 // global or shared counter, up to `end`) and walks them in step: lanes of one
 // direction share the table entries and load neighbouring words; the warp
@@ -405,6 +599,40 @@ static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __gri
 // no spills; the extra resident warps hide the mask loads' latency).
 static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
   walk_groups<4, TableWalker>(q, q.counter, q.total);
+}
+
+// Lanes per item of the step-table walk.  With more resident lanes than
+// items, the walks' dependent steps (not the lanes) bound the launch, so G
+// lanes share an item: G = the largest power of two <= resident lanes /
+// items, at most 32 (1: k_walk_queue_tab, one lane per item).  RC_WALK_GROUP
+// = 1, 2, 4, 8, 16 or 32 fixes it.
+inline int walk_group(int64_t items, int64_t resident_blocks) {
+  const char* e = getenv("RC_WALK_GROUP");
+  if (e) {
+    const int v = atoi(e);
+    if (v == 1 || v == 2 || v == 4 || v == 8 || v == 16 || v == 32) return v;
+  }
+  const int64_t lanes = resident_blocks * kQueueThreads;
+  int g = 1;
+  while (g < 32 && (int64_t)(2 * g) * items <= lanes) g *= 2;
+  return g;
+}
+
+// The step-table walk of `q` (its counter already zeroed, q.total items):
+// enough blocks for G lanes per item, at most the `resident` blocks that fit
+// the GPU at once (every warp takes items until the queue is empty).
+inline void launch_table_walk(const QueueArgs& q, int64_t resident, cudaStream_t s) {
+  const int g = walk_group(q.total, resident);
+  const unsigned blocks = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>((q.total * g + kQueueThreads - 1) / kQueueThreads, resident));
+  switch (g) {
+    case 2: k_walk_queue_coop<2><<<blocks, kQueueThreads, 0, s>>>(q); break;
+    case 4: k_walk_queue_coop<4><<<blocks, kQueueThreads, 0, s>>>(q); break;
+    case 8: k_walk_queue_coop<8><<<blocks, kQueueThreads, 0, s>>>(q); break;
+    case 16: k_walk_queue_coop<16><<<blocks, kQueueThreads, 0, s>>>(q); break;
+    case 32: k_walk_queue_coop<32><<<blocks, kQueueThreads, 0, s>>>(q); break;
+    default: k_walk_queue_tab<<<blocks, kQueueThreads, 0, s>>>(q); break;
+  }
 }
 
 // Merge of a narrow level from its walk records, probe p: parent texels

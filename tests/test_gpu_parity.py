@@ -131,6 +131,29 @@ def test_walk_step_tables_match_the_walk_dda_bit_for_bit(grid, N, monkeypatch):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("grid,N", [(64, 5), ((96, 64, 160), 5), (256, 6)])
+def test_cooperative_walk_groups_match_one_lane_per_item_bit_for_bit(grid, N, monkeypatch):
+    """The step-table walk runs G lanes per item (RC_WALK_GROUP = 4, 8, 16,
+    32: lane j takes every G-th step, first hits by an OR-scan over the
+    group) or one lane per item (1).  All give the same records, so every
+    level's radiance and the fluence are identical bit for bit."""
+    g3 = (grid,) * 3 if isinstance(grid, int) else grid
+    if grid == 256:
+        boxes, spheres = R.workload_scene("c256", frame=5)
+    else:
+        boxes, spheres = R.generate_scene(R.scene_spec(g3, 60, (3, 20), 8, (1.5, 5.0), (1.0, 20.0)), 9)
+    out = {}
+    for g in ("1", "2", "4", "8", "16", "32"):
+        monkeypatch.setenv("RC_WALK_GROUP", g)
+        out[g] = _solve_gpu(R.make_params(g3, N), boxes=boxes, spheres=spheres)
+    f1, L1 = out["1"]
+    for g in ("2", "4", "8", "16", "32"):
+        f, L = out[g]
+        assert np.array_equal(f, f1), g
+        for a, b in zip(L, L1):
+            assert np.array_equal(a, b), g
+
+
 def test_moving_emitters_incremental_update_matches_fresh_solve():
     boxes, spheres = R.workload_scene("c64")
     p = R.make_params(64, 5)
