@@ -313,14 +313,13 @@ def cpu_port_batch_scenes_per_s(items, threads, budget_s=20.0):
     return len(items) / batch_s, done, t_total
 
 
-def run_batch(args, rank, world):
-    """Scenes/s of the batched workload (replicas: every rank solves its own copy)."""
+def batch_measure(args, R, local, dist, world, steps):
+    """The batched workload on this rank: scenes/s of the graph-launched
+    persistent solve with the scenes resident, the same scenes as one context
+    each back to back, and e2e through the public API (per step every scene's
+    emitters move one frame and are uploaded from host arrays, one solve, every
+    fluence read back into pinned host memory with one synchronisation)."""
     import torch
-    import radiancecascade_gb300 as R
-
-    local = _env_int("LOCAL_RANK", 0)
-    dist = init_replicas(world, local)
-    torch.cuda.set_device(local)
     items = R.batch_workload()
     prec = args.precision
     b = R.Batch([R.make_params(e, N, precision=prec) for e, N, _, _ in items], device=local)
@@ -339,7 +338,7 @@ def run_batch(args, rank, world):
     clocks.start()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         b.solve(sp)
     t1.record(stream)
     t1.synchronize()
@@ -347,7 +346,7 @@ def run_batch(args, rank, world):
     torch.cuda.synchronize()
     clock_info = clocks.stop()
     ms = max_over_ranks(t0.elapsed_time(t1), dist)
-    value = world * len(items) * args.steps / (ms / 1000.0)
+    value = world * len(items) * steps / (ms / 1000.0)
 
     # the same scenes as separate contexts (fastest per-level kernels), one after another
     engines = []
@@ -362,69 +361,150 @@ def run_batch(args, rank, world):
     torch.cuda.synchronize()
     s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         for g in engines:
             g.solve(sp)
     s1.record(stream)
     s1.synchronize()
-    seq_ms = s0.elapsed_time(s1) / args.steps
+    seq_ms = s0.elapsed_time(s1) / steps
     for g in engines:
         g.close()
 
-    # e2e: every step re-voxelises each scene from host box/sphere arrays, solves, reads every fluence
-    nbytes_in = sum(int(bx.nbytes + sx.nbytes) for _, _, bx, sx in items)
-    outs = [np.empty((b.fluence(k).size,), np.float32) for k in range(len(items))]
-    nbytes_out = sum(o.nbytes for o in outs)
-    e2e_steps = max(1, min(args.steps, 10))
+    # e2e: per step every scene's spheres advance one frame and are uploaded
+    # (incremental re-voxelisation on the batch stream), one solve, one read of
+    # every fluence into pinned host memory
+    sph = [sx.copy() for _, _, _, sx in items]
+    nbytes_in = sum(int(sx.nbytes) for sx in sph)
+    flat = torch.empty(b.fluence_elems(), dtype=torch.float32, pin_memory=True).numpy()
+    nbytes_out = int(flat.nbytes)
+
+    def e2e_step():
+        for k, (edge, _, _, _) in enumerate(items):
+            R.advance_spheres(sph[k], edge, 1)
+            b.set_spheres(k, sph[k])
+        b.solve()
+        b.fluence_all(flat)
+
+    for _ in range(2):
+        e2e_step()
     if dist:
         dist.barrier()
+    e2e_steps = max(3, min(steps, 50))
     w0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for k, (_, _, boxes, spheres) in enumerate(items):
-            b.set_scene(k, boxes, spheres)
-        b.solve()
-        for k in range(len(items)):
-            outs[k][:] = b.fluence(k).reshape(-1)
+        e2e_step()
     e2e_s = max_over_ranks(time.perf_counter() - w0, dist)
     e2e_value = world * len(items) * e2e_steps / e2e_s
 
     elem = 2 if prec == "fp16" else 4
     B = batch_bytes(items, elem)
-    per_batch_s = ms / args.steps / 1000.0
-    achieved = B / per_batch_s / 1e9
+    achieved = B / (ms / steps / 1000.0) / 1e9
     peak, peak_kind = measured_peak_gbs()
-    line = {
-        "metric": "scenes/s, batched uneven scenes in one persistent launch",
-        "value": round(value, 3), "unit": "scenes/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec == "fp16" else "f32",
-        "data": "synthetic",
-        "config": {"workload": BATCH_DESC, "scenes": len(items), "precision": prec,
-                   "tile": dict(tiles, tune_ms=round(tune_ms, 4)),
-                   "parallelism": "replicas" if world > 1 else "single-gpu",
-                   "l2": "inputs larger than L2 (%.1f GB of scene + radiance)" % (B / 1e9)},
+    b.close()
+    return {
+        "items": items, "value": value, "ms_per_step": ms / steps, "clock_info": clock_info,
+        "tile": dict(tiles, tune_ms=round(tune_ms, 4)), "seq_ms": seq_ms, "B": B,
         "e2e": {"value": round(e2e_value, 3), "unit": "scenes/s", "h2d_bytes_per_step": nbytes_in,
-                "d2h_bytes_per_step": nbytes_out},
-        "gpu_launches": args.steps,
-        "per_scene_contexts_ms_per_batch": round(seq_ms, 4),
+                "d2h_bytes_per_step": nbytes_out, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": None,
                      "kernel": "k_batch_persistent", "algorithmic_bytes_per_step": B},
     }
-    if clock_info:
-        line["clocks"] = clock_info
+
+
+def run_batch(args, rank, world):
+    """Scenes/s of the batched workload (replicas: every rank solves its own copy)."""
+    import torch
+    import radiancecascade_gb300 as R
+
+    local = _env_int("LOCAL_RANK", 0)
+    dist = init_replicas(world, local)
+    torch.cuda.set_device(local)
+    m = batch_measure(args, R, local, dist, world, args.steps)
+    items, B = m["items"], m["B"]
+    prec = args.precision
+    line = {
+        "metric": "scenes/s, batched uneven scenes in one persistent launch",
+        "value": round(m["value"], 3), "unit": "scenes/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(m["ms_per_step"], 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16" if prec == "fp16" else "f32",
+        "data": "synthetic",
+        "config": {"workload": BATCH_DESC, "scenes": len(items), "precision": prec, "tile": m["tile"],
+                   "parallelism": "replicas" if world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (%.1f GB of scene + radiance)" % (B / 1e9)},
+        "e2e": m["e2e"],
+        "gpu_launches": args.steps,
+        "per_scene_contexts_ms_per_batch": round(m["seq_ms"], 4),
+        "roofline": m["roofline"],
+    }
+    if m["clock_info"]:
+        line["clocks"] = m["clock_info"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, done, secs = cpu_port_batch_scenes_per_s(items, threads)
         line["cpu_baseline"] = {"value": round(v, 4), "unit": "scenes/s", "cores": threads, "kind": "port",
                                 "sample": "first %d scenes of the batch (%.1f s, FP32, OpenMP), scaled to the "
                                           "batch by voxel count" % (done, secs)}
-    b.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def fp16_report(R, local, frames=6):
+    """The FP16 storage form of the 64^3 workload: per frame (emitters moving
+    one step per frame) the fluence relative L2 and max-abs error against the
+    FP64 oracle and against the plain FP32 path; and frame 0 at 256^3."""
+    from oracle import oracle as O
+
+    def err(a, b):
+        a = np.asarray(a, np.float64)
+        b = np.asarray(b, np.float64)
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b)), float(np.abs(a - b).max())
+
+    out = {"workload": "64^3 c64 scene (24 boxes, 4 spheres), 5 cascades; spheres advance one frame per row",
+           "frames": []}
+    boxes, sph = R.workload_scene("c64")
+    sph = sph.copy()
+    e16 = R.Engine(R.make_params(64, 5, precision="fp16"), device=local)
+    e32 = R.Engine(R.make_params(64, 5), device=local)
+    for e in (e16, e32):
+        e.set_boxes(boxes)
+    for f in range(frames):
+        for e in (e16, e32):
+            e.set_spheres(sph)
+            e.solve()
+        g16, g32 = e16.fluence(), e32.fluence()
+        ref, _ = O.solve(O.params(64, 5), O.voxelise(64, boxes, sph))
+        r64, m64 = err(g16, ref)
+        r32, m32 = err(g16, g32)
+        out["frames"].append({"frame": f, "rel_l2_vs_fp64": r64, "max_abs_vs_fp64": m64,
+                              "rel_l2_vs_fp32": r32, "max_abs_vs_fp32": m32,
+                              "fp32_rel_l2_vs_fp64": err(g32, ref)[0]})
+        R.advance_spheres(sph, 64, 1)
+    e16.close()
+    e32.close()
+    b256, s256 = R.workload_scene(WORKLOAD)
+    e = R.Engine(R.make_params(256, 6, precision="fp16"), device=local)
+    e.set_boxes(b256)
+    e.set_spheres(s256)
+    e.solve()
+    g16 = e.fluence()
+    e.close()
+    e = R.Engine(R.make_params(256, 6), device=local)
+    e.set_boxes(b256)
+    e.set_spheres(s256)
+    e.solve()
+    g32 = e.fluence()
+    e.close()
+    ref, _ = O.solve(O.params(256, 6), O.voxelise(256, b256, s256), jump=True)
+    r64, m64 = err(g16, ref)
+    r32, m32 = err(g16, g32)
+    out["c256_frame0"] = {"rel_l2_vs_fp64": r64, "max_abs_vs_fp64": m64, "rel_l2_vs_fp32": r32,
+                          "max_abs_vs_fp32": m32}
+    out["storage"] = "radiance f16, transmittance decisions exact, merge accumulation f32"
+    return out
 
 
 RENDER_DESC = ("256^3 procedural room mesh (walls, 40 blocks, a 131k-triangle sphere) voxelised on the GPU, "
@@ -548,6 +628,7 @@ def main():
     ap.add_argument("--learned-warmup", type=int, default=48,
                     help="frames the radiance cache learns before the learned form is timed")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned+FP16 form")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched workload's figures")
     ap.add_argument("--learned-first-level", type=int, default=4, help="first cascade the radiance cache serves")
     ap.add_argument("--learned-threshold", type=float, default=0.01,
                     help="held-out relative error above which a tile falls back to the plain walk")
@@ -658,6 +739,12 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "traffic": traffic,
+                     "frac_measured": (round(traffic / (level_ms / 1000.0) / 1e9 / peak, 4)
+                                       if traffic else None),
+                     "frac_basis": "frac: algorithmic bytes B (8 B/voxel scene read per cascade, radiance "
+                                   "written and read once, fluence) / summed level time / measured HBM peak; "
+                                   "frac_measured: DRAM bytes of the level kernels measured by ncu "
+                                   "(profiles/frame_c256_launch_list.md) / the same time / the same peak",
                      "kernel": "cascade levels: k_level0_tma + k_level_bits_up (wide) + k_walk_queue / k_level_merge (narrow)",
                      "algorithmic_bytes_per_frame": B,
                      "level_ms_per_frame": round(level_ms, 4),
@@ -679,6 +766,14 @@ def main():
                             "fluence_max_abs_vs_fp64": float(np.abs(g - ref).max())}
     if rank == 0 and world == 1 and not args.no_learned:
         line["learned"] = learned_form(args, R, local, boxes, spheres, value)
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        line["fp16"] = fp16_report(R, local)
+    if rank == 0 and world == 1 and not args.no_batch:
+        m = batch_measure(args, R, local, None, 1, min(args.steps, 50))
+        line["batch"] = {"workload": BATCH_DESC, "scenes": len(m["items"]), "scenes_per_s": round(m["value"], 3),
+                         "ms_per_batch": round(m["ms_per_step"], 4), "e2e": m["e2e"],
+                         "per_scene_contexts_ms_per_batch": round(m["seq_ms"], 4), "tile": m["tile"],
+                         "roofline": m["roofline"]}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, _ = cpu_port_frames_per_s(args.cpu_frames, threads)

@@ -249,6 +249,19 @@ rc_status rc_batch_get_fluence(rc_batch* b, int32_t scene, float* out,
                                int64_t elems, int32_t where);
 rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level,
                                 void* out, int64_t bytes, int32_t where);
+/* Replaces the emitters of scene `scene` (the static scene stays): only the
+ * voxels under the previous and the new spheres are rewritten, on the batch's
+ * stream, so the update is ordered after the solves already enqueued and
+ * before the next one, with no host wait (the host array may be freed on
+ * return).  The scene must have been set with rc_batch_scene_set. */
+rc_status rc_batch_set_spheres(rc_batch* b, int32_t scene,
+                               const rc_sphere* spheres, int32_t n);
+/* Every scene's cascade-0 fluence, scene after scene (each RGB interleaved,
+ * rc_fluence_elems of its params), in one buffer of exactly their total
+ * size; one synchronisation for the whole batch.  Pinned host memory lets
+ * the copies run at full speed. */
+rc_status rc_batch_get_fluence_all(rc_batch* b, float* out, int64_t elems,
+                                   int32_t where);
 /* Tile shape of the batch's queue items. */
 typedef struct rc_batch_tiles {
   int32_t probes_per_item;  /* narrow levels: probes per item               */

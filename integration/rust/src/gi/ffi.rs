@@ -237,6 +237,8 @@ extern "C" {
         -> rc_status;
     pub fn rc_batch_get_radiance(b: *mut rc_batch, scene: i32, level: i32, out: *mut c_void, bytes: i64,
                                  where_: i32) -> rc_status;
+    pub fn rc_batch_set_spheres(b: *mut rc_batch, scene: i32, spheres: *const rc_sphere, n: i32) -> rc_status;
+    pub fn rc_batch_get_fluence_all(b: *mut rc_batch, out: *mut f32, elems: i64, where_: i32) -> rc_status;
     pub fn rc_batch_set_tiles(b: *mut rc_batch, tiles: *const rc_batch_tiles) -> rc_status;
     pub fn rc_batch_get_tiles(b: *const rc_batch, out: *mut rc_batch_tiles) -> rc_status;
     pub fn rc_batch_tune(b: *mut rc_batch, iters: i32, best: *mut rc_batch_tiles, best_ms: *mut f32)

@@ -1889,6 +1889,44 @@ rc_status rc_batch_get_fluence(rc_batch* b, int32_t scene, float* out, int64_t e
   return rc_get_fluence(b->scenes[scene], out, elems, where);
 }
 
+rc_status rc_batch_set_spheres(rc_batch* b, int32_t scene, const rc_sphere* spheres, int32_t n) {
+  if (batch_check(b, "rc_batch_set_spheres") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (scene < 0 || scene >= b->n) {
+    rcx::set_error("rc_batch_set_spheres: scene %d out of range", scene);
+    return RC_ERR_INVALID_ARG;
+  }
+  // The scene's emitter update (sphere upload + re-voxelisation of the voxels
+  // the old and new spheres cover) goes on the batch stream, in order with
+  // the solves: the solve in flight reads the old volume, the next the new.
+  rc_context* c = b->scenes[scene];
+  DeviceGuard g(b->device);
+  cudaStream_t own = c->stream;
+  c->stream = b->stream;
+  const rc_status s = rc_scene_set_spheres(c, spheres, n);  // its message names the failing check
+  c->stream = own;
+  return s;
+}
+
+rc_status rc_batch_get_fluence_all(rc_batch* b, float* out, int64_t elems, int32_t where) {
+  if (batch_check(b, "rc_batch_get_fluence_all") != RC_OK) return RC_ERR_INVALID_ARG;
+  int64_t need = 0;
+  for (int k = 0; k < b->n; ++k) need += b->scenes[k]->geom[0].probes() * 3;
+  if (!out || elems != need || (where != RC_MEM_HOST && where != RC_MEM_DEVICE)) {
+    rcx::set_error("rc_batch_get_fluence_all: need a non-NULL buffer of exactly %lld floats", (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(b->device);
+  const cudaMemcpyKind kind = where == RC_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  int64_t off = 0;
+  for (int k = 0; k < b->n; ++k) {
+    const rc_context* c = b->scenes[k];
+    const size_t bytes = (size_t)c->geom[0].probes() * 3 * sizeof(float);
+    RC_CUDA(cudaMemcpyAsync(out + off, c->fluence, bytes, kind, b->stream), "rc_batch_get_fluence_all");
+    off += c->geom[0].probes() * 3;
+  }
+  return rc_batch_synchronize(b);
+}
+
 rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level, void* out, int64_t bytes, int32_t where) {
   if (batch_check(b, "rc_batch_get_radiance") != RC_OK) return RC_ERR_INVALID_ARG;
   if (scene < 0 || scene >= b->n) {

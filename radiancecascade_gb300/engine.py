@@ -666,6 +666,23 @@ class Batch:
         s = np.ascontiguousarray(spheres, dtype=SPHERE_DT)
         F.check(self._lib.rc_batch_scene_set(self.handle, k, F.ptr(b), len(b), F.ptr(s), len(s)))
 
+    def set_spheres(self, k: int, spheres: np.ndarray) -> None:
+        """Scene k's emitters for the next solve (asynchronous, incremental)."""
+        s = np.ascontiguousarray(spheres, dtype=SPHERE_DT)
+        F.check(self._lib.rc_batch_set_spheres(self.handle, k, F.ptr(s), len(s)))
+
+    def fluence_elems(self) -> int:
+        return sum(3 * int(np.prod(level_info(p, 0).probes)) for p in self.params)
+
+    def fluence_all(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Every scene's fluence, scene after scene, flat float32 (one synchronisation);
+        `out` may be a preallocated (pinned) array of fluence_elems() floats."""
+        n = self.fluence_elems()
+        if out is None:
+            out = np.empty(n, np.float32)
+        F.check(self._lib.rc_batch_get_fluence_all(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
+        return out
+
     def solve(self, stream: Optional[int] = None) -> None:
         F.check(self._lib.rc_batch_solve(self.handle, C.c_void_p(stream) if stream else None))
 

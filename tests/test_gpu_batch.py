@@ -173,3 +173,33 @@ def test_batch64_workload_parity_and_properties():
             assert rel_l2(g, ref) <= FP32_REL_L2, (k, edge)
             assert np.abs(g - ref).max() <= FP32_MAX_REL * max(1.0, ref.max()), (k, edge)
         assert seen == set(R.BATCH_EDGES)
+
+
+def test_moving_emitters_between_solves_and_one_fluence_read():
+    """rc_batch_set_spheres updates each scene's emitters on the batch stream
+    with no host wait, in order with the solves: after three solves with the
+    spheres advanced one frame before each, every scene matches the oracle on
+    the third frame's spheres, and rc_batch_get_fluence_all returns the same
+    floats as the per-scene reads, scene after scene."""
+    b = _batch()
+    try:
+        sph = [_scene(grid, seed)[1].copy() for grid, _, seed in SCENES]
+        for frame in range(1, 4):
+            for k, (grid, _, _) in enumerate(SCENES):
+                R.advance_spheres(sph[k], grid, 1)
+                b.set_spheres(k, sph[k])
+            b.solve()
+        flat = b.fluence_all()
+        off = 0
+        for k, (grid, N, seed) in enumerate(SCENES):
+            one = b.fluence(k).reshape(-1)
+            assert np.array_equal(flat[off:off + one.size], one), k
+            off += one.size
+            boxes, _ = _scene(grid, seed)
+            oflu, _ = O.solve(O.params(grid, N), O.voxelise(grid, boxes, sph[k]), jump=True)
+            assert rel_l2(one.reshape(-1, 3), oflu) <= FP32_REL_L2, k
+        assert off == flat.size
+        with pytest.raises(R.RCError):
+            F.check(F.lib().rc_batch_get_fluence_all(b.handle, F.ptr(flat), flat.size - 1, F.RC_MEM_HOST))
+    finally:
+        b.close()
