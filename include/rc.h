@@ -226,6 +226,16 @@ rc_status rc_get_stream(rc_context* ctx, void** out);
  * 1 + num_cascades floats.  Synchronises. */
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
+/* Per-solve stage timing.  With timing on, every rc_solve records CUDA
+ * events between its stages on the solve's stream (no host wait);
+ * rc_get_stage_ms then waits for the last solve and writes ms_out[0] = the
+ * whole solve and ms_out[1 + i] = cascade i (the top cascade's figure holds
+ * the walk launch of the narrow cascades and, with the radiance cache on,
+ * the cache's whole schedule).  Needs 1 + num_cascades floats.  Diagnostics:
+ * the RC_LOG environment variable prints every error (1), also context
+ * lifetime (2), also one line per solve (3) on stderr. */
+rc_status rc_set_stage_timing(rc_context* ctx, int32_t enable);
+rc_status rc_get_stage_ms(rc_context* ctx, float* ms_out, int32_t count);
 
 /* ---- batched solve --------------------------------------------------- */
 /* Many independent scenes (each with its own rc_params: grid, cascades)

@@ -10,6 +10,6 @@ from .engine import (Engine, Batch, GiStage, GiState, make_params, level_info, s
                      advance_spheres, voxelise_host, directions, solid_angles, WORKLOADS, workload_scene,
                      batch_workload, BATCH_EDGES, BATCH_CASCADES, load_obj, mesh_to_grid, mesh_materials,
                      room_mesh, camera_view_proj, shade_vertices, shade_material, mesh_tbn,
-                     frames)
+                     frames, FrameLog)
 
 _load_lib()

@@ -126,6 +126,8 @@ SIGNATURES = {
     "rc_batch_get_fluence": (_S, [_P, C.c_int32, _P, C.c_int64, C.c_int32]),
     "rc_batch_get_radiance": (_S, [_P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int32]),
     "rc_batch_set_spheres": (_S, [_P, C.c_int32, _P, C.c_int32]),
+    "rc_set_stage_timing": (_S, [_P, C.c_int32]),
+    "rc_get_stage_ms": (_S, [_P, _P, C.c_int32]),
     "rc_batch_get_fluence_all": (_S, [_P, _P, C.c_int64, C.c_int32]),
     "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_get_tiles": (_S, [_P, C.POINTER(BatchTiles)]),

@@ -71,6 +71,8 @@ void release(rc_context* c) {
   }
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (cudaEvent_t ev : c->tev)
+    if (ev) cudaEventDestroy(ev);
   void* bufs[] = {c->err, c->recs, c->qcounter, c->base, c->vol, c->occ, c->emis, c->masks, c->dirs, c->rad, c->avg, c->flu[0], c->d_sph, c->qsteps, c->qstep_begin};  // d_reg, d_slist point into d_sph
   for (void* b : bufs)
     if (b) cudaFree(b);
@@ -438,6 +440,7 @@ namespace {
 // needs it.
 rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
   int near = c->nlev;
+  if (c->timing) cudaEventRecord(c->tev[0], s);
   if (nrc_active(c)) {
     near = nrc_first_level(c);
     bool queue_near = false;
@@ -448,10 +451,17 @@ rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
     if (queue_near && !nrc_walks_near(c)) launch_queue_walk(c, s, ~((1u << near) - 1u));
     rc_status st = nrc_enqueue_far(c, s);
     if (st != RC_OK) return st;
+    // the cache's whole schedule counts under the top cascade
+    if (c->timing)
+      for (int i = c->nlev - 1; i >= near; --i) cudaEventRecord(c->tev[c->nlev - i], s);
   } else {
     launch_queue_walk(c, s);
   }
-  for (int i = near - 1; i >= 0; --i) plain_level(c, i, s);
+  for (int i = near - 1; i >= 0; --i) {
+    plain_level(c, i, s);
+    if (c->timing) cudaEventRecord(c->tev[c->nlev - i], s);
+  }
+  c->timed = c->timing;
   return RC_OK;
 }
 
@@ -758,6 +768,8 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
     setup_tma_up(c);
   }
   *out = c;
+  rcx::log_message(2, "context %p: grid %dx%dx%d, %d cascades, %s, device %d%s", (void*)c, p->grid[0], p->grid[1],
+                   p->grid[2], c->nlev, c->elem == 2 ? "fp16" : "fp32", device, minimal ? " (batch scene)" : "");
   return RC_OK;
 }
 
@@ -968,6 +980,9 @@ rc_status rc_solve(rc_context* c, void* stream) {
   rc_status st = enqueue_solve(c, s);
   if (st != RC_OK) return st;
   RC_CUDA(cudaGetLastError(), "rc_solve: launch");
+  ++c->solves;
+  rcx::log_message(3, "solve %lld of context %p enqueued (grid %dx%dx%d, %d cascades%s)", (long long)c->solves,
+                   (void*)c, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->nlev, nrc_active(c) ? ", cache on" : "");
   if (s != c->stream) {
     RC_CUDA(cudaEventRecord(c->ev_out, s), "rc_solve: event");
     RC_CUDA(cudaStreamWaitEvent(c->stream, c->ev_out, 0), "rc_solve: wait");
@@ -1340,6 +1355,39 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
   for (int i = 0; i < c->nlev + 2; ++i) cudaEventDestroy(ev[i]);
   if (st != RC_OK) return st;
   for (int i = 0; i <= c->nlev; ++i) ms_out[i] = (float)(acc[i] / iters);
+  return RC_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+rc_status rc_set_stage_timing(rc_context* c, int32_t enable) {
+  if (check_ctx(c, "rc_set_stage_timing") != RC_OK) return RC_ERR_INVALID_ARG;
+  DeviceGuard g(c->device);
+  if (enable && !c->tev[0])
+    for (int i = 0; i <= c->nlev; ++i)
+      RC_CUDA(cudaEventCreate(&c->tev[i]), "rc_set_stage_timing: events");
+  c->timing = enable != 0;
+  c->timed = false;
+  return RC_OK;
+}
+
+rc_status rc_get_stage_ms(rc_context* c, float* ms_out, int32_t count) {
+  if (check_ctx(c, "rc_get_stage_ms") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!ms_out || count < 1 + c->nlev) {
+    rcx::set_error("rc_get_stage_ms: need 1 + num_cascades floats");
+    return RC_ERR_INVALID_ARG;
+  }
+  if (!c->timed) {
+    rcx::set_error("rc_get_stage_ms: no solve since rc_set_stage_timing(ctx, 1)");
+    return RC_ERR_STATE;
+  }
+  DeviceGuard g(c->device);
+  RC_CUDA(cudaEventSynchronize(c->tev[c->nlev]), "rc_get_stage_ms");
+  RC_CUDA(cudaEventElapsedTime(&ms_out[0], c->tev[0], c->tev[c->nlev]), "rc_get_stage_ms");
+  for (int i = 0; i < c->nlev; ++i)
+    RC_CUDA(cudaEventElapsedTime(&ms_out[1 + i], c->tev[c->nlev - 1 - i], c->tev[c->nlev - i]), "rc_get_stage_ms");
   return RC_OK;
 }
 

@@ -87,6 +87,13 @@ struct rc_context {
 
   rcx::NrcState* nrc = nullptr;  // neural radiance cache (rc_nrc_enable), or null
 
+  // per-solve stage timing (rc_set_stage_timing): tev[0] before the solve,
+  // tev[nlev - i] after cascade i
+  bool timing = false;
+  bool timed = false;  // a solve has recorded the events
+  cudaEvent_t tev[rcx::kMaxCascades + 1] = {};
+  int64_t solves = 0;
+
   // device scratch of the shading pass, grown on demand and kept
   void* scratch[12] = {};
   size_t scratch_cap[12] = {};

@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -24,11 +25,30 @@ namespace rcx {
 
 static thread_local char g_last_error[512] = "no error";
 
+int log_level() {
+  static const int level = [] {
+    const char* e = getenv("RC_LOG");
+    return e ? atoi(e) : 0;
+  }();
+  return level;
+}
+
+void log_message(int level, const char* fmt, ...) {
+  if (log_level() < level) return;
+  char buf[640];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  fprintf(stderr, "rc[%s] %s\n", level <= 1 ? "error" : level == 2 ? "info" : "frame", buf);
+}
+
 void set_error(const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
   vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
   va_end(ap);
+  log_message(1, "%s", g_last_error);
 }
 
 static bool fail(char* msg, size_t cap, const char* text) {

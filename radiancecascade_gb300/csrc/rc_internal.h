@@ -107,4 +107,9 @@ int update_regions(const QSphere* old_sph, const QSphere* new_sph, int n, const 
 int64_t sphere_lists(const QSphere* sph, int n, const int32_t grid[3], Region* regs, int nreg, int32_t* list,
                      int64_t cap);
 void set_error(const char* fmt, ...);
+// Diagnostics on stderr by the RC_LOG environment variable (read once):
+// 0 or unset = silent, 1 = every error as it is set, 2 = also context
+// lifetime and configuration, 3 = also one line per solve.
+int log_level();
+void log_message(int level, const char* fmt, ...);
 }  // namespace rcx

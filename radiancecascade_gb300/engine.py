@@ -566,6 +566,16 @@ class Engine:
         F.check(self._lib.rc_profile_levels(self.handle, iters, F.ptr(out), out.size))
         return out
 
+    def set_stage_timing(self, enable: bool = True) -> None:
+        """CUDA events between the stages of every solve (no host wait)."""
+        F.check(self._lib.rc_set_stage_timing(self.handle, 1 if enable else 0))
+
+    def stage_ms(self) -> np.ndarray:
+        """[whole solve, cascade 0, cascade 1, ...] ms of the last solve (waits for it)."""
+        out = np.zeros(1 + self.params.num_cascades, np.float32)
+        F.check(self._lib.rc_get_stage_ms(self.handle, F.ptr(out), out.size))
+        return out
+
     def radiance_device_ptr(self, level: int) -> int:
         p = C.c_void_p()
         F.check(self._lib.rc_radiance_device_ptr(self.handle, level, C.byref(p)))
@@ -583,9 +593,16 @@ class Engine:
     def nrc_enable(self, params: Optional[F.NrcParams] = None, **kw) -> None:
         p = params if params is not None else self.nrc_params(**kw)
         F.check(self._lib.rc_nrc_enable(self.handle, C.byref(p)))
+        self._nrc_on = True
 
     def nrc_disable(self) -> None:
         F.check(self._lib.rc_nrc_disable(self.handle))
+        self._nrc_on = False
+
+    @property
+    def nrc_on(self) -> bool:
+        """Whether the radiance cache serves the far cascades."""
+        return getattr(self, "_nrc_on", False)
 
     def nrc_stats(self) -> dict:
         st = F.NrcStats()
@@ -783,3 +800,50 @@ def frames(stage: GiStage, spheres: np.ndarray, grid, count: int, start: int = 0
 __all__ = ["Engine", "GiStage", "GiState", "make_params", "level_info", "scene_spec", "generate_scene",
            "advance_spheres", "voxelise_host", "directions", "solid_angles", "WORKLOADS", "workload_scene",
            "frames", "RCError", "VOXEL_DT", "BOX_DT", "SPHERE_DT"]
+
+
+class FrameLog:
+    """Per-frame metrics as JSON lines: frame, ms of the whole solve and of each
+    cascade (the engine's stage timing), algorithmic GB/s of the solve, the
+    radiance cache's loss and fallback-tile fraction when it is on, and any
+    extra fields the caller adds (e.g. the fluence error against an oracle).
+
+        log = FrameLog("frames.jsonl", engine, algorithmic_bytes=B)
+        for f in range(n):
+            engine.set_spheres(spheres); engine.solve()
+            log.write(f, fluence_rel_l2=...)
+    """
+
+    def __init__(self, path_or_file, engine: "Engine", algorithmic_bytes: Optional[float] = None):
+        import json  # noqa: F401  (used in write)
+        self._own = isinstance(path_or_file, (str, os.PathLike))
+        self._f = open(path_or_file, "w") if self._own else path_or_file
+        self._eng = engine
+        self._bytes = algorithmic_bytes
+        engine.set_stage_timing(True)
+
+    def record(self, frame: int, **extra) -> dict:
+        ms = self._eng.stage_ms()
+        rec = {"frame": int(frame), "solve_ms": round(float(ms[0]), 5),
+               "cascade_ms": [round(float(x), 5) for x in ms[1:]]}
+        if self._bytes:
+            rec["algorithmic_gb_per_s"] = round(self._bytes / (float(ms[0]) / 1000.0) / 1e9, 2)
+        if self._eng.nrc_on:
+            st = self._eng.nrc_stats()
+            rec["nrc_loss"] = float(st["last_loss"])
+            rec["nrc_fallback_fraction"] = float(st["fallback_tiles"]) / max(1, int(st["tiles"]))
+            rec["nrc_served_levels"] = int(st["served_levels"])
+        rec.update(extra)
+        return rec
+
+    def write(self, frame: int, **extra) -> dict:
+        import json
+        rec = self.record(frame, **extra)
+        self._f.write(json.dumps(rec) + "\n")
+        self._f.flush()
+        return rec
+
+    def close(self) -> None:
+        self._eng.set_stage_timing(False)
+        if self._own:
+            self._f.close()

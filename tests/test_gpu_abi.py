@@ -155,3 +155,36 @@ def test_contexts_of_different_sizes_coexist():
     finally:
         small.close()
         big.close()
+
+
+def test_stage_timing_and_frame_log(tmp_path):
+    """Stage timing records events inside every solve: the cascades' times are
+    non-negative and add up to the whole solve; the JSONL frame log writes one
+    line per frame with them, the algorithmic GB/s and the cache's figures."""
+    import json
+    params = R.make_params(64, 5)
+    boxes, spheres = R.workload_scene("c64")
+    with R.Engine(params) as e:
+        e.set_boxes(boxes)
+        e.set_spheres(spheres)
+        with pytest.raises(R.RCError):
+            e.stage_ms()  # timing is off
+        log = R.FrameLog(str(tmp_path / "frames.jsonl"), e, algorithmic_bytes=29e6)
+        for f in range(3):
+            e.solve()
+            log.write(f, note="plain")
+        e.nrc_enable(first_level=3)
+        e.solve()
+        log.write(3)
+        log.close()
+        ms = None
+        with pytest.raises(R.RCError):
+            ms = e.stage_ms()
+    lines = [json.loads(x) for x in open(tmp_path / "frames.jsonl")]
+    assert [x["frame"] for x in lines] == [0, 1, 2, 3] and ms is None
+    for x in lines:
+        assert x["solve_ms"] > 0 and len(x["cascade_ms"]) == 5
+        assert min(x["cascade_ms"]) >= 0 and abs(sum(x["cascade_ms"]) - x["solve_ms"]) <= 1e-3 + 1e-3 * x["solve_ms"]
+        assert x["algorithmic_gb_per_s"] > 0
+    assert lines[0]["note"] == "plain" and "nrc_loss" not in lines[0]
+    assert 0.0 <= lines[3]["nrc_fallback_fraction"] <= 1.0

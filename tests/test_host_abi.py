@@ -159,3 +159,21 @@ def test_cpp_driver_host_calls(tmp_path):
     r = subprocess.run([exe, "host"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert "host ok" in r.stdout
+
+
+def test_rc_log_prints_errors_to_stderr():
+    """RC_LOG=1 prints every error as it is set; unset, the library is silent."""
+    import subprocess
+    import sys
+    code = ("import ctypes as C, radiancecascade_gb300 as R\n"
+            "from radiancecascade_gb300 import _ffi as F\n"
+            "p = R.make_params(64, 5); p.num_cascades = 0\n"
+            "assert F.lib().rc_params_validate(C.byref(p)) == F.RC_ERR_INVALID_ARG\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, RC_LOG="1", PYTHONPATH=root)
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0, r.stderr
+    assert "rc[error]" in r.stderr and "num_cascades" in r.stderr
+    env.pop("RC_LOG")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, cwd=root)
+    assert r.returncode == 0 and "rc[error]" not in r.stderr
