@@ -237,6 +237,18 @@ rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
 rc_status rc_set_stage_timing(rc_context* ctx, int32_t enable);
 rc_status rc_get_stage_ms(rc_context* ctx, float* ms_out, int32_t count);
 
+/* ---- checked build ---------------------------------------------------- */
+/* librc_checked.so (the same sources built with RC_CHECKED) tests the
+ * kernels' buffer accesses before making them: global accesses against the
+ * library's allocations and borrowed caller buffers, shared accesses against
+ * the block's shared memory.  An access that fails is skipped, counted, and
+ * the first one's site and address kept; no kernel traps.  This call waits
+ * for `device`, reads and clears those words: RC_OK when no access failed,
+ * RC_ERR_STATE (message: count, site, address) otherwise; in the ordinary
+ * library RC_ERR_UNSUPPORTED. */
+rc_status rc_check_status(int32_t device, uint64_t* first_failure,
+                          uint32_t* failures);
+
 /* ---- batched solve --------------------------------------------------- */
 /* Many independent scenes (each with its own rc_params: grid, cascades)
  * solved together.  rc_batch_solve launches one CUDA graph holding one

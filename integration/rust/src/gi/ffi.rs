@@ -226,6 +226,7 @@ extern "C" {
     pub fn rc_profile_levels(ctx: *mut rc_context, iters: i32, ms_out: *mut f32, count: i32) -> rc_status;
     pub fn rc_set_stage_timing(ctx: *mut rc_context, enable: i32) -> rc_status;
     pub fn rc_get_stage_ms(ctx: *mut rc_context, ms_out: *mut f32, count: i32) -> rc_status;
+    pub fn rc_check_status(device: i32, first_failure: *mut u64, failures: *mut u32) -> rc_status;
 
     // batched form (many scenes, one persistent launch)
     pub fn rc_batch_create(params: *const rc_params, nscenes: i32, device: i32, out: *mut *mut rc_batch)

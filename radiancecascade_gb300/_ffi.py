@@ -127,6 +127,7 @@ SIGNATURES = {
     "rc_batch_get_radiance": (_S, [_P, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int32]),
     "rc_batch_set_spheres": (_S, [_P, C.c_int32, _P, C.c_int32]),
     "rc_set_stage_timing": (_S, [_P, C.c_int32]),
+    "rc_check_status": (_S, [C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     "rc_get_stage_ms": (_S, [_P, _P, C.c_int32]),
     "rc_batch_get_fluence_all": (_S, [_P, _P, C.c_int64, C.c_int32]),
     "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
@@ -154,13 +155,15 @@ class RCError(RuntimeError):
 
 
 def lib() -> C.CDLL:
-    """Load librc.so.  Raises (never falls back) when it was not built."""
+    """Load librc.so (or the library RC_LIBRARY names, e.g. the checked build
+    librc_checked.so).  Raises (never falls back) when it was not built."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            raise ImportError("librc.so is missing at %s: build it first "
-                              "(python -m radiancecascade_gb300.build or __graft_entry__.build())" % LIB_PATH)
-        L = C.CDLL(LIB_PATH)
+        path = os.environ.get("RC_LIBRARY") or LIB_PATH
+        if not os.path.exists(path):
+            raise ImportError("%s is missing: build it first "
+                              "(python -m radiancecascade_gb300.build or __graft_entry__.build())" % path)
+        L = C.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res

@@ -18,6 +18,9 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "librc.so")
+# the checked build (-DRC_CHECKED): bounds-tested kernels, see csrc/rc_check.cuh
+OBJ_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(PKG, "librc_checked.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -34,17 +37,19 @@ def _sources():
     return cu, cpp, hdr
 
 
-def _compile(src: str) -> str:
-    out = os.path.join(OBJ, os.path.basename(src) + ".o")
+def _compile(src: str, checked: bool = False) -> str:
+    obj = OBJ_CHECKED if checked else OBJ
+    defs = ["-DRC_CHECKED"] if checked else []
+    out = os.path.join(obj, os.path.basename(src) + ".o")
     if src.endswith(".cu"):
-        cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+        cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", *defs, "-Xcompiler", "-fPIC,-ffp-contract=off",
                "-Xptxas", "-v", "-c", src, "-o", out]
     else:
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", *defs,
                "-I", os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include"),
                "-c", src, "-o", out]
     r = subprocess.run(cmd, capture_output=True, text=True)
-    log = os.path.join(OBJ, os.path.basename(src) + ".log")
+    log = os.path.join(obj, os.path.basename(src) + ".log")
     with open(log, "w") as f:
         f.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
     if r.returncode != 0:
@@ -52,28 +57,31 @@ def _compile(src: str) -> str:
     return out
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    """Builds librc.so, or with `checked` librc_checked.so (same sources with
+    RC_CHECKED: every instrumented buffer access is tested before it is made)."""
+    lib, obj = (LIB_CHECKED, OBJ_CHECKED) if checked else (LIB, OBJ)
     cu, cpp, hdr = _sources()
     srcs = cu + cpp
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
+    if not force and os.path.exists(lib):
+        t = os.path.getmtime(lib)
         if all(os.path.getmtime(s) <= t for s in srcs + hdr + [__file__]):
-            return LIB
-    os.makedirs(OBJ, exist_ok=True)
+            return lib
+    os.makedirs(obj, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=max(2, min(len(srcs), os.cpu_count() or 2))) as ex:
-        objs = list(ex.map(_compile, srcs))
-    tmp = LIB + ".tmp%d" % os.getpid()
+        objs = list(ex.map(lambda src: _compile(src, checked), srcs))
+    tmp = lib + ".tmp%d" % os.getpid()
     cmd = [_nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (" ".join(cmd), r.stderr[-4000:]))
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     if verbose:
         for s in srcs:
-            with open(os.path.join(OBJ, os.path.basename(s) + ".log")) as f:
+            with open(os.path.join(obj, os.path.basename(s) + ".log")) as f:
                 sys.stdout.write(f.read())
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -47,6 +47,10 @@ rc_status dev_alloc(void** ptr, size_t bytes, const char* what) {
     (void)cudaGetLastError();
     return cuda_fail(e, what);
   }
+#ifdef RC_CHECKED
+  check_register(*ptr, bytes);
+  if ((e = check_prepare()) != cudaSuccess) return cuda_fail(e, "checked build: range upload");
+#endif
   return RC_OK;
 }
 
@@ -130,6 +134,7 @@ rc_status ensure_sphere_capacity(rc_context* c, int n) {
 // Recompose the given regions of the volume from the base and the current
 // spheres.  regions == nullptr means the whole grid.
 rc_status recompose(rc_context* c, const Region* regions, int nreg) {
+  RC_CUDA(check_prepare(), "checked build: range upload");
   const int n = (int)c->cur.size();
   rc_status s = ensure_sphere_capacity(c, std::max(n, 1));
   if (s != RC_OK) return s;
@@ -439,6 +444,7 @@ namespace {
 // up) come from the cache and the walk queue runs only when a near level
 // needs it.
 rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
+  RC_CUDA(check_prepare(), "checked build: range upload");
   int near = c->nlev;
   if (c->timing) cudaEventRecord(c->tev[0], s);
   if (nrc_active(c)) {
@@ -1362,6 +1368,32 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
 
 extern "C" {
 
+rc_status rc_check_status(int32_t device, uint64_t* first_failure, uint32_t* failures) {
+#ifdef RC_CHECKED
+  DeviceGuard g(device);
+  unsigned long long f0 = 0, f1 = 0;
+  unsigned n0 = 0, n1 = 0;
+  RC_CUDA(check_read(&f0, &n0), "rc_check_status");
+  RC_CUDA(nrc_check_read(&f1, &n1), "rc_check_status");
+  const unsigned long long first = f0 ? f0 : f1;
+  const unsigned count = n0 + n1;
+  if (first_failure) *first_failure = first;
+  if (failures) *failures = count;
+  if (count) {
+    rcx::set_error("checked build: %u out-of-range accesses skipped; the first touched %s at 0x%llx", count,
+                   rcx::check_site_name((int)(first >> 56)), first & ((1ull << 56) - 1));
+    return RC_ERR_STATE;
+  }
+  return RC_OK;
+#else
+  (void)device;
+  if (first_failure) *first_failure = 0;
+  if (failures) *failures = 0;
+  rcx::set_error("rc_check_status: this library was built without RC_CHECKED (librc_checked.so has the checks)");
+  return RC_ERR_UNSUPPORTED;
+#endif
+}
+
 rc_status rc_set_stage_timing(rc_context* c, int32_t enable) {
   if (check_ctx(c, "rc_set_stage_timing") != RC_OK) return RC_ERR_INVALID_ARG;
   DeviceGuard g(c->device);
@@ -1536,7 +1568,21 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     if ((e = allow_bits_smem<float>()) != cudaSuccess || (e = allow_bits_smem<__half>()) != cudaSuccess)
       return cuda_fail(e, "rc_solve_noalloc: shared memory attribute");
     g_noalloc_scratch_ptr[dev] = ptr;
+#ifdef RC_CHECKED
+    check_register(ptr, RC_NOALLOC_SCRATCH_BYTES);
+#endif
   }
+#ifdef RC_CHECKED
+  {
+    // the caller's buffers are the kernels' to read and write
+    size_t rb = 0;
+    for (int i = 0; i < v.nlev; ++i) rb += (size_t)3 * v.geom[i].ndirs * v.geom[i].probes() * v.elem;
+    check_register(voxels, (size_t)p->grid[0] * p->grid[1] * p->grid[2] * sizeof(rc_voxel));
+    check_register(fluence, (size_t)v.geom[0].probes() * 3 * sizeof(float));
+    check_register(radiance, rb);
+    RC_CUDA(check_prepare(), "checked build: range upload");
+  }
+#endif
   char* scratch = static_cast<char*>(g_noalloc_scratch_ptr[dev]);
 
   // Walk tables, built on the host and copied into the scratch.
@@ -1899,6 +1945,10 @@ rc_status rc_batch_scene_set(rc_batch* b, int32_t scene, const rc_box* boxes, in
 
 rc_status rc_batch_solve(rc_batch* b, void* stream) {
   if (batch_check(b, "rc_batch_solve") != RC_OK) return RC_ERR_INVALID_ARG;
+  {
+    DeviceGuard g(b->device);
+    RC_CUDA(check_prepare(), "checked build: range upload");
+  }
   for (int k = 0; k < b->n; ++k)
     if (!b->scenes[k]->have_base) {
       rcx::set_error("rc_batch_solve: scene %d has no scene data", k);

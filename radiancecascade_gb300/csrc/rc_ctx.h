@@ -140,6 +140,9 @@ int nrc_first_level(const rc_context* c);  // first cascade the cache serves
 // Whether the cache's far walk also walks the near levels that use the walk
 // queue (both use step tables); then the solve launches no near walk.
 bool nrc_walks_near(const rc_context* c);
+// Checked build: the radiance-cache translation unit's failure words (read
+// and cleared; zeros in the ordinary build).
+cudaError_t nrc_check_read(unsigned long long* first, unsigned* count);
 // Enqueues the cache's per-frame work for the far cascades (training-sample
 // walks, refit, inference, fallback walks) and their merges, top level down to
 // the first far level.  Called from the solve before the near levels.

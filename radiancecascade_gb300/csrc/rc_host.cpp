@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <vector>
 
 #include "rc_internal.h"
@@ -49,6 +50,33 @@ void set_error(const char* fmt, ...) {
   vsnprintf(g_last_error, sizeof g_last_error, fmt, ap);
   va_end(ap);
   log_message(1, "%s", g_last_error);
+}
+
+static std::mutex g_check_mutex;
+static std::vector<CheckRange> g_check;
+static uint64_t g_check_version = 0;
+
+void check_register(const void* p, size_t bytes) {
+  if (!p || !bytes) return;
+  std::lock_guard<std::mutex> lock(g_check_mutex);
+  const uint64_t lo = (uint64_t)(uintptr_t)p, hi = lo + bytes;
+  for (const CheckRange& r : g_check)
+    if (r.lo == lo && r.hi == hi) return;
+  g_check.push_back(CheckRange{lo, hi});
+  ++g_check_version;
+}
+
+std::vector<CheckRange> check_ranges(uint64_t* version) {
+  std::lock_guard<std::mutex> lock(g_check_mutex);
+  if (version) *version = g_check_version;
+  return g_check;
+}
+
+const char* check_site_name(int site) {
+  static const char* names[] = {"unknown",           "radiance",      "voxel volume",     "opacity bits",
+                                "decimated opacity", "walk records",  "walk tables",      "fluence",
+                                "shared memory",     "hash table",    "cache buffers",    "emitter regions"};
+  return (site >= 0 && site < (int)(sizeof names / sizeof names[0])) ? names[site] : "unknown";
 }
 
 static bool fail(char* msg, size_t cap, const char* text) {

@@ -4,6 +4,8 @@
 
 #include <stdint.h>
 
+#include <vector>
+
 #include "../../include/rc.h"
 
 #ifdef __CUDACC__
@@ -107,6 +109,17 @@ int update_regions(const QSphere* old_sph, const QSphere* new_sph, int n, const 
 int64_t sphere_lists(const QSphere* sph, int n, const int32_t grid[3], Region* regs, int nreg, int32_t* list,
                      int64_t cap);
 void set_error(const char* fmt, ...);
+
+// Device ranges the checked build's kernels may touch (rc_check.cuh):
+// registered by dev_alloc and by the entry points that borrow caller
+// buffers; check_ranges returns a copy and a version that changes with
+// every registration.  No-ops' worth of bookkeeping in the ordinary build.
+struct CheckRange {
+  uint64_t lo, hi;
+};
+void check_register(const void* p, size_t bytes);
+std::vector<CheckRange> check_ranges(uint64_t* version);
+const char* check_site_name(int site);
 // Diagnostics on stderr by the RC_LOG environment variable (read once):
 // 0 or unset = silent, 1 = every error as it is set, 2 = also context
 // lifetime and configuration, 3 = also one line per solve.

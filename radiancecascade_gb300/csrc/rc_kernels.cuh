@@ -12,6 +12,7 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "rc_check.cuh"
 #include "rc_internal.h"
 
 namespace rcx {
@@ -20,17 +21,25 @@ template <typename T>
 struct Store;
 template <>
 struct Store<float> {
-  static __device__ __forceinline__ float load(const float* p) { return __ldg(p); }
-  static __device__ __forceinline__ void store(float* p, float v) { *p = v; }
+  static __device__ __forceinline__ float load(const float* p) { return RC_CHK(p, kChkRadiance) ? __ldg(p) : 0.f; }
+  static __device__ __forceinline__ void store(float* p, float v) {
+    if (RC_CHK(p, kChkRadiance)) *p = v;
+  }
   // write-once outputs: evict-first, so they do not push reused data out of L2
-  static __device__ __forceinline__ void stream(float* p, float v) { __stcs(p, v); }
+  static __device__ __forceinline__ void stream(float* p, float v) {
+    if (RC_CHK(p, kChkRadiance)) __stcs(p, v);
+  }
 };
 template <>
 struct Store<__half> {
-  static __device__ __forceinline__ float load(const __half* p) { return __half2float(__ldg(p)); }
-  static __device__ __forceinline__ void store(__half* p, float v) { *p = __float2half_rn(v); }
+  static __device__ __forceinline__ float load(const __half* p) {
+    return RC_CHK(p, kChkRadiance) ? __half2float(__ldg(p)) : 0.f;
+  }
+  static __device__ __forceinline__ void store(__half* p, float v) {
+    if (RC_CHK(p, kChkRadiance)) *p = __float2half_rn(v);
+  }
   static __device__ __forceinline__ void stream(__half* p, float v) {
-    __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
+    if (RC_CHK(p, kChkRadiance)) __stcs(reinterpret_cast<unsigned short*>(p), __half_as_ushort(__float2half_rn(v)));
   }
 };
 
@@ -44,13 +53,20 @@ struct Store<__half> {
 template <typename T, bool CG>
 __device__ __forceinline__ float load_up(const T* p);
 template <>
-__device__ __forceinline__ float load_up<float, false>(const float* p) { return __ldg(p); }
+__device__ __forceinline__ float load_up<float, false>(const float* p) {
+  return RC_CHK(p, kChkRadiance) ? __ldg(p) : 0.f;
+}
 template <>
-__device__ __forceinline__ float load_up<float, true>(const float* p) { return __ldca(p); }
+__device__ __forceinline__ float load_up<float, true>(const float* p) {
+  return RC_CHK(p, kChkRadiance) ? __ldca(p) : 0.f;
+}
 template <>
-__device__ __forceinline__ float load_up<__half, false>(const __half* p) { return __half2float(__ldg(p)); }
+__device__ __forceinline__ float load_up<__half, false>(const __half* p) {
+  return RC_CHK(p, kChkRadiance) ? __half2float(__ldg(p)) : 0.f;
+}
 template <>
 __device__ __forceinline__ float load_up<__half, true>(const __half* p) {
+  if (!RC_CHK(p, kChkRadiance)) return 0.f;
   return __half2float(__ushort_as_half(__ldca(reinterpret_cast<const unsigned short*>(p))));
 }
 
@@ -85,7 +101,8 @@ struct LevelArgs {
 };
 
 __device__ __forceinline__ bool opaque_at(const uint32_t* __restrict__ occ, int W, int Gy, int x, int y, int z) {
-  return (__ldg(&occ[((int64_t)z * Gy + y) * W + (x >> 5)]) >> (x & 31)) & 1u;
+  const uint32_t* w = &occ[((int64_t)z * Gy + y) * W + (x >> 5)];
+  return RC_CHK(w, kChkOccupancy) && ((__ldg(w) >> (x & 31)) & 1u);
 }
 
 // Exact integer voxel walk of one interval.  Returns the linear index of the
@@ -117,14 +134,14 @@ __device__ __forceinline__ int64_t walk_interval(const uint32_t* __restrict__ oc
 }
 
 __device__ __forceinline__ void voxel_emission(const uint2* __restrict__ vol, int64_t idx, float r[3]) {
-  const uint2 v = __ldg(&vol[idx]);
+  const uint2 v = RC_CHK(&vol[idx], kChkVolume) ? __ldg(&vol[idx]) : make_uint2(0u, 0u);
   r[0] = __half2float(__ushort_as_half((unsigned short)(v.x & 0xFFFFu)));
   r[1] = __half2float(__ushort_as_half((unsigned short)(v.x >> 16)));
   r[2] = __half2float(__ushort_as_half((unsigned short)(v.y & 0xFFFFu)));
 }
 
 __device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol, uint32_t idx, int ch) {
-  const uint2 v = __ldg(&vol[idx]);
+  const uint2 v = RC_CHK(&vol[idx], kChkVolume) ? __ldg(&vol[idx]) : make_uint2(0u, 0u);
   const uint32_t w = ch == 2 ? v.y : v.x;
   return __half2float(__ushort_as_half((unsigned short)(ch == 1 ? (w >> 16) : (w & 0xFFFFu))));
 }
@@ -214,7 +231,8 @@ __device__ __forceinline__ void scalar_probe(const LevelArgs& a, int64_t p, int 
   }
   if (L0) {
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
+    for (int ch = 0; ch < 3; ++ch)
+      if (RC_CHK(&a.fluence[p * 3 + ch], kChkFluence)) a.fluence[p * 3 + ch] = acc[ch];
   }
 }
 
@@ -245,7 +263,7 @@ static __global__ void k_boxes_to_base(uint2* __restrict__ base, int Gx, int Gy,
         break;
       }
     }
-    base[idx] = v;
+    if (RC_CHK(&base[idx], kChkVolume)) base[idx] = v;
   }
 }
 

@@ -26,7 +26,7 @@ struct Vec4;
 template <>
 struct Vec4<float> {
   static __device__ __forceinline__ void stream(float* p, float a, float b, float c, float d) {
-    __stcs(reinterpret_cast<float4*>(p), make_float4(a, b, c, d));
+    if (RC_CHK(reinterpret_cast<float4*>(p), kChkRadiance)) __stcs(reinterpret_cast<float4*>(p), make_float4(a, b, c, d));
   }
 };
 template <>
@@ -36,7 +36,7 @@ struct Vec4<__half> {
     uint2 u;
     u.x = *reinterpret_cast<const uint32_t*>(&lo);
     u.y = *reinterpret_cast<const uint32_t*>(&hi);
-    __stcs(reinterpret_cast<uint2*>(p), u);
+    if (RC_CHK(reinterpret_cast<uint2*>(p), kChkRadiance)) __stcs(reinterpret_cast<uint2*>(p), u);
   }
 };
 
@@ -46,19 +46,23 @@ template <typename T, bool CG>
 __device__ __forceinline__ float2 load2(const T* p);
 template <>
 __device__ __forceinline__ float2 load2<float, false>(const float* p) {
-  return __ldg(reinterpret_cast<const float2*>(p));
+  const float2* q = reinterpret_cast<const float2*>(p);
+  return RC_CHK(q, kChkRadiance) ? __ldg(q) : make_float2(0.f, 0.f);
 }
 template <>
 __device__ __forceinline__ float2 load2<float, true>(const float* p) {
-  return __ldca(reinterpret_cast<const float2*>(p));
+  const float2* q = reinterpret_cast<const float2*>(p);
+  return RC_CHK(q, kChkRadiance) ? __ldca(q) : make_float2(0.f, 0.f);
 }
 template <>
 __device__ __forceinline__ float2 load2<__half, false>(const __half* p) {
-  return __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+  const __half2* q = reinterpret_cast<const __half2*>(p);
+  return RC_CHK(q, kChkRadiance) ? __half22float2(__ldg(q)) : make_float2(0.f, 0.f);
 }
 template <>
 __device__ __forceinline__ float2 load2<__half, true>(const __half* p) {
-  const unsigned u = __ldca(reinterpret_cast<const unsigned*>(p));
+  const unsigned* q = reinterpret_cast<const unsigned*>(p);
+  const unsigned u = RC_CHK(q, kChkRadiance) ? __ldca(q) : 0u;
   return __half22float2(*reinterpret_cast<const __half2*>(&u));
 }
 
@@ -92,8 +96,10 @@ __device__ __forceinline__ void level0_direct_warp(const LevelArgs& a, int64_t w
     if (active && (zc == 0 || zok1)) {
       const int64_t w = ((int64_t)vz * a.G[1] + vy) * a.W + ((8 * lq) >> 5);
       const int sh = (8 * lq) & 31;
-      ow[zc] |= ((__ldg(&a.occ[w]) >> sh) & 0xFFu) << (8 * (r & 3));
-      ew[zc] |= ((__ldg(&a.emis[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+      const uint32_t wo = RC_CHK(&a.occ[w], kChkOccupancy) ? __ldg(&a.occ[w]) : 0u;
+      const uint32_t we = RC_CHK(&a.emis[w], kChkOccupancy) ? __ldg(&a.emis[w]) : 0u;
+      ow[zc] |= ((wo >> sh) & 0xFFu) << (8 * (r & 3));
+      ew[zc] |= ((we >> sh) & 0xFFu) << (8 * (r & 3));
     }
   }
 
@@ -227,7 +233,8 @@ __device__ __forceinline__ void level0_direct_warp(const LevelArgs& a, int64_t w
       if (!(active && (zc == 0 || zok1))) continue;
       float* f = a.fluence + (p0 + zc * plane) * 3 + ch;
 #pragma unroll
-      for (int e = 0; e < 4; ++e) f[3 * e] = flu[zc][e];
+      for (int e = 0; e < 4; ++e)
+        if (RC_CHK(&f[3 * e], kChkFluence)) f[3 * e] = flu[zc][e];
     }
   }
 }
@@ -293,8 +300,10 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
     if (active && (zc == 0 || zok1)) {
       const int64_t w = ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.W + ((8 * lq) >> 5);
       const int sh = (8 * lq) & 31;
-      ow[zc] |= ((__ldg(&a.occ[w]) >> sh) & 0xFFu) << (8 * (r & 3));
-      ew[zc] |= ((__ldg(&a.emis[w]) >> sh) & 0xFFu) << (8 * (r & 3));
+      const uint32_t wo = RC_CHK(&a.occ[w], kChkOccupancy) ? __ldg(&a.occ[w]) : 0u;
+      const uint32_t we = RC_CHK(&a.emis[w], kChkOccupancy) ? __ldg(&a.emis[w]) : 0u;
+      ow[zc] |= ((wo >> sh) & 0xFFu) << (8 * (r & 3));
+      ew[zc] |= ((we >> sh) & 0xFFu) << (8 * (r & 3));
     }
   }
   uint32_t oct_opq[2] = {0u, 0u}, oct_ems[2] = {0u, 0u};
@@ -412,10 +421,10 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
 #pragma unroll
           for (int k = 0; k < PZ; ++k) {
             const T* row = tile + rowoff[r][k];
-            cv[k][0] = to_float(row[lcol]);
-            cv[k][1] = to_float(row[c0]);
-            cv[k][2] = to_float(row[c0 + 1]);
-            cv[k][3] = to_float(row[rcol]);
+            cv[k][0] = RC_CHK(&row[lcol], kChkShared) ? to_float(row[lcol]) : 0.f;
+            cv[k][1] = RC_CHK(&row[c0], kChkShared) ? to_float(row[c0]) : 0.f;
+            cv[k][2] = RC_CHK(&row[c0 + 1], kChkShared) ? to_float(row[c0 + 1]) : 0.f;
+            cv[k][3] = RC_CHK(&row[rcol], kChkShared) ? to_float(row[rcol]) : 0.f;
           }
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
@@ -464,6 +473,7 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
       float* f = a.fluence + (p0 + zc * plane) * 3;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
+        if (!RC_CHK(&f[3 * e + 2], kChkFluence) || !RC_CHK(&f[3 * e], kChkFluence)) continue;
         f[3 * e] = flu[0][zc][e];
         f[3 * e + 1] = flu[1][zc][e];
         f[3 * e + 2] = flu[2][zc][e];

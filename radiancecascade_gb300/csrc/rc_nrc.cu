@@ -174,6 +174,7 @@ void init_params(NrcState* n, std::vector<float>& mlp, std::vector<float>& hash)
 }
 
 rc_status upload_params(NrcState* n, const std::vector<float>& mlp, const std::vector<float>& hash) {
+  RC_CUDA(check_prepare(), "checked build: range upload");
   RC_CUDA(cudaMemcpy(n->mlp, mlp.data(), mlp.size() * 4, cudaMemcpyHostToDevice), "cache upload");
   RC_CUDA(cudaMemcpy(n->hash_master, hash.data(), hash.size() * 4, cudaMemcpyHostToDevice), "cache upload");
   std::vector<__half> hh(hash.size());
@@ -197,6 +198,16 @@ rc_status upload_params(NrcState* n, const std::vector<float>& mlp, const std::v
 bool nrc_active(const rc_context* c) { return c && c->nrc; }
 int nrc_first_level(const rc_context* c) { return c->nrc ? c->nrc->first : c->nlev; }
 bool nrc_walks_near(const rc_context* c) { return c->nrc && c->nrc->ftab && c->qtab; }
+
+cudaError_t nrc_check_read(unsigned long long* first, unsigned* count) {
+#ifdef RC_CHECKED
+  return check_read(first, count);
+#else
+  *first = 0;
+  *count = 0;
+  return cudaSuccess;
+#endif
+}
 
 void nrc_release(rc_context* c) {
   if (!c || !c->nrc) return;
@@ -283,6 +294,7 @@ void launch_merge(const rc_context* c, const NrcState* n, int i, cudaStream_t s)
 }  // namespace
 
 rc_status nrc_enqueue_far(rc_context* c, cudaStream_t s) {
+  RC_CUDA(check_prepare(), "checked build: range upload");
   NrcState* n = c->nrc;
   const int ph = (int)(n->solves % n->nph), hp = (ph + n->nph / 2) % n->nph;
   const int64_t tr0 = n->tile_begin[ph], ntr = n->tile_begin[ph + 1] - tr0;
@@ -633,6 +645,7 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
     if ((s = dev_alloc((void**)&n->hparts, (size_t)(np + nd) * kNrcHashLevels * sizeof(uint32_t),
                        "hash parts")) != RC_OK)
       return fail(s);
+    RC_CUDA(check_prepare(), "checked build: range upload");
     int64_t po = 0, dof = np;
     for (int i = n->first; i < c->nlev; ++i) {
       NrcLevel& L = n->base.lv[i];
@@ -937,6 +950,7 @@ rc_status rc_nrc_query(rc_context* c, int32_t level, const int32_t* probes, cons
   if (s != RC_OK) return s;
   cudaStream_t st = c->stream;
   RC_CUDA(cudaMemcpyAsync(n->qtiles, t.data(), count * sizeof(NrcTile), cudaMemcpyHostToDevice, st), "rc_nrc_query");
+  RC_CUDA(check_prepare(), "checked build: range upload");
   NrcArgs a = n->base;
   a.tiles = n->qtiles;
   a.ntiles = count;
@@ -978,6 +992,7 @@ rc_status rc_nrc_tile_gradient(rc_context* c, int32_t level, int32_t probe, int3
   RC_CUDA(cudaMemcpyAsync(n->qout, tg.data(), tg.size() * 4, cudaMemcpyHostToDevice, st), "rc_nrc_tile_gradient");
   RC_CUDA(cudaMemsetAsync(n->dbg_g, 0, kNrcParams * 4, st), "rc_nrc_tile_gradient");
   RC_CUDA(cudaMemsetAsync(n->epos_grad, 0, kNrcPosFeat * 4, st), "rc_nrc_tile_gradient");
+  RC_CUDA(check_prepare(), "checked build: range upload");
   NrcArgs a = n->base;
   a.hash.grad = nullptr;  // a probe: nothing is scattered into the table gradient
   a.tiles = n->qtiles;

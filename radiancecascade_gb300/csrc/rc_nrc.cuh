@@ -250,7 +250,8 @@ __device__ __forceinline__ void nrc_rows(const NrcArgs& a, int li, int64_t p, in
   const uint32_t T = 1u << a.hash.log2T, mask = T - 1u;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const uint4 P = __ldg(hp + j), D = __ldg(hd + j);
+    const uint4 P = RC_CHK(hp + j, kChkHash) ? __ldg(hp + j) : make_uint4(0u, 0u, 0u, 0u);
+    const uint4 D = RC_CHK(hd + j, kChkHash) ? __ldg(hd + j) : make_uint4(0u, 0u, 0u, 0u);
     rows[4 * j + 0] = (4 * j + 0) * T + ((P.x ^ D.x) & mask);
     rows[4 * j + 1] = (4 * j + 1) * T + ((P.y ^ D.y) & mask);
     rows[4 * j + 2] = (4 * j + 2) * T + ((P.z ^ D.z) & mask);
@@ -268,7 +269,8 @@ __device__ __forceinline__ void nrc_input(const NrcArgs& a, bool valid, int li, 
   nrc_rows(a, li, p, d, rows);
 #pragma unroll
   for (int l = 0; l < kNrcHashLevels; ++l) {
-    const float2 f = __half22float2(__ldg(reinterpret_cast<const __half2*>(a.hash.table) + rows[l]));
+    const __half2* hp = reinterpret_cast<const __half2*>(a.hash.table) + rows[l];
+    const float2 f = RC_CHK(hp, kChkHash) ? __half22float2(__ldg(hp)) : make_float2(0.f, 0.f);
     x[2 * l] = f.x;
     x[2 * l + 1] = f.y;
   }
@@ -325,7 +327,10 @@ __device__ __forceinline__ void nrc_encode_row(const NrcArgs& a, bool valid, int
   nrc_rows(a, li, p, d, rows);
   __half2 f[kNrcHashLevels];
 #pragma unroll
-  for (int l = 0; l < kNrcHashLevels; ++l) f[l] = __ldg(reinterpret_cast<const __half2*>(a.hash.table) + rows[l]);
+  for (int l = 0; l < kNrcHashLevels; ++l) {
+    const __half2* hp = reinterpret_cast<const __half2*>(a.hash.table) + rows[l];
+    f[l] = RC_CHK(hp, kChkHash) ? __ldg(hp) : __float2half2_rn(0.f);
+  }
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     __nv_bfloat162 h[4];
@@ -508,10 +513,12 @@ __global__ void __launch_bounds__(kFwdThreads, 3) k_nrc_forward(const __grid_con
       float sv[4];
       nrc_serve(o, a.scale, sv);
 #pragma unroll
-      for (int c = 0; c < 4; ++c) L.rt[c * plane + off] = __float2half_rn(sv[c]);
+      for (int c = 0; c < 4; ++c)
+        if (RC_CHK(&L.rt[c * plane + off], kChkCache)) L.rt[c * plane + off] = __float2half_rn(sv[c]);
     } else {
       float4 r4 = make_float4(o[0], o[1], o[2], o[3]);
-      *reinterpret_cast<float4*>(a.out + (t * kNrcThreads + row) * 4) = r4;
+      float4* op = reinterpret_cast<float4*>(a.out + (t * kNrcThreads + row) * 4);
+      if (RC_CHK(op, kChkCache)) *op = r4;
     }
   }
   if (!ok) mbar_wait_bounded(bar, phase ^ 1u);  // the group that timed out, if it still runs
@@ -642,7 +649,8 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant
     {
       float e[4] = {0.f, 0.f, 0.f, 0.f};
       if (valid) {
-        const float4 y = *reinterpret_cast<const float4*>(a.target + (t * kNrcThreads + tid) * 4);
+        const float4* yp = reinterpret_cast<const float4*>(a.target + (t * kNrcThreads + tid) * 4);
+        const float4 y = RC_CHK(yp, kChkCache) ? *yp : make_float4(0.f, 0.f, 0.f, 0.f);
         const float yv[4] = {y.x * a.scale, y.y * a.scale, y.z * a.scale, y.w};
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
@@ -733,6 +741,7 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_train(const __grid_constant
 #pragma unroll
         for (int l = 0; l < kNrcHashLevels; ++l) {
           const uint32_t row = rows[l];
+          if (!RC_CHK(a.hash.grad + 2 * (size_t)row + 1, kChkHash)) continue;
           if (v[2 * l] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row, v[2 * l]);
           if (v[2 * l + 1] != 0.f) atomicAdd(a.hash.grad + 2 * (size_t)row + 1, v[2 * l + 1]);
         }
@@ -916,7 +925,7 @@ __global__ void k_nrc_words(const __grid_constant__ NrcWordArgs w) {
     const int64_t p = nrc_slot_probe(L.M, L.wpp, L.l2px, slot, b);
     if (p >= 0) on = __ldg(w.flag + nrc_cell(L, p, w.tile_shift, w.TX, w.TY)) != 0;
   }
-  L.word_on[slot] = on;
+  if (RC_CHK(&L.word_on[slot], kChkCache)) L.word_on[slot] = on;
 }
 
 // Training / held-out targets: row r of tile t is the tile's r-th direction
@@ -932,9 +941,11 @@ __global__ void k_nrc_targets(const __grid_constant__ NrcArgs a, const uint2* __
     const NrcLevel& L = a.lv[t.level];
     const int64_t p = t.list ? t.probe + r / t.list : t.probe;
     const int d = t.list ? __ldg(a.dlist + t.d0 + r % t.list) : t.d0 + r;
-    nrc_record_rt(vol, __ldg(L.rec + nrc_rec_index(L, p, d)), rt);
+    const uint32_t* rp = L.rec + nrc_rec_index(L, p, d);
+    nrc_record_rt(vol, RC_CHK(rp, kChkRecord) ? __ldg(rp) : kBlack, rt);
   }
-  *reinterpret_cast<float4*>(target + i * 4) = make_float4(rt[0], rt[1], rt[2], rt[3]);
+  float4* tp = reinterpret_cast<float4*>(target + i * 4);
+  if (RC_CHK(tp, kChkCache)) *tp = make_float4(rt[0], rt[1], rt[2], rt[3]);
 }
 
 // Trilinear taps of probe p of a level into the next level's probes (child
@@ -988,8 +999,10 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_heldout(const __grid_consta
   float e2 = 0.f, s2 = 0.f;
   if (r < t.n) {
     const int64_t i = (int64_t)blockIdx.x * kNrcThreads + r;
-    const float4 pr = *reinterpret_cast<const float4*>(pred + i * 4);
-    const float4 y = *reinterpret_cast<const float4*>(target + i * 4);
+    const float4* pp = reinterpret_cast<const float4*>(pred + i * 4);
+    const float4* yp = reinterpret_cast<const float4*>(target + i * 4);
+    const float4 pr = RC_CHK(pp, kChkCache) ? *pp : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 y = RC_CHK(yp, kChkCache) ? *yp : make_float4(0.f, 0.f, 0.f, 0.f);
     const float po[4] = {pr.x, pr.y, pr.z, pr.w};
     float sv[4];
     nrc_serve(po, a.scale, sv);
@@ -1032,6 +1045,7 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_heldout(const __grid_consta
   const int next = __shfl_down_sync(0xFFFFFFFFu, key, 1);
   if (r < t.n && (lane == 31 || next != key)) {
     const int64_t cell = nrc_cell(a.lv[t.level], p, a.tile_shift, a.TX, a.TY);
+    if (!RC_CHK(&num[cell], kChkCache) || !RC_CHK(&den[cell], kChkCache)) return;
     atomicAdd(&num[cell], e2);
     // the smallest normal float marks the cell as scored this solve even where
     // no light reaches its probes
@@ -1121,10 +1135,11 @@ __global__ void __launch_bounds__(128) k_level_merge_nrc(const __grid_constant__
     const int64_t off = (int64_t)d * a.P + p;
     float rv[4];
     if (walked) {
-      nrc_record_rt(a.vol, __ldg(NL.rec + nrc_rec_index(NL, p, d)), rv);
+      const uint32_t* rp = NL.rec + nrc_rec_index(NL, p, d);
+      nrc_record_rt(a.vol, RC_CHK(rp, kChkRecord) ? __ldg(rp) : kBlack, rv);
     } else {
 #pragma unroll
-      for (int ch = 0; ch < 4; ++ch) rv[ch] = __half2float(rt[ch * plane + off]);
+      for (int ch = 0; ch < 4; ++ch) rv[ch] = RC_CHK(&rt[ch * plane + off], kChkCache) ? __half2float(rt[ch * plane + off]) : 0.f;
     }
     if (!TOP && rv[3] > 0.f) {
 #pragma unroll

@@ -88,8 +88,10 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
           uint32_t* w = m.base + plane_base(m, lane, phy, phz, zc) + (g >> 5);
           const int sh = (int)(g & 31);
           const uint32_t fmask = (width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u)) << sh;
-          atomicAnd(w, ~fmask);
-          if (field) atomicOr(w, field << sh);
+          if (RC_CHK(w, kChkMask)) {
+            atomicAnd(w, ~fmask);
+            if (field) atomicOr(w, field << sh);
+          }
         }
       }
     } else if (x < Gx) {
@@ -97,6 +99,7 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
       const int64_t g = ((int64_t)yc << m.l2px) + xc;
       uint32_t* w = m.base + plane_base(m, x & (s - 1), phy, phz, zc) + (g >> 5);
       const uint32_t b = 1u << (g & 31);
+      if (!RC_CHK(w, kChkMask)) continue;
       if ((bits >> lane) & 1u) atomicOr(w, b);
       else atomicAnd(w, ~b);
     }
@@ -127,10 +130,12 @@ static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __
     bool opaque = false, emissive = false;
     if (x < Gx) {
       const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
-      uint2 v = base[idx];
+      uint2 v = RC_CHK(&base[idx], kChkVolume) ? base[idx] : make_uint2(0u, 0u);
       const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
       for (int k = 0; k < nt; ++k) {
-        const QSphere& S = sph[r.sn < 0 ? k : __ldg(slist + r.s0 + k)];
+        const int si = r.sn < 0 ? k : (RC_CHK(slist + r.s0 + k, kChkSpheres) ? __ldg(slist + r.s0 + k) : 0);
+        if (!RC_CHK(&sph[si], kChkSpheres)) continue;
+        const QSphere& S = sph[si];
         const int64_t dx = px - S.c[0], dy = py - S.c[1], dz = pz - S.c[2];
         if (dx > S.r || -dx > S.r || dy > S.r || -dy > S.r || dz > S.r || -dz > S.r) continue;
         if (dx * dx + dy * dy + dz * dz <= S.r * S.r) {
@@ -138,13 +143,14 @@ static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __
           v.y = (uint32_t)S.value.emission[2] | ((uint32_t)S.value.albedo_occ << 16);
         }
       }
-      vol[idx] = v;
+      if (RC_CHK(&vol[idx], kChkVolume)) vol[idx] = v;
       opaque = (v.y >> 31) & 1u;
       emissive = opaque && (((v.x & 0x7FFF7FFFu) | (v.y & 0x7FFFu)) != 0u);
     }
     const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
     const unsigned ebits = __ballot_sync(0xFFFFFFFFu, emissive);
-    if (lane == 0) {
+    if (lane == 0 && RC_CHK(&occ[((int64_t)z * Gy + y) * W + wx], kChkOccupancy) &&
+        RC_CHK(&emis[((int64_t)z * Gy + y) * W + wx], kChkOccupancy)) {
       occ[((int64_t)z * Gy + y) * W + wx] = bits;
       emis[((int64_t)z * Gy + y) * W + wx] = ebits;
     }
@@ -248,8 +254,9 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       const uint32_t* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * a.wpp;
       const int gs = g0 + (ay >> l2s) * Px + (ax >> l2s);
       const int q = gs >> 5;
-      lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp) ? __ldg(plane + q) : 0u;
-      hi_[u] = (zin && (unsigned)(q + 1) < (unsigned)a.wpp) ? __ldg(plane + q + 1) : 0u;
+      lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp && RC_CHK(plane + q, kChkMask)) ? __ldg(plane + q) : 0u;
+      hi_[u] = (zin && (unsigned)(q + 1) < (unsigned)a.wpp && RC_CHK(plane + q + 1, kChkMask)) ? __ldg(plane + q + 1)
+                                                                                                 : 0u;
     }
     bool stop = false;
 #pragma unroll
@@ -284,8 +291,9 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
           const int g = g0 + b;
           const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
           const int64_t row = (int64_t)vz * a.G[1] + vy;
-          const uint32_t e = __ldg(&a.emis[row * a.W + (vx >> 5)]);
-          hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * a.G[0] + vx) : kBlack;
+          const uint32_t* ep = &a.emis[row * a.W + (vx >> 5)];
+          const uint32_t e = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
+          if (RC_CHK(&hit[b], kChkShared)) hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * a.G[0] + vx) : kBlack;
         } while (nw);
       }
       if (done == 0xFFFFFFFFu) stop = true;
@@ -458,7 +466,8 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         const uint32_t* hrow = s_hit + (dl * kTileSlots + slot0) * kHitStride + lane;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          rec[i] = ((okmask >> i) & 1u) ? hrow[((i >> 1) * 16 + ((i & 1) << cl2)) * kHitStride] : kBlack;
+          const uint32_t* hp = &hrow[((i >> 1) * 16 + ((i & 1) << cl2)) * kHitStride];
+          rec[i] = ((okmask >> i) & 1u) && RC_CHK(hp, kChkShared) ? *hp : kBlack;
           missm |= (rec[i] == kMiss) << i;
           emism |= (rec[i] < kBlack) << i;
         }
@@ -474,7 +483,8 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
               const T* tile = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(up_tiles) +
                                                          (ust * 3 + ch) * tstride);
 #pragma unroll
-              for (int q = 0; q < 9; ++q) av[q] = ploader ? to_float(tile[soff[q]]) : 0.f;
+              for (int q = 0; q < 9; ++q)
+                av[q] = ploader && RC_CHK(&tile[soff[q]], kChkShared) ? to_float(tile[soff[q]]) : 0.f;
             } else {
               const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
 #pragma unroll
@@ -556,7 +566,8 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         if (!((okmask >> i) & 1u)) continue;
         const int64_t p = p0 + cstep[i];
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[i][ch];
+        for (int ch = 0; ch < 3; ++ch)
+          if (RC_CHK(&a.fluence[p * 3 + ch], kChkFluence)) a.fluence[p * 3 + ch] = acc[i][ch];
       }
     }
   }

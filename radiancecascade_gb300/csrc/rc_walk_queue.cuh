@@ -217,8 +217,10 @@ struct Walker {
       gs_[u] = gs;
       const int q0 = gs >> 5;
       const uint32_t* plane = mask + ((((pz << l2s) + py) << l2s) + px) * mzw + (zl + cz) * wpp;
-      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
-      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0) : 0u;
+      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
+                   ? __ldg(plane + q0 + 1)
+                   : 0u;
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -235,8 +237,9 @@ struct Walker {
           const int g = g0 + b;
           const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
           const int64_t row = (int64_t)vz * q.G[1] + vy;
-          const uint32_t e = __ldg(&q.emis[row * q.W + (vx >> 5)]);
-          rec[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+          const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
+          const uint32_t e = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
+          if (RC_CHK(&rec[b], kChkRecord)) rec[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
         } while (nw);
       }
       if (done == 0xFFFFFFFFu) return true;
@@ -249,7 +252,7 @@ struct Walker {
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      rec[b] = kMiss;
+      if (RC_CHK(&rec[b], kChkRecord)) rec[b] = kMiss;
     }
   }
 };
@@ -334,7 +337,7 @@ struct TableWalker {
     const int sm = (1 << l2s) - 1, Px = 1 << l2px;
     uint2 e[kBatch];
 #pragma unroll
-    for (int u = 0; u < kBatch; ++u) e[u] = u < n ? __ldg(st + u) : make_uint2(0u, 0u);
+    for (int u = 0; u < kBatch; ++u) e[u] = u < n ? (RC_CHK(st + u, kChkTable) ? __ldg(st + u) : make_uint2(0u, 0u)) : make_uint2(0u, 0u);
     int gs_[kBatch];
     uint32_t lo_[kBatch], hi_[kBatch], inr_[kBatch];
     bool ok_[kBatch];
@@ -348,8 +351,10 @@ struct TableWalker {
       gs_[u] = gs;
       const int q0 = gs >> 5;
       const uint32_t* plane = mask + (int64_t)e[u].x * mzw + zoff;
-      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp) ? __ldg(plane + q0) : 0u;
-      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp) ? __ldg(plane + q0 + 1) : 0u;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0) : 0u;
+      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
+                   ? __ldg(plane + q0 + 1)
+                   : 0u;
     }
     st += kBatch;
     n -= kBatch;
@@ -373,8 +378,10 @@ struct TableWalker {
           const int g = g0 + b;
           const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
           const int64_t row = (int64_t)vz * q.G[1] + vy;
-          const uint32_t ev = __ldg(&q.emis[row * q.W + (vx >> 5)]);
-          rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+          const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
+          const uint32_t ev = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
+          if (RC_CHK(&rec[b], kChkRecord))
+            rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
         } while (nw);
       }
       if (done == 0xFFFFFFFFu) return true;
@@ -387,7 +394,7 @@ struct TableWalker {
     while (m) {
       const int b = __ffs(m) - 1;
       m &= m - 1;
-      rec[b] = kMiss;
+      if (RC_CHK(&rec[b], kChkRecord)) rec[b] = kMiss;
     }
   }
 };
@@ -462,7 +469,7 @@ struct CoopWalker {
     uint32_t ph = 0u, pc = 0u;
     if (active) {
       const bool step_ok = sub < n;
-      const uint2 e = step_ok ? __ldg(st + sub) : make_uint2(0u, 0u);
+      const uint2 e = (step_ok && RC_CHK(st + sub, kChkTable)) ? __ldg(st + sub) : make_uint2(0u, 0u);
       ph = e.x;
       pc = e.y;
       const int cx = (int)(int8_t)(pc & 0xFFu), cy = (int)(int8_t)((pc >> 8) & 0xFFu),
@@ -481,8 +488,9 @@ struct CoopWalker {
         const int gs = g0 + cy * Px + cx;
         const int q0 = gs >> 5;
         const uint32_t* plane = mask + (int64_t)ph * mzw + (int64_t)(zl + cz) * wpp;
-        const uint32_t lo = (unsigned)q0 < (unsigned)wpp ? __ldg(plane + q0) : 0u;
-        const uint32_t hi = (unsigned)(q0 + 1) < (unsigned)wpp ? __ldg(plane + q0 + 1) : 0u;
+        const uint32_t lo = (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask) ? __ldg(plane + q0) : 0u;
+        const uint32_t hi =
+            (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask) ? __ldg(plane + q0 + 1) : 0u;
         h = __funnelshift_r(lo, hi, gs & 31) & inr & ~done;
         out = ~inr;
       }
@@ -509,8 +517,10 @@ struct CoopWalker {
         const int g = g0 + b;
         const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
         const int64_t row = (int64_t)vz * q.G[1] + vy;
-        const uint32_t ev = __ldg(&q.emis[row * q.W + (vx >> 5)]);
-        rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+        const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
+        const uint32_t ev = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
+        if (RC_CHK(&rec[b], kChkRecord))
+          rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
       } while (nw);
     }
     // group totals: probes hit, probes out of the grid, walk ended
@@ -534,7 +544,7 @@ struct CoopWalker {
   __device__ __forceinline__ void finish(int sub) {
     const uint32_t m = valid & ~hits;
     for (int b = sub; b < 32; b += G)
-      if ((m >> b) & 1u) rec[b] = kMiss;
+      if (((m >> b) & 1u) && RC_CHK(&rec[b], kChkRecord)) rec[b] = kMiss;
   }
 };
 
@@ -686,7 +696,7 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
       d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
     }
     const uint32_t* rp = &rec[(int64_t)d * slots * 32 + rbase];
-    const uint32_t r = CG ? __ldca(rp) : __ldg(rp);
+    const uint32_t r = !RC_CHK(rp, kChkRecord) ? kBlack : CG ? __ldca(rp) : __ldg(rp);
     float rv[3] = {0.f, 0.f, 0.f};
     if (r == kMiss) {
       if (!TOP) {
@@ -724,7 +734,8 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
   }
   if (L0) {
 #pragma unroll
-    for (int ch = 0; ch < 3; ++ch) a.fluence[p * 3 + ch] = acc[ch];
+    for (int ch = 0; ch < 3; ++ch)
+      if (RC_CHK(&a.fluence[p * 3 + ch], kChkFluence)) a.fluence[p * 3 + ch] = acc[ch];
   }
 }
 

@@ -177,3 +177,12 @@ def test_rc_log_prints_errors_to_stderr():
     env.pop("RC_LOG")
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, cwd=root)
     assert r.returncode == 0 and "rc[error]" not in r.stderr
+
+
+def test_ordinary_library_has_no_checked_words():
+    """rc_check_status answers RC_ERR_UNSUPPORTED in the ordinary library (the
+    checked one is librc_checked.so); it needs no GPU to say so."""
+    first, count = C.c_uint64(7), C.c_uint32(7)
+    assert F.lib().rc_check_status(0, C.byref(first), C.byref(count)) == F.RC_ERR_UNSUPPORTED
+    assert first.value == 0 and count.value == 0
+    assert "RC_CHECKED" in F.last_error()
