@@ -233,7 +233,9 @@ rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
  * the walk launch of the narrow cascades and, with the radiance cache on,
  * the cache's whole schedule).  Needs 1 + num_cascades floats.  Diagnostics:
  * the RC_LOG environment variable prints every error (1), also context
- * lifetime (2), also one line per solve (3) on stderr. */
+ * lifetime (2), also one line per solve (3) on stderr; RC_NVTX=1 wraps every
+ * solve's launches in NVTX ranges "rc_solve" / "walks", "cascade i",
+ * "radiance cache" for profilers. */
 rc_status rc_set_stage_timing(rc_context* ctx, int32_t enable);
 rc_status rc_get_stage_ms(rc_context* ctx, float* ms_out, int32_t count);
 

@@ -9,6 +9,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -443,8 +444,35 @@ namespace {
 // With the neural radiance cache on, the far levels (from its first level
 // up) come from the cache and the walk queue runs only when a near level
 // needs it.
+// NVTX ranges on the enqueueing thread (RC_NVTX=1): "rc_solve", inside it
+// "walks" and "cascade i" around the launches of each stage, so that a
+// profiler can select a cascade's kernels (ncu --nvtx-include "rc_solve/cascade 3/").
+struct NvtxRange {
+  bool on;
+  NvtxRange(bool enable, const char* name) : on(enable) {
+    if (on) nvtxRangePushA(name);
+  }
+  ~NvtxRange() {
+    if (on) nvtxRangePop();
+  }
+};
+bool nvtx_enabled() {
+  static const bool on = [] {
+    const char* e = getenv("RC_NVTX");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+const char* cascade_range_name(int i) {
+  static const char* names[kMaxCascades] = {"cascade 0", "cascade 1", "cascade 2", "cascade 3", "cascade 4",
+                                            "cascade 5", "cascade 6", "cascade 7", "cascade 8", "cascade 9"};
+  return names[i];
+}
+
 rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
   RC_CUDA(check_prepare(), "checked build: range upload");
+  const bool nv = nvtx_enabled();
+  NvtxRange solve_range(nv, "rc_solve");
   int near = c->nlev;
   if (c->timing) cudaEventRecord(c->tev[0], s);
   if (nrc_active(c)) {
@@ -454,16 +482,22 @@ rc_status enqueue_solve(rc_context* c, cudaStream_t s) {
     // the far levels' walks, where they run at all, are launched by the cache
     // (the cache's second far walk takes the near levels' walks along when
     // both use step tables: one launch balances them together)
-    if (queue_near && !nrc_walks_near(c)) launch_queue_walk(c, s, ~((1u << near) - 1u));
+    if (queue_near && !nrc_walks_near(c)) {
+      NvtxRange r(nv, "walks");
+      launch_queue_walk(c, s, ~((1u << near) - 1u));
+    }
+    NvtxRange r(nv, "radiance cache");
     rc_status st = nrc_enqueue_far(c, s);
     if (st != RC_OK) return st;
     // the cache's whole schedule counts under the top cascade
     if (c->timing)
       for (int i = c->nlev - 1; i >= near; --i) cudaEventRecord(c->tev[c->nlev - i], s);
   } else {
+    NvtxRange r(nv, "walks");
     launch_queue_walk(c, s);
   }
   for (int i = near - 1; i >= 0; --i) {
+    NvtxRange r(nv, cascade_range_name(i));
     plain_level(c, i, s);
     if (c->timing) cudaEventRecord(c->tev[c->nlev - i], s);
   }
