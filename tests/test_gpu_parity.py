@@ -89,6 +89,9 @@ def test_golden_fixtures(name, walk):
     ((32, 16, 48), 3, {}),
     ((32, 32, 32), 2, dict(spacing0=4, dir_res0=2, interval0=2, ratio=3)),
     ((48, 48, 48), 4, {}),
+    # elongated grids: 1024 voxels (the largest edge) along one axis, few along the others
+    ((1024, 32, 64), 5, {}),
+    ((32, 512, 32), 4, dict(dir_res0=6)),
 ])
 def test_other_shapes_match_oracle(grid, N, kw, walk):
     spec = R.scene_spec(grid, 12, (3, 12), 3, (1.5, 4.0), (1.0, 20.0))
