@@ -31,15 +31,18 @@ struct NrcState {
   unsigned char* img = nullptr;
   __nv_bfloat16* denc = nullptr;
   __half* rt = nullptr;
-  int64_t total_queries = 0, enum_tiles = 0;
-  // tiles of the sample probes (all their directions), grouped by phase; a
-  // tile's slot is its probe's index in the phase
+  int64_t enum_tiles = 0;
+  // sample tiles grouped by phase: every far probe with the directions of the
+  // phase (rows of up to 128; short direction lists pack several probes); a
+  // tile's slot is its first probe's index in the phase
   NrcTile* tiles = nullptr;
   std::vector<NrcTile> h_tiles;
   std::vector<uint8_t> probe_tile;  // tiles that hold a far probe
   std::vector<int64_t> tile_begin;
   int32_t* dlist = nullptr;  // directions of the sample tiles, per level and phase
   int64_t dlist_base[kMaxCascades]{};  // a level's directions in dlist
+  // per level and phase pair q: start (in the level's directions) and length
+  // of the run of phases q and q + nph/2 in dlist
   std::vector<std::vector<int64_t>> pair_start = std::vector<std::vector<int64_t>>(kMaxCascades),
                                     pair_len = std::vector<std::vector<int64_t>>(kMaxCascades);
   int64_t max_tiles2 = 0, max_held = 0;
@@ -468,7 +471,6 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
     dirs += c->geom[i].ndirs;
     n->total_probes += c->geom[i].probes();
   }
-  n->total_queries = queries;
   if ((s = dev_alloc((void**)&n->denc, dirs * kNrcDirFeat * 2, "direction features")) != RC_OK) return fail(s);
   if ((s = dev_alloc((void**)&n->rt, queries * 4 * 2, "cached (R, T)")) != RC_OK) return fail(s);
   {
