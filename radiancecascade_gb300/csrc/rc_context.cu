@@ -335,6 +335,24 @@ rc_status check_device_error(rc_context* c, const char* fn) {
   return RC_OK;
 }
 
+// A level kernel that may start while the one before it in the stream
+// finishes (programmatic stream serialization): it waits on the device
+// (grid_dep_wait) before it reads what that kernel wrote.
+template <typename... KArgs, typename... Args>
+void launch_overlapped(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 template <typename T, bool L0, bool TOP>
 void launch_one(const rc_context* c, int level, cudaStream_t s) {
   const LevelArgs& a = c->args[level];
@@ -344,7 +362,8 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
       const unsigned groups = L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2);  // two parent texels per block
       if (!L0 && !TOP && c->tma_up[level]) {
         const size_t smem = bits_up_smem(up_tile_stride(a.up_rows, a.UM[0], (int)sizeof(T)));
-        k_level_bits_up<T><<<(unsigned)a.tiles * groups, kBitsThreads, smem, s>>>(a, c->tmap_up[level], c->err);
+        launch_overlapped(k_level_bits_up<T>, dim3((unsigned)a.tiles * groups), dim3(kBitsThreads), smem, s, a,
+                          c->tmap_up[level], c->err);
       } else {
         k_level_bits<T, L0, TOP><<<(unsigned)a.tiles * groups, kBitsThreads, kBitsSmem, s>>>(a);
       }
@@ -358,8 +377,8 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
         // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
         const size_t stage =
             3 * (((size_t)(kL0Planes + 1) * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
-        k_level0_tma<T, kL0Planes><<<blocks, kL0Threads, kL0Stages * stage + 8 * kL0Stages + 128, s>>>(
-            a, c->tma0, c->tma0_py, c->err);
+        launch_overlapped(k_level0_tma<T, kL0Planes>, dim3(blocks), dim3(kL0Threads),
+                          kL0Stages * stage + 8 * kL0Stages + 128, s, a, c->tma0, c->tma0_py, c->err);
       }
       break;
     }
@@ -372,7 +391,8 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
     }
     case kModeQueue: {
       dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2));
-      k_level_merge<T, L0, TOP><<<grid, threads, 0, s>>>(a, c->rec_level[level], c->rec_slots[level]);
+      launch_overlapped(k_level_merge<T, L0, TOP>, grid, dim3(threads), 0, s, a,
+                        (const uint32_t*)c->rec_level[level], (int)c->rec_slots[level]);
       break;
     }
     default: {
@@ -556,7 +576,6 @@ void setup_queue(rc_context* c, uint32_t* recs, unsigned long long* counter) {
   QueueArgs& q = c->qargs;
   memset(&q, 0, sizeof q);
   c->qcounter = counter;
-  q.emis = c->emis;
   q.counter = counter;
   for (int a = 0; a < 3; ++a) q.G[a] = c->p.grid[a];
   q.W = c->W;
@@ -684,7 +703,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
   if ((s = dev_alloc((void**)&c->emis, (size_t)c->W * p->grid[1] * p->grid[2] * 4, "emissive bits")) != RC_OK)
     return fail(s);
   {
-    // Decimated opacity per level (bit-parallel walk).
+    // Decimated opacity and emissive bits per level (bit-parallel walk).
     const bool force_scalar = getenv("RC_WALK") && strcmp(getenv("RC_WALK"), "scalar") == 0;
     int64_t total = 0;
     int64_t off[kMaxCascades];
@@ -697,8 +716,9 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
       off[i] = total;
       if (mg.bits) total += (mg.words + 63) & ~(int64_t)63;
     }
-    if (total && (s = dev_alloc((void**)&c->masks, total * 4, "decimated opacity")) != RC_OK) return fail(s);
-    if (total && (e = cudaMemset(c->masks, 0, total * 4)) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
+    if (total && (s = dev_alloc((void**)&c->masks, total * 8, "decimated opacity and emission")) != RC_OK)
+      return fail(s);
+    if (total && (e = cudaMemset(c->masks, 0, total * 8)) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
     for (int i = 0; i < c->nlev; ++i) {
       if (!c->bits_level[i]) continue;
       const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
@@ -1516,7 +1536,7 @@ __global__ void k_masks_from_volume(const uint2* __restrict__ vol, uint32_t* __r
       occ[((int64_t)z * Gy + y) * W + wx] = bits;
       emis[((int64_t)z * Gy + y) * W + wx] = ebits;
     }
-    update_masks(ms, lane, wx, x, y, z, Gx, bits);
+    update_masks(ms, lane, wx, x, y, z, Gx, bits, ebits);
   }
 }
 
@@ -1575,7 +1595,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     v.bits_level[i] = mgs[i].bits;
     v.mode[i] = (i == 0 && level0_direct(*p, v.geom[0], force_scalar)) ? kModeDirect0 : mgs[i].mode;
     v.rec_slots[i] = v.geom[i].M[2] * mgs[i].wpp;
-    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 4);
+    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 8);
   }
   mask_bytes = off - mask_begin;
   size_t avg_off[kMaxCascades] = {};
@@ -1657,7 +1677,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     while ((1 << l2s) < g.spacing) ++l2s;
     if (v.bits_level[i]) {
       MaskLevel& m = v.mset.lv[v.mset.n++];
-      m.base = reinterpret_cast<uint32_t*>(scratch + mask_off[i]);
+      m.base = reinterpret_cast<uint2*>(scratch + mask_off[i]);
       m.l2s = l2s;
       for (int ax = 0; ax < 3; ++ax) m.M[ax] = g.M[ax];
       m.l2px = mgs[i].l2px;

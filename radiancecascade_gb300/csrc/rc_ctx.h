@@ -34,7 +34,7 @@ struct rc_context {
   uint32_t* occ = nullptr;   // opacity bits
   uint32_t* emis = nullptr;  // emissive bits (opaque with nonzero emission)
   int W = 0;                 // words per x row
-  uint32_t* masks = nullptr; // decimated opacity of the levels that walk bit-parallel
+  uint2* masks = nullptr;    // decimated (opacity, emissive) bits of the levels that walk bit-parallel
   rcx::MaskSet mset{};
   bool bits_level[rcx::kMaxCascades]{};   // level has decimated opacity
   int mode[rcx::kMaxCascades]{};          // how the level is solved (kMode*)

@@ -74,7 +74,7 @@ __device__ __forceinline__ float to_float(float v) { return v; }
 __device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
 
 struct LevelArgs {
-  const uint32_t* mask;  // this level's decimated opacity (bit-parallel walk)
+  const uint2* mask;     // this level's decimated (opacity, emissive) bits (bit-parallel walk)
   const uint32_t* emis;  // full-resolution emissive bits, same layout as occ
   int32_t l2s;           // log2(spacing)
   int32_t l2px;          // log2 of the decimated plane row pitch

@@ -706,7 +706,6 @@ rc_status rc_nrc_enable(rc_context* c, const rc_nrc_params* prm) {
       return fail(s);
     QueueArgs& fq = n->fq;
     memset(&fq, 0, sizeof fq);
-    fq.emis = c->emis;
     fq.counter = n->fcounter;
     for (int a3 = 0; a3 < 3; ++a3) fq.G[a3] = c->p.grid[a3];
     fq.W = c->W;

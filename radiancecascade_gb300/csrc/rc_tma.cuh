@@ -19,6 +19,16 @@ __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialization may start while the kernel before it in the stream still
+// runs; grid_dep_wait() returns once that kernel has completed and its
+// writes are visible (at once when the launch was ordinary).
+// grid_dep_release() lets the next such kernel start; a kernel calls it only
+// after its own wait, so a kernel that starts early still finds every kernel
+// before its predecessor complete.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }

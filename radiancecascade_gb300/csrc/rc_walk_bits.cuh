@@ -14,7 +14,10 @@
 //   each (phase, zc) plane of the coarse grid is a row-major bit array with a
 //   power-of-two row pitch Px >= Mx bits, packed into wpp = ceil(My*Px/32)
 //   words:  mask[phz][phy][phx][zc][word];  bit g = yc*Px + xc of the plane
-//   is the opacity of voxel (xc*s + phx, yc*s + phy, zc*s + phz).
+//   is the opacity of voxel (xc*s + phx, yc*s + phy, zc*s + phz).  Words are
+//   uint2 pairs: .x the opacity bits, .y the emissive bits of the same voxels
+//   (an emissive voxel is opaque), so a walk that hits a voxel knows from the
+//   same load whether to record its index or kBlack.
 // Every coarse shift (cx, cy) is a shift of the plane by cy*Px + cx bits, so
 // any Mx uses all 32 bits of a lane.
 #pragma once
@@ -33,7 +36,7 @@ constexpr uint32_t kBlack = 0xFFFFFFFEu;  // opaque voxel without emission
 constexpr size_t kBitsSmem = sizeof(uint32_t) * kTileDirs * kTileSlots * kHitStride;
 
 struct MaskLevel {
-  uint32_t* base;
+  uint2* base;  // (opacity, emissive) word pairs
   int32_t l2s;
   int32_t M[3];
   int32_t l2px;  // log2 of the plane row pitch Px
@@ -65,13 +68,14 @@ __device__ __forceinline__ uint32_t range_bits(int lo, int hi) {
   return upto & ~((1u << lo) - 1u);
 }
 
-// Updates every level's decimated opacity for the 32 voxels x = 32*wx + lane
-// of row (y, z); `bits` is the warp's opacity ballot.  The coarse cells a
+// Updates every level's decimated opacity and emissive bits for the 32
+// voxels x = 32*wx + lane of row (y, z); `bits` and `ebits` are the warp's
+// opacity and emissive ballots.  The coarse cells a
 // warp touches in one (level, phase) plane form one bit field that no other
 // warp writes, so clear-then-set is race free (a region processed twice
 // writes the same values).
 __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx, int x, int y, int z, int Gx,
-                                             uint32_t bits) {
+                                             uint32_t bits, uint32_t ebits) {
   for (int i = 0; i < ms.n; ++i) {
     const MaskLevel& m = ms.lv[i];
     const int s = 1 << m.l2s;
@@ -82,26 +86,35 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
         const int xc0 = (32 * wx) >> m.l2s;
         const int width = min(per, m.M[0] - xc0);
         if (width > 0) {
-          uint32_t field = 0;
-          for (int j = 0; j < width; ++j) field |= ((bits >> (lane + j * s)) & 1u) << j;
+          uint32_t field = 0, efield = 0;
+          for (int j = 0; j < width; ++j) {
+            field |= ((bits >> (lane + j * s)) & 1u) << j;
+            efield |= ((ebits >> (lane + j * s)) & 1u) << j;
+          }
           const int64_t g = ((int64_t)yc << m.l2px) + xc0;
-          uint32_t* w = m.base + plane_base(m, lane, phy, phz, zc) + (g >> 5);
+          uint2* w2 = m.base + plane_base(m, lane, phy, phz, zc) + (g >> 5);
+          uint32_t* w = reinterpret_cast<uint32_t*>(w2);
           const int sh = (int)(g & 31);
           const uint32_t fmask = (width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u)) << sh;
-          if (RC_CHK(w, kChkMask)) {
+          if (RC_CHK(w2, kChkMask)) {
             atomicAnd(w, ~fmask);
             if (field) atomicOr(w, field << sh);
+            atomicAnd(w + 1, ~fmask);
+            if (efield) atomicOr(w + 1, efield << sh);
           }
         }
       }
     } else if (x < Gx) {
       const int xc = x >> m.l2s;
       const int64_t g = ((int64_t)yc << m.l2px) + xc;
-      uint32_t* w = m.base + plane_base(m, x & (s - 1), phy, phz, zc) + (g >> 5);
+      uint2* w2 = m.base + plane_base(m, x & (s - 1), phy, phz, zc) + (g >> 5);
+      uint32_t* w = reinterpret_cast<uint32_t*>(w2);
       const uint32_t b = 1u << (g & 31);
-      if (!RC_CHK(w, kChkMask)) continue;
+      if (!RC_CHK(w2, kChkMask)) continue;
       if ((bits >> lane) & 1u) atomicOr(w, b);
       else atomicAnd(w, ~b);
+      if ((ebits >> lane) & 1u) atomicOr(w + 1, b);
+      else atomicAnd(w + 1, ~b);
     }
   }
 }
@@ -154,7 +167,7 @@ static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __
       occ[((int64_t)z * Gy + y) * W + wx] = bits;
       emis[((int64_t)z * Gy + y) * W + wx] = ebits;
     }
-    update_masks(ms, lane, wx, x, y, z, Gx, bits);
+    update_masks(ms, lane, wx, x, y, z, Gx, bits, ebits);
   }
 }
 
@@ -186,7 +199,9 @@ __device__ __forceinline__ Tile tile_of(const LevelArgs& a, int tile) {
 }
 
 // Phase 1: walk the interval of direction `di` for the 32 probes of plane
-// word `wl` in coarse plane `zl`; record each probe's first opaque voxel.
+// word `wl` in coarse plane `zl`; record each probe's first opaque voxel in
+// hit[0..31] (every entry is written: the voxel index of an emissive hit at
+// once, kBlack or kMiss for the others when the walk ends).
 // The voxel sequence does not depend on what is loaded, so the walk runs in
 // batches of kWalkBatch steps: the mask words of a whole batch are requested
 // before the first of them is tested.  Level 0's interval is one voxel long,
@@ -208,9 +223,8 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
     valid = range_bits(0, Mx) * a.rep;  // the row pattern replicated over the word's 32/Px rows
     valid &= range_bits(0, (My - wy0) * Px);
   }
-  if (valid == 0u) return;
-  uint32_t done = ~valid;
-  const uint32_t* zbase = a.mask + (int64_t)zl * a.wpp;
+  uint32_t done = ~valid, hits = 0u, ehits = 0u;
+  const uint2* zbase = a.mask + (int64_t)zl * a.wpp;
   const int64_t phase_stride = (int64_t)Mz * a.wpp;
   int ax = h + di.start_off[0], ay = h + di.start_off[1], az = h + di.start_off[2];
   int tx = di.first_T[0], ty = di.first_T[1], tz = di.first_T[2];
@@ -218,9 +232,9 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
   const int dx = di.step_T[0], dy = di.step_T[1], dz = di.step_T[2];
   int k = di.steps;
   bool first = test_start;
-  for (;;) {
+  for (; valid != 0u;) {
     int bx_[kWalkBatch], by_[kWalkBatch], bz_[kWalkBatch];
-    uint32_t lo_[kWalkBatch], hi_[kWalkBatch];
+    uint2 lo_[kWalkBatch], hi_[kWalkBatch];
     bool ok_[kWalkBatch];
 #pragma unroll
     for (int u = 0; u < kWalkBatch; ++u) {
@@ -251,12 +265,13 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       const bool zin = step_ok && (unsigned)zc < (unsigned)Mz;
       ok_[u] = step_ok;
       const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
-      const uint32_t* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * a.wpp;
+      const uint2* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * a.wpp;
       const int gs = g0 + (ay >> l2s) * Px + (ax >> l2s);
       const int q = gs >> 5;
-      lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp && RC_CHK(plane + q, kChkMask)) ? __ldg(plane + q) : 0u;
+      lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp && RC_CHK(plane + q, kChkMask)) ? __ldg(plane + q)
+                                                                                     : make_uint2(0u, 0u);
       hi_[u] = (zin && (unsigned)(q + 1) < (unsigned)a.wpp && RC_CHK(plane + q + 1, kChkMask)) ? __ldg(plane + q + 1)
-                                                                                                 : 0u;
+                                                                                                 : make_uint2(0u, 0u);
     }
     bool stop = false;
 #pragma unroll
@@ -281,25 +296,32 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       }
       done |= ~inr;
       const int gs = g0 + cy * Px + cx;
-      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs & 31) & ~done;
+      const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs & 31) & ~done;
       if (nw) {
         done |= nw;
-        const int vz = (zl << l2s) + bz_[u];
-        do {
-          const int b = __ffs(nw) - 1;
-          nw &= nw - 1;
-          const int g = g0 + b;
-          const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
-          const int64_t row = (int64_t)vz * a.G[1] + vy;
-          const uint32_t* ep = &a.emis[row * a.W + (vx >> 5)];
-          const uint32_t e = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
-          if (RC_CHK(&hit[b], kChkShared)) hit[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * a.G[0] + vx) : kBlack;
-        } while (nw);
+        hits |= nw;
+        uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs & 31) & nw;
+        if (ew) {  // emissive hits (rare): the voxel's index
+          ehits |= ew;
+          const int vz = (zl << l2s) + bz_[u];
+          do {
+            const int b = __ffs(ew) - 1;
+            ew &= ew - 1;
+            const int g = g0 + b;
+            const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
+            const int64_t row = (int64_t)vz * a.G[1] + vy;
+            if (RC_CHK(&hit[b], kChkShared)) hit[b] = (uint32_t)(row * a.G[0] + vx);
+          } while (ew);
+        }
       }
       if (done == 0xFFFFFFFFu) stop = true;
     }
     if (stop) break;
   }
+  // the other probes: opaque without emission, or no hit (probes that do not exist included)
+#pragma unroll 8
+  for (int b = 0; b < 32; ++b)
+    if (!((ehits >> b) & 1u) && RC_CHK(&hit[b], kChkShared)) hit[b] = ((hits >> b) & 1u) ? kBlack : kMiss;
 }
 
 
@@ -316,7 +338,9 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
 }
 
 // Directions staged ahead in k_level_bits_up: the first kUpStages copies are
-// issued before the walk phase, so the walks hide them.
+// issued at the end of the walk phase (the walk reads only the scene, so with
+// a programmatic launch it runs while the previous level's kernel finishes;
+// the copies wait for that kernel).
 constexpr int kUpStages = 4;
 
 // Bytes of one channel tile of the next level's box staged per direction
@@ -344,7 +368,9 @@ __host__ __device__ __forceinline__ uint32_t up_tile_stride(int up_rows, int umx
 // TM: the next level's values come from shared memory instead: per direction
 // one TMA copy per channel of the block's parent box (all UM[0] columns,
 // up_rows rows, 3 planes) through `tmap` into s_up (128-byte aligned,
-// kUpStages stages of three channel tiles, then kUpStages mbarriers).
+// kUpStages stages of three channel tiles, then kUpStages mbarriers).  Only
+// thread 0, which issues the copies, waits for the launch that wrote them
+// (grid_dep_wait); the block then lets the next level's launch start.
 template <typename T, bool L0, bool TOP, bool CG, bool TM = false>
 __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, uint32_t* s_hit,
                                                  const CUtensorMap* tmap = nullptr, unsigned char* s_up = nullptr,
@@ -412,7 +438,6 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
       for (int jj = 0; jj < 3; ++jj)
         soff[k * 3 + jj] = ((min(max(t.z0 / 2 - 1 + k, 0), a.UM[2] - 1) - zs) * BY +
                             (min(max(y0 / 2 - 1 + jj, 0), a.UM[1] - 1) - ys)) * a.UM[0] + qx;
-    const uint32_t tbytes = up_tile_bytes(BY, a.UM[0], (int)sizeof(T));
     tstride = up_tile_stride(BY, a.UM[0], (int)sizeof(T));
     up_tiles = reinterpret_cast<T*>(s_up);
     ubar = reinterpret_cast<uint64_t*>(s_up + kUpStages * 3 * tstride);
@@ -422,7 +447,16 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
       mbar_fence_init();
     }
     __syncthreads();
-    if (tid == 0) {
+  }
+  // TM: the walk phase reads only the scene; the next level's values are
+  // staged after it, once the launch that wrote them has completed
+  auto stage_first = [&]() {
+    if (TM && tid == 0) {
+      grid_dep_wait();
+      const int BY = a.up_rows;
+      const int ys = max(0, min(((t.w0 << 5) >> a.l2px) / 2 - 1, a.UM[1] - BY));
+      const int zs = max(0, min(t.z0 / 2 - 1, a.UM[2] - 3));
+      const uint32_t tbytes = up_tile_bytes(BY, a.UM[0], (int)sizeof(T));
       for (int k = 0; k < kUpStages && k < 8; ++k) {
         const int d = block_dir<L0>(a, 0, dgroup, k);
         mbar_arrive_expect_tx(&ubar[k], 3u * tbytes);
@@ -432,7 +466,7 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
                       (ch * a.ndirs + d) * a.UM[2] + zs, &ubar[k]);
       }
     }
-  }
+  };
 
   float acc[4][3];
 #pragma unroll
@@ -442,16 +476,19 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
     // ---- phase 1: lane = word of the tile, warp = direction
     {
       uint32_t* hit = s_hit + (warp * kTileSlots + lane) * kHitStride;
-#pragma unroll 8
-      for (int b = 0; b < 32; ++b) hit[b] = kMiss;
       const int d = block_dir<L0>(a, pass, dgroup, warp);
       const int zl = t.z0 + lane / t.TW, wl = t.w0 + lane % t.TW;
       if (d >= 0 && lane < t.TZ * t.TW && zl < Mz && wl < a.wpp) {
         const DirInfo di = a.dirs[d];
-        walk_word<L0 ? 2 : 4>(a, di, zl, wl, L0, hit);
+        walk_word<L0 ? 2 : 4>(a, di, zl, wl, L0, hit);  // writes all 32 entries
+      } else {
+#pragma unroll 8
+        for (int b = 0; b < 32; ++b) hit[b] = kMiss;
       }
     }
+    if (TM && pass == 0) stage_first();
     __syncthreads();
+    if (TM && pass == 0) grid_dep_release();
     // ---- phase 2
     if (WIDE) {
 #pragma unroll 1

@@ -25,7 +25,7 @@
 namespace rcx {
 
 struct QueueLevel {
-  const uint32_t* mask;
+  const uint2* mask;  // decimated (opacity, emissive) word pairs
   const DirInfo* dirs;
   uint32_t* rec;
   int64_t item_begin;  // first queue item of this level
@@ -67,7 +67,6 @@ __device__ __forceinline__ void queue_item(const QueueLevel& L, int64_t r, int& 
 }
 
 struct QueueArgs {
-  const uint32_t* emis;
   unsigned long long* counter;  // zeroed before every launch
   int64_t total;                // items over all levels
   int32_t G[3];
@@ -77,6 +76,28 @@ struct QueueArgs {
   QueueLevel lv[kMaxCascades];
 };
 
+// The records of one item when its walk ends: emissive hits already hold
+// their voxel index (written at the hit); every other entry gets kBlack (hit
+// without emission) or kMiss, four entries per 16-byte store.  rec is 128-byte
+// aligned (32 entries per item from an aligned base); entries of probes that
+// do not exist get kMiss.
+__device__ __forceinline__ void write_records(uint32_t* rec, uint32_t valid, uint32_t hits, uint32_t ehits) {
+  uint4* r4 = reinterpret_cast<uint4*>(rec);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (!((valid >> (4 * j)) & 0xFu)) continue;
+    const uint32_t h4 = (hits >> (4 * j)) & 0xFu, e4 = (ehits >> (4 * j)) & 0xFu;
+    uint4 old = make_uint4(0u, 0u, 0u, 0u);
+    if (e4 && RC_CHK(&r4[j], kChkRecord)) old = r4[j];  // this lane's own writes
+    uint4 v;
+    v.x = (e4 & 1u) ? old.x : (h4 & 1u) ? kBlack : kMiss;
+    v.y = (e4 & 2u) ? old.y : (h4 & 2u) ? kBlack : kMiss;
+    v.z = (e4 & 4u) ? old.z : (h4 & 4u) ? kBlack : kMiss;
+    v.w = (e4 & 8u) ? old.w : (h4 & 8u) ? kBlack : kMiss;
+    if (RC_CHK(&r4[j], kChkRecord)) r4[j] = v;
+  }
+}
+
 // One lane's walk of one queue item, advanced kBatch steps at a time.  The
 // voxel offset a = (cell c, phase ph) per axis is kept split (a = c s + ph):
 // a step moves one phase by +-1 and only when it wraps does the coarse cell
@@ -84,12 +105,12 @@ struct QueueArgs {
 // (inr) and whether the z plane exists (zin), which are therefore recomputed
 // only then.
 struct Walker {
-  const uint32_t* mask;
+  const uint2* mask;
   uint32_t* rec;
   int l2s, l2px, wpp, Mx, My, Mz;
   uint32_t rep;
   int zl, g0, wy0, wx0;
-  uint32_t valid, done, hits;
+  uint32_t valid, done, hits, ehits;
   int ax, ay, az, tx, ty, tz, k;
   int sx, sy, sz, dx, dy, dz;
   int px, py, pz, cx, cy, cz;  // phase and coarse cell of the current offset
@@ -140,6 +161,7 @@ struct Walker {
     rec = L.rec + ((int64_t)d * L.slots + slot) * 32;
     done = ~valid;
     hits = 0u;
+    ehits = 0u;
     const DirInfo di = L.dirs[d];
     const int h = 1 << (l2s - 1);
     ax = h + di.start_off[0];
@@ -173,7 +195,8 @@ struct Walker {
     const int sm = (1 << l2s) - 1, Px = 1 << l2px;
     const int mzw = Mz * wpp;  // words per phase
     int bx_[kBatch], by_[kBatch], bz_[kBatch], gs_[kBatch];
-    uint32_t lo_[kBatch], hi_[kBatch], inr_[kBatch];
+    uint2 lo_[kBatch], hi_[kBatch];
+    uint32_t inr_[kBatch];
     bool ok_[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -216,59 +239,55 @@ struct Walker {
       const int gs = g0 + cy * Px + cx;
       gs_[u] = gs;
       const int q0 = gs >> 5;
-      const uint32_t* plane = mask + ((((pz << l2s) + py) << l2s) + px) * mzw + (zl + cz) * wpp;
-      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0) : 0u;
+      const uint2* plane = mask + ((((pz << l2s) + py) << l2s) + px) * mzw + (zl + cz) * wpp;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0)
+                                                                                       : make_uint2(0u, 0u);
       hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
                    ? __ldg(plane + q0 + 1)
-                   : 0u;
+                   : make_uint2(0u, 0u);
     }
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
       if (!ok_[u]) return true;  // interval finished, or the walk left the grid in z
       done |= ~inr_[u];
-      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs_[u] & 31) & ~done;
+      const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs_[u] & 31) & ~done;
       if (nw) {
         done |= nw;
         hits |= nw;
-        const int vz = (zl << l2s) + bz_[u];
-        do {
-          const int b = __ffs(nw) - 1;
-          nw &= nw - 1;
-          const int g = g0 + b;
-          const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
-          const int64_t row = (int64_t)vz * q.G[1] + vy;
-          const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
-          const uint32_t e = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
-          if (RC_CHK(&rec[b], kChkRecord)) rec[b] = ((e >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
-        } while (nw);
+        uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs_[u] & 31) & nw;
+        if (ew) {  // emissive hits (rare): the voxel's index
+          ehits |= ew;
+          const int vz = (zl << l2s) + bz_[u];
+          do {
+            const int b = __ffs(ew) - 1;
+            ew &= ew - 1;
+            const int g = g0 + b;
+            const int vx = ((g & (Px - 1)) << l2s) + bx_[u], vy = ((g >> l2px) << l2s) + by_[u];
+            const int64_t row = (int64_t)vz * q.G[1] + vy;
+            if (RC_CHK(&rec[b], kChkRecord)) rec[b] = (uint32_t)(row * q.G[0] + vx);
+          } while (ew);
+        }
       }
       if (done == 0xFFFFFFFFu) return true;
     }
     return false;
   }
 
-  __device__ __forceinline__ void finish() {
-    uint32_t m = valid & ~hits;
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      if (RC_CHK(&rec[b], kChkRecord)) rec[b] = kMiss;
-    }
-  }
+  __device__ __forceinline__ void finish() { write_records(rec, valid, hits, ehits); }
 };
 
 // The same walk driven by a level's step table instead of its own DDA: a step
 // is one 8-byte load (shared by the lanes on the same direction) and the
 // per-cell state changes only when the table's coarse cell does.
 struct TableWalker {
-  const uint32_t* mask;
+  const uint2* mask;
   uint32_t* rec;
   const uint2* st;  // next step
   int n;            // steps left
   int l2s, l2px, wpp, Mx, My, Mz, mzw;
   uint32_t rep;
   int zl, g0, wy0, wx0;
-  uint32_t valid, done, hits;
+  uint32_t valid, done, hits, ehits;
   uint32_t cell;   // packed coarse cell of the current step
   int gcell;       // cy * Px + cx
   int64_t zoff;    // (zl + cz) * wpp
@@ -324,6 +343,7 @@ struct TableWalker {
     rec = L.rec + ((int64_t)d * L.slots + slot) * 32;
     done = ~valid;
     hits = 0u;
+    ehits = 0u;
     const int b0 = __ldg(L.step_begin + d);
     st = L.steps + b0;
     n = __ldg(L.step_begin + d + 1) - b0;
@@ -339,7 +359,8 @@ struct TableWalker {
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) e[u] = u < n ? (RC_CHK(st + u, kChkTable) ? __ldg(st + u) : make_uint2(0u, 0u)) : make_uint2(0u, 0u);
     int gs_[kBatch];
-    uint32_t lo_[kBatch], hi_[kBatch], inr_[kBatch];
+    uint2 lo_[kBatch], hi_[kBatch];
+    uint32_t inr_[kBatch];
     bool ok_[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
@@ -350,11 +371,12 @@ struct TableWalker {
       const int gs = g0 + gcell;
       gs_[u] = gs;
       const int q0 = gs >> 5;
-      const uint32_t* plane = mask + (int64_t)e[u].x * mzw + zoff;
-      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0) : 0u;
+      const uint2* plane = mask + (int64_t)e[u].x * mzw + zoff;
+      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0)
+                                                                                       : make_uint2(0u, 0u);
       hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
                    ? __ldg(plane + q0 + 1)
-                   : 0u;
+                   : make_uint2(0u, 0u);
     }
     st += kBatch;
     n -= kBatch;
@@ -362,41 +384,34 @@ struct TableWalker {
     for (int u = 0; u < kBatch; ++u) {
       if (!ok_[u]) return true;  // table finished, or the walk left the grid in z
       done |= ~inr_[u];
-      uint32_t nw = __funnelshift_r(lo_[u], hi_[u], gs_[u] & 31) & ~done;
+      const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs_[u] & 31) & ~done;
       if (nw) {
         done |= nw;
         hits |= nw;
-        // the step's voxel offset from its table entry
-        const uint32_t ph = e[u].x, pc = e[u].y;
-        const int bx = ((int)(int8_t)(pc & 0xFFu) << l2s) + (int)(ph & sm);
-        const int by = ((int)(int8_t)((pc >> 8) & 0xFFu) << l2s) + (int)((ph >> l2s) & sm);
-        const int bz = ((int)(int8_t)((pc >> 16) & 0xFFu) << l2s) + (int)(ph >> (2 * l2s));
-        const int vz = (zl << l2s) + bz;
-        do {
-          const int b = __ffs(nw) - 1;
-          nw &= nw - 1;
-          const int g = g0 + b;
-          const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
-          const int64_t row = (int64_t)vz * q.G[1] + vy;
-          const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
-          const uint32_t ev = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
-          if (RC_CHK(&rec[b], kChkRecord))
-            rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
-        } while (nw);
+        uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs_[u] & 31) & nw;
+        if (ew) {  // emissive hits (rare): the voxel's index, from the step's table entry
+          ehits |= ew;
+          const uint32_t ph = e[u].x, pc = e[u].y;
+          const int bx = ((int)(int8_t)(pc & 0xFFu) << l2s) + (int)(ph & sm);
+          const int by = ((int)(int8_t)((pc >> 8) & 0xFFu) << l2s) + (int)((ph >> l2s) & sm);
+          const int bz = ((int)(int8_t)((pc >> 16) & 0xFFu) << l2s) + (int)(ph >> (2 * l2s));
+          const int vz = (zl << l2s) + bz;
+          do {
+            const int b = __ffs(ew) - 1;
+            ew &= ew - 1;
+            const int g = g0 + b;
+            const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
+            const int64_t row = (int64_t)vz * q.G[1] + vy;
+            if (RC_CHK(&rec[b], kChkRecord)) rec[b] = (uint32_t)(row * q.G[0] + vx);
+          } while (ew);
+        }
       }
       if (done == 0xFFFFFFFFu) return true;
     }
     return n <= 0;
   }
 
-  __device__ __forceinline__ void finish() {
-    uint32_t m = valid & ~hits;
-    while (m) {
-      const int b = __ffs(m) - 1;
-      m &= m - 1;
-      if (RC_CHK(&rec[b], kChkRecord)) rec[b] = kMiss;
-    }
-  }
+  __device__ __forceinline__ void finish() { write_records(rec, valid, hits, ehits); }
 };
 
 constexpr int kQueueThreads = 256;
@@ -414,7 +429,7 @@ constexpr int kQueueThreads = 256;
 // ---------------------------------------------------------------------------
 template <int G>
 struct CoopWalker {
-  const uint32_t* mask;
+  const uint2* mask;
   uint32_t* rec;
   const uint2* st;
   int n;  // steps left
@@ -464,7 +479,7 @@ struct CoopWalker {
   // One round of G steps; every lane of the warp calls it (inactive groups
   // with active = false).  Returns true when this group's item is finished.
   __device__ __forceinline__ bool round(const QueueArgs& q, bool active, int sub) {
-    uint32_t h = 0u, out = 0u;
+    uint32_t h = 0u, he = 0u, out = 0u;  // he: emissive bits of the step's voxels
     bool stop = false;
     uint32_t ph = 0u, pc = 0u;
     if (active) {
@@ -487,11 +502,13 @@ struct CoopWalker {
       if (ok) {
         const int gs = g0 + cy * Px + cx;
         const int q0 = gs >> 5;
-        const uint32_t* plane = mask + (int64_t)ph * mzw + (int64_t)(zl + cz) * wpp;
-        const uint32_t lo = (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask) ? __ldg(plane + q0) : 0u;
-        const uint32_t hi =
-            (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask) ? __ldg(plane + q0 + 1) : 0u;
-        h = __funnelshift_r(lo, hi, gs & 31) & inr & ~done;
+        const uint2* plane = mask + (int64_t)ph * mzw + (int64_t)(zl + cz) * wpp;
+        const uint2 lo =
+            (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask) ? __ldg(plane + q0) : make_uint2(0u, 0u);
+        const uint2 hi = (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask) ? __ldg(plane + q0 + 1)
+                                                                                              : make_uint2(0u, 0u);
+        h = __funnelshift_r(lo.x, hi.x, gs & 31) & inr & ~done;
+        he = __funnelshift_r(lo.y, hi.y, gs & 31);
         out = ~inr;
       }
     }
@@ -517,10 +534,7 @@ struct CoopWalker {
         const int g = g0 + b;
         const int vx = ((g & (Px - 1)) << l2s) + bx, vy = ((g >> l2px) << l2s) + by;
         const int64_t row = (int64_t)vz * q.G[1] + vy;
-        const uint32_t* ep = &q.emis[row * q.W + (vx >> 5)];
-        const uint32_t ev = RC_CHK(ep, kChkOccupancy) ? __ldg(ep) : 0u;
-        if (RC_CHK(&rec[b], kChkRecord))
-          rec[b] = ((ev >> (vx & 31)) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
+        if (RC_CHK(&rec[b], kChkRecord)) rec[b] = ((he >> b) & 1u) ? (uint32_t)(row * q.G[0] + vx) : kBlack;
       } while (nw);
     }
     // group totals: probes hit, probes out of the grid, walk ended
@@ -573,6 +587,8 @@ __device__ __forceinline__ void walk_groups_coop(const QueueArgs& q, unsigned lo
 
 template <int G>
 static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_coop(const __grid_constant__ QueueArgs q) {
+  grid_dep_wait();
+  grid_dep_release();
   walk_groups_coop<G>(q, q.counter, q.total);
 }
 
@@ -606,8 +622,12 @@ static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __gri
 }
 
 // The walks of levels that all have step tables (4 blocks/SM: 64 registers,
-// no spills; the extra resident warps hide the mask loads' latency).
+// no spills; the extra resident warps hide the mask loads' latency).  The
+// walks are launched in the ordinary way (the wait returns at once) and let
+// the top level's merge launch early: it waits for their records.
 static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
+  grid_dep_wait();
+  grid_dep_release();
   walk_groups<4, TableWalker>(q, q.counter, q.total);
 }
 
@@ -743,6 +763,8 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
 template <typename T, bool L0, bool TOP>
 __global__ void __launch_bounds__(128) k_level_merge(const __grid_constant__ LevelArgs a,
                                                      const uint32_t* __restrict__ rec, int slots) {
+  grid_dep_wait();  // the records and the next level's radiance
+  grid_dep_release();
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.P) return;
   merge_probe<T, L0, TOP, false>(a, rec, slots, p, blockIdx.y);

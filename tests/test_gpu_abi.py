@@ -188,3 +188,30 @@ def test_stage_timing_and_frame_log(tmp_path):
         assert x["algorithmic_gb_per_s"] > 0
     assert lines[0]["note"] == "plain" and "nrc_loss" not in lines[0]
     assert 0.0 <= lines[3]["nrc_fallback_fraction"] <= 1.0
+
+
+def test_overlapped_level_launches_match_serialised_ones():
+    """The level kernels start while the previous level's kernel finishes
+    (programmatic launches; each waits on the device for what it reads).  With
+    stage timing on, events between the kernels serialise them: both orders
+    must give the same bits, frame after frame, at 128^3 (every level kind:
+    walk queue, merges, TMA-staged wide levels, cascade 0)."""
+    params = R.make_params(128, 5)
+    boxes, spheres = R.generate_scene(R.scene_spec(128, 96, (4, 24), 12, (2.0, 6.0), (1.0, 30.0)), 21)
+    out = []
+    for timing in (False, True):
+        with R.Engine(params) as e:
+            e.set_boxes(boxes)
+            e.set_stage_timing(timing)
+            s2 = spheres.copy()
+            frames = []
+            for _ in range(3):
+                e.set_spheres(s2)
+                e.solve()
+                R.advance_spheres(s2, 128, 2)
+                frames.append((e.fluence().copy(), [e.radiance(i).copy() for i in range(5)]))
+            out.append(frames)
+    for (fa, la), (fb, lb) in zip(*out):
+        assert np.array_equal(fa, fb)
+        for x, y in zip(la, lb):
+            assert np.array_equal(x, y)
