@@ -223,7 +223,10 @@ rc_status rc_get_stream(rc_context* ctx, void** out);
  * recomposition under the current spheres (the per-frame emitter update),
  * ms_out[1 + i] = cascade level i (the top level's figure includes the one
  * launch that walks every level with fewer than 32 probes per row).  Needs
- * 1 + num_cascades floats.  Synchronises. */
+ * 1 + num_cascades floats; with 2 + num_cascades, ms_out[1 + num_cascades]
+ * is the whole level set of a frame timed without events between its
+ * kernels (as rc_solve runs it: each level kernel may start while the one
+ * before it finishes), from another `iters` frames.  Synchronises. */
 rc_status rc_profile_levels(rc_context* ctx, int32_t iters, float* ms_out,
                             int32_t count);
 /* Per-solve stage timing.  With timing on, every rc_solve records CUDA

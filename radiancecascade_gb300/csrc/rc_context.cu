@@ -247,6 +247,36 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // Cascade 0 through k_level0_tma: the walk-free cascade 0 with its parent
 // tiles staged by TMA.  Needs a tensor map over cascade 1's child-averaged
 // radiance viewed as [3 * dirs0 * UMz][UMy][UMx] with 16-byte aligned rows.
+// Tensor map over a level's child-averaged radiance ([dir][probe][4] texels
+// of es-byte values) for boxes of UMx x rows x planes texels starting at x =
+// 0: FP32 as a 4-D map (channel, x, y, direction x plane) -- a texel is 16
+// bytes, the smallest inner box; FP16 as a 3-D map of 8-byte texels, which
+// needs an even UMx for 16-byte rows.  False when the box breaks a copy rule.
+bool encode_rgb4_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, const void* A, int UMx, int UMy,
+                     int64_t zplanes, int rows, int planes, size_t es) {
+  if (UMx < 2 || UMx > 256 || rows > 256 || planes > 256) return false;
+  CUresult r;
+  if (es == 4) {
+    cuuint64_t dims[4] = {4, (cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)zplanes};
+    cuuint64_t strides[3] = {16, (cuuint64_t)UMx * 16, (cuuint64_t)UMx * UMy * 16};
+    cuuint32_t box[4] = {4, (cuuint32_t)UMx, (cuuint32_t)rows, (cuuint32_t)planes};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(A), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  } else {
+    if (UMx % 2 != 0) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)zplanes};
+    cuuint64_t strides[2] = {(cuuint64_t)UMx * 8, (cuuint64_t)UMx * UMy * 8};
+    cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)rows, (cuuint32_t)planes};
+    cuuint32_t estr[3] = {1, 1, 1};
+    r = enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<void*>(A), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  }
+  return r == CUDA_SUCCESS;
+}
+
 bool setup_tma0(rc_context* c) {
   if (c->nlev < 2 || c->mode[0] != kModeDirect0) return false;
   const LevelArgs& a = c->args[0];
@@ -255,6 +285,7 @@ bool setup_tma0(rc_context* c) {
   if (UMx < 2 || UMx > 256 || (UMx * es) % 16 != 0) return false;
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
+  // cascade 1's child averages in the planar layout (set_average_layouts)
   const int py = std::min(6, UMy);
   cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
   cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
@@ -295,17 +326,9 @@ void setup_tma_up(rc_context* c) {
     const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
     const int BY = (512 >> a.l2px) / 2 + 2;  // a block tile holds 512 / Px rows of each of its two planes
     const size_t es = c->elem;
-    if (UMx < 2 || UMx > 256 || (UMx * es) % 16 != 0 || UMy < BY || UMz < 3) continue;
+    if (UMy < BY || UMz < 3) continue;
     if (!enc && !(enc = tensor_map_encoder())) return;
-    cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
-    cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
-    cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)BY, 3};
-    cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = enc(&c->tmap_up[i], es == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
-                           3, const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) continue;
+    if (!encode_rgb4_map(enc, &c->tmap_up[i], a.A_up, UMx, UMy, (int64_t)UMz * a.ndirs, BY, 3, es)) continue;
     // the kernel's shared-memory limit: the largest box any level can need
     // (512 / Px rows / 2 + 2 rows of Px / 2 FP32 values; largest at Px = 256)
     const int smem = (int)bits_up_smem(up_tile_stride((512 >> 8) / 2 + 2, 128, 4));
@@ -744,7 +767,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
     c->rad_off[i] = rad_bytes;
     rad_bytes += ((size_t)3 * g.ndirs * g.probes() * c->elem + 255) & ~(size_t)255;
     c->avg_off[i] = avg_bytes;
-    if (i >= 1) avg_bytes += ((size_t)3 * c->geom[i - 1].ndirs * g.probes() * c->elem + 255) & ~(size_t)255;
+    if (i >= 1) avg_bytes += ((size_t)4 * c->geom[i - 1].ndirs * g.probes() * c->elem + 255) & ~(size_t)255;
   }
   if ((s = dev_alloc(&c->rad, rad_bytes, "cascade radiance")) != RC_OK) return fail(s);
   if (avg_bytes && (s = dev_alloc(&c->avg, avg_bytes, "child-averaged radiance")) != RC_OK) return fail(s);
@@ -785,6 +808,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
     a.P = g.probes();
     a.L = static_cast<char*>(c->rad) + c->rad_off[i];
     a.A_out = i >= 1 ? static_cast<char*>(c->avg) + c->avg_off[i] : nullptr;
+    a.a_out_planar = (i == 1 && (c->mode[0] == kModeDirect0 || c->mode[0] == kModeTma0)) ? 1 : 0;
     a.A_up = (i + 1 < c->nlev) ? static_cast<char*>(c->avg) + c->avg_off[i + 1] : nullptr;
     a.P_up = (i + 1 < c->nlev) ? c->geom[i + 1].probes() : 0;
     a.fluence = c->fluence;
@@ -1370,8 +1394,8 @@ rc_status rc_get_stream(rc_context* c, void** out) {
 
 rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t count) {
   if (check_ctx(c, "rc_profile_levels") != RC_OK) return RC_ERR_INVALID_ARG;
-  if (!ms_out || count != 1 + c->nlev || iters < 1) {
-    rcx::set_error("rc_profile_levels: need iters >= 1 and %d output floats", 1 + c->nlev);
+  if (!ms_out || (count != 1 + c->nlev && count != 2 + c->nlev) || iters < 1) {
+    rcx::set_error("rc_profile_levels: need iters >= 1 and %d or %d output floats", 1 + c->nlev, 2 + c->nlev);
     return RC_ERR_INVALID_ARG;
   }
   if (!c->have_base) {
@@ -1412,9 +1436,29 @@ rc_status rc_profile_levels(rc_context* c, int32_t iters, float* ms_out, int32_t
       acc[1 + i] += ms;
     }
   }
+  // the level set as a solve launches it: events only around it
+  double whole = 0.0;
+  for (int it = 0; it < iters && st == RC_OK && count == 2 + c->nlev; ++it) {
+    cudaEventRecord(ev[0], c->stream);
+    launch_queue_walk(c, c->stream);
+    for (int i = c->nlev - 1; i >= 0; --i) {
+      if (c->elem == 2) launch_level<__half>(c, i, c->stream);
+      else launch_level<float>(c, i, c->stream);
+    }
+    cudaEventRecord(ev[1], c->stream);
+    cudaError_t e = cudaEventSynchronize(ev[1]);
+    if (e != cudaSuccess) {
+      st = cuda_fail(e, "rc_profile_levels");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]);
+    whole += ms;
+  }
   for (int i = 0; i < c->nlev + 2; ++i) cudaEventDestroy(ev[i]);
   if (st != RC_OK) return st;
   for (int i = 0; i <= c->nlev; ++i) ms_out[i] = (float)(acc[i] / iters);
+  if (count == 2 + c->nlev) ms_out[1 + c->nlev] = (float)(whole / iters);
   return RC_OK;
 }
 
@@ -1600,7 +1644,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
   mask_bytes = off - mask_begin;
   size_t avg_off[kMaxCascades] = {};
   for (int i = 1; i < v.nlev; ++i)
-    avg_off[i] = carve(off, (size_t)3 * v.geom[i - 1].ndirs * v.geom[i].probes() * v.elem);
+    avg_off[i] = carve(off, (size_t)4 * v.geom[i - 1].ndirs * v.geom[i].probes() * v.elem);
   size_t ndirs_total = 0;
   for (int i = 0; i < v.nlev; ++i) ndirs_total += (size_t)v.geom[i].ndirs;
   const size_t dirs_off = carve(off, ndirs_total * sizeof(DirInfo));
@@ -1706,6 +1750,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     a.L = static_cast<char*>(radiance) + rad_off;
     rad_off += (size_t)3 * g.ndirs * g.probes() * v.elem;
     a.A_out = i >= 1 ? scratch + avg_off[i] : nullptr;
+    a.a_out_planar = (i == 1 && (v.mode[0] == kModeDirect0 || v.mode[0] == kModeTma0)) ? 1 : 0;
     a.A_up = (i + 1 < v.nlev) ? scratch + avg_off[i + 1] : nullptr;
     a.P_up = (i + 1 < v.nlev) ? v.geom[i + 1].probes() : 0;
     a.fluence = fluence;

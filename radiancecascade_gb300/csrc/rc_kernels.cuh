@@ -4,8 +4,11 @@
 //   vol   rc_voxel[Gz][Gy][Gx]               8 B/voxel composed scene
 //   occ   uint32  [Gz][Gy][ceil(Gx/32)]      1 bit/voxel opacity, x fastest
 //   L_i   T       [3][dirs_i][Mz][My][Mx]     merged radiance of level i (T = f32 | f16)
-//   A_i   T       [3][dirs_{i-1}][Mz][My][Mx] L_i averaged over each 2x2 child-texel
-//                                             block; read by level i-1's merge
+//   A_i   T       [dirs_{i-1}][Mz][My][Mx][4] L_i averaged over each 2x2 child-texel
+//                                             block, RGB + a zero per (direction, probe);
+//                                             read by level i-1's merge.  A_1 read by
+//                                             the walk-free cascade 0 is planar instead:
+//                                             [3][dirs_0][Mz][My][Mx] (a_out_planar)
 //   flu   float   [Mz0][My0][Mx0][3]          cascade-0 fluence
 #pragma once
 
@@ -73,6 +76,81 @@ __device__ __forceinline__ float load_up<__half, true>(const __half* p) {
 __device__ __forceinline__ float to_float(float v) { return v; }
 __device__ __forceinline__ float to_float(__half v) { return __half2float(v); }
 
+// Child-averaged radiance A_i is stored [parent direction][probe][4]: the
+// three channels of one (direction, probe) side by side and a zero, so that
+// a blend tap is one 16-byte (FP32) or 8-byte (FP16) load and one TMA copy
+// stages every channel.  rgb4_at(A, d, P, probe) is the tap's first value.
+template <typename T>
+__device__ __forceinline__ const T* rgb4_at(const T* A, int d, int64_t P, int64_t probe) {
+  return A + ((int64_t)d * P + probe) * 4;
+}
+template <typename T>
+__device__ __forceinline__ T* rgb4_at(T* A, int d, int64_t P, int64_t probe) {
+  return A + ((int64_t)d * P + probe) * 4;
+}
+
+__device__ __forceinline__ float3 half4_rgb(uint2 u) {
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  return make_float3(a.x, a.y, b.x);
+}
+
+// One tap from global memory (CG as for load_up).
+template <typename T, bool CG>
+__device__ __forceinline__ float3 load_rgb(const T* p);
+template <>
+__device__ __forceinline__ float3 load_rgb<float, false>(const float* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 v = RC_CHK(q, kChkRadiance) ? __ldg(q) : make_float4(0.f, 0.f, 0.f, 0.f);
+  return make_float3(v.x, v.y, v.z);
+}
+template <>
+__device__ __forceinline__ float3 load_rgb<float, true>(const float* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 v = RC_CHK(q, kChkRadiance) ? __ldca(q) : make_float4(0.f, 0.f, 0.f, 0.f);
+  return make_float3(v.x, v.y, v.z);
+}
+template <>
+__device__ __forceinline__ float3 load_rgb<__half, false>(const __half* p) {
+  const uint2* q = reinterpret_cast<const uint2*>(p);
+  return half4_rgb(RC_CHK(q, kChkRadiance) ? __ldg(q) : make_uint2(0u, 0u));
+}
+template <>
+__device__ __forceinline__ float3 load_rgb<__half, true>(const __half* p) {
+  const uint2* q = reinterpret_cast<const uint2*>(p);
+  return half4_rgb(RC_CHK(q, kChkRadiance) ? __ldca(q) : make_uint2(0u, 0u));
+}
+
+// One tap from a staged shared-memory tile.
+__device__ __forceinline__ float3 lds_rgb(const float* p) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+  const float4 v = RC_CHK(q, kChkShared) ? *q : make_float4(0.f, 0.f, 0.f, 0.f);
+  return make_float3(v.x, v.y, v.z);
+}
+__device__ __forceinline__ float3 lds_rgb(const __half* p) {
+  const uint2* q = reinterpret_cast<const uint2*>(p);
+  return half4_rgb(RC_CHK(q, kChkShared) ? *q : make_uint2(0u, 0u));
+}
+
+// Writes one (direction, probe) of a child average (each channel rounded as
+// a single store of it would be).
+__device__ __forceinline__ void store_rgb(float* p, float r, float g, float b) {
+  float4* q = reinterpret_cast<float4*>(p);
+  if (RC_CHK(q, kChkRadiance)) *q = make_float4(r, g, b, 0.f);
+}
+__device__ __forceinline__ void store_rgb(__half* p, float r, float g, float b) {
+  uint2* q = reinterpret_cast<uint2*>(p);
+  const __half2 lo = __floats2half2_rn(r, g), hi = __floats2half2_rn(b, 0.f);
+  uint2 u;
+  u.x = *reinterpret_cast<const uint32_t*>(&lo);
+  u.y = *reinterpret_cast<const uint32_t*>(&hi);
+  if (RC_CHK(q, kChkRadiance)) *q = u;
+}
+
+struct LevelArgs;
+template <typename T>
+__device__ __forceinline__ void store_avg(const LevelArgs& a, int dp, int64_t p, float r, float g, float b);
+
 struct LevelArgs {
   const uint2* mask;     // this level's decimated (opacity, emissive) bits (bit-parallel walk)
   const uint32_t* emis;  // full-resolution emissive bits, same layout as occ
@@ -93,12 +171,28 @@ struct LevelArgs {
   int32_t ndirs;
   int64_t P;           // probes at this level
   void* L;             // out: merged radiance
-  void* A_out;         // out: child-averaged radiance (levels >= 1)
-  const void* A_up;    // in: next level's child-averaged radiance (not top)
+  void* A_out;         // out: child-averaged radiance (levels >= 1), [parent dir][probe][4]
+  int32_t a_out_planar;  // A_out planar [3][parent dir][probe] instead (read by the walk-free cascade 0)
+  const void* A_up;    // in: next level's child-averaged radiance (not top), [dir][probe][4]
   int32_t UM[3];       // probes per axis at the next level
   int64_t P_up;
   float* fluence;      // out: level 0 only
 };
+
+// One (parent direction dp, probe p) of the level's child average, in its
+// output layout.
+template <typename T>
+__device__ __forceinline__ void store_avg(const LevelArgs& a, int dp, int64_t p, float r, float g, float b) {
+  T* A = static_cast<T*>(a.A_out);
+  if (a.a_out_planar) {
+    const int64_t npar = (int64_t)(a.n >> 1) * (a.n >> 1);
+    Store<T>::store(A + (int64_t)dp * a.P + p, r);
+    Store<T>::store(A + (npar + dp) * a.P + p, g);
+    Store<T>::store(A + (2 * npar + dp) * a.P + p, b);
+  } else {
+    store_rgb(rgb4_at(A, dp, a.P, p), r, g, b);
+  }
+}
 
 __device__ __forceinline__ bool opaque_at(const uint32_t* __restrict__ occ, int W, int Gy, int x, int y, int z) {
   const uint32_t* w = &occ[((int64_t)z * Gy + y) * W + (x >> 5)];
@@ -204,13 +298,13 @@ __device__ __forceinline__ void scalar_probe(const LevelArgs& a, int64_t p, int 
       r[0] = r[1] = r[2] = 0.f;
     } else {
       const T* Au = static_cast<const T*>(a.A_up);
+      r[0] = r[1] = r[2] = 0.f;
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        const T* base = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-        float s = 0.f;
-#pragma unroll
-        for (int t = 0; t < 8; ++t) s = fmaf(tap_w[t], load_up<T, CG>(base + tap_off[t]), s);
-        r[ch] = s;
+      for (int t = 0; t < 8; ++t) {
+        const float3 v = load_rgb<T, CG>(rgb4_at(Au, d, a.P_up, tap_off[t]));
+        r[0] = fmaf(tap_w[t], v.x, r[0]);
+        r[1] = fmaf(tap_w[t], v.y, r[1]);
+        r[2] = fmaf(tap_w[t], v.z, r[2]);
       }
     }
 #pragma unroll
@@ -219,14 +313,9 @@ __device__ __forceinline__ void scalar_probe(const LevelArgs& a, int64_t p, int 
       acc[ch] = L0 ? fmaf(di.omega, r[ch], acc[ch]) : acc[ch] + r[ch];
     }
     if (!L0 && (c & 3) == 3) {
-      T* A = static_cast<T*>(a.A_out);
-      const int64_t npar = (int64_t)hn * hn;
       const int dp = dp0 + (c >> 2);
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
-        acc[ch] = 0.f;
-      }
+      store_avg<T>(a, dp, p, 0.25f * acc[0], 0.25f * acc[1], 0.25f * acc[2]);
+      acc[0] = acc[1] = acc[2] = 0.f;
     }
   }
   if (L0) {

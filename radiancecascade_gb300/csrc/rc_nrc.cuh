@@ -1016,10 +1016,11 @@ __global__ void __launch_bounds__(kNrcThreads) k_nrc_heldout(const __grid_consta
       merge_taps(la, p, tap_off, tap_w);
       const T* Au = static_cast<const T*>(la.A_up);
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        const T* src = Au + ((int64_t)ch * la.ndirs + d) * la.P_up;
-#pragma unroll
-        for (int tp = 0; tp < 8; ++tp) M[ch] = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), M[ch]);
+      for (int tp = 0; tp < 8; ++tp) {
+        const float3 v = load_rgb<T, false>(rgb4_at(Au, d, la.P_up, tap_off[tp]));
+        M[0] = fmaf(tap_w[tp], v.x, M[0]);
+        M[1] = fmaf(tap_w[tp], v.y, M[1]);
+        M[2] = fmaf(tap_w[tp], v.z, M[2]);
       }
     }
     const float om = __ldg(L.omega + d);
@@ -1124,7 +1125,6 @@ __global__ void __launch_bounds__(128) k_level_merge_nrc(const __grid_constant__
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
   const int hn = a.n >> 1;
-  const int64_t npar = (int64_t)hn * hn;
   const int64_t plane = (int64_t)a.ndirs * a.P;
   const __half* rt = NL.rt;
   float acc[3] = {0.f, 0.f, 0.f};
@@ -1142,14 +1142,16 @@ __global__ void __launch_bounds__(128) k_level_merge_nrc(const __grid_constant__
       for (int ch = 0; ch < 4; ++ch) rv[ch] = RC_CHK(&rt[ch * plane + off], kChkCache) ? __half2float(rt[ch * plane + off]) : 0.f;
     }
     if (!TOP && rv[3] > 0.f) {
+      float sum[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-        float sum = 0.f;
-#pragma unroll
-        for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], Store<T>::load(src + tap_off[tp]), sum);
-        rv[ch] = fmaf(rv[3], sum, rv[ch]);
+      for (int tp = 0; tp < 8; ++tp) {
+        const float3 v = load_rgb<T, false>(rgb4_at(Au, d, a.P_up, tap_off[tp]));
+        sum[0] = fmaf(tap_w[tp], v.x, sum[0]);
+        sum[1] = fmaf(tap_w[tp], v.y, sum[1]);
+        sum[2] = fmaf(tap_w[tp], v.z, sum[2]);
       }
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) rv[ch] = fmaf(rv[3], sum[ch], rv[ch]);
     }
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -1157,12 +1159,8 @@ __global__ void __launch_bounds__(128) k_level_merge_nrc(const __grid_constant__
       acc[ch] += rv[ch];
     }
     if ((dl & 3) == 3) {
-      T* A = static_cast<T*>(a.A_out);
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) {
-        Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
-        acc[ch] = 0.f;
-      }
+      store_avg<T>(a, dp, p, 0.25f * acc[0], 0.25f * acc[1], 0.25f * acc[2]);
+      acc[0] = acc[1] = acc[2] = 0.f;
     }
   }
 }

@@ -83,4 +83,24 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// 4-D tiled TMA load of the box at (x, y, z, w) (x on a 16-byte boundary).
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int x, int y, int z, int w,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// A box of child-averaged radiance ([dir][probe][4] texels) at row y and
+// plane z (= direction * planes + plane) of the map: for FP32 a 4-D map
+// (channel, x, y, z), for FP16 a 3-D map of 8-byte texels (x, y, z).  The
+// box always starts at channel 0 and x = 0.
+template <typename T>
+__device__ __forceinline__ void tma_load_rgb4(void* dst, const CUtensorMap* map, int y, int z, uint64_t* bar) {
+  if (sizeof(T) == 4) tma_load_4d(dst, map, 0, 0, y, z, bar);
+  else tma_load_3d(dst, map, 0, y, z, bar);
+}
+
 }  // namespace rcx

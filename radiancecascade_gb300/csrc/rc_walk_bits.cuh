@@ -93,14 +93,15 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
           }
           const int64_t g = ((int64_t)yc << m.l2px) + xc0;
           uint2* w2 = m.base + plane_base(m, lane, phy, phz, zc) + (g >> 5);
-          uint32_t* w = reinterpret_cast<uint32_t*>(w2);
+          // the pair as one 64-bit word: opacity in the low half (.x), emission in the high half
+          unsigned long long* w = reinterpret_cast<unsigned long long*>(w2);
           const int sh = (int)(g & 31);
           const uint32_t fmask = (width == 32 ? 0xFFFFFFFFu : ((1u << width) - 1u)) << sh;
+          const unsigned long long set =
+              (unsigned long long)(field << sh) | ((unsigned long long)(efield << sh) << 32);
           if (RC_CHK(w2, kChkMask)) {
-            atomicAnd(w, ~fmask);
-            if (field) atomicOr(w, field << sh);
-            atomicAnd(w + 1, ~fmask);
-            if (efield) atomicOr(w + 1, efield << sh);
+            atomicAnd(w, ~((unsigned long long)fmask | ((unsigned long long)fmask << 32)));
+            if (set) atomicOr(w, set);
           }
         }
       }
@@ -108,13 +109,12 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
       const int xc = x >> m.l2s;
       const int64_t g = ((int64_t)yc << m.l2px) + xc;
       uint2* w2 = m.base + plane_base(m, x & (s - 1), phy, phz, zc) + (g >> 5);
-      uint32_t* w = reinterpret_cast<uint32_t*>(w2);
-      const uint32_t b = 1u << (g & 31);
+      unsigned long long* w = reinterpret_cast<unsigned long long*>(w2);
+      const unsigned long long b = 1ull << (g & 31), eb = b << 32;
       if (!RC_CHK(w2, kChkMask)) continue;
-      if ((bits >> lane) & 1u) atomicOr(w, b);
-      else atomicAnd(w, ~b);
-      if ((ebits >> lane) & 1u) atomicOr(w + 1, b);
-      else atomicAnd(w + 1, ~b);
+      const unsigned long long set = (((bits >> lane) & 1u) ? b : 0ull) | (((ebits >> lane) & 1u) ? eb : 0ull);
+      if (set != (b | eb)) atomicAnd(w, ~((b | eb) & ~set));
+      if (set) atomicOr(w, set);
     }
   }
 }
@@ -325,6 +325,19 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
 }
 
 
+// The y blends (child rows ey = 0, 1) of one channel's three z-blended parent
+// rows, then the x blend through the lanes' columns (lane l holds parent
+// column (l + 1) / 2 - 1 + ...: src_near / src_far are the weight-3/4 and
+// weight-1/4 columns of the lane's child).  All lanes take part.
+__device__ __forceinline__ void yx_blend(const float zv[3], int src_near, int src_far, float& out0, float& out1) {
+  const float v0 = fmaf(3.f, zv[1], zv[0]);
+  const float v1 = fmaf(3.f, zv[1], zv[2]);
+  const float n0 = __shfl_sync(0xFFFFFFFFu, v0, src_near), f0 = __shfl_sync(0xFFFFFFFFu, v0, src_far);
+  const float n1 = __shfl_sync(0xFFFFFFFFu, v1, src_near), f1 = __shfl_sync(0xFFFFFFFFu, v1, src_far);
+  out0 = fmaf(3.f, n0, f0) * (1.f / 64.f);
+  out1 = fmaf(3.f, n1, f1) * (1.f / 64.f);
+}
+
 // Direction of block-local slot dl (0..15) in pass `pass`, or -1.
 template <bool L0>
 __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgroup, int dl) {
@@ -343,10 +356,11 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
 // the copies wait for that kernel).
 constexpr int kUpStages = 4;
 
-// Bytes of one channel tile of the next level's box staged per direction
-// (3 planes x up_rows rows x UM[0] values), and its 128-byte aligned stride.
+// Bytes of the next level's box staged per direction (3 planes x up_rows
+// rows x UM[0] texels of 4 values: every channel in one copy), and its
+// 128-byte aligned stride.
 __host__ __device__ __forceinline__ uint32_t up_tile_bytes(int up_rows, int umx, int elem) {
-  return 3u * (uint32_t)up_rows * (uint32_t)umx * (uint32_t)elem;
+  return 12u * (uint32_t)up_rows * (uint32_t)umx * (uint32_t)elem;
 }
 __host__ __device__ __forceinline__ uint32_t up_tile_stride(int up_rows, int umx, int elem) {
   return (up_tile_bytes(up_rows, umx, elem) + 127u) & ~127u;
@@ -366,9 +380,9 @@ __host__ __device__ __forceinline__ uint32_t up_tile_stride(int up_rows, int umx
 // s_hit of kBitsSmem bytes); CG: the next level was written during the same
 // launch (see load_up).
 // TM: the next level's values come from shared memory instead: per direction
-// one TMA copy per channel of the block's parent box (all UM[0] columns,
-// up_rows rows, 3 planes) through `tmap` into s_up (128-byte aligned,
-// kUpStages stages of three channel tiles, then kUpStages mbarriers).  Only
+// one TMA copy of the block's parent box (all UM[0] columns, up_rows rows, 3
+// planes, every channel) through `tmap` into s_up (128-byte aligned,
+// kUpStages stage tiles, then kUpStages mbarriers).  Only
 // thread 0, which issues the copies, waits for the launch that wrote them
 // (grid_dep_wait); the block then lets the next level's launch start.
 template <typename T, bool L0, bool TOP, bool CG, bool TM = false>
@@ -383,8 +397,6 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
   const Tile t = tile_of(a, tile_id);
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
   const int npass = L0 ? (a.ndirs + kTileDirs - 1) / kTileDirs : 1;
-  const int hn = a.n >> 1;
-  const int64_t npar = (int64_t)hn * hn;
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
 
@@ -440,7 +452,7 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
                             (min(max(y0 / 2 - 1 + jj, 0), a.UM[1] - 1) - ys)) * a.UM[0] + qx;
     tstride = up_tile_stride(BY, a.UM[0], (int)sizeof(T));
     up_tiles = reinterpret_cast<T*>(s_up);
-    ubar = reinterpret_cast<uint64_t*>(s_up + kUpStages * 3 * tstride);
+    ubar = reinterpret_cast<uint64_t*>(s_up + kUpStages * tstride);
     if (tid == 0) {
 #pragma unroll
       for (int st = 0; st < kUpStages; ++st) mbar_init(&ubar[st], 1);
@@ -459,11 +471,9 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
       const uint32_t tbytes = up_tile_bytes(BY, a.UM[0], (int)sizeof(T));
       for (int k = 0; k < kUpStages && k < 8; ++k) {
         const int d = block_dir<L0>(a, 0, dgroup, k);
-        mbar_arrive_expect_tx(&ubar[k], 3u * tbytes);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch)
-          tma_load_3d(reinterpret_cast<unsigned char*>(up_tiles) + (k * 3 + ch) * tstride, tmap, 0, ys,
-                      (ch * a.ndirs + d) * a.UM[2] + zs, &ubar[k]);
+        mbar_arrive_expect_tx(&ubar[k], tbytes);
+        tma_load_rgb4<T>(reinterpret_cast<unsigned char*>(up_tiles) + k * tstride, tmap, ys, d * a.UM[2] + zs,
+                         &ubar[k]);
       }
     }
   };
@@ -511,39 +521,52 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         const bool merge = !TOP && __any_sync(0xFFFFFFFFu, missm != 0);
         const float om = L0 ? a.dirs[d].omega : 0.f;
         float val[4][3];
+        float mv[3][4];  // [channel][child i = ez * 2 + ey]
+        if (merge && TM) {
+          // staged taps (q = plane * 3 + row): every channel in one shared load;
+          // per child plane the middle parent plane (weight 3/4) and plane 0 or 2
+          const T* tile = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(up_tiles) + ust * tstride);
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          float mv[4] = {0.f, 0.f, 0.f, 0.f};
-          if (merge) {
-            float av[9];
-            if (TM) {
-              const T* tile = reinterpret_cast<const T*>(reinterpret_cast<const unsigned char*>(up_tiles) +
-                                                         (ust * 3 + ch) * tstride);
+          for (int ez = 0; ez < 2; ++ez) {
+            float3 pm[3], po[3];
 #pragma unroll
-              for (int q = 0; q < 9; ++q)
-                av[q] = ploader && RC_CHK(&tile[soff[q]], kChkShared) ? to_float(tile[soff[q]]) : 0.f;
-            } else {
-              const T* src = Au + (ch * a.ndirs + d) * (int)a.P_up;
-#pragma unroll
-              for (int q = 0; q < 9; ++q) av[q] = ploader ? load_up<T, CG>(src + aoff[q]) : 0.f;
+            for (int jy = 0; jy < 3; ++jy) {
+              pm[jy] = ploader ? lds_rgb(tile + 4 * soff[3 + jy]) : make_float3(0.f, 0.f, 0.f);
+              po[jy] = ploader ? lds_rgb(tile + 4 * soff[ez == 0 ? jy : 6 + jy]) : make_float3(0.f, 0.f, 0.f);
             }
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              float zv[3];
+#pragma unroll
+              for (int jy = 0; jy < 3; ++jy) {
+                const float m = ch == 0 ? pm[jy].x : ch == 1 ? pm[jy].y : pm[jy].z;
+                const float o = ch == 0 ? po[jy].x : ch == 1 ? po[jy].y : po[jy].z;
+                zv[jy] = fmaf(3.f, m, o);
+              }
+              yx_blend(zv, src_near, src_far, mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
+            }
+          }
+        } else if (!TM && merge) {
+          // taps from global memory, one channel at a time (value (d, probe q, ch) at Au[4 (d P_up + q) + ch])
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch) {
+            const T* src = Au + (int64_t)d * a.P_up * 4 + ch;
+            float av[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) av[q] = ploader ? load_up<T, CG>(src + 4 * aoff[q]) : 0.f;
 #pragma unroll
             for (int ez = 0; ez < 2; ++ez) {
               float zv[3];
 #pragma unroll
-              for (int jy = 0; jy < 3; ++jy)
-                zv[jy] = fmaf(3.f, av[3 + jy], ez == 0 ? av[jy] : av[6 + jy]);
-              const float v0 = fmaf(3.f, zv[1], zv[0]);
-              const float v1 = fmaf(3.f, zv[1], zv[2]);
-              const float n0 = __shfl_sync(0xFFFFFFFFu, v0, src_near), f0 = __shfl_sync(0xFFFFFFFFu, v0, src_far);
-              const float n1 = __shfl_sync(0xFFFFFFFFu, v1, src_near), f1 = __shfl_sync(0xFFFFFFFFu, v1, src_far);
-              mv[ez * 2 + 0] = fmaf(3.f, n0, f0) * (1.f / 64.f);
-              mv[ez * 2 + 1] = fmaf(3.f, n1, f1) * (1.f / 64.f);
+              for (int jy = 0; jy < 3; ++jy) zv[jy] = fmaf(3.f, av[3 + jy], ez == 0 ? av[jy] : av[6 + jy]);
+              yx_blend(zv, src_near, src_far, mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
             }
           }
-#pragma unroll
-          for (int i = 0; i < 4; ++i) val[i][ch] = ((missm >> i) & 1u) ? mv[i] : 0.f;
         }
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) val[i][ch] = (merge && ((missm >> i) & 1u)) ? mv[ch][i] : 0.f;
         if (emism) {  // emissive hits are rare: patch them in
 #pragma unroll
           for (int i = 0; i < 4; ++i)
@@ -559,16 +582,12 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
           }
         }
         if (!L0 && (k & 3) == 3) {
-          T* A = static_cast<T*>(a.A_out);
           const int dp = dgroup * 2 + (dl >> 2);
 #pragma unroll
-          for (int ch = 0; ch < 3; ++ch) {
-            T* dst = A + (ch * (int)npar + dp) * (int)a.P + p0;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              if ((okmask >> i) & 1u) Store<T>::store(dst + cstep[i], 0.25f * acc[i][ch]);
-              acc[i][ch] = 0.f;
-            }
+          for (int i = 0; i < 4; ++i) {
+            if ((okmask >> i) & 1u)
+              store_avg<T>(a, dp, p0 + cstep[i], 0.25f * acc[i][0], 0.25f * acc[i][1], 0.25f * acc[i][2]);
+            acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
           }
         }
         if (TM) {
@@ -579,11 +598,9 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
             const int ys = max(0, min(((t.w0 << 5) >> a.l2px) / 2 - 1, a.UM[1] - BY));
             const int zs = max(0, min(t.z0 / 2 - 1, a.UM[2] - 3));
             fence_proxy_async();
-            mbar_arrive_expect_tx(&ubar[ust], 3u * up_tile_bytes(BY, a.UM[0], (int)sizeof(T)));
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch)
-              tma_load_3d(reinterpret_cast<unsigned char*>(up_tiles) + (ust * 3 + ch) * tstride, tmap, 0, ys,
-                          (ch * a.ndirs + dn) * a.UM[2] + zs, &ubar[ust]);
+            mbar_arrive_expect_tx(&ubar[ust], up_tile_bytes(BY, a.UM[0], (int)sizeof(T)));
+            tma_load_rgb4<T>(reinterpret_cast<unsigned char*>(up_tiles) + ust * tstride, tmap, ys,
+                             dn * a.UM[2] + zs, &ubar[ust]);
           }
         }
       }
@@ -617,12 +634,13 @@ __global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const __grid_con
 }
 
 // A wide level between cascade 0 and the top with the next level's values
-// staged by TMA (tmap: 3D map over A_up, x = UM[0], y = UM[1], z = channel x
-// direction x UM[2]; box UM[0] x up_rows x 3).  Shared memory: up to 127
-// bytes to align, the hit records, then the stages and their barriers.
+// staged by TMA (tmap over A_up: texels of 4 values, x = UM[0], y = UM[1],
+// z = direction x UM[2]; box UM[0] x up_rows x 3 texels, see tma_load_rgb4).
+// Shared memory: up to 127 bytes to align, the hit records, then the stages
+// and their barriers.
 constexpr size_t kBitsHitBytes = (kBitsSmem + 127) & ~(size_t)127;
 __host__ __device__ constexpr size_t bits_up_smem(uint32_t tile_stride) {
-  return 128 + kBitsHitBytes + (size_t)kUpStages * 3 * tile_stride + 8 * kUpStages;
+  return 128 + kBitsHitBytes + (size_t)kUpStages * tile_stride + 8 * kUpStages;
 }
 
 template <typename T>

@@ -702,7 +702,6 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
   const int hn = a.n >> 1;
-  const int64_t npar = (int64_t)hn * hn;
   const int ndl = L0 ? a.ndirs : 8;
   float acc[3] = {0.f, 0.f, 0.f};
   // two directions per pass: their parent taps are in flight together
@@ -721,12 +720,11 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
     if (r == kMiss) {
       if (!TOP) {
 #pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          const T* src = Au + ((int64_t)ch * a.ndirs + d) * a.P_up;
-          float sum = 0.f;
-#pragma unroll
-          for (int tp = 0; tp < 8; ++tp) sum = fmaf(tap_w[tp], load_up<T, CG>(src + tap_off[tp]), sum);
-          rv[ch] = sum;
+        for (int tp = 0; tp < 8; ++tp) {
+          const float3 v = load_rgb<T, CG>(rgb4_at(Au, d, a.P_up, tap_off[tp]));
+          rv[0] = fmaf(tap_w[tp], v.x, rv[0]);
+          rv[1] = fmaf(tap_w[tp], v.y, rv[1]);
+          rv[2] = fmaf(tap_w[tp], v.z, rv[2]);
         }
       }
     } else if (r != kBlack) {
@@ -742,13 +740,9 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
 #pragma unroll
       for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
       if ((dl & 3) == 3) {
-        T* A = static_cast<T*>(a.A_out);
         const int dp = dpair * 2 + (dl >> 2);
-#pragma unroll
-        for (int ch = 0; ch < 3; ++ch) {
-          Store<T>::store(A + ((int64_t)ch * npar + dp) * a.P + p, 0.25f * acc[ch]);
-          acc[ch] = 0.f;
-        }
+        store_avg<T>(a, dp, p, 0.25f * acc[0], 0.25f * acc[1], 0.25f * acc[2]);
+        acc[0] = acc[1] = acc[2] = 0.f;
       }
     }
   }

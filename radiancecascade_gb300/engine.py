@@ -560,9 +560,11 @@ class Engine:
         F.check(self._lib.rc_get_stream(self.handle, C.byref(p)))
         return p.value or 0
 
-    def profile_levels(self, iters: int = 5) -> np.ndarray:
-        """Mean ms per launch: [compose, level 0, level 1, ...] (CUDA events)."""
-        out = np.zeros(1 + self.params.num_cascades, np.float32)
+    def profile_levels(self, iters: int = 5, whole: bool = False) -> np.ndarray:
+        """Mean ms per launch: [compose, level 0, level 1, ...] (CUDA events);
+        with whole=True one more entry: the frame's level set timed without
+        events between its kernels (they overlap as in a solve)."""
+        out = np.zeros(1 + self.params.num_cascades + (1 if whole else 0), np.float32)
         F.check(self._lib.rc_profile_levels(self.handle, iters, F.ptr(out), out.size))
         return out
 

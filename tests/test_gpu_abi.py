@@ -215,3 +215,22 @@ def test_overlapped_level_launches_match_serialised_ones():
         assert np.array_equal(fa, fb)
         for x, y in zip(la, lb):
             assert np.array_equal(x, y)
+
+
+def test_profile_levels_per_launch_and_whole_frame():
+    """rc_profile_levels: the per-launch means, and with one more float the
+    frame's level set timed as a solve launches it (no events between the
+    kernels), which cannot take much longer than the per-launch sum."""
+    params = R.make_params(128, 5)
+    boxes, spheres = R.generate_scene(R.scene_spec(128, 96, (4, 24), 12, (2.0, 6.0), (1.0, 30.0)), 21)
+    with R.Engine(params) as e:
+        e.set_boxes(boxes)
+        e.set_spheres(spheres)
+        e.solve()
+        per = e.profile_levels(3)
+        both = e.profile_levels(3, whole=True)
+        assert per.shape == (6,) and both.shape == (7,)
+        assert (per > 0).all() and (both > 0).all()
+        assert both[-1] <= 1.25 * float(both[1:-1].sum()) + 0.05
+        bad = np.zeros(8, np.float32)
+        assert F.lib().rc_profile_levels(e.handle, 1, F.ptr(bad), 8) == F.RC_ERR_INVALID_ARG
