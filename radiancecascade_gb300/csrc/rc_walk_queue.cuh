@@ -702,20 +702,18 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
   T* L = static_cast<T*>(a.L);
   const T* Au = static_cast<const T*>(a.A_up);
   const int hn = a.n >> 1;
-  const int ndl = L0 ? a.ndirs : 8;
   float acc[3] = {0.f, 0.f, 0.f};
-  // two directions per pass: their parent taps are in flight together
-#pragma unroll 2
-  for (int dl = 0; dl < ndl; ++dl) {
-    int d;
-    if (L0) {
-      d = dl;
-    } else {
-      const int dp = dpair * 2 + (dl >> 2), c = dl & 3;
-      d = (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
-    }
+  auto dir_of = [&](int dl) {
+    if (L0) return dl;
+    const int dp = dpair * 2 + (dl >> 2), c = dl & 3;
+    return (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
+  };
+  auto record = [&](int d) -> uint32_t {
     const uint32_t* rp = &rec[(int64_t)d * slots * 32 + rbase];
-    const uint32_t r = !RC_CHK(rp, kChkRecord) ? kBlack : CG ? __ldca(rp) : __ldg(rp);
+    return !RC_CHK(rp, kChkRecord) ? kBlack : CG ? __ldca(rp) : __ldg(rp);
+  };
+  // one direction: its radiance from the record, the stores, the sums
+  auto one = [&](int dl, int d, uint32_t r) {
     float rv[3] = {0.f, 0.f, 0.f};
     if (r == kMiss) {
       if (!TOP) {
@@ -745,6 +743,18 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
         acc[0] = acc[1] = acc[2] = 0.f;
       }
     }
+  };
+  if (L0) {
+    // two directions per pass: their parent taps are in flight together
+#pragma unroll 2
+    for (int dl = 0; dl < a.ndirs; ++dl) one(dl, dl, record(dl));
+  } else {
+    // the eight directions' records are requested together, then merged in order
+    uint32_t r8[8];
+#pragma unroll
+    for (int dl = 0; dl < 8; ++dl) r8[dl] = record(dir_of(dl));
+#pragma unroll
+    for (int dl = 0; dl < 8; ++dl) one(dl, dir_of(dl), r8[dl]);
   }
   if (L0) {
 #pragma unroll
