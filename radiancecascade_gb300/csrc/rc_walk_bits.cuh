@@ -350,10 +350,10 @@ __device__ __forceinline__ int block_dir(const LevelArgs& a, int pass, int dgrou
   return (2 * (dp / hn) + (c >> 1)) * a.n + 2 * (dp % hn) + (c & 1);
 }
 
-// Directions staged ahead in k_level_bits_up: the first kUpStages copies are
-// issued at the end of the walk phase (the walk reads only the scene, so with
-// a programmatic launch it runs while the previous level's kernel finishes;
-// the copies wait for that kernel).
+// Directions staged ahead in k_level_bits_up: thread 0 issues the first
+// kUpStages copies before the walk phase, once the previous level's kernel
+// has completed (with a programmatic launch the other warps' walks, which
+// read only the scene, run meanwhile).
 constexpr int kUpStages = 4;
 
 // Bytes of the next level's box staged per direction (3 planes x up_rows
@@ -382,9 +382,12 @@ __host__ __device__ __forceinline__ uint32_t up_tile_stride(int up_rows, int umx
 // TM: the next level's values come from shared memory instead: per direction
 // one TMA copy of the block's parent box (all UM[0] columns, up_rows rows, 3
 // planes, every channel) through `tmap` into s_up (128-byte aligned,
-// kUpStages stage tiles, then kUpStages mbarriers).  Only
-// thread 0, which issues the copies, waits for the launch that wrote them
-// (grid_dep_wait); the block then lets the next level's launch start.
+// kUpStages stage tiles, then kUpStages "full" mbarriers the copies complete
+// and kUpStages "empty" ones each warp arrives at when it is done with a
+// stage; thread 0 refills a stage once every warp has arrived, so the warps
+// never wait for one another at a block barrier).  Only thread 0, which
+// issues the copies, waits for the launch that wrote them (grid_dep_wait);
+// the block then lets the next level's launch start.
 template <typename T, bool L0, bool TOP, bool CG, bool TM = false>
 __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, uint32_t* s_hit,
                                                  const CUtensorMap* tmap = nullptr, unsigned char* s_up = nullptr,
@@ -455,13 +458,16 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
     ubar = reinterpret_cast<uint64_t*>(s_up + kUpStages * tstride);
     if (tid == 0) {
 #pragma unroll
-      for (int st = 0; st < kUpStages; ++st) mbar_init(&ubar[st], 1);
+      for (int st = 0; st < kUpStages; ++st) {
+        mbar_init(&ubar[st], 1);
+        mbar_init(&ubar[kUpStages + st], kBitsThreads / 32);  // empty: one arrival per warp
+      }
       mbar_fence_init();
     }
     __syncthreads();
   }
   // TM: the walk phase reads only the scene; the next level's values are
-  // staged after it, once the launch that wrote them has completed
+  // staged by thread 0 once the launch that wrote them has completed
   auto stage_first = [&]() {
     if (TM && tid == 0) {
       grid_dep_wait();
@@ -477,6 +483,8 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
       }
     }
   };
+
+  stage_first();  // thread 0 waits for the previous launch, the other warps start walking
 
   float acc[4][3];
 #pragma unroll
@@ -496,7 +504,6 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         for (int b = 0; b < 32; ++b) hit[b] = kMiss;
       }
     }
-    if (TM && pass == 0) stage_first();
     __syncthreads();
     if (TM && pass == 0) grid_dep_release();
     // ---- phase 2
@@ -591,7 +598,13 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
           }
         }
         if (TM) {
-          __syncthreads();  // every warp is done with stage ust: refill it with direction k + kUpStages
+          // this warp is done with stage ust; thread 0 refills it with direction
+          // k + kUpStages once every warp is
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&ubar[kUpStages + ust]);
+          if (tid == 0 && k + kUpStages < 8 &&
+              !mbar_wait_bounded(&ubar[kUpStages + ust], (uint32_t)(k / kUpStages) & 1u))
+            atomicExch(err, 3);
           if (tid == 0 && k + kUpStages < 8) {
             const int kn = k + kUpStages, dn = block_dir<L0>(a, pass, dgroup, kn);
             const int BY = a.up_rows;
@@ -640,7 +653,7 @@ __global__ void __launch_bounds__(kBitsThreads, 3) k_level_bits(const __grid_con
 // and their barriers.
 constexpr size_t kBitsHitBytes = (kBitsSmem + 127) & ~(size_t)127;
 __host__ __device__ constexpr size_t bits_up_smem(uint32_t tile_stride) {
-  return 128 + kBitsHitBytes + (size_t)kUpStages * tile_stride + 8 * kUpStages;
+  return 128 + kBitsHitBytes + (size_t)kUpStages * tile_stride + 16 * kUpStages;
 }
 
 template <typename T>
