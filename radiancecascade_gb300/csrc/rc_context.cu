@@ -301,7 +301,7 @@ bool setup_tma0(rc_context* c) {
   // barriers and up to 127 bytes to align the base), so that a later context
   // never lowers it under an earlier one.
   const size_t stage = 3 * (((size_t)(kL0Planes + 1) * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
-  const int smem = (int)(kL0Stages * stage + 8 * kL0Stages + 128);
+  const int smem = (int)(kL0Stages * stage + 16 * kL0Stages + 128);
   cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half, kL0Planes>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
                           : cudaFuncSetAttribute(k_level0_tma<float, kL0Planes>,
@@ -401,7 +401,7 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
         const size_t stage =
             3 * (((size_t)(kL0Planes + 1) * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
         launch_overlapped(k_level0_tma<T, kL0Planes>, dim3(blocks), dim3(kL0Threads),
-                          kL0Stages * stage + 8 * kL0Stages + 128, s, a, c->tma0, c->tma0_py, c->err);
+                          kL0Stages * stage + 16 * kL0Stages + 128, s, a, c->tma0, c->tma0_py, c->err);
       }
       break;
     }

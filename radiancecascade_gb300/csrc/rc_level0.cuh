@@ -248,13 +248,18 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 // ZC planes of one 128-probe chunk.  For every direction the parent tiles of
 // cascade 1's child-averaged radiance -- per channel the full parent row width
 // x PY rows x (ZC + 1) planes -- are brought into shared memory by three
-// cp.async.bulk.tensor copies while the previous direction's tiles are
-// consumed (two stages, one mbarrier each); one iteration serves all three
-// channels.  Lanes read their 4 parent columns from shared memory.
-// Every barrier wait is bounded: on timeout the block records *err = 1, waits
-// (bounded) for the copy it may still have in flight, and returns.
+// cp.async.bulk.tensor copies while earlier directions' tiles are consumed
+// (kL0Stages stages); one iteration serves all three channels.  Lanes read
+// their 4 parent columns from shared memory.  Each stage has a "full"
+// mbarrier the copies complete and an "empty" one every warp arrives at when
+// it is done with the stage; thread 0 refills a stage once all warps have
+// arrived, so warps never meet at a block barrier and may run a stage apart.
+// Every barrier wait is bounded: a wait that runs out marks the block aborted
+// (s_abort), every warp leaves its loop at its next wait, the block records
+// *err = 1, and thread 0 waits (bounded) for the copies it may still have in
+// flight before the block's shared memory goes.
 constexpr int kL0TmaRows = 8;
-constexpr int kL0Stages = 2;  // parent tiles in flight: the copy for iteration it + 1 starts at iteration it
+constexpr int kL0Stages = 3;  // parent tiles in flight: the copy for iteration it + 2 starts at iteration it
 // Child planes per block (ZC).  ZC = 1 halves the per-lane accumulators (80
 // registers, 3 blocks/SM) but reads 4 parent values per output instead of 3;
 // at 256^3 it measured 160 us against 153 us for ZC = 2 (128 registers, 2 blocks/SM).
@@ -361,10 +366,16 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
       tma_load_3d(tiles + st * stage_elems + ch * tile_stride_elems, &tmap, 0, ys, (ch * a.ndirs + dd) * UMz + zs,
                   &bar[st]);
   };
+  // bar[0 .. S-1]: a stage's copy has landed; bar[S .. 2S-1]: every warp is done with it
+  __shared__ int s_abort;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < kL0Stages; ++k) mbar_init(&bar[k], 1);
+    for (int k = 0; k < kL0Stages; ++k) {
+      mbar_init(&bar[k], 1);
+      mbar_init(&bar[kL0Stages + k], kL0Threads / 32);
+    }
     mbar_fence_init();
+    s_abort = 0;
   }
   __syncthreads();
   // a destination off its 128-byte boundary is reported and never copied to
@@ -389,13 +400,17 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
     const int d = it;
     const int st = it % kL0Stages;
     const int nx_ = it + kL0Stages - 1;
-    // stage nx_ % S was last read in iteration it - 1 and released by its closing barrier
+    // stage nx_ % S last held direction nx_ - S: refill it once every warp is done with that
     if (threadIdx.x == 0 && nx_ < total && aligned) {
+      const int prev = nx_ - kL0Stages;
+      if (prev >= 0 && !mbar_wait_bounded(&bar[kL0Stages + nx_ % kL0Stages], (uint32_t)(prev / kL0Stages) & 1u))
+        atomicExch(&s_abort, 1);
       fence_proxy_async();
       issue(nx_, nx_ % kL0Stages);
     }
-    const bool ok = mbar_wait_bounded(&bar[st], (uint32_t)(it / kL0Stages) & 1u);
-    if (__syncthreads_or(!ok)) {
+    const bool ok = !*(volatile int*)&s_abort && mbar_wait_bounded(&bar[st], (uint32_t)(it / kL0Stages) & 1u);
+    if (__any_sync(0xFFFFFFFFu, !ok)) {
+      if (lane == 0) atomicExch(&s_abort, 1);
       failed = true;
       break;
     }
@@ -465,7 +480,8 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
         if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + ch * chstride + zc * plane, o[0], o[1], o[2], o[3]);
       }
     }
-    __syncthreads();  // this stage may be refilled from the next iteration on
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&bar[kL0Stages + st]);  // this warp is done with the stage
   }
   if (!failed) {
 #pragma unroll
@@ -481,9 +497,10 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
       }
     }
   }
+  if (failed && lane == 0) atomicExch(err, 1);
   if (failed && threadIdx.x == 0) {
-    atomicExch(err, 1);
-    // the copies for iterations it .. it + S - 1 may still be in flight: let them land first
+    // thread 0 issued the copies up to direction it + S - 1 and waited for those
+    // before it: let the others land before the block's shared memory goes
     for (int j = it; j < it + kL0Stages && j < total; ++j)
       (void)mbar_wait_bounded(&bar[j % kL0Stages], (uint32_t)(j / kL0Stages) & 1u);
   }
