@@ -153,6 +153,39 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
     nreg = 1;
   }
   if (nreg == 0) return RC_OK;
+  {
+    // a small update travels in the launch's parameters: no copy, no staging slot
+    const size_t reg_off = (sizeof(QSphere) * (size_t)n + 15) & ~(size_t)15;
+    const size_t list_off = reg_off + sizeof(Region) * (size_t)nreg;
+    if (regions != &whole && list_off <= (size_t)kComposeInlineBytes) {
+      ComposeInline in;
+      if (n) memcpy(in.b, c->cur.data(), sizeof(QSphere) * n);
+      Region* ireg = reinterpret_cast<Region*>(in.b + reg_off);
+      memcpy(ireg, regions, sizeof(Region) * nreg);
+      // per-region sphere lists where they fit (sphere_lists falls back to
+      // "test every sphere" itself when they do not)
+      const int64_t room = ((int64_t)kComposeInlineBytes - (int64_t)list_off) / (int64_t)sizeof(int32_t);
+      if (room > 0)
+        (void)sphere_lists(c->cur.data(), n, c->p.grid, ireg, nreg, reinterpret_cast<int32_t*>(in.b + list_off), room);
+      else
+        for (int i = 0; i < nreg; ++i) {
+          ireg[i].s0 = 0;
+          ireg[i].sn = -1;
+        }
+      int64_t words = 0;
+      for (int i = 0; i < nreg; ++i)
+        words = std::max<int64_t>(words, (int64_t)(regions[i].w1 - regions[i].w0) * (regions[i].y1 - regions[i].y0) *
+                                             (regions[i].z1 - regions[i].z0));
+      const int threads = 256;
+      int64_t blocks = (words * 32 + threads - 1) / threads;
+      blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
+      k_compose_masks_inline<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
+          c->base, c->vol, c->occ, c->emis, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, n, (int)reg_off,
+          (int)list_off, c->mset, in);
+      RC_CUDA(cudaGetLastError(), "compose launch");
+      return RC_OK;
+    }
+  }
   char* st = static_cast<char*>(c->h_stage) + k * c->slot_bytes;
   if (n) memcpy(st, c->cur.data(), sizeof(QSphere) * n);
   Region* sreg = reinterpret_cast<Region*>(st + sizeof(QSphere) * c->sph_cap);
