@@ -248,9 +248,11 @@ __device__ __forceinline__ float emission_channel(const uint2* __restrict__ vol,
 // coordinate m/2 - 1/4, clamped at the border) of the child-averaged radiance.
 template <typename T, bool L0, bool TOP, bool CG>
 __device__ __forceinline__ void scalar_probe(const LevelArgs& a, int64_t p, int dp0, int ndp) {
-  const int mx = (int)(p % a.M[0]);
-  const int my = (int)((p / a.M[0]) % a.M[1]);
-  const int mz = (int)(p / ((int64_t)a.M[0] * a.M[1]));
+  // probe coordinates in 32-bit arithmetic (a level has fewer than 2^31 probes)
+  const uint32_t pu = (uint32_t)p, rowi = pu / (uint32_t)a.M[0];
+  const int mx = (int)(pu - rowi * (uint32_t)a.M[0]);
+  const int mz = (int)(rowi / (uint32_t)a.M[1]);
+  const int my = (int)(rowi - (uint32_t)mz * (uint32_t)a.M[1]);
   const int h = a.spacing >> 1;
   const int ox = mx * a.spacing + h, oy = my * a.spacing + h, oz = mz * a.spacing + h;
 

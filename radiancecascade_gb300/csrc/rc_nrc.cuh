@@ -952,7 +952,9 @@ __global__ void k_nrc_targets(const __grid_constant__ NrcArgs a, const uint2* __
 // index m sits at parent coordinate m/2 - 1/4, clamped): offsets and weights.
 __device__ __forceinline__ void merge_taps(const LevelArgs& a, int64_t p, int tap_off[8], float tap_w[8]) {
   const int Mx = a.M[0], My = a.M[1];
-  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  // probe coordinates in 32-bit arithmetic (a level has fewer than 2^31 probes)
+  const uint32_t pu = (uint32_t)p, rowi = pu / (uint32_t)Mx;
+  const int mx = (int)(pu - rowi * (uint32_t)Mx), mz = (int)(rowi / (uint32_t)My), my = (int)(rowi - (uint32_t)mz * (uint32_t)My);
   int qq[3][2];
   float wt[3][2];
   const int m[3] = {mx, my, mz};

@@ -124,6 +124,9 @@ __device__ __forceinline__ void update_masks(const MaskSet& ms, int lane, int wx
 // inside a sphere takes the value of the last such sphere of the list, else
 // its base value.  Each region tests only its own list of spheres (ascending
 // indices), or all of them.
+// INL: spheres, regions and lists sit in the launch's parameter block (their
+// reads need no range check: the block's size bounds them by construction).
+template <bool INL>
 static __device__ __forceinline__ void compose_masks_body(const uint2* __restrict__ base, uint2* __restrict__ vol, uint32_t* __restrict__ occ,
                                 uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W,
                                 const QSphere* __restrict__ sph, int ns, const Region* __restrict__ regs,
@@ -146,8 +149,8 @@ static __device__ __forceinline__ void compose_masks_body(const uint2* __restric
       uint2 v = RC_CHK(&base[idx], kChkVolume) ? base[idx] : make_uint2(0u, 0u);
       const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
       for (int k = 0; k < nt; ++k) {
-        const int si = r.sn < 0 ? k : (RC_CHK(slist + r.s0 + k, kChkSpheres) ? slist[r.s0 + k] : 0);
-        if (!RC_CHK(&sph[si], kChkSpheres)) continue;
+        const int si = r.sn < 0 ? k : ((INL || RC_CHK(slist + r.s0 + k, kChkSpheres)) ? slist[r.s0 + k] : 0);
+        if (!INL && !RC_CHK(&sph[si], kChkSpheres)) continue;
         const QSphere& S = sph[si];
         const int64_t dx = px - S.c[0], dy = py - S.c[1], dz = pz - S.c[2];
         if (dx > S.r || -dx > S.r || dy > S.r || -dy > S.r || dz > S.r || -dz > S.r) continue;
@@ -175,7 +178,7 @@ static __global__ void k_compose_masks(const uint2* __restrict__ base, uint2* __
                                 uint32_t* __restrict__ emis, int Gx, int Gy, int Gz, int W,
                                 const QSphere* __restrict__ sph, int ns, const Region* __restrict__ regs,
                                 const int32_t* __restrict__ slist, const MaskSet ms) {
-  compose_masks_body(base, vol, occ, emis, Gx, Gy, Gz, W, sph, ns, regs, slist, ms);
+  compose_masks_body<false>(base, vol, occ, emis, Gx, Gy, Gz, W, sph, ns, regs, slist, ms);
 }
 
 // The same update with the spheres, regions and sphere lists carried in the
@@ -189,7 +192,7 @@ static __global__ void k_compose_masks_inline(const uint2* __restrict__ base, ui
                                               uint32_t* __restrict__ occ, uint32_t* __restrict__ emis, int Gx, int Gy,
                                               int Gz, int W, int ns, int reg_off, int list_off, const MaskSet ms,
                                               const __grid_constant__ ComposeInline in) {
-  compose_masks_body(base, vol, occ, emis, Gx, Gy, Gz, W, reinterpret_cast<const QSphere*>(in.b), ns,
+  compose_masks_body<true>(base, vol, occ, emis, Gx, Gy, Gz, W, reinterpret_cast<const QSphere*>(in.b), ns,
                      reinterpret_cast<const Region*>(in.b + reg_off), reinterpret_cast<const int32_t*>(in.b + list_off),
                      ms);
 }

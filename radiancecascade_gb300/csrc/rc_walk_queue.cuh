@@ -675,7 +675,9 @@ template <typename T, bool L0, bool TOP, bool CG>
 __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* __restrict__ rec, int slots,
                                             int64_t p, int dpair) {
   const int Mx = a.M[0], My = a.M[1];
-  const int mx = (int)(p % Mx), my = (int)((p / Mx) % My), mz = (int)(p / ((int64_t)Mx * My));
+  // probe coordinates in 32-bit arithmetic (a level has fewer than 2^31 probes)
+  const uint32_t pu = (uint32_t)p, rowi = pu / (uint32_t)Mx;
+  const int mx = (int)(pu - rowi * (uint32_t)Mx), mz = (int)(rowi / (uint32_t)My), my = (int)(rowi - (uint32_t)mz * (uint32_t)My);
   const int g = (my << a.l2px) + mx;
   const int64_t rbase = (int64_t)(mz * a.wpp + (g >> 5)) * 32 + (g & 31);
   int tap_off[8];

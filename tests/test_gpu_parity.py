@@ -200,6 +200,34 @@ def test_incremental_updates_keep_the_volume_exact():
         assert rel_l2(e.fluence().astype(np.float64), oflu) <= FP32_REL_L2
 
 
+def test_large_and_small_updates_keep_the_volume_exact():
+    """An update whose spheres, regions and sphere lists fit 4 KB travels in
+    the compose launch's parameters; a larger one (here 120 moving spheres,
+    5.8 KB of spheres alone) goes through the pinned staging copy.  Through
+    moves of each kind (the sphere count fixed, so only the regions the
+    spheres left and entered are recomposed) the composed volume equals a
+    fresh voxelisation bit for bit, and the solve matches the oracle."""
+    boxes, _ = R.workload_scene("c64")
+    rng = np.random.default_rng(11)
+    many = np.zeros(120, R.SPHERE_DT)
+    many["centre"] = rng.uniform(0.0, 64.0, (120, 3))
+    many["radius"] = rng.uniform(1.0, 3.0, 120)
+    many["value"]["emission"] = np.float16(2.0).view(np.uint16)
+    many["value"]["albedo_occ"] = 0x8000
+    with R.Engine(R.make_params(64, 5)) as e:
+        e.set_boxes(boxes)
+        for sph in (many, many[:6].copy()):
+            for f in range(4):  # the first set recomposes the whole grid, then moves
+                if f:
+                    sph["centre"] += rng.uniform(-0.6, 0.6, (len(sph), 3))
+                e.set_spheres(sph)
+                want = O.voxelise(64, boxes, sph)
+                assert np.array_equal(e.volume().view(np.uint64), want.view(np.uint64)), (len(sph), f)
+            e.solve()
+            oflu, _ = O.solve(O.params(64, 5), O.voxelise(64, boxes, sph))
+            assert rel_l2(e.fluence().astype(np.float64), oflu) <= FP32_REL_L2
+
+
 def test_empty_scene_is_dark():
     gflu, gL = _solve_gpu(R.make_params(32, 4), vox=volume(np.zeros((32, 32, 32), bool), 0))
     assert not gflu.any() and all(not x.any() for x in gL)
