@@ -621,14 +621,18 @@ static __global__ void __launch_bounds__(kQueueThreads) k_walk_queue(const __gri
   walk_groups<4, Walker>(q, q.counter, q.total);
 }
 
-// The walks of levels that all have step tables (4 blocks/SM: 64 registers,
-// no spills; the extra resident warps hide the mask loads' latency).  The
+// The walks of levels that all have step tables: 10 steps per load batch, so
+// a lane has 20 mask loads in flight before it tests the first, at 2
+// blocks/SM (124 registers, no spills) -- the walks wait on those loads, and
+// more loads in flight per lane pay more than more resident warps (4
+// steps at 4 blocks/SM took 134 us where this takes 116 at 256^3).  The
 // walks are launched in the ordinary way (the wait returns at once) and let
 // the top level's merge launch early: it waits for their records.
-static __global__ void __launch_bounds__(kQueueThreads, 4) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
+constexpr int kTableWalkBatch = 10;
+static __global__ void __launch_bounds__(kQueueThreads, 2) k_walk_queue_tab(const __grid_constant__ QueueArgs q) {
   grid_dep_wait();
   grid_dep_release();
-  walk_groups<4, TableWalker>(q, q.counter, q.total);
+  walk_groups<kTableWalkBatch, TableWalker>(q, q.counter, q.total);
 }
 
 // Lanes per item of the step-table walk.  With more resident lanes than
@@ -648,13 +652,31 @@ inline int walk_group(int64_t items, int64_t resident_blocks) {
   return g;
 }
 
+// Blocks of the cooperative walk that fit the GPU at once (every G shares
+// the launch bounds and about the same registers).
+inline int64_t coop_walk_resident() {
+  static const int64_t r = [] {
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_queue_coop<8>, kQueueThreads, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return (int64_t)152 * 4;
+    }
+    return (int64_t)std::max(1, sms * per_sm);
+  }();
+  return r;
+}
+
 // The step-table walk of `q` (its counter already zeroed, q.total items):
-// enough blocks for G lanes per item, at most the `resident` blocks that fit
-// the GPU at once (every warp takes items until the queue is empty).
+// enough blocks for G lanes per item, at most the blocks that fit the GPU at
+// once (`resident` for one lane per item, the cooperative kernels' own
+// figure otherwise; every warp takes items until the queue is empty).
 inline void launch_table_walk(const QueueArgs& q, int64_t resident, cudaStream_t s) {
-  const int g = walk_group(q.total, resident);
+  const int64_t coop_resident = coop_walk_resident();
+  const int g = walk_group(q.total, coop_resident);
+  const int64_t cap = g > 1 ? coop_resident : resident;
   const unsigned blocks = (unsigned)std::max<int64_t>(
-      1, std::min<int64_t>((q.total * g + kQueueThreads - 1) / kQueueThreads, resident));
+      1, std::min<int64_t>((q.total * g + kQueueThreads - 1) / kQueueThreads, cap));
   switch (g) {
     case 2: k_walk_queue_coop<2><<<blocks, kQueueThreads, 0, s>>>(q); break;
     case 4: k_walk_queue_coop<4><<<blocks, kQueueThreads, 0, s>>>(q); break;
