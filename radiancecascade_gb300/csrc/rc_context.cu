@@ -132,6 +132,24 @@ rc_status ensure_sphere_capacity(rc_context* c, int n) {
   return RC_OK;
 }
 
+// A level kernel that may start while the one before it in the stream
+// finishes (programmatic stream serialization): it waits on the device
+// (grid_dep_wait) before it reads what that kernel wrote.
+template <typename... KArgs, typename... Args>
+void launch_overlapped(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Recompose the given regions of the volume from the base and the current
 // spheres.  regions == nullptr means the whole grid.
 rc_status recompose(rc_context* c, const Region* regions, int nreg) {
@@ -179,9 +197,11 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
       const int threads = 256;
       int64_t blocks = (words * 32 + threads - 1) / threads;
       blocks = std::min<int64_t>(std::max<int64_t>(blocks, 1), 152 * 16);
-      k_compose_masks_inline<<<dim3((unsigned)blocks, (unsigned)nreg), threads, 0, c->stream>>>(
-          c->base, c->vol, c->occ, c->emis, c->p.grid[0], c->p.grid[1], c->p.grid[2], c->W, n, (int)reg_off,
-          (int)list_off, c->mset, in);
+      // programmatic: the base reads and sphere tests overlap the previous
+      // frame's cascade 0, the writes wait for it on the device
+      launch_overlapped(k_compose_masks_inline, dim3((unsigned)blocks, (unsigned)nreg), dim3(threads), 0, c->stream,
+                        (const uint2*)c->base, c->vol, c->occ, c->emis, c->p.grid[0], c->p.grid[1], c->p.grid[2],
+                        c->W, n, (int)reg_off, (int)list_off, c->mset, in);
       RC_CUDA(cudaGetLastError(), "compose launch");
       return RC_OK;
     }
@@ -389,24 +409,6 @@ rc_status check_device_error(rc_context* c, const char* fn) {
     return RC_ERR_TIMEOUT;
   }
   return RC_OK;
-}
-
-// A level kernel that may start while the one before it in the stream
-// finishes (programmatic stream serialization): it waits on the device
-// (grid_dep_wait) before it reads what that kernel wrote.
-template <typename... KArgs, typename... Args>
-void launch_overlapped(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k, args...);
 }
 
 template <typename T, bool L0, bool TOP>

@@ -382,6 +382,7 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
   const bool aligned = ((smem_u32(tiles) | tile_stride) & 127u) == 0u;
   if (threadIdx.x == 0) {
     grid_dep_wait();  // cascade 1's child averages: the masks above came from earlier launches
+    grid_dep_release();  // the next frame's emitter update may start (it waits before it writes)
     if (aligned) {
       for (int k = 0; k < kL0Stages - 1 && k < total; ++k) issue(k, k);
     } else {

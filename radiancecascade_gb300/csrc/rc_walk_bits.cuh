@@ -144,9 +144,10 @@ static __device__ __forceinline__ void compose_masks_body(const uint2* __restric
     const int z = r.z0 + (int)(w / (nw * ny));
     const int x = wx * 32 + lane;
     bool opaque = false, emissive = false;
+    const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
+    uint2 v = make_uint2(0u, 0u);
     if (x < Gx) {
-      const int64_t idx = ((int64_t)z * Gy + y) * Gx + x;
-      uint2 v = RC_CHK(&base[idx], kChkVolume) ? base[idx] : make_uint2(0u, 0u);
+      v = RC_CHK(&base[idx], kChkVolume) ? base[idx] : make_uint2(0u, 0u);
       const int64_t px = (int64_t)(2 * x + 1) * 128, py = (int64_t)(2 * y + 1) * 128, pz = (int64_t)(2 * z + 1) * 128;
       for (int k = 0; k < nt; ++k) {
         const int si = r.sn < 0 ? k : ((INL || RC_CHK(slist + r.s0 + k, kChkSpheres)) ? slist[r.s0 + k] : 0);
@@ -159,10 +160,14 @@ static __device__ __forceinline__ void compose_masks_body(const uint2* __restric
           v.y = (uint32_t)S.value.emission[2] | ((uint32_t)S.value.albedo_occ << 16);
         }
       }
-      if (RC_CHK(&vol[idx], kChkVolume)) vol[idx] = v;
       opaque = (v.y >> 31) & 1u;
       emissive = opaque && (((v.x & 0x7FFF7FFFu) | (v.y & 0x7FFFu)) != 0u);
     }
+    // everything above reads only the static base and the spheres: with a
+    // programmatic launch it ran while the previous frame's last kernel,
+    // which reads the volume and bit planes, finished; the writes wait for it
+    grid_dep_wait();
+    if (x < Gx && RC_CHK(&vol[idx], kChkVolume)) vol[idx] = v;
     const unsigned bits = __ballot_sync(0xFFFFFFFFu, opaque);
     const unsigned ebits = __ballot_sync(0xFFFFFFFFu, emissive);
     if (lane == 0 && RC_CHK(&occ[((int64_t)z * Gy + y) * W + wx], kChkOccupancy) &&
