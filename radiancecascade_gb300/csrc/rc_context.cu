@@ -242,6 +242,13 @@ rc_status recompose(rc_context* c, const Region* regions, int nreg) {
 // merge kernel (narrow levels).
 enum { kModeScalar = 0, kModeFused = 1, kModeQueue = 2, kModeDirect0 = 3, kModeTma0 = 4 };
 
+// A level keeps decimated masks when it walks bit-parallel; the walk-free
+// cascade 0 reads the full-resolution bit planes instead, so its masks are
+// neither allocated nor updated.
+bool needs_mask(const bool* bits_level, const int* mode, int i) {
+  return bits_level[i] && !(i == 0 && (mode[0] == kModeDirect0 || mode[0] == kModeTma0));
+}
+
 struct MaskGeom {
   bool bits;
   int mode;
@@ -772,13 +779,13 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
       c->mode[i] = (i == 0 && level0_direct(*p, c->geom[0], force_scalar)) ? kModeDirect0 : mg.mode;
       c->rec_slots[i] = c->geom[i].M[2] * mg.wpp;
       off[i] = total;
-      if (mg.bits) total += (mg.words + 63) & ~(int64_t)63;
+      if (needs_mask(c->bits_level, c->mode, i)) total += (mg.words + 63) & ~(int64_t)63;
     }
     if (total && (s = dev_alloc((void**)&c->masks, total * 8, "decimated opacity and emission")) != RC_OK)
       return fail(s);
     if (total && (e = cudaMemset(c->masks, 0, total * 8)) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
     for (int i = 0; i < c->nlev; ++i) {
-      if (!c->bits_level[i]) continue;
+      if (!needs_mask(c->bits_level, c->mode, i)) continue;
       const MaskGeom mg = mask_geom(c->geom[i], force_scalar);
       MaskLevel& m = c->mset.lv[c->mset.n++];
       const LevelGeom& g = c->geom[i];
@@ -1674,7 +1681,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     v.bits_level[i] = mgs[i].bits;
     v.mode[i] = (i == 0 && level0_direct(*p, v.geom[0], force_scalar)) ? kModeDirect0 : mgs[i].mode;
     v.rec_slots[i] = v.geom[i].M[2] * mgs[i].wpp;
-    if (v.bits_level[i]) mask_off[i] = carve(off, (size_t)mgs[i].words * 8);
+    if (needs_mask(v.bits_level, v.mode, i)) mask_off[i] = carve(off, (size_t)mgs[i].words * 8);
   }
   mask_bytes = off - mask_begin;
   size_t avg_off[kMaxCascades] = {};
@@ -1754,7 +1761,7 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
     memset(&a, 0, sizeof a);
     int l2s = 0;
     while ((1 << l2s) < g.spacing) ++l2s;
-    if (v.bits_level[i]) {
+    if (needs_mask(v.bits_level, v.mode, i)) {
       MaskLevel& m = v.mset.lv[v.mset.n++];
       m.base = reinterpret_cast<uint2*>(scratch + mask_off[i]);
       m.l2s = l2s;
