@@ -256,10 +256,11 @@ rc_status rc_check_status(int32_t device, uint64_t* first_failure,
 
 /* ---- batched solve --------------------------------------------------- */
 /* Many independent scenes (each with its own rc_params: grid, cascades)
- * solved together.  rc_batch_solve launches one CUDA graph holding one
+ * solved together.  rc_batch_solve launches one CUDA graph holding either one
  * persistent kernel that takes (scene, level, tile) items from a queue, top
- * level first; a level waits (bounded) for the level above of its own scene.
- * Every scene must use the same precision. */
+ * level first, a level waiting (bounded) for the level above of its own
+ * scene; or every scene's own level launches as parallel branches (see
+ * rc_batch_tune for which).  Every scene must use the same precision. */
 typedef struct rc_batch rc_batch;
 rc_status rc_batch_create(const rc_params* params, int32_t nscenes,
                           int32_t device, rc_batch** out);
@@ -299,9 +300,17 @@ typedef struct rc_batch_tiles {
 /* Every field in [1, 65536]; rebuilds the queue (synchronises). */
 rc_status rc_batch_set_tiles(rc_batch* b, const rc_batch_tiles* tiles);
 rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out);
-/* Autotuner: coordinate descent over the tile shape, each candidate timed
- * over `iters` solves of the current scenes; keeps the fastest and reports it
- * (outputs may be NULL). */
+/* The form rc_batch_solve uses: *scene_launches = 1 for the scenes' own
+ * level launches as parallel graph branches, 0 for the persistent kernel. */
+rc_status rc_batch_get_form(const rc_batch* b, int32_t* scene_launches);
+/* Autotuner: coordinate descent over the tile shape of the persistent
+ * kernel, each candidate timed over `iters` solves of the current scenes;
+ * then one more candidate, the scenes' own level launches as parallel
+ * branches of the batch's graph.  Keeps the fastest form and reports it (the
+ * tiles are the persistent kernel's best; outputs may be NULL).  The
+ * environment variable RC_BATCH_MODE=persistent or =scenes, read when the
+ * batch is created, fixes the form instead (the tuner then times only it);
+ * rc_batch_set_tiles selects the persistent kernel. */
 rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best,
                         float* best_ms);
 

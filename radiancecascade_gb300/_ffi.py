@@ -132,6 +132,7 @@ SIGNATURES = {
     "rc_batch_get_fluence_all": (_S, [_P, _P, C.c_int64, C.c_int32]),
     "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_get_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
+    "rc_batch_get_form": (_S, [_P, C.POINTER(C.c_int32)]),
     "rc_batch_tune": (_S, [_P, C.c_int32, C.POINTER(BatchTiles), C.POINTER(C.c_float)]),
     "rc_nrc_param_count": (C.c_int32, []),
     "rc_nrc_params_default": (_S, [C.POINTER(NrcParams)]),

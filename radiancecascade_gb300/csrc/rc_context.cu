@@ -697,8 +697,9 @@ cudaError_t allow_bits_smem() {
 
 }  // namespace
 
-// Creates a context.  A minimal context (a scene of a batch) is solved only
-// through the batch kernel: it sets up no TMA descriptor.
+// Creates a context.  A minimal context is a scene of a batch (solved by the
+// batch's persistent kernel or by its own level launches inside the batch's
+// graph).
 static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc_context** out) {
   if (!out) {
     rcx::set_error("rc_create: out is NULL");
@@ -889,7 +890,7 @@ static rc_status create_ctx(const rc_params* p, int32_t device, bool minimal, rc
   }
   if ((s = dev_alloc((void**)&c->err, sizeof(int), "error flag")) != RC_OK) return fail(s);
   if ((e = cudaMemset(c->err, 0, sizeof(int))) != cudaSuccess) return fail(cuda_fail(e, "rc_create: memset"));
-  if (!minimal && !(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) {
+  if (!(getenv("RC_TMA") && strcmp(getenv("RC_TMA"), "0") == 0)) {
     setup_tma0(c);
     setup_tma_up(c);
   }
@@ -1829,6 +1830,14 @@ struct rc_batch {
   BatchTiles tiles{256, 4, 1, 1024};
   int blocks = 0;
   bool fp16 = false;
+  // per_scene: the solve is every scene's own level launches, as parallel
+  // branches of the graph (side streams while capturing), instead of the
+  // persistent kernel; the scenes' error flags are gathered into d_err
+  bool per_scene = false;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr;
+  int** d_errs = nullptr;
   cudaGraphExec_t graph = nullptr;
 };
 
@@ -1878,7 +1887,7 @@ rc_status batch_build(rc_batch* b, const BatchTiles& ts) {
         L.mode = kBatchBits;
         L.units = a.tiles * (i == 0 ? 1 : (a.n / 2) * (a.n / 2) / 2);
         L.ntiles = (L.units + ts.upi - 1) / ts.upi;
-      } else if (c->mode[i] == kModeDirect0) {
+      } else if (c->mode[i] == kModeDirect0 || c->mode[i] == kModeTma0) {  // the walk-free form either way
         L.mode = kBatchDirect0;
         const int64_t warps = (int64_t)((a.M[0] + 127) / 128) * a.M[1] * ((a.M[2] + 1) / 2);
         L.units = (int)((warps + 7) / 8);
@@ -1958,12 +1967,64 @@ void batch_enqueue(rc_batch* b, cudaStream_t s) {
                                                                           b->tiles, b->d_next, b->d_done, b->d_err);
 }
 
-// The whole batch solve as one CUDA graph (two counter resets + one launch).
+// A scene's bounded waits report into its own flag: after a per-scene solve
+// the flags are moved into the batch's.
+__global__ void k_gather_errors(int* const* errs, int n, int* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int f = *errs[i];
+    if (f) {
+      atomicMax(out, f);
+      *errs[i] = 0;
+    }
+  }
+}
+
+// Every scene's solve on its own branch: fork from the batch stream, one side
+// stream per scene (up to 64, reused round robin), join, gather the flags.
+void batch_enqueue_scenes(rc_batch* b, cudaStream_t s) {
+  cudaEventRecord(b->fork, s);
+  const int ns = (int)b->side.size();
+  for (int k = 0; k < b->n; ++k) {
+    cudaStream_t sk = b->side[k % ns];
+    if (k < ns) cudaStreamWaitEvent(sk, b->fork, 0);
+    (void)enqueue_solve(b->scenes[k], sk);
+  }
+  for (int j = 0; j < ns; ++j) {
+    cudaEventRecord(b->joins[j], b->side[j]);
+    cudaStreamWaitEvent(s, b->joins[j], 0);
+  }
+  k_gather_errors<<<1, 256, 0, s>>>(b->d_errs, b->n, b->d_err);
+}
+
+rc_status batch_side_streams(rc_batch* b) {
+  if (!b->side.empty()) return RC_OK;
+  const int ns = std::min(b->n, 64);
+  RC_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch fork event");
+  for (int j = 0; j < ns; ++j) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    RC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "batch side stream");
+    b->side.push_back(st);
+    RC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "batch join event");
+    b->joins.push_back(ev);
+  }
+  return RC_OK;
+}
+
+// The whole batch solve as one CUDA graph: two counter resets + the
+// persistent launch, or the scenes' own launches in parallel branches.
 rc_status batch_graph(rc_batch* b) {
   if (b->graph) return RC_OK;
+  if (b->per_scene) {
+    rc_status s = batch_side_streams(b);
+    if (s != RC_OK) return s;
+  }
   cudaGraph_t graph = nullptr;
   RC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture");
-  batch_enqueue(b, b->stream);
+  if (b->per_scene)
+    batch_enqueue_scenes(b, b->stream);
+  else
+    batch_enqueue(b, b->stream);
   cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
   if (e != cudaSuccess) return cuda_fail(e, "batch capture");
   e = cudaGraphInstantiate(&b->graph, graph, 0);
@@ -2044,7 +2105,16 @@ rc_status rc_batch_create(const rc_params* params, int32_t nscenes, int32_t devi
     if ((e = cudaMemcpy(b->d_qargs, qa.data(), qa.size() * sizeof(QueueArgs), cudaMemcpyHostToDevice)) != cudaSuccess)
       return fail(cuda_fail(e, "rc_batch_create: upload"));
   }
+  {
+    std::vector<int*> errs((size_t)nscenes);
+    for (int k = 0; k < nscenes; ++k) errs[k] = b->scenes[k]->err;
+    if ((s = dev_alloc((void**)&b->d_errs, errs.size() * sizeof(int*), "batch scene flags")) != RC_OK) return fail(s);
+    if ((e = cudaMemcpy(b->d_errs, errs.data(), errs.size() * sizeof(int*), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(cuda_fail(e, "rc_batch_create: upload"));
+  }
   if ((s = batch_build(b, b->tiles)) != RC_OK) return fail(s);
+  // RC_BATCH_MODE=scenes / persistent fixes the form (the autotuner then keeps it)
+  if (const char* m = getenv("RC_BATCH_MODE")) b->per_scene = strcmp(m, "scenes") == 0;
   *out = b;
   return RC_OK;
 }
@@ -2055,9 +2125,12 @@ rc_status rc_batch_destroy(rc_batch* b) {
     DeviceGuard g(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     batch_free_graph(b);
-    void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err};
+    void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err, b->d_errs};
     for (void* x : bufs)
       if (x) cudaFree(x);
+    for (cudaStream_t st : b->side) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->stream) cudaStreamDestroy(b->stream);
   }
   for (rc_context* c : b->scenes) release(c);
@@ -2186,6 +2259,7 @@ rc_status rc_batch_set_tiles(rc_batch* b, const rc_batch_tiles* tiles) {
   DeviceGuard g(b->device);
   RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_set_tiles");
   const BatchTiles ts{tiles->probes_per_item, tiles->dirs_per_item, tiles->blocks_per_item, tiles->walks_per_item};
+  if (!getenv("RC_BATCH_MODE")) b->per_scene = false;  // tiles shape the persistent kernel
   return batch_build(b, ts);
 }
 
@@ -2202,9 +2276,21 @@ rc_status rc_batch_get_tiles(const rc_batch* b, rc_batch_tiles* out) {
   return RC_OK;
 }
 
+rc_status rc_batch_get_form(const rc_batch* b, int32_t* scene_launches) {
+  if (batch_check(b, "rc_batch_get_form") != RC_OK) return RC_ERR_INVALID_ARG;
+  if (!scene_launches) {
+    rcx::set_error("rc_batch_get_form: out is NULL");
+    return RC_ERR_INVALID_ARG;
+  }
+  *scene_launches = b->per_scene ? 1 : 0;
+  return RC_OK;
+}
+
 // Coordinate descent over the tile shape: each parameter in turn over its
 // candidates with the others held, two sweeps, every candidate timed over
-// `iters` graph launches after one warm-up launch.
+// `iters` graph launches after one warm-up launch; then the scenes' own
+// launches as parallel graph branches, kept when faster (RC_BATCH_MODE fixes
+// the form instead).
 rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best_out, float* best_ms) {
   if (batch_check(b, "rc_batch_tune") != RC_OK) return RC_ERR_INVALID_ARG;
   if (iters < 1) {
@@ -2219,6 +2305,9 @@ rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best_out, fl
   BatchTiles best = b->tiles;
   float best_t = 3.4e38f;
   rc_status st = RC_OK;
+  const bool fixed = getenv("RC_BATCH_MODE") != nullptr;
+  const bool scenes_only = fixed && b->per_scene;
+  if (!scenes_only) b->per_scene = false;
   auto time_shape = [&](const BatchTiles& ts, float* ms) -> rc_status {
     rc_status r;
     if ((r = batch_build(b, ts)) != RC_OK) return r;
@@ -2233,7 +2322,7 @@ rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best_out, fl
     return RC_OK;
   };
   st = time_shape(best, &best_t);
-  for (int sweep = 0; sweep < 2 && st == RC_OK; ++sweep)
+  for (int sweep = 0; sweep < 2 && st == RC_OK && !scenes_only; ++sweep)
     for (int dim = 0; dim < 4 && st == RC_OK; ++dim)
       for (int ci = 0; ci < 4 && st == RC_OK; ++ci) {
         BatchTiles ts = best;
@@ -2247,6 +2336,16 @@ rc_status rc_batch_tune(rc_batch* b, int32_t iters, rc_batch_tiles* best_out, fl
           best = ts;
         }
       }
+  if (st == RC_OK && !fixed) {
+    // the scenes' own launches, in parallel graph branches
+    b->per_scene = true;
+    float ms = 0.f;
+    st = time_shape(best, &ms);
+    if (st == RC_OK && ms < best_t)
+      best_t = ms;
+    else
+      b->per_scene = false;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st != RC_OK) return st;

@@ -734,6 +734,13 @@ class Batch:
         F.check(self._lib.rc_batch_get_tiles(self.handle, C.byref(t)))
         return {k: getattr(t, k) for k, _ in t._fields_}
 
+    def form(self) -> str:
+        """"scenes" (every scene's own launches as parallel graph branches) or
+        "persistent" (one persistent kernel over a queue of tiles)."""
+        v = C.c_int32()
+        F.check(self._lib.rc_batch_get_form(self.handle, C.byref(v)))
+        return "scenes" if v.value else "persistent"
+
     def tune(self, iters: int = 3):
         """Autotunes the tile shape; -> (tiles dict, ms per solve of the best)."""
         t, ms = F.BatchTiles(), C.c_float()

@@ -106,9 +106,13 @@ def test_batch_matches_single_contexts():
 
 
 def test_batch_autotuner_keeps_a_candidate(oracle_results):
+    """The tuner times the persistent kernel's tile shapes and the scenes' own
+    launches, keeps the faster form (persistent until tuned), and either gives
+    the oracle's results."""
     with _batch() as b:
+        assert b.form() == "persistent"
         tiles, ms = b.tune(iters=1)
-        assert tiles == b.tiles() and ms > 0
+        assert tiles == b.tiles() and ms > 0 and b.form() in ("persistent", "scenes")
         b.solve()
         _check_all(b, oracle_results)
 
@@ -203,3 +207,28 @@ def test_moving_emitters_between_solves_and_one_fluence_read():
             F.check(F.lib().rc_batch_get_fluence_all(b.handle, F.ptr(flat), flat.size - 1, F.RC_MEM_HOST))
     finally:
         b.close()
+
+
+def test_batch_as_parallel_scene_launches_matches_oracle(monkeypatch, oracle_results):
+    """The other form of the batched solve (RC_BATCH_MODE=scenes): every
+    scene's own level launches as parallel branches of one graph.  Every
+    scene matches the oracle, a second launch of the graph gives the same
+    results, and moving emitters between solves are seen in order."""
+    monkeypatch.setenv("RC_BATCH_MODE", "scenes")
+    with _batch() as b:
+        assert b.form() == "scenes"
+        b.solve()
+        _check_all(b, oracle_results)
+        b.solve()
+        _check_all(b, oracle_results)
+        tiles, ms = b.tune(iters=1)  # the form is fixed: only timed
+        assert ms > 0 and b.form() == "scenes"
+        sph = [_scene(grid, seed)[1].copy() for grid, _, seed in SCENES]
+        for k, (grid, _, _) in enumerate(SCENES):
+            R.advance_spheres(sph[k], grid, 2)
+            b.set_spheres(k, sph[k])
+        b.solve()
+        for k, (grid, N, seed) in enumerate(SCENES):
+            boxes, _ = _scene(grid, seed)
+            oflu, _ = O.solve(O.params(grid, N), O.voxelise(grid, boxes, sph[k]), jump=True)
+            assert rel_l2(b.fluence(k).reshape(-1, 3).astype(np.float64), oflu) <= FP32_REL_L2, k
