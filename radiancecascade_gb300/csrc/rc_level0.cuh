@@ -389,6 +389,18 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
       atomicExch(err, 2);
     }
   }
+  // every direction's start octant and solid angle, lane l holding
+  // directions l and l + 32 (handed out by shuffles; more than 64 directions
+  // read the table in the loop)
+  int oct_lane[2] = {0, 0};
+  float om_lane[2] = {0.f, 0.f};
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+    if (lane + 32 * h < total) {
+      const DirInfo& dl = a.dirs[lane + 32 * h];
+      oct_lane[h] = (dl.start_off[0] + 1) + 2 * (dl.start_off[1] + 1) + 4 * (dl.start_off[2] + 1);
+      om_lane[h] = dl.omega;
+    }
   float flu[3][ZC][4];
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch)
@@ -415,14 +427,22 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
       failed = true;
       break;
     }
-    const DirInfo& di = a.dirs[d];
-    const int ox = di.start_off[0] + 1, oy = di.start_off[1] + 1, oz = di.start_off[2] + 1;
-    const int oct = ox + 2 * oy + 4 * oz;
+    int oct;
+    float om;
+    if (total <= 64) {
+      const bool h = d >= 32;
+      oct = __shfl_sync(0xFFFFFFFFu, h ? oct_lane[1] : oct_lane[0], d & 31);
+      om = __shfl_sync(0xFFFFFFFFu, h ? om_lane[1] : om_lane[0], d & 31);
+    } else {
+      const DirInfo& di = a.dirs[d];
+      oct = (di.start_off[0] + 1) + 2 * (di.start_off[1] + 1) + 4 * (di.start_off[2] + 1);
+      om = di.omega;
+    }
+    const int ox = oct & 1, oy = (oct >> 1) & 1, oz = oct >> 2;
     const bool hi_oct = oct >= 4;
     const unsigned opq = ((hi_oct ? oct_opq[1] : oct_opq[0]) >> (8 * (oct & 3))) & 0xFFu;
     const unsigned ems = ((hi_oct ? oct_ems[1] : oct_ems[0]) >> (8 * (oct & 3))) & 0xFFu;
     const bool merge = __any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u);
-    const float om = di.omega;
     T* lrow = L + (int64_t)d * a.P + p0;
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {

@@ -92,6 +92,8 @@ def test_golden_fixtures(name, walk):
     # elongated grids: 1024 voxels (the largest edge) along one axis, few along the others
     ((1024, 32, 64), 5, {}),
     ((32, 512, 32), 4, dict(dir_res0=6)),
+    # 100 directions at cascade 0: more than the walk-free kernel keeps in lanes
+    ((64, 64, 64), 3, dict(dir_res0=10)),
 ])
 def test_other_shapes_match_oracle(grid, N, kw, walk):
     spec = R.scene_spec(grid, 12, (3, 12), 3, (1.5, 4.0), (1.0, 20.0))
