@@ -232,3 +232,13 @@ def test_batch_as_parallel_scene_launches_matches_oracle(monkeypatch, oracle_res
             boxes, _ = _scene(grid, seed)
             oflu, _ = O.solve(O.params(grid, N), O.voxelise(grid, boxes, sph[k]), jump=True)
             assert rel_l2(b.fluence(k).reshape(-1, 3).astype(np.float64), oflu) <= FP32_REL_L2, k
+
+
+def test_batch_as_parallel_scene_launches_fp16(monkeypatch, oracle_results):
+    """The scene-launch form with FP16 radiance storage: every scene within
+    1% of the FP64 oracle."""
+    monkeypatch.setenv("RC_BATCH_MODE", "scenes")
+    with _batch("fp16") as b:
+        assert b.form() == "scenes"
+        b.solve()
+        _check_all(b, oracle_results, rel=1e-2, max_rel=None)
