@@ -373,27 +373,31 @@ def batch_measure(args, R, local, dist, world, steps):
 
     # e2e: per step every scene's spheres advance one frame and are uploaded
     # (incremental re-voxelisation on the batch stream), one solve, one read of
-    # every fluence into pinned host memory
+    # every fluence into pinned host memory -- started without waiting, into
+    # one of two buffers in turn, so the next step's host work overlaps this
+    # step's solve and read-back (every read is complete at the final wait)
     sph = [sx.copy() for _, _, _, sx in items]
     nbytes_in = sum(int(sx.nbytes) for sx in sph)
-    flat = torch.empty(b.fluence_elems(), dtype=torch.float32, pin_memory=True).numpy()
-    nbytes_out = int(flat.nbytes)
+    flats = [torch.empty(b.fluence_elems(), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+    nbytes_out = int(flats[0].nbytes)
 
-    def e2e_step():
+    def e2e_step(f):
         for k, (edge, _, _, _) in enumerate(items):
             R.advance_spheres(sph[k], edge, 1)
             b.set_spheres(k, sph[k])
         b.solve()
-        b.fluence_all(flat)
+        b.fluence_all_async(flats[f & 1])
 
-    for _ in range(2):
-        e2e_step()
+    for f in range(2):
+        e2e_step(f)
+    b.synchronize()
     if dist:
         dist.barrier()
     e2e_steps = max(3, min(steps, 50))
     w0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
+    for f in range(e2e_steps):
+        e2e_step(f)
+    b.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - w0, dist)
     e2e_value = world * len(items) * e2e_steps / e2e_s
 

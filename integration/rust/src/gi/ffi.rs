@@ -242,6 +242,7 @@ extern "C" {
                                  where_: i32) -> rc_status;
     pub fn rc_batch_set_spheres(b: *mut rc_batch, scene: i32, spheres: *const rc_sphere, n: i32) -> rc_status;
     pub fn rc_batch_get_fluence_all(b: *mut rc_batch, out: *mut f32, elems: i64, where_: i32) -> rc_status;
+    pub fn rc_batch_get_fluence_all_async(b: *mut rc_batch, out: *mut f32, elems: i64) -> rc_status;
     pub fn rc_batch_set_tiles(b: *mut rc_batch, tiles: *const rc_batch_tiles) -> rc_status;
     pub fn rc_batch_get_tiles(b: *const rc_batch, out: *mut rc_batch_tiles) -> rc_status;
     pub fn rc_batch_get_form(b: *const rc_batch, scene_launches: *mut i32) -> rc_status;

@@ -130,6 +130,7 @@ SIGNATURES = {
     "rc_check_status": (_S, [C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_uint32)]),
     "rc_get_stage_ms": (_S, [_P, _P, C.c_int32]),
     "rc_batch_get_fluence_all": (_S, [_P, _P, C.c_int64, C.c_int32]),
+    "rc_batch_get_fluence_all_async": (_S, [_P, _P, C.c_int64]),
     "rc_batch_set_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_get_tiles": (_S, [_P, C.POINTER(BatchTiles)]),
     "rc_batch_get_form": (_S, [_P, C.POINTER(C.c_int32)]),

@@ -2239,6 +2239,27 @@ rc_status rc_batch_get_fluence_all(rc_batch* b, float* out, int64_t elems, int32
   return rc_batch_synchronize(b);
 }
 
+rc_status rc_batch_get_fluence_all_async(rc_batch* b, float* out, int64_t elems) {
+  if (batch_check(b, "rc_batch_get_fluence_all_async") != RC_OK) return RC_ERR_INVALID_ARG;
+  int64_t need = 0;
+  for (int k = 0; k < b->n; ++k) need += b->scenes[k]->geom[0].probes() * 3;
+  if (!out || elems != need) {
+    rcx::set_error("rc_batch_get_fluence_all_async: need a non-NULL host buffer of exactly %lld floats",
+                   (long long)need);
+    return RC_ERR_INVALID_ARG;
+  }
+  DeviceGuard g(b->device);
+  int64_t off = 0;
+  for (int k = 0; k < b->n; ++k) {
+    const rc_context* c = b->scenes[k];
+    const size_t bytes = (size_t)c->geom[0].probes() * 3 * sizeof(float);
+    RC_CUDA(cudaMemcpyAsync(out + off, c->fluence, bytes, cudaMemcpyDeviceToHost, b->stream),
+            "rc_batch_get_fluence_all_async");
+    off += c->geom[0].probes() * 3;
+  }
+  return RC_OK;
+}
+
 rc_status rc_batch_get_radiance(rc_batch* b, int32_t scene, int32_t level, void* out, int64_t bytes, int32_t where) {
   if (batch_check(b, "rc_batch_get_radiance") != RC_OK) return RC_ERR_INVALID_ARG;
   if (scene < 0 || scene >= b->n) {

@@ -702,6 +702,12 @@ class Batch:
         F.check(self._lib.rc_batch_get_fluence_all(self.handle, F.ptr(out), n, F.RC_MEM_HOST))
         return out
 
+    def fluence_all_async(self, out: np.ndarray) -> None:
+        """Starts reading every scene's fluence into `out` (a pinned array of
+        fluence_elems() floats) after the solves enqueued so far; complete
+        after synchronize()."""
+        F.check(self._lib.rc_batch_get_fluence_all_async(self.handle, F.ptr(out), out.size))
+
     def solve(self, stream: Optional[int] = None) -> None:
         F.check(self._lib.rc_batch_solve(self.handle, C.c_void_p(stream) if stream else None))
 

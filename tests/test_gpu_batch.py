@@ -242,3 +242,26 @@ def test_batch_as_parallel_scene_launches_fp16(monkeypatch, oracle_results):
         assert b.form() == "scenes"
         b.solve()
         _check_all(b, oracle_results, rel=1e-2, max_rel=None)
+
+
+def test_async_fluence_read_matches_the_synchronous_one():
+    """rc_batch_get_fluence_all_async starts the read on the batch stream and
+    returns; after synchronize it holds the same floats as the synchronous
+    read, and an emitter update plus solve enqueued right after it do not
+    disturb it (they run after the copies)."""
+    b = _batch()
+    try:
+        b.solve()
+        want = b.fluence_all()
+        got = np.full(want.size, np.nan, np.float32)
+        b.fluence_all_async(got)
+        sph = _scene(SCENES[0][0], SCENES[0][2])[1].copy()
+        R.advance_spheres(sph, SCENES[0][0], 3)
+        b.set_spheres(0, sph)
+        b.solve()
+        b.synchronize()
+        assert np.array_equal(got, want)
+        with pytest.raises(R.RCError):
+            F.check(F.lib().rc_batch_get_fluence_all_async(b.handle, F.ptr(got), got.size - 1))
+    finally:
+        b.close()
