@@ -1837,6 +1837,12 @@ struct rc_batch {
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> joins;
   cudaEvent_t fork = nullptr;
+  // scene-launch form: emitter updates run on the side streams, each after
+  // the batch stream's work so far (ev_batch), and the next solve waits for
+  // the side streams used since the last one (pending)
+  cudaEvent_t ev_batch = nullptr;
+  std::vector<cudaEvent_t> ev_side;
+  std::vector<char> pending;
   int** d_errs = nullptr;
   cudaGraphExec_t graph = nullptr;
 };
@@ -2000,13 +2006,29 @@ rc_status batch_side_streams(rc_batch* b) {
   if (!b->side.empty()) return RC_OK;
   const int ns = std::min(b->n, 64);
   RC_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch fork event");
+  RC_CUDA(cudaEventCreateWithFlags(&b->ev_batch, cudaEventDisableTiming), "batch event");
   for (int j = 0; j < ns; ++j) {
     cudaStream_t st = nullptr;
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t ev = nullptr, es = nullptr;
     RC_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "batch side stream");
     b->side.push_back(st);
     RC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "batch join event");
     b->joins.push_back(ev);
+    RC_CUDA(cudaEventCreateWithFlags(&es, cudaEventDisableTiming), "batch side event");
+    b->ev_side.push_back(es);
+  }
+  b->pending.assign((size_t)ns, 0);
+  return RC_OK;
+}
+
+// Before work on the batch stream that reads what emitter updates on side
+// streams wrote: the batch stream waits for every side stream used since.
+rc_status batch_join_updates(rc_batch* b) {
+  for (size_t j = 0; j < b->pending.size(); ++j) {
+    if (!b->pending[j]) continue;
+    RC_CUDA(cudaEventRecord(b->ev_side[j], b->side[j]), "batch update join");
+    RC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_side[j], 0), "batch update join");
+    b->pending[j] = 0;
   }
   return RC_OK;
 }
@@ -2128,9 +2150,12 @@ rc_status rc_batch_destroy(rc_batch* b) {
     void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err, b->d_errs};
     for (void* x : bufs)
       if (x) cudaFree(x);
+    for (cudaStream_t st : b->side) cudaStreamSynchronize(st);
     for (cudaStream_t st : b->side) cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : b->ev_side) cudaEventDestroy(ev);
     if (b->fork) cudaEventDestroy(b->fork);
+    if (b->ev_batch) cudaEventDestroy(b->ev_batch);
     if (b->stream) cudaStreamDestroy(b->stream);
   }
   for (rc_context* c : b->scenes) release(c);
@@ -2146,8 +2171,10 @@ rc_status rc_batch_scene_set(rc_batch* b, int32_t scene, const rc_box* boxes, in
     return RC_ERR_INVALID_ARG;
   }
   {
-    // the scene's volume must not change under a solve in flight
+    // the scene's volume must not change under a solve or an update in flight
     DeviceGuard g(b->device);
+    rc_status s0 = batch_join_updates(b);
+    if (s0 != RC_OK) return s0;
     RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_scene_set");
   }
   rc_status s = rc_scene_set_boxes(b->scenes[scene], boxes, nboxes);
@@ -2171,11 +2198,18 @@ rc_status rc_batch_solve(rc_batch* b, void* stream) {
   DeviceGuard g(b->device);
   rc_status s = batch_graph(b);
   if (s != RC_OK) return s;
+  if ((s = batch_join_updates(b)) != RC_OK) return s;
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  cudaEvent_t ev = nullptr;
+  if (st != b->stream) {
+    // the caller's stream first waits for the batch stream's work (emitter
+    // updates), then the batch stream for the solve
+    RC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "rc_batch_solve: event");
+    cudaEventRecord(ev, b->stream);
+    cudaStreamWaitEvent(st, ev, 0);
+  }
   RC_CUDA(cudaGraphLaunch(b->graph, st), "rc_batch_solve: graph launch");
   if (st != b->stream) {
-    cudaEvent_t ev;
-    RC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "rc_batch_solve: event");
     cudaEventRecord(ev, st);
     cudaStreamWaitEvent(b->stream, ev, 0);
     cudaEventDestroy(ev);
@@ -2186,6 +2220,8 @@ rc_status rc_batch_solve(rc_batch* b, void* stream) {
 rc_status rc_batch_synchronize(rc_batch* b) {
   if (batch_check(b, "rc_batch_synchronize") != RC_OK) return RC_ERR_INVALID_ARG;
   DeviceGuard g(b->device);
+  rc_status s = batch_join_updates(b);  // emitter updates still on side streams
+  if (s != RC_OK) return s;
   RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_synchronize");
   return batch_error_flag(b, "rc_batch_synchronize");
 }
@@ -2213,7 +2249,20 @@ rc_status rc_batch_set_spheres(rc_batch* b, int32_t scene, const rc_sphere* sphe
   rc_context* c = b->scenes[scene];
   DeviceGuard g(b->device);
   cudaStream_t own = c->stream;
-  c->stream = b->stream;
+  cudaStream_t st = b->stream;
+  if (b->per_scene) {
+    // the scene-launch form: the update runs on the scene's side stream,
+    // after everything enqueued on the batch stream so far (the solve that
+    // reads the old volume); the next solve waits for it
+    rc_status s0 = batch_side_streams(b);
+    if (s0 != RC_OK) return s0;
+    const size_t j = (size_t)scene % b->side.size();
+    RC_CUDA(cudaEventRecord(b->ev_batch, b->stream), "rc_batch_set_spheres: event");
+    RC_CUDA(cudaStreamWaitEvent(b->side[j], b->ev_batch, 0), "rc_batch_set_spheres: wait");
+    st = b->side[j];
+    b->pending[j] = 1;
+  }
+  c->stream = st;
   const rc_status s = rc_scene_set_spheres(c, spheres, n);  // its message names the failing check
   c->stream = own;
   return s;
