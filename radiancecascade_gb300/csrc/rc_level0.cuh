@@ -66,6 +66,14 @@ __device__ __forceinline__ float2 load2<__half, true>(const __half* p) {
   return __half22float2(*reinterpret_cast<const __half2*>(&u));
 }
 
+// Two adjacent shared-memory values at an even index (one 8- or 4-byte load).
+__device__ __forceinline__ float2 lds_pair(const float* p) {
+  return RC_CHK(p + 1, kChkShared) ? *reinterpret_cast<const float2*>(p) : make_float2(0.f, 0.f);
+}
+__device__ __forceinline__ float2 lds_pair(const __half* p) {
+  return RC_CHK(p + 1, kChkShared) ? __half22float2(*reinterpret_cast<const __half2*>(p)) : make_float2(0.f, 0.f);
+}
+
 // Requires (checked on the host): probe spacing 2 (centres 2m+1, so the 8
 // candidate voxels are 2m, 2m+1 per axis), every cascade-0 direction takes 0
 // steps, and M[0] % 4 == 0.
@@ -443,6 +451,15 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
     const unsigned opq = ((hi_oct ? oct_opq[1] : oct_opq[0]) >> (8 * (oct & 3))) & 0xFFu;
     const unsigned ems = ((hi_oct ? oct_ems[1] : oct_ems[0]) >> (8 * (oct & 3))) & 0xFFu;
     const bool merge = __any_sync(0xFFFFFFFFu, (valid & ~opq) != 0u);
+    const unsigned emv = ems & valid;
+    // Each output's final scale, taken once per direction for all channels:
+    // 1/64 where the start voxel is clear, 0 where it is opaque (the blend of
+    // non-negative radiance times 0 is +0, as the plain select gave).
+    float sc[ZC][4];
+#pragma unroll
+    for (int zc = 0; zc < ZC; ++zc)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) sc[zc][e] = ((opq >> (zc * 4 + e)) & 1u) ? 0.f : (1.f / 64.f);
     T* lrow = L + (int64_t)d * a.P + p0;
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) {
@@ -459,8 +476,9 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
           for (int k = 0; k < PZ; ++k) {
             const T* row = tile + rowoff[r][k];
             cv[k][0] = RC_CHK(&row[lcol], kChkShared) ? to_float(row[lcol]) : 0.f;
-            cv[k][1] = RC_CHK(&row[c0], kChkShared) ? to_float(row[c0]) : 0.f;
-            cv[k][2] = RC_CHK(&row[c0 + 1], kChkShared) ? to_float(row[c0 + 1]) : 0.f;
+            const float2 own = lds_pair(row + c0);  // c0 and the row offsets are even (UMx is)
+            cv[k][1] = own.x;
+            cv[k][2] = own.y;
             cv[k][3] = RC_CHK(&row[rcol], kChkShared) ? to_float(row[rcol]) : 0.f;
           }
 #pragma unroll
@@ -478,26 +496,28 @@ __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
           float v[4];
 #pragma unroll
           for (int c = 0; c < 4; ++c) v[c] = fmaf(3.f, zr[zc][0][c], zr[zc][1][c]);
-          mv[zc][0] = fmaf(3.f, v[1], v[0]) * (1.f / 64.f);
-          mv[zc][1] = fmaf(3.f, v[1], v[2]) * (1.f / 64.f);
-          mv[zc][2] = fmaf(3.f, v[2], v[1]) * (1.f / 64.f);
-          mv[zc][3] = fmaf(3.f, v[2], v[3]) * (1.f / 64.f);
+          mv[zc][0] = fmaf(3.f, v[1], v[0]) * sc[zc][0];
+          mv[zc][1] = fmaf(3.f, v[1], v[2]) * sc[zc][1];
+          mv[zc][2] = fmaf(3.f, v[2], v[1]) * sc[zc][2];
+          mv[zc][3] = fmaf(3.f, v[2], v[3]) * sc[zc][3];
         }
       }
 #pragma unroll
       for (int zc = 0; zc < ZC; ++zc) {
         float o[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int bit = zc * 4 + e;
-          o[e] = ((opq >> bit) & 1u) ? 0.f : mv[zc][e];
-          if ((ems >> bit) & 1u) {  // emissive start voxel (rare)
-            const int64_t vidx =
-                ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + 2 * (x0 + e) + ox;
-            o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
-          }
-          flu[ch][zc][e] = fmaf(om, o[e], flu[ch][zc][e]);
+        for (int e = 0; e < 4; ++e) o[e] = mv[zc][e];
+        if ((emv >> (zc * 4)) & 0xFu) {  // an emissive start voxel in this plane (rare)
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if ((emv >> (zc * 4 + e)) & 1u) {
+              const int64_t vidx =
+                  ((int64_t)(2 * (z0 + zc) + oz) * a.G[1] + (2 * y + oy)) * a.G[0] + 2 * (x0 + e) + ox;
+              o[e] = emission_channel(a.vol, (uint32_t)vidx, ch);
+            }
         }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) flu[ch][zc][e] = fmaf(om, o[e], flu[ch][zc][e]);
         if ((valid >> (zc * 4)) & 1u) Vec4<T>::stream(lrow + ch * chstride + zc * plane, o[0], o[1], o[2], o[3]);
       }
     }

@@ -359,14 +359,17 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
 // The y blends (child rows ey = 0, 1) of one channel's three z-blended parent
 // rows, then the x blend through the lanes' columns (lane l holds parent
 // column (l + 1) / 2 - 1 + ...: src_near / src_far are the weight-3/4 and
-// weight-1/4 columns of the lane's child).  All lanes take part.
-__device__ __forceinline__ void yx_blend(const float zv[3], int src_near, int src_far, float& out0, float& out1) {
+// weight-1/4 columns of the lane's child).  All lanes take part.  s0, s1:
+// each child's final scale, 1/64 (the three blends' factor) where its ray
+// missed and 0 where it hit, so that no select follows.
+__device__ __forceinline__ void yx_blend(const float zv[3], int src_near, int src_far, float s0, float s1, float& out0,
+                                         float& out1) {
   const float v0 = fmaf(3.f, zv[1], zv[0]);
   const float v1 = fmaf(3.f, zv[1], zv[2]);
   const float n0 = __shfl_sync(0xFFFFFFFFu, v0, src_near), f0 = __shfl_sync(0xFFFFFFFFu, v0, src_far);
   const float n1 = __shfl_sync(0xFFFFFFFFu, v1, src_near), f1 = __shfl_sync(0xFFFFFFFFu, v1, src_far);
-  out0 = fmaf(3.f, n0, f0) * (1.f / 64.f);
-  out1 = fmaf(3.f, n1, f1) * (1.f / 64.f);
+  out0 = fmaf(3.f, n0, f0) * s0;
+  out1 = fmaf(3.f, n1, f1) * s1;
 }
 
 // Direction of block-local slot dl (0..15) in pass `pass`, or -1.
@@ -560,6 +563,12 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
         const float om = L0 ? a.dirs[d].omega : 0.f;
         float val[4][3];
         float mv[3][4];  // [channel][child i = ez * 2 + ey]
+        float scl[4];    // 1/64 for a child whose ray missed, else 0 (mv stays 0 without a merge)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          scl[i] = ((missm >> i) & 1u) ? (1.f / 64.f) : 0.f;
+          mv[0][i] = mv[1][i] = mv[2][i] = 0.f;
+        }
         if (merge && TM) {
           // staged taps (q = plane * 3 + row): every channel in one shared load;
           // per child plane the middle parent plane (weight 3/4) and plane 0 or 2
@@ -581,7 +590,7 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
                 const float o = ch == 0 ? po[jy].x : ch == 1 ? po[jy].y : po[jy].z;
                 zv[jy] = fmaf(3.f, m, o);
               }
-              yx_blend(zv, src_near, src_far, mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
+              yx_blend(zv, src_near, src_far, scl[ez * 2], scl[ez * 2 + 1], mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
             }
           }
         } else if (!TM && merge) {
@@ -597,14 +606,14 @@ __device__ __forceinline__ void level_bits_block(const LevelArgs& a, int bid, ui
               float zv[3];
 #pragma unroll
               for (int jy = 0; jy < 3; ++jy) zv[jy] = fmaf(3.f, av[3 + jy], ez == 0 ? av[jy] : av[6 + jy]);
-              yx_blend(zv, src_near, src_far, mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
+              yx_blend(zv, src_near, src_far, scl[ez * 2], scl[ez * 2 + 1], mv[ch][ez * 2], mv[ch][ez * 2 + 1]);
             }
           }
         }
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch)
 #pragma unroll
-          for (int i = 0; i < 4; ++i) val[i][ch] = (merge && ((missm >> i) & 1u)) ? mv[ch][i] : 0.f;
+          for (int i = 0; i < 4; ++i) val[i][ch] = mv[ch][i];
         if (emism) {  // emissive hits are rare: patch them in
 #pragma unroll
           for (int i = 0; i < 4; ++i)

@@ -736,8 +736,39 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
     const uint32_t* rp = &rec[(int64_t)d * slots * 32 + rbase];
     return !RC_CHK(rp, kChkRecord) ? kBlack : CG ? __ldca(rp) : __ldg(rp);
   };
-  // one direction: its radiance from the record, the stores, the sums
-  auto one = [&](int dl, int d, uint32_t r) {
+  // Levels above cascade 0 take two directions at a time: both directions'
+  // taps are requested before either's stores (loaded whatever the record,
+  // which keeps the loads out of a branch; a record that is not a miss
+  // replaces the blend).  Every tap lies inside the next level.
+  auto gather = [&](int d, uint32_t r, float rv[3]) {
+    rv[0] = rv[1] = rv[2] = 0.f;
+    if (!TOP) {
+#pragma unroll
+      for (int tp = 0; tp < 8; ++tp) {
+        const float3 v = load_rgb<T, CG>(rgb4_at(Au, d, a.P_up, tap_off[tp]));
+        rv[0] = fmaf(tap_w[tp], v.x, rv[0]);
+        rv[1] = fmaf(tap_w[tp], v.y, rv[1]);
+        rv[2] = fmaf(tap_w[tp], v.z, rv[2]);
+      }
+    }
+    if (r != kMiss) {
+      rv[0] = rv[1] = rv[2] = 0.f;
+      if (r != kBlack) voxel_emission(a.vol, r, rv);
+    }
+  };
+  auto finish = [&](int dl, int d, const float rv[3]) {
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) Store<T>::stream(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
+    if ((dl & 3) == 3) {
+      const int dp = dpair * 2 + (dl >> 2);
+      store_avg<T>(a, dp, p, 0.25f * acc[0], 0.25f * acc[1], 0.25f * acc[2]);
+      acc[0] = acc[1] = acc[2] = 0.f;
+    }
+  };
+  // cascade 0, one direction: its radiance from the record, the stores, the fluence
+  auto one = [&](int d, uint32_t r) {
     float rv[3] = {0.f, 0.f, 0.f};
     if (r == kMiss) {
       if (!TOP) {
@@ -754,31 +785,27 @@ __device__ __forceinline__ void merge_probe(const LevelArgs& a, const uint32_t* 
     }
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) Store<T>::stream(L + ((int64_t)ch * a.ndirs + d) * a.P + p, rv[ch]);
-    if (L0) {
-      const float om = a.dirs[d].omega;
+    const float om = a.dirs[d].omega;
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) acc[ch] = fmaf(om, rv[ch], acc[ch]);
-    } else {
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch) acc[ch] += rv[ch];
-      if ((dl & 3) == 3) {
-        const int dp = dpair * 2 + (dl >> 2);
-        store_avg<T>(a, dp, p, 0.25f * acc[0], 0.25f * acc[1], 0.25f * acc[2]);
-        acc[0] = acc[1] = acc[2] = 0.f;
-      }
-    }
+    for (int ch = 0; ch < 3; ++ch) acc[ch] = fmaf(om, rv[ch], acc[ch]);
   };
   if (L0) {
     // two directions per pass: their parent taps are in flight together
 #pragma unroll 2
-    for (int dl = 0; dl < a.ndirs; ++dl) one(dl, dl, record(dl));
+    for (int dl = 0; dl < a.ndirs; ++dl) one(dl, record(dl));
   } else {
     // the eight directions' records are requested together, then merged in order
     uint32_t r8[8];
 #pragma unroll
     for (int dl = 0; dl < 8; ++dl) r8[dl] = record(dir_of(dl));
 #pragma unroll
-    for (int dl = 0; dl < 8; ++dl) one(dl, dir_of(dl), r8[dl]);
+    for (int dl = 0; dl < 8; dl += 2) {
+      float ra[3], rb[3];
+      gather(dir_of(dl), r8[dl], ra);
+      gather(dir_of(dl + 1), r8[dl + 1], rb);
+      finish(dl, dir_of(dl), ra);
+      finish(dl + 1, dir_of(dl + 1), rb);
+    }
   }
   if (L0) {
 #pragma unroll
