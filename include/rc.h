@@ -290,11 +290,15 @@ rc_status rc_batch_set_spheres(rc_batch* b, int32_t scene,
  * the copies run at full speed. */
 rc_status rc_batch_get_fluence_all(rc_batch* b, float* out, int64_t elems,
                                    int32_t where);
-/* The same read started on the batch stream, after the solves enqueued so
- * far, without waiting: `out` (host memory of the same size; pinned memory
- * overlaps, pageable memory copies synchronously) is complete after
- * rc_batch_synchronize or any later call that synchronises.  Emitter updates
- * and solves enqueued afterwards run after the copies, so a caller that
+/* The same read started after the solves enqueued so far, without
+ * waiting: `out` (host memory of the same size; pinned memory overlaps,
+ * pageable memory copies synchronously) is complete after
+ * rc_batch_synchronize or any later call that synchronises.  The fluences
+ * are first gathered into one device buffer on the batch stream (the first
+ * call allocates it: the total size of the batch's fluence), then copied to
+ * `out` on the batch's own copy stream; emitter updates and solves enqueued
+ * afterwards wait only for the gather, so the copy to the host overlaps the
+ * next solve, and the next read waits for this one's copy.  A caller that
  * alternates two output buffers overlaps its next frame's host work with
  * this frame's solve and read-back. */
 rc_status rc_batch_get_fluence_all_async(rc_batch* b, float* out, int64_t elems);

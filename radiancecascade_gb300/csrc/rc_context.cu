@@ -1814,6 +1814,14 @@ extern "C" rc_status rc_solve_noalloc(const rc_params* p, const rc_voxel* voxels
 // ---------------------------------------------------------------------------
 // Batched solve: many scenes, one persistent launch in a CUDA graph.
 // ---------------------------------------------------------------------------
+// One scene's share of the batch's gathered fluence: n floats from src to
+// offset off of the staging buffer.
+struct FluSeg {
+  const float* src;
+  int64_t off;
+  int64_t n;
+};
+
 struct rc_batch {
   int device = 0;
   int n = 0;
@@ -1845,6 +1853,16 @@ struct rc_batch {
   std::vector<char> pending;
   int** d_errs = nullptr;
   cudaGraphExec_t graph = nullptr;
+  // Asynchronous read-back: every scene's fluence is gathered into one
+  // device buffer on the batch stream (the solves after it may then start),
+  // and copied to the host from there on copy_stream; the next gather waits
+  // for that copy (ev_copied).
+  float* flu_stage = nullptr;
+  FluSeg* d_flu_seg = nullptr;
+  int64_t flu_max_seg = 0;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_gathered = nullptr, ev_copied = nullptr;
+  bool copy_pending = false;
 };
 
 namespace {
@@ -1971,6 +1989,14 @@ void batch_enqueue(rc_batch* b, cudaStream_t s) {
   else
     k_batch_persistent<float><<<b->blocks, kBatchThreads, kBitsSmem, s>>>(b->d_levels, b->d_items, b->nitems,
                                                                           b->tiles, b->d_next, b->d_done, b->d_err);
+}
+
+// Every scene's fluence into one contiguous buffer: block row blockIdx.y
+// copies segment blockIdx.y (n floats from src to dst + off).
+__global__ void k_gather_fluence(const FluSeg* __restrict__ seg, float* __restrict__ dst) {
+  const FluSeg g = seg[blockIdx.y];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[g.off + i] = __ldcs(g.src + i);
 }
 
 // A scene's bounded waits report into its own flag: after a per-scene solve
@@ -2147,9 +2173,14 @@ rc_status rc_batch_destroy(rc_batch* b) {
     DeviceGuard g(b->device);
     if (b->stream) cudaStreamSynchronize(b->stream);
     batch_free_graph(b);
-    void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err, b->d_errs};
+    if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
+    void* bufs[] = {b->d_levels, b->d_items, b->d_qargs, b->d_next, b->d_done, b->d_err, b->d_errs,
+                    b->flu_stage, b->d_flu_seg};
     for (void* x : bufs)
       if (x) cudaFree(x);
+    if (b->ev_gathered) cudaEventDestroy(b->ev_gathered);
+    if (b->ev_copied) cudaEventDestroy(b->ev_copied);
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
     for (cudaStream_t st : b->side) cudaStreamSynchronize(st);
     for (cudaStream_t st : b->side) cudaStreamDestroy(st);
     for (cudaEvent_t ev : b->joins) cudaEventDestroy(ev);
@@ -2223,6 +2254,10 @@ rc_status rc_batch_synchronize(rc_batch* b) {
   rc_status s = batch_join_updates(b);  // emitter updates still on side streams
   if (s != RC_OK) return s;
   RC_CUDA(cudaStreamSynchronize(b->stream), "rc_batch_synchronize");
+  if (b->copy_stream) {
+    RC_CUDA(cudaStreamSynchronize(b->copy_stream), "rc_batch_synchronize");
+    b->copy_pending = false;
+  }
   return batch_error_flag(b, "rc_batch_synchronize");
 }
 
@@ -2298,14 +2333,36 @@ rc_status rc_batch_get_fluence_all_async(rc_batch* b, float* out, int64_t elems)
     return RC_ERR_INVALID_ARG;
   }
   DeviceGuard g(b->device);
-  int64_t off = 0;
-  for (int k = 0; k < b->n; ++k) {
-    const rc_context* c = b->scenes[k];
-    const size_t bytes = (size_t)c->geom[0].probes() * 3 * sizeof(float);
-    RC_CUDA(cudaMemcpyAsync(out + off, c->fluence, bytes, cudaMemcpyDeviceToHost, b->stream),
-            "rc_batch_get_fluence_all_async");
-    off += c->geom[0].probes() * 3;
+  if (!b->flu_stage) {
+    // first read: the staging buffer, its segment table, the copy stream
+    std::vector<FluSeg> seg((size_t)b->n);
+    int64_t off = 0;
+    for (int k = 0; k < b->n; ++k) {
+      const int64_t nk = b->scenes[k]->geom[0].probes() * 3;
+      seg[(size_t)k] = FluSeg{b->scenes[k]->fluence, off, nk};
+      b->flu_max_seg = std::max(b->flu_max_seg, nk);
+      off += nk;
+    }
+    rc_status s = dev_alloc((void**)&b->flu_stage, (size_t)need * sizeof(float), "batch fluence staging");
+    if (s == RC_OK) s = dev_alloc((void**)&b->d_flu_seg, seg.size() * sizeof(FluSeg), "batch fluence segments");
+    if (s != RC_OK) return s;
+    RC_CUDA(cudaMemcpy(b->d_flu_seg, seg.data(), seg.size() * sizeof(FluSeg), cudaMemcpyHostToDevice),
+            "rc_batch_get_fluence_all_async: segments");
+    RC_CUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking), "rc_batch_get_fluence_all_async");
+    RC_CUDA(cudaEventCreateWithFlags(&b->ev_gathered, cudaEventDisableTiming), "rc_batch_get_fluence_all_async");
+    RC_CUDA(cudaEventCreateWithFlags(&b->ev_copied, cudaEventDisableTiming), "rc_batch_get_fluence_all_async");
   }
+  // the staging buffer is free once the previous read's copy is done
+  if (b->copy_pending) RC_CUDA(cudaStreamWaitEvent(b->stream, b->ev_copied, 0), "rc_batch_get_fluence_all_async");
+  const unsigned bx = (unsigned)std::min<int64_t>((b->flu_max_seg + 1023) / 1024, 64);
+  k_gather_fluence<<<dim3(bx, (unsigned)b->n), 256, 0, b->stream>>>(b->d_flu_seg, b->flu_stage);
+  RC_CUDA(cudaGetLastError(), "rc_batch_get_fluence_all_async: gather");
+  RC_CUDA(cudaEventRecord(b->ev_gathered, b->stream), "rc_batch_get_fluence_all_async");
+  RC_CUDA(cudaStreamWaitEvent(b->copy_stream, b->ev_gathered, 0), "rc_batch_get_fluence_all_async");
+  RC_CUDA(cudaMemcpyAsync(out, b->flu_stage, (size_t)need * sizeof(float), cudaMemcpyDeviceToHost, b->copy_stream),
+          "rc_batch_get_fluence_all_async: copy");
+  RC_CUDA(cudaEventRecord(b->ev_copied, b->copy_stream), "rc_batch_get_fluence_all_async");
+  b->copy_pending = true;
   return RC_OK;
 }
 
