@@ -337,6 +337,19 @@ bool encode_rgb4_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, co
   return r == CUDA_SUCCESS;
 }
 
+// The shared-memory limit of every k_level0_tma instantiation of element type T.
+template <typename T>
+cudaError_t level0_tma_smem(int smem) {
+  cudaError_t e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
 bool setup_tma0(rc_context* c) {
   if (c->nlev < 2 || c->mode[0] != kModeDirect0) return false;
   const LevelArgs& a = c->args[0];
@@ -346,7 +359,7 @@ bool setup_tma0(rc_context* c) {
   PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) return false;
   // cascade 1's child averages in the planar layout (set_average_layouts)
-  const int py = std::min(6, UMy);
+  const int py = std::min(kL0TileRows, UMy);
   cuuint64_t dims[3] = {(cuuint64_t)UMx, (cuuint64_t)UMy, (cuuint64_t)UMz * 3 * (cuuint64_t)a.ndirs};
   cuuint64_t strides[2] = {(cuuint64_t)UMx * es, (cuuint64_t)UMx * UMy * es};
   cuuint32_t box[3] = {(cuuint32_t)UMx, (cuuint32_t)py, (cuuint32_t)(kL0Planes + 1)};
@@ -362,10 +375,7 @@ bool setup_tma0(rc_context* c) {
   // never lowers it under an earlier one.
   const size_t stage = 3 * (((size_t)(kL0Planes + 1) * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
   const int smem = (int)(kL0Stages * stage + 16 * kL0Stages + 128);
-  cudaError_t e = es == 2 ? cudaFuncSetAttribute(k_level0_tma<__half, kL0Planes>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem)
-                          : cudaFuncSetAttribute(k_level0_tma<float, kL0Planes>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = es == 2 ? level0_tma_smem<__half>(smem) : level0_tma_smem<float>(smem);
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
@@ -442,8 +452,19 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
         // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
         const size_t stage =
             3 * (((size_t)(kL0Planes + 1) * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
-        launch_overlapped(k_level0_tma<T, kL0Planes>, dim3(blocks), dim3(kL0Threads),
-                          kL0Stages * stage + 16 * kL0Stages + 128, s, a, c->tma0, c->tma0_py, c->err);
+        const size_t smem = kL0Stages * stage + 16 * kL0Stages + 128;
+        // the common row widths with their tile geometry fixed at compile time
+        auto launch = [&](auto kernel) {
+          launch_overlapped(kernel, dim3(blocks), dim3(kL0Threads), smem, s, a, c->tma0, c->tma0_py, c->err);
+        };
+        if (c->tma0_py == kL0TileRows && a.UM[0] == 32)
+          launch(k_level0_tma<T, kL0Planes, 32>);
+        else if (c->tma0_py == kL0TileRows && a.UM[0] == 64)
+          launch(k_level0_tma<T, kL0Planes, 64>);
+        else if (c->tma0_py == kL0TileRows && a.UM[0] == 128)
+          launch(k_level0_tma<T, kL0Planes, 128>);
+        else
+          launch(k_level0_tma<T, kL0Planes>);
       }
       break;
     }

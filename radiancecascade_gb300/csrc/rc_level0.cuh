@@ -273,15 +273,21 @@ constexpr int kL0Stages = 3;  // parent tiles in flight: the copy for iteration 
 // at 256^3 it measured 160 us against 153 us for ZC = 2 (128 registers, 2 blocks/SM).
 constexpr int kL0Planes = 2;
 
-template <typename T, int ZC>
+// UMXC: cascade 1's row width (UM[0]) fixed at compile time, with tiles of
+// kL0TileRows rows (0: both taken from the arguments).  Fixed, every tile and
+// stage offset is a constant and the shared-memory addresses need no
+// per-direction arithmetic (116.7 against 120.5 us at 256^3).
+constexpr int kL0TileRows = 6;
+template <typename T, int ZC, int UMXC = 0>
 __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
-    k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int PY, int* err) {
+    k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int py, int* err) {
   static_assert(ZC == 1 || ZC == 2, "one or two child planes per block");
+  const int PY = UMXC ? kL0TileRows : py;
   constexpr int PZ = ZC + 1;  // parent planes in a tile
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int Mx = a.M[0], My = a.M[1], Mz = a.M[2];
-  const int UMx = a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
+  const int UMx = UMXC ? UMXC : a.UM[0], UMy = a.UM[1], UMz = a.UM[2];
   // TMA writes to shared memory must start on a 128-byte boundary: both stages
   // start at multiples of 128 from a 128-byte aligned base.
   const int tile_elems = PZ * PY * UMx;

@@ -92,6 +92,11 @@ def test_golden_fixtures(name, walk):
     # elongated grids: 1024 voxels (the largest edge) along one axis, few along the others
     ((1024, 32, 64), 5, {}),
     ((32, 512, 32), 4, dict(dir_res0=6)),
+    # cascade 0 through the staged kernel at the compiled row widths 32 and 128
+    # (64 is the 256^3 workload's), and at a width of 48 that none fixes
+    ((128, 24, 40), 3, {}),
+    ((512, 48, 32), 4, {}),
+    ((192, 32, 24), 3, {}),
     # 100 directions at cascade 0: more than the walk-free kernel keeps in lanes
     ((64, 64, 64), 3, dict(dir_res0=10)),
 ])
