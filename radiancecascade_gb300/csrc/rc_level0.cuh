@@ -267,7 +267,10 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 // *err = 1, and thread 0 waits (bounded) for the copies it may still have in
 // flight before the block's shared memory goes.
 constexpr int kL0TmaRows = 8;
-constexpr int kL0Stages = 3;  // parent tiles in flight: the copy for iteration it + 2 starts at iteration it
+// Parent tiles in flight: the copy for iteration it + S - 1 starts at
+// iteration it.  Four stages: 113.4 against 116.3 us for three at 256^3 (55 KB
+// of shared memory per block at 64-wide rows).
+constexpr int kL0Stages = 4;
 // Child planes per block (ZC).  ZC = 1 halves the per-lane accumulators (80
 // registers, 3 blocks/SM) but reads 4 parent values per output instead of 3;
 // at 256^3 it measured 160 us against 153 us for ZC = 2 (128 registers, 2 blocks/SM).

@@ -265,3 +265,38 @@ def test_async_fluence_read_matches_the_synchronous_one():
             F.check(F.lib().rc_batch_get_fluence_all_async(b.handle, F.ptr(got), got.size - 1))
     finally:
         b.close()
+
+
+def test_async_reads_in_flight_over_moving_frames():
+    """Four moving-emitter frames, each read asynchronously into one of two
+    pinned buffers with no wait in between (the copy to the host runs beside
+    the next solve, from the device staging buffer): after the final
+    synchronize the two buffers hold the last two frames, equal to a second
+    batch stepped the same way and read synchronously."""
+    torch = pytest.importorskip("torch")
+    a, b = _batch(), _batch()
+    try:
+        n = a.fluence_elems()
+        bufs = [torch.empty(n, dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+        for x in bufs:
+            x[:] = np.nan
+        sph_a = [_scene(g, seed)[1].copy() for g, _, seed in SCENES]
+        sph_b = [x.copy() for x in sph_a]
+        want = []
+        for f in range(4):
+            for k, (grid, _, _) in enumerate(SCENES):
+                R.advance_spheres(sph_a[k], grid, 1)
+                a.set_spheres(k, sph_a[k])
+                R.advance_spheres(sph_b[k], grid, 1)
+                b.set_spheres(k, sph_b[k])
+            a.solve()
+            a.fluence_all_async(bufs[f & 1])
+            b.solve()
+            want.append(b.fluence_all())
+        a.synchronize()
+        assert not np.array_equal(want[2], want[3])  # the emitters moved
+        assert np.array_equal(bufs[0], want[2])
+        assert np.array_equal(bufs[1], want[3])
+    finally:
+        a.close()
+        b.close()
