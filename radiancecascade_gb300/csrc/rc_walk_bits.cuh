@@ -304,19 +304,14 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       hi_[u] = (zin && (unsigned)(q + 1) < (unsigned)a.wpp && RC_CHK(plane + q + 1, kChkMask)) ? __ldg(plane + q + 1)
                                                                                                  : make_uint2(0u, 0u);
     }
+    // Branch-free over the batch: a step past the interval or outside the
+    // grid in z (both final: the walk is monotone) loaded zeros and hits
+    // nothing, and so does every step after all probes are done.
     bool stop = false;
 #pragma unroll
     for (int u = 0; u < kWalkBatch; ++u) {
-      if (stop) continue;
-      if (!ok_[u]) {
-        stop = true;
-        continue;
-      }
       const int cz = bz_[u] >> l2s, cy = by_[u] >> l2s, cx = bx_[u] >> l2s;
-      if ((unsigned)(zl + cz) >= (unsigned)Mz) {  // every probe of the word left the grid
-        stop = true;
-        continue;
-      }
+      stop |= !ok_[u] || (unsigned)(zl + cz) >= (unsigned)Mz;  // every probe of the word left the grid
       // probes whose cell (x + cx, y + cy) is still inside the grid
       uint32_t inr;
       if (wide) {
@@ -328,9 +323,9 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       done |= ~inr;
       const int gs = g0 + cy * Px + cx;
       const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs & 31) & ~done;
-      if (nw) {
-        done |= nw;
-        hits |= nw;
+      done |= nw;
+      hits |= nw;
+      {
         uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs & 31) & nw;
         if (ew) {  // emissive hits (rare): the voxel's index
           ehits |= ew;
@@ -345,9 +340,8 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
           } while (ew);
         }
       }
-      if (done == 0xFFFFFFFFu) stop = true;
     }
-    if (stop) break;
+    if (stop || done == 0xFFFFFFFFu) break;
   }
   // the other probes: opaque without emission, or no hit (probes that do not exist included)
 #pragma unroll 8

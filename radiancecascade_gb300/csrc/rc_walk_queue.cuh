@@ -246,14 +246,14 @@ struct Walker {
                    ? __ldg(plane + q0 + 1)
                    : make_uint2(0u, 0u);
     }
+    // Branch-free over the batch, as in TableWalker::batch.
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (!ok_[u]) return true;  // interval finished, or the walk left the grid in z
       done |= ~inr_[u];
       const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs_[u] & 31) & ~done;
-      if (nw) {
-        done |= nw;
-        hits |= nw;
+      done |= nw;
+      hits |= nw;
+      {
         uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs_[u] & 31) & nw;
         if (ew) {  // emissive hits (rare): the voxel's index
           ehits |= ew;
@@ -268,9 +268,8 @@ struct Walker {
           } while (ew);
         }
       }
-      if (done == 0xFFFFFFFFu) return true;
     }
-    return false;
+    return !ok_[kBatch - 1] || done == 0xFFFFFFFFu;
   }
 
   __device__ __forceinline__ void finish() { write_records(rec, valid, hits, ehits); }
@@ -380,14 +379,17 @@ struct TableWalker {
     }
     st += kBatch;
     n -= kBatch;
+    // Branch-free over the batch: a step that is not ok (past the table's end,
+    // or outside the grid in z -- both final, the walk is monotone) loaded
+    // zeros and hits nothing, and steps after every probe is done hit
+    // nothing either, so no step needs its own exit test.
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) {
-      if (!ok_[u]) return true;  // table finished, or the walk left the grid in z
       done |= ~inr_[u];
       const uint32_t nw = __funnelshift_r(lo_[u].x, hi_[u].x, gs_[u] & 31) & ~done;
-      if (nw) {
-        done |= nw;
-        hits |= nw;
+      done |= nw;
+      hits |= nw;
+      {
         uint32_t ew = __funnelshift_r(lo_[u].y, hi_[u].y, gs_[u] & 31) & nw;
         if (ew) {  // emissive hits (rare): the voxel's index, from the step's table entry
           ehits |= ew;
@@ -406,9 +408,8 @@ struct TableWalker {
           } while (ew);
         }
       }
-      if (done == 0xFFFFFFFFu) return true;
     }
-    return n <= 0;
+    return !ok_[kBatch - 1] || done == 0xFFFFFFFFu || n <= 0;
   }
 
   __device__ __forceinline__ void finish() { write_records(rec, valid, hits, ehits); }
