@@ -264,8 +264,10 @@ MaskGeom mask_geom(const LevelGeom& g, bool force_scalar) {
   const int64_t px = (int64_t)1 << m.l2px;
   m.wpp = (int32_t)((g.M[1] * px + 31) / 32);
   m.words = (int64_t)g.spacing * g.spacing * g.spacing * g.M[2] * m.wpp;
-  // the bit-parallel kernel addresses a level's radiance with 32-bit element offsets
-  m.bits = !force_scalar && px <= 256 && 3 * (int64_t)g.ndirs * g.probes() < ((int64_t)1 << 31);
+  // the bit-parallel kernels address a level's radiance and its decimated
+  // words with 32-bit element offsets
+  m.bits = !force_scalar && px <= 256 && 3 * (int64_t)g.ndirs * g.probes() < ((int64_t)1 << 31) &&
+           m.words < ((int64_t)1 << 31);
   m.rep = 0;
   if (px < 32)
     for (int r = 0; r < 32 / px; ++r) m.rep |= 1u << (r * px);

@@ -256,7 +256,7 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
   }
   uint32_t done = ~valid, hits = 0u, ehits = 0u;
   const uint2* zbase = a.mask + (int64_t)zl * a.wpp;
-  const int64_t phase_stride = (int64_t)Mz * a.wpp;
+  const int phase_stride = Mz * a.wpp;  // a level's decimated words fit 32 bits (checked on the host)
   int ax = h + di.start_off[0], ay = h + di.start_off[1], az = h + di.start_off[2];
   int tx = di.first_T[0], ty = di.first_T[1], tz = di.first_T[2];
   const int sx = di.sgn[0], sy = di.sgn[1], sz = di.sgn[2];
@@ -295,8 +295,8 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       const int zc = zl + (az >> l2s);
       const bool zin = step_ok && (unsigned)zc < (unsigned)Mz;
       ok_[u] = step_ok;
-      const int64_t phase = ((((int64_t)(az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
-      const uint2* plane = zbase + phase * phase_stride + (int64_t)(az >> l2s) * a.wpp;
+      const int phase = ((((az & (s - 1)) << l2s) + (ay & (s - 1))) << l2s) + (ax & (s - 1));
+      const uint2* plane = zbase + (phase * phase_stride + (az >> l2s) * a.wpp);
       const int gs = g0 + (ay >> l2s) * Px + (ax >> l2s);
       const int q = gs >> 5;
       lo_[u] = (zin && (unsigned)q < (unsigned)a.wpp && RC_CHK(plane + q, kChkMask)) ? __ldg(plane + q)
