@@ -289,7 +289,7 @@ struct TableWalker {
   uint32_t valid, done, hits, ehits;
   uint32_t cell;   // packed coarse cell of the current step
   int gcell;       // cy * Px + cx
-  int64_t zoff;    // (zl + cz) * wpp
+  int zoff;        // (zl + cz) * wpp
   uint32_t inr;
   bool zin;
 
@@ -306,7 +306,7 @@ struct TableWalker {
     }
     zin = (unsigned)(zl + cz) < (unsigned)Mz;
     gcell = cy * Px + cx;
-    zoff = (int64_t)(zl + cz) * wpp;
+    zoff = (zl + cz) * wpp;
   }
 
   // Returns false when the item holds no probe.
@@ -370,7 +370,7 @@ struct TableWalker {
       const int gs = g0 + gcell;
       gs_[u] = gs;
       const int q0 = gs >> 5;
-      const uint2* plane = mask + (int64_t)e[u].x * mzw + zoff;
+      const uint2* plane = mask + ((int)e[u].x * mzw + zoff);  // a level's words fit 32 bits
       lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0)
                                                                                        : make_uint2(0u, 0u);
       hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
