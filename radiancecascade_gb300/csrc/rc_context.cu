@@ -339,16 +339,29 @@ bool encode_rgb4_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, co
   return r == CUDA_SUCCESS;
 }
 
-// The shared-memory limit of every k_level0_tma instantiation of element type T.
+// Dynamic shared memory of one k_level0_tma block: `stages` stages of three
+// 128-byte aligned channel tiles (ZC + 1 planes x rows x umx values of es
+// bytes), their barriers, up to 127 bytes to align the base.
+size_t level0_tma_bytes(int stages, int rows, int umx, size_t es) {
+  const size_t stage = 3 * (((size_t)(kL0Planes + 1) * rows * umx * es + 127) & ~(size_t)127);
+  return stages * stage + 16 * (size_t)stages + 128;
+}
+
+// The shared-memory limit of every k_level0_tma instantiation of element type
+// T: the most any context can need (the generic form: rows of up to 256
+// values), so that a later context never lowers it under an earlier one.
 template <typename T>
-cudaError_t level0_tma_smem(int smem) {
-  cudaError_t e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+cudaError_t level0_tma_smem() {
+  auto set = [](auto kernel, size_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  };
+  cudaError_t e = set(k_level0_tma<T, kL0Planes>, level0_tma_bytes(l0_stages(0), kL0TileRows, 256, sizeof(float)));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = set(k_level0_tma<T, kL0Planes, 32>, level0_tma_bytes(l0_stages(32), kL0TileRows, 32, sizeof(T)));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = set(k_level0_tma<T, kL0Planes, 64>, level0_tma_bytes(l0_stages(64), kL0TileRows, 64, sizeof(T)));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_level0_tma<T, kL0Planes, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = set(k_level0_tma<T, kL0Planes, 128>, level0_tma_bytes(l0_stages(128), kL0TileRows, 128, sizeof(T)));
   return e;
 }
 
@@ -370,14 +383,8 @@ bool setup_tma0(rc_context* c) {
                          const_cast<void*>(a.A_up), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return false;
-  // The shared-memory limit is a property of the kernel, not of this context:
-  // set it to the largest any context needs (parent rows of up to 256 FP32
-  // values; kL0Stages stages of three 128-byte aligned channel tiles, their
-  // barriers and up to 127 bytes to align the base), so that a later context
-  // never lowers it under an earlier one.
-  const size_t stage = 3 * (((size_t)(kL0Planes + 1) * 6 * 256 * sizeof(float) + 127) & ~(size_t)127);
-  const int smem = (int)(kL0Stages * stage + 16 * kL0Stages + 128);
-  cudaError_t e = es == 2 ? level0_tma_smem<__half>(smem) : level0_tma_smem<float>(smem);
+  // The shared-memory limit is a property of the kernel, not of this context.
+  cudaError_t e = es == 2 ? level0_tma_smem<__half>() : level0_tma_smem<float>();
   if (e != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
@@ -451,22 +458,19 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
         const int yblocks = (a.M[1] + kL0TmaRows - 1) / kL0TmaRows;
         const unsigned blocks =
             (unsigned)(((a.M[0] + 127) / 128) * yblocks * ((a.M[2] + kL0Planes - 1) / kL0Planes));
-        // per stage three 128-byte aligned channel tiles; the barriers; up to 127 bytes to align the base
-        const size_t stage =
-            3 * (((size_t)(kL0Planes + 1) * c->tma0_py * a.UM[0] * sizeof(T) + 127) & ~(size_t)127);
-        const size_t smem = kL0Stages * stage + 16 * kL0Stages + 128;
-        // the common row widths with their tile geometry fixed at compile time
-        auto launch = [&](auto kernel) {
+        // the common row widths with their tile geometry (and stage count) fixed at compile time
+        auto launch = [&](auto kernel, int umxc) {
+          const size_t smem = level0_tma_bytes(l0_stages(umxc), c->tma0_py, a.UM[0], sizeof(T));
           launch_overlapped(kernel, dim3(blocks), dim3(kL0Threads), smem, s, a, c->tma0, c->tma0_py, c->err);
         };
         if (c->tma0_py == kL0TileRows && a.UM[0] == 32)
-          launch(k_level0_tma<T, kL0Planes, 32>);
+          launch(k_level0_tma<T, kL0Planes, 32>, 32);
         else if (c->tma0_py == kL0TileRows && a.UM[0] == 64)
-          launch(k_level0_tma<T, kL0Planes, 64>);
+          launch(k_level0_tma<T, kL0Planes, 64>, 64);
         else if (c->tma0_py == kL0TileRows && a.UM[0] == 128)
-          launch(k_level0_tma<T, kL0Planes, 128>);
+          launch(k_level0_tma<T, kL0Planes, 128>, 128);
         else
-          launch(k_level0_tma<T, kL0Planes>);
+          launch(k_level0_tma<T, kL0Planes>, 0);
       }
       break;
     }

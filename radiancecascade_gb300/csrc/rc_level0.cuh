@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 // cascade 1's child-averaged radiance -- per channel the full parent row width
 // x PY rows x (ZC + 1) planes -- are brought into shared memory by three
 // cp.async.bulk.tensor copies while earlier directions' tiles are consumed
-// (kL0Stages stages); one iteration serves all three channels.  Lanes read
+// (l0_stages stages); one iteration serves all three channels.  Lanes read
 // their 4 parent columns from shared memory.  Each stage has a "full"
 // mbarrier the copies complete and an "empty" one every warp arrives at when
 // it is done with the stage; thread 0 refills a stage once all warps have
@@ -267,10 +267,11 @@ __global__ void __launch_bounds__(kL0Threads, 3) k_level0_direct(const __grid_co
 // *err = 1, and thread 0 waits (bounded) for the copies it may still have in
 // flight before the block's shared memory goes.
 constexpr int kL0TmaRows = 8;
-// Parent tiles in flight: the copy for iteration it + S - 1 starts at
-// iteration it.  Four stages: 113.4 against 116.3 us for three at 256^3 (55 KB
-// of shared memory per block at 64-wide rows).
-constexpr int kL0Stages = 4;
+// Parent tiles in flight (S): the copy for iteration it + S - 1 starts at
+// iteration it.  Four stages (113.4 against 116.3 us for three at 256^3), five
+// for the compiled 32- and 64-wide rows (111.6 us; 69 KB of shared memory per
+// block at 64-wide rows, still two blocks per SM -- wider rows keep four).
+__host__ __device__ constexpr int l0_stages(int umxc) { return umxc == 32 || umxc == 64 ? 5 : 4; }
 // Child planes per block (ZC).  ZC = 1 halves the per-lane accumulators (80
 // registers, 3 blocks/SM) but reads 4 parent values per output instead of 3;
 // at 256^3 it measured 160 us against 153 us for ZC = 2 (128 registers, 2 blocks/SM).
@@ -285,6 +286,7 @@ template <typename T, int ZC, int UMXC = 0>
 __global__ void __launch_bounds__(kL0Threads, ZC == 1 ? 3 : 2)
     k_level0_tma(const LevelArgs a, const __grid_constant__ CUtensorMap tmap, int py, int* err) {
   static_assert(ZC == 1 || ZC == 2, "one or two child planes per block");
+  constexpr int kL0Stages = l0_stages(UMXC);
   const int PY = UMXC ? kL0TileRows : py;
   constexpr int PZ = ZC + 1;  // parent planes in a tile
   extern __shared__ __align__(128) unsigned char smem[];
