@@ -483,8 +483,12 @@ void launch_one(const rc_context* c, int level, cudaStream_t s) {
     }
     case kModeQueue: {
       dim3 grid((unsigned)((a.P + threads - 1) / threads), L0 ? 1u : (unsigned)((a.n / 2) * (a.n / 2) / 2));
-      launch_overlapped(k_level_merge<T, L0, TOP>, grid, dim3(threads), 0, s, a,
-                        (const uint32_t*)c->rec_level[level], (int)c->rec_slots[level]);
+      if constexpr (TOP)
+        launch_overlapped(k_level_merge_top<T, L0>, grid, dim3(threads), 0, s, a,
+                          (const uint32_t*)c->rec_level[level], (int)c->rec_slots[level]);
+      else
+        launch_overlapped(k_level_merge<T, L0, false>, grid, dim3(threads), 0, s, a,
+                          (const uint32_t*)c->rec_level[level], (int)c->rec_slots[level]);
       break;
     }
     default: {
