@@ -288,10 +288,10 @@ struct TableWalker {
   int zl, g0, wy0, wx0;
   uint32_t valid, done, hits, ehits;
   uint32_t cell;   // packed coarse cell of the current step
-  int gcell;       // cy * Px + cx
-  int zoff;        // (zl + cz) * wpp
+  int qoff;        // (zl + cz) * wpp + the first of the two words holding the probes' cells
+  int sh;          // bit of that word where the word's probe 0 falls
   uint32_t inr;
-  bool zin;
+  bool zin, lo_en, hi_en;  // the plane exists; and the first / second word
 
   __device__ __forceinline__ void set_cell(uint32_t packed) {
     cell = packed;
@@ -305,8 +305,11 @@ struct TableWalker {
       inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
     }
     zin = (unsigned)(zl + cz) < (unsigned)Mz;
-    gcell = cy * Px + cx;
-    zoff = (zl + cz) * wpp;
+    const int gs = g0 + cy * Px + cx, q0 = gs >> 5;
+    sh = gs & 31;
+    qoff = (zl + cz) * wpp + q0;
+    lo_en = zin && (unsigned)q0 < (unsigned)wpp;
+    hi_en = zin && (unsigned)(q0 + 1) < (unsigned)wpp;
   }
 
   // Returns false when the item holds no probe.
@@ -357,7 +360,7 @@ struct TableWalker {
     uint2 e[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u) e[u] = u < n ? (RC_CHK(st + u, kChkTable) ? __ldg(st + u) : make_uint2(0u, 0u)) : make_uint2(0u, 0u);
-    int gs_[kBatch];
+    int gs_[kBatch];  // the shift of each step's word pair
     uint2 lo_[kBatch], hi_[kBatch];
     uint32_t inr_[kBatch];
     bool ok_[kBatch];
@@ -367,15 +370,10 @@ struct TableWalker {
       if (step_ok && e[u].y != cell) set_cell(e[u].y);
       ok_[u] = step_ok && zin;
       inr_[u] = step_ok ? inr : 0u;
-      const int gs = g0 + gcell;
-      gs_[u] = gs;
-      const int q0 = gs >> 5;
-      const uint2* plane = mask + ((int)e[u].x * mzw + zoff);  // a level's words fit 32 bits
-      lo_[u] = (ok_[u] && (unsigned)q0 < (unsigned)wpp && RC_CHK(plane + q0, kChkMask)) ? __ldg(plane + q0)
-                                                                                       : make_uint2(0u, 0u);
-      hi_[u] = (ok_[u] && (unsigned)(q0 + 1) < (unsigned)wpp && RC_CHK(plane + q0 + 1, kChkMask))
-                   ? __ldg(plane + q0 + 1)
-                   : make_uint2(0u, 0u);
+      gs_[u] = sh;
+      const uint2* wp = mask + ((int)e[u].x * mzw + qoff);  // a level's words fit 32 bits
+      lo_[u] = (step_ok && lo_en && RC_CHK(wp, kChkMask)) ? __ldg(wp) : make_uint2(0u, 0u);
+      hi_[u] = (step_ok && hi_en && RC_CHK(wp + 1, kChkMask)) ? __ldg(wp + 1) : make_uint2(0u, 0u);
     }
     st += kBatch;
     n -= kBatch;
