@@ -342,10 +342,16 @@ bool encode_rgb4_map(PFN_cuTensorMapEncodeTiled_v12000 enc, CUtensorMap* map, co
 // Dynamic shared memory of one k_level0_tma block: `stages` stages of three
 // 128-byte aligned channel tiles (ZC + 1 planes x rows x umx values of es
 // bytes), their barriers, up to 127 bytes to align the base.
-size_t level0_tma_bytes(int stages, int rows, int umx, size_t es) {
-  const size_t stage = 3 * (((size_t)(kL0Planes + 1) * rows * umx * es + 127) & ~(size_t)127);
-  return stages * stage + 16 * (size_t)stages + 128;
+constexpr size_t level0_tma_bytes(int stages, int rows, int umx, size_t es) {
+  return stages * (3 * (((size_t)(kL0Planes + 1) * rows * umx * es + 127) & ~(size_t)127)) + 16 * (size_t)stages + 128;
 }
+// Every instantiation fits a block's 227 KB limit, and the compiled 32- and
+// 64-wide forms (five stages) still fit two blocks in an SM's 228 KB (1 KB of
+// it reserved per block).
+static_assert(level0_tma_bytes(l0_stages(0), kL0TileRows, 256, sizeof(float)) <= 227 * 1024, "generic cascade-0 tiles");
+static_assert(level0_tma_bytes(l0_stages(128), kL0TileRows, 128, sizeof(float)) <= 227 * 1024, "128-wide cascade-0 tiles");
+static_assert(2 * (level0_tma_bytes(l0_stages(64), kL0TileRows, 64, sizeof(float)) + 1024) <= 228 * 1024,
+              "two blocks per SM with 64-wide cascade-0 tiles");
 
 // The shared-memory limit of every k_level0_tma instantiation of element type
 // T: the most any context can need (the generic form: rows of up to 256
