@@ -263,6 +263,10 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
   const int dx = di.step_T[0], dy = di.step_T[1], dz = di.step_T[2];
   int k = di.steps;
   bool first = test_start;
+  // wide rows: the in-grid probes of a cell column cx (every lane of the warp
+  // walks the same offsets, so the recompute on a change of cx is uniform)
+  int pcx = INT_MIN;
+  uint32_t rx = 0u;
   for (; valid != 0u;) {
     int bx_[kWalkBatch], by_[kWalkBatch], bz_[kWalkBatch];
     uint2 lo_[kWalkBatch], hi_[kWalkBatch];
@@ -315,7 +319,11 @@ __device__ __forceinline__ void walk_word(const LevelArgs& a, const DirInfo& di,
       // probes whose cell (x + cx, y + cy) is still inside the grid
       uint32_t inr;
       if (wide) {
-        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? range_bits(-cx - wx0, Mx - cx - wx0) : 0u;
+        if (cx != pcx) {
+          pcx = cx;
+          rx = range_bits(-cx - wx0, Mx - cx - wx0);
+        }
+        inr = ((unsigned)(wy0 + cy) < (unsigned)My) ? rx : 0u;
       } else {
         inr = range_bits(max(0, -cx), min(Mx, Mx - cx)) * a.rep;
         inr &= range_bits((-cy - wy0) * Px, (My - cy - wy0) * Px);
