@@ -22,6 +22,8 @@
 // any Mx uses all 32 bits of a lane.
 #pragma once
 
+#include <climits>
+
 #include "rc_kernels.cuh"
 #include "rc_tma.cuh"
 
